@@ -1,0 +1,153 @@
+"""ctypes binding of libflowmc.so (the C ABI declared in include/flowmc.h).
+
+The library is loaded lazily from this package directory. There is no
+fallback: if the library is missing or the tensors are not on a CUDA device,
+the call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+from pathlib import Path
+
+import torch
+
+LIB_PATH = Path(__file__).resolve().parent / "libflowmc.so"
+
+FMC_OK = 0
+FMC_ERR_INVALID_ARG = 1
+FMC_ERR_UNSUPPORTED = 2
+FMC_ERR_CUDA = 3
+FMC_ERR_TIMEOUT = 4
+FMC_ERR_NONFINITE = 5
+_STATUS = {1: "INVALID_ARG", 2: "UNSUPPORTED", 3: "CUDA_ERROR", 4: "TIMEOUT", 5: "NONFINITE"}
+
+TARGET_DIAG_GAUSSIAN = 0
+TARGET_DUAL_MOON = 1
+TARGET_GAUSS_MIXTURE = 2
+TARGET_ROSENBROCK = 3
+TARGET_DENSE_GAUSSIAN = 4
+
+KERNEL_MALA = 0
+KERNEL_HMC = 1
+KERNEL_GRW = 2
+
+c_float_p = ctypes.POINTER(ctypes.c_float)
+
+
+class FmcTarget(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("n_dim", ctypes.c_int32),
+        ("n_comp", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("mean", ctypes.c_void_p),
+        ("inv_var", ctypes.c_void_p),
+        ("log_w", ctypes.c_void_p),
+        ("precision", ctypes.c_void_p),
+        ("scalars", ctypes.c_float * 8),
+    ]
+
+
+class FmcLocalParams(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("n_leapfrog", ctypes.c_int32),
+        ("step_size", ctypes.c_float),
+        ("lanes_per_chain", ctypes.c_int32),
+        ("momentum_scale", ctypes.c_void_p),
+        ("metric_colsum", ctypes.c_void_p),
+    ]
+
+
+class FlowMCError(RuntimeError):
+    """A libflowmc entry point returned a non-zero status."""
+
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"libflowmc {_STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+_lock = threading.Lock()
+_lib = None
+
+_SIGNATURES = {
+    "fmc_local_steps": (ctypes.c_int, [
+        ctypes.POINTER(FmcTarget), ctypes.POINTER(FmcLocalParams), ctypes.c_void_p, ctypes.c_void_p,
+        ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64, ctypes.c_uint64,
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+        ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "fmc_target_value_grad": (ctypes.c_int, [
+        ctypes.POINTER(FmcTarget), ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+        ctypes.c_void_p, ctypes.c_void_p]),
+    "fmc_last_error": (ctypes.c_char_p, []),
+    "fmc_version": (ctypes.c_int, []),
+    "fmc_device_sm_count": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int32)]),
+}
+
+EXPORTED = tuple(_SIGNATURES)
+
+
+def _register(lib, name, restype, argtypes):
+    fn = getattr(lib, name)
+    fn.restype = restype
+    fn.argtypes = argtypes
+
+
+def lib():
+    """The loaded library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            if not LIB_PATH.exists():
+                raise RuntimeError(
+                    f"{LIB_PATH} is missing: build it with `python -m flowmc_gb300.build` "
+                    "(there is no CPU fallback)")
+            h = ctypes.CDLL(str(LIB_PATH))
+            for name, (rt, at) in _SIGNATURES.items():
+                _register(h, name, rt, at)
+            _lib = h
+    return _lib
+
+
+def register_extra(name: str, restype, argtypes) -> None:
+    """Declare another exported entry point (used by sibling modules)."""
+    _SIGNATURES[name] = (restype, argtypes)
+    global EXPORTED
+    EXPORTED = tuple(_SIGNATURES)
+    if _lib is not None:
+        _register(_lib, name, restype, argtypes)
+
+
+def check(status: int) -> None:
+    if status != FMC_OK:
+        msg = lib().fmc_last_error()
+        raise FlowMCError(status, msg.decode() if msg else "")
+
+
+def stream_handle(device: torch.device | None = None) -> int:
+    """cudaStream_t of torch's current stream on `device`."""
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def ptr(t: torch.Tensor | None) -> int | None:
+    """Device pointer of a CUDA tensor (None -> NULL); raises for CPU tensors."""
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise RuntimeError("libflowmc takes CUDA tensors only (there is no CPU path)")
+    return t.data_ptr()
+
+
+def require_cuda_f32(t: torch.Tensor, name: str, shape: tuple | None = None) -> torch.Tensor:
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise RuntimeError(f"{name} must be a CUDA tensor (there is no CPU path)")
+    if t.dtype != torch.float32:
+        raise TypeError(f"{name} must be float32, got {t.dtype}")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+    if shape is not None and tuple(t.shape) != tuple(shape):
+        raise ValueError(f"{name} has shape {tuple(t.shape)}, expected {tuple(shape)}")
+    return t

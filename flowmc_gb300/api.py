@@ -1,0 +1,12 @@
+"""Public API in one namespace (and the import that registers every C entry point)."""
+from .random import PRNGKey, split  # noqa: F401
+from .resource.buffers import Buffer  # noqa: F401
+from .resource.states import State  # noqa: F401
+from .resource.logPDF import LogPDF, Variable  # noqa: F401
+from .resource.kernel.MALA import MALA  # noqa: F401
+from .resource.kernel.HMC import HMC  # noqa: F401
+from .resource.kernel.Gaussian_random_walk import GaussianRandomWalk  # noqa: F401
+from .strategy.take_steps import TakeSerialSteps, TakeGroupSteps  # noqa: F401
+from .strategy.lambda_function import Lambda  # noqa: F401
+from .strategy.update_state import UpdateState  # noqa: F401
+from . import targets  # noqa: F401

@@ -1,0 +1,164 @@
+// common.cuh -- shared device helpers for libflowmc (sm_103a).
+//
+//  * status plumbing: thread-local error text, FMC_TRY / CUDA_TRY macros
+//  * Philox-4x32-10 counter-based RNG (Salmon, Moraes, Dror, Shaw,
+//    "Parallel random numbers: as easy as 1, 2, 3", SC'11), with normals by
+//    the Box-Muller transform (Box & Muller, Ann. Math. Stat. 29, 1958)
+//  * lane-group reductions (warp shuffles)
+//  * float-float ("double-single") sums after Knuth's TwoSum (TAOCP vol. 2,
+//    4.2.2) for the Metropolis-Hastings log-ratio
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string>
+#include "../../include/flowmc.h"
+
+namespace fmc {
+
+// ---------------------------------------------------------------- errors
+void set_error(const char* fmt, ...);
+
+#define FMC_CHECK_ARG(cond, ...)                 \
+  do {                                           \
+    if (!(cond)) {                               \
+      ::fmc::set_error(__VA_ARGS__);             \
+      return FMC_ERR_INVALID_ARG;                \
+    }                                            \
+  } while (0)
+
+#define FMC_CHECK_SUPPORTED(cond, ...)           \
+  do {                                           \
+    if (!(cond)) {                               \
+      ::fmc::set_error(__VA_ARGS__);             \
+      return FMC_ERR_UNSUPPORTED;                \
+    }                                            \
+  } while (0)
+
+#define FMC_CUDA_TRY(expr)                                                   \
+  do {                                                                       \
+    cudaError_t _e = (expr);                                                 \
+    if (_e != cudaSuccess) {                                                 \
+      ::fmc::set_error("%s failed: %s (%s:%d)", #expr, cudaGetErrorString(_e), \
+                       __FILE__, __LINE__);                                  \
+      return FMC_ERR_CUDA;                                                   \
+    }                                                                        \
+  } while (0)
+
+#define FMC_LAUNCH_CHECK()                                                   \
+  do {                                                                       \
+    cudaError_t _e = cudaGetLastError();                                     \
+    if (_e != cudaSuccess) {                                                 \
+      ::fmc::set_error("kernel launch failed: %s (%s:%d)",                  \
+                       cudaGetErrorString(_e), __FILE__, __LINE__);          \
+      return FMC_ERR_CUDA;                                                   \
+    }                                                                        \
+  } while (0)
+
+int sm_count();  // cached per device
+
+// ---------------------------------------------------------------- Philox
+// Philox-4x32 with 10 rounds, constants from the SC'11 paper (Table 2 and
+// the Weyl key schedule). counter = 4 x u32, key = 2 x u32.
+struct u32x4 { uint32_t x, y, z, w; };
+
+__device__ __forceinline__ u32x4 philox4x32_10(u32x4 c, uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+  const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+    const uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+    c = u32x4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    k0 += W0;
+    k1 += W1;
+  }
+  return c;
+}
+
+// u32 -> uniform in (0, 1]: 24 significant bits, never 0 (log finite).
+__device__ __forceinline__ float u32_to_unit(uint32_t v) {
+  return (float)((v >> 8) + 1u) * (1.0f / 16777216.0f);
+}
+
+// Box-Muller: two uniforms -> two independent standard normals.
+__device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float& z0, float& z1) {
+  const float u1 = u32_to_unit(a);
+  const float u2 = u32_to_unit(b);
+  const float r = sqrtf(-2.0f * __logf(u1));
+  float s, c;
+  // angle 2*pi*u2 - pi keeps the argument inside [-pi, pi] for __sincosf
+  __sincosf(6.28318530717958647692f * u2 - 3.14159265358979323846f, &s, &c);
+  z0 = r * c;
+  z1 = r * s;
+}
+
+// Counter layout shared by every kernel: (x, y) = 64-bit stream position
+// (chain index and step), z = draw slot within the step, w = stream tag.
+enum : uint32_t {
+  RNG_TAG_LOCAL_NORMAL = 0x4c4e0000u,
+  RNG_TAG_LOCAL_UNIFORM = 0x4c550000u,
+  RNG_TAG_NF_NORMAL = 0x4e4e0000u,
+  RNG_TAG_NF_UNIFORM = 0x4e550000u,
+};
+
+struct Rng {
+  uint32_t k0, k1;     // key = seed
+  uint64_t ctr_base;   // call counter, folded into the step word
+  __device__ __forceinline__ u32x4 draw(uint64_t row, uint64_t step, uint32_t slot, uint32_t tag) const {
+    const uint64_t s = step + (ctr_base << 32);
+    u32x4 c{(uint32_t)row, (uint32_t)(row >> 32) ^ (uint32_t)(s >> 32), slot, tag ^ (uint32_t)s};
+    return philox4x32_10(c, k0, k1);
+  }
+};
+
+// ---------------------------------------------------------------- groups
+// A "group" is G consecutive lanes of a warp that own one chain.
+template <int G>
+__device__ __forceinline__ float group_sum(float v) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, G);
+  return v;
+}
+template <int G>
+__device__ __forceinline__ float group_max(float v) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o, G));
+  return v;
+}
+template <int G>
+__device__ __forceinline__ float group_bcast(float v, int src_lane_in_group) {
+  return __shfl_sync(0xffffffffu, v, src_lane_in_group, G);
+}
+
+// ---------------------------------------------------------------- float-float
+struct ff { float hi, lo; };
+__device__ __forceinline__ ff two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return ff{s, e};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  ff s = two_sum(a.hi, b.hi);
+  const float lo = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+  return two_sum(s.hi, lo);
+}
+__device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.hi, -a.lo}; }
+// exact product of two floats as float-float (FMA-based TwoProduct)
+__device__ __forceinline__ ff two_prod(float a, float b) {
+  const float p = __fmul_rn(a, b);
+  const float e = __fmaf_rn(a, b, -p);
+  return ff{p, e};
+}
+__device__ __forceinline__ ff ff_mul_f(ff a, float b) {
+  ff p = two_prod(a.hi, b);
+  const float lo = __fmaf_rn(a.lo, b, p.lo);
+  return two_sum(p.hi, lo);
+}
+// a < b where a is a float and b a float-float
+__device__ __forceinline__ bool f_lt_ff(float a, ff b) {
+  return (a < b.hi) || (a == b.hi && 0.0f < b.lo);
+}
+
+}  // namespace fmc

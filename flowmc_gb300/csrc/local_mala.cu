@@ -1,0 +1,9 @@
+// local_mala.cu -- instantiations of the K1 persistent local-step kernel for FMC_KERNEL_MALA
+// (split per kernel kind so the instantiations compile in parallel).
+#include "local_steps.cuh"
+
+namespace fmc {
+int launch_local_mala(const LocalArgs& a, Shape sh, cudaStream_t st) {
+  return launch_local_kind<FMC_KERNEL_MALA>(a, sh, st);
+}
+}  // namespace fmc

@@ -1,0 +1,363 @@
+// local_steps.cuh -- K1: the persistent local-step kernel.
+//
+// One launch runs n_steps of MALA, HMC or Gaussian random walk for every
+// chain. A chain is owned by a group of G lanes (lanes_per_chain) that keep
+// its position, log-density and gradient in registers for the whole call;
+// noise comes from in-kernel Philox (or an explicit array for parity runs),
+// the Metropolis-Hastings accept is fused in, and every `thinning`-th state
+// is written straight into flowMC's buffers [n_chains, buf_len, n_dim] with
+// vectorised streaming stores (the G lanes of a chain cover one contiguous
+// row, so the store of a step is one coalesced segment).
+//
+// Reference semantics reproduced (flowMC v0.4.5):
+//  * TakeSerialSteps.sample: lp0 = logpdf(x0); scan over steps
+//    (strategy/take_steps.py:164-180); thinning positions[:, ::thinning]
+//    (take_steps.py:134-138); the strategy returns the last *thinned*
+//    position (take_steps.py:144).
+//  * MALA.kernel (resource/kernel/MALA.py:26-89): proposal
+//    x + dt^2 g(x)/2 + dt xi, log-ratio with the two isotropic Gaussian
+//    proposal densities, accept iff log(u) < ratio, lp recomputed at x.
+//    The (lp0, g0) the reference recomputes every step equals the cached
+//    value of the previous step bit for bit, so it is cached here.
+//  * HMC.kernel (resource/kernel/HMC.py:98-151): momentum xi @
+//    cholesky(inv(M)).T, kinetic 0.5 * sum(p^2 * M) (broadcast: column sums
+//    of M), leapfrog table rows [0,.5], [1,1] x n_leapfrog, [1,.5]
+//    (HMC.py:47-50, 71-80) = n_leapfrog+1 drifts with half kicks at both
+//    ends; H uses the incoming log_prob (HMC.py:137).
+//  * GaussianRandomWalk.kernel (Gaussian_random_walk.py:48-61).
+//
+// The MH log-ratio is assembled in float-float arithmetic (about 48
+// significant bits) instead of FP64: this GPU's FP64 rate is too low for a
+// per-chain-step operation, and the inputs (lp, squared norms) are FP32.
+#pragma once
+#include "targets.cuh"
+
+namespace fmc {
+
+struct LocalArgs {
+  FmcTarget tgt;
+  int32_t n_leapfrog;
+  float step;
+  const float* mscale;  // HMC momentum scale (diag of cholesky(inv(M)))
+  const float* mcol;    // HMC column sums of M
+  const float* x0;
+  const float* lp0;
+  int32_t C, d, S, thin;
+  Rng rng;
+  const float* noise;
+  const float* unif;
+  float* out_pos;
+  float* out_logp;
+  float* out_acc;
+  int64_t buf_len, start;
+  float* x_last;
+  float* lp_last;
+  int64_t C_pad;
+};
+
+template <int V>
+__device__ __forceinline__ void draw_normals(const LocalArgs& a, int64_t c, int s, int gl,
+                                             float (&xi)[V]) {
+  const int d = a.d;
+  if (a.noise) {
+    const float* row = a.noise + ((int64_t)c * a.S + s) * d;
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const int j = gl * V + v;
+      xi[v] = (j < d) ? __ldcs(row + j) : 0.f;
+    }
+    return;
+  }
+#pragma unroll
+  for (int q = 0; q < V; q += 4) {
+    const u32x4 r = a.rng.draw(c, s, (uint32_t)(gl * V + q), RNG_TAG_LOCAL_NORMAL);
+    float z0, z1, z2, z3;
+    box_muller(r.x, r.y, z0, z1);
+    xi[q] = z0;
+    if (q + 1 < V) xi[q + 1] = z1;
+    if (q + 2 < V) {
+      box_muller(r.z, r.w, z2, z3);
+      xi[q + 2] = z2;
+      if (q + 3 < V) xi[q + 3] = z3;
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < V; ++v)
+    if (gl * V + v >= d) xi[v] = 0.f;
+}
+
+__device__ __forceinline__ float draw_uniform(const LocalArgs& a, int64_t c, int s) {
+  if (a.unif) return __ldcs(a.unif + (int64_t)c * a.S + s);
+  return u32_to_unit(a.rng.draw(c, s, 0u, RNG_TAG_LOCAL_UNIFORM).x);
+}
+
+template <int G, int V>
+__device__ __forceinline__ void store_row(float* dst, const float (&x)[V], int gl, int d) {
+  // dst points at element 0 of the row
+  if constexpr (V % 4 == 0) {
+    if (d % 4 == 0) {
+      if (gl * V < d) {
+#pragma unroll
+        for (int q = 0; q < V; q += 4)
+          __stcs(reinterpret_cast<float4*>(dst + gl * V + q), make_float4(x[q], x[q + 1], x[q + 2], x[q + 3]));
+      }
+      return;
+    }
+  }
+  if constexpr (V % 2 == 0) {
+    if (d % 2 == 0) {
+      if (gl * V < d) {
+#pragma unroll
+        for (int q = 0; q < V; q += 2)
+          __stcs(reinterpret_cast<float2*>(dst + gl * V + q), make_float2(x[q], x[q + 1]));
+      }
+      return;
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    const int j = gl * V + v;
+    if (j < d) __stcs(dst + j, x[v]);
+  }
+}
+
+template <int KIND, int TGT, int G, int V>
+__global__ void __launch_bounds__(256) k_local_steps(const LocalArgs a) {
+  extern __shared__ float smem[];
+  const int gl = threadIdx.x % G;
+  const int64_t groups_per_block = blockDim.x / G;
+  const int64_t gib = threadIdx.x / G;
+  const int d = a.d;
+  float* stage = (TGT == FMC_TARGET_DENSE_GAUSSIAN) ? smem + gib * d : nullptr;
+  const float dt = a.step;
+
+  for (int64_t c = blockIdx.x * groups_per_block + gib; c < a.C_pad;
+       c += (int64_t)gridDim.x * groups_per_block) {
+    const bool active = c < a.C;
+    const int64_t cc = active ? c : 0;
+    float x[V], g[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const int j = gl * V + v;
+      x[v] = (j < d) ? __ldg(a.x0 + cc * d + j) : 0.f;
+    }
+    float lp = target_eval<TGT, G, V, KIND != FMC_KERNEL_GRW>(a.tgt, x, g, gl, stage);
+    if (KIND != FMC_KERNEL_MALA && a.lp0 != nullptr) lp = __ldg(a.lp0 + cc);
+    float xr[V], lpr = lp;
+#pragma unroll
+    for (int v = 0; v < V; ++v) xr[v] = x[v];
+
+    for (int s = 0; s < a.S; ++s) {
+      float xi[V];
+      draw_normals<V>(a, cc, s, gl, xi);
+      const float logu = logf(draw_uniform(a, cc, s));
+      bool acc;
+      if constexpr (KIND == FMC_KERNEL_MALA) {
+        const float dt2 = dt * dt;
+        float mean0[V], prop[V], g1[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          mean0[v] = x[v] + dt2 * g[v] / 2.0f;
+          prop[v] = mean0[v] + dt * xi[v];
+        }
+        const float lp1 = target_eval<TGT, G, V, true>(a.tgt, prop, g1, gl, stage);
+        float sa = 0.f, sb = 0.f;
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          const float ea = prop[v] - mean0[v];
+          const float eb = x[v] - (prop[v] + dt2 * g1[v] / 2.0f);
+          sa += ea * ea;
+          sb += eb * eb;
+        }
+        sa = group_sum<G>(sa);
+        sb = group_sum<G>(sb);
+        // ratio = (lp1 - lp0) - (|prop - mean0|^2 - |x - mean1|^2) / (2 dt^2)
+        const ff q = two_sum(sa, -sb);
+        const ff ratio = ff_add(two_sum(lp1, -lp), ff_neg(ff_mul_f(q, 0.5f / dt2)));
+        acc = f_lt_ff(logu, ratio);
+        if (acc) {
+#pragma unroll
+          for (int v = 0; v < V; ++v) { x[v] = prop[v]; g[v] = g1[v]; }
+          lp = lp1;
+        }
+      } else if constexpr (KIND == FMC_KERNEL_HMC) {
+        float p[V], mc[V], xq[V], gq[V];
+        float k0 = 0.f;
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          const int j = gl * V + v;
+          const bool in = j < d;
+          p[v] = xi[v] * (in ? ldg_or(a.mscale, j, 1.f) : 0.f);
+          mc[v] = in ? ldg_or(a.mcol, j, 1.f) : 0.f;
+          k0 += p[v] * p[v] * mc[v];
+          xq[v] = x[v];
+        }
+        k0 = 0.5f * group_sum<G>(k0);
+        // row 0: drift coefficient 0, kick 0.5 with the gradient at x
+        const float e0 = dt * 0.5f;
+#pragma unroll
+        for (int v = 0; v < V; ++v) p[v] = p[v] + e0 * g[v];
+        float lpq = lp;
+        const int nlf = a.n_leapfrog;
+        for (int r = 1; r <= nlf + 1; ++r) {
+          const float ek = (r == nlf + 1) ? dt * 0.5f : dt;
+#pragma unroll
+          for (int v = 0; v < V; ++v) xq[v] = xq[v] + dt * (p[v] * mc[v]);
+          lpq = target_eval<TGT, G, V, true>(a.tgt, xq, gq, gl, stage);
+#pragma unroll
+          for (int v = 0; v < V; ++v) p[v] = p[v] + ek * gq[v];
+        }
+        float k1 = 0.f;
+#pragma unroll
+        for (int v = 0; v < V; ++v) k1 += p[v] * p[v] * mc[v];
+        k1 = 0.5f * group_sum<G>(k1);
+        // log_acc = (-lp + K0) - (-lpq + K1)
+        const ff h0 = two_sum(-lp, k0);
+        const ff h1 = two_sum(-lpq, k1);
+        const ff log_acc = ff_add(h0, ff_neg(h1));
+        acc = f_lt_ff(logu, log_acc);
+        if (acc) {
+#pragma unroll
+          for (int v = 0; v < V; ++v) { x[v] = xq[v]; g[v] = gq[v]; }
+          lp = lpq;
+        }
+      } else {  // GRW
+        float prop[V], gdummy[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) prop[v] = x[v] + xi[v] * dt;
+        const float lpp = target_eval<TGT, G, V, false>(a.tgt, prop, gdummy, gl, stage);
+        acc = f_lt_ff(logu, two_sum(lpp, -lp));
+        if (acc) {
+#pragma unroll
+          for (int v = 0; v < V; ++v) x[v] = prop[v];
+          lp = lpp;
+        }
+      }
+      if (s % a.thin == 0) {
+        if (active) {
+          const int64_t row = cc * a.buf_len + a.start + s / a.thin;
+          store_row<G, V>(a.out_pos + row * d, x, gl, d);
+          if (gl == 0) {
+            __stcs(a.out_logp + row, lp);
+            __stcs(a.out_acc + row, acc ? 1.f : 0.f);
+          }
+        }
+#pragma unroll
+        for (int v = 0; v < V; ++v) xr[v] = x[v];
+        lpr = lp;
+      }
+    }
+    if (active) {
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        const int j = gl * V + v;
+        if (j < d) a.x_last[cc * d + j] = xr[v];
+      }
+      if (gl == 0) a.lp_last[cc] = lpr;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ batch eval
+template <int TGT, int G, int V>
+__global__ void __launch_bounds__(256) k_target_eval(const FmcTarget t, const float* __restrict__ x,
+                                                     int64_t n, int64_t n_pad, float* logp, float* grad) {
+  extern __shared__ float smem[];
+  const int gl = threadIdx.x % G;
+  const int64_t gpb = blockDim.x / G, gib = threadIdx.x / G;
+  const int d = t.n_dim;
+  float* stage = (TGT == FMC_TARGET_DENSE_GAUSSIAN) ? smem + gib * d : nullptr;
+  for (int64_t r = blockIdx.x * gpb + gib; r < n_pad; r += (int64_t)gridDim.x * gpb) {
+    const bool active = r < n;
+    const int64_t rr = active ? r : 0;
+    float xv[V], gv[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const int j = gl * V + v;
+      xv[v] = (j < d) ? x[rr * d + j] : 0.f;
+    }
+    const float lp = target_eval<TGT, G, V, true>(t, xv, gv, gl, stage);
+    if (active) {
+      if (gl == 0) logp[rr] = lp;
+      if (grad) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          const int j = gl * V + v;
+          if (j < d) grad[rr * d + j] = gv[v];
+        }
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ dispatch
+// Instantiated (lanes per chain, coordinates per lane) shapes.
+struct Shape { int G, V; };
+
+// choose the default (G, V) for a dimension: the fewest lanes whose capacity
+// covers n_dim with at most 8 coordinates per lane, preferring wide groups
+// only when the dimension needs them.
+inline Shape default_shape(int d) {
+  if (d <= 4) return {4, 1};
+  if (d <= 8) return {8, 1};
+  if (d <= 16) return {8, 2};
+  if (d <= 32) return {8, 4};
+  if (d <= 64) return {16, 4};
+  if (d <= 128) return {32, 4};
+  return {32, 8};
+}
+
+template <int KIND, int TGT, int G, int V>
+int launch_local_t(const LocalArgs& a0, cudaStream_t st) {
+  LocalArgs a = a0;
+  const int threads = 256;
+  const int gpb = threads / G;
+  const int gpw = 32 / G;
+  a.C_pad = ((int64_t)a.C + gpw - 1) / gpw * gpw;
+  const size_t smem = (TGT == FMC_TARGET_DENSE_GAUSSIAN) ? (size_t)gpb * a.d * sizeof(float) : 0;
+  auto kern = k_local_steps<KIND, TGT, G, V>;
+  if (smem > 48 * 1024) {
+    FMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  }
+  int per_sm = 0;
+  FMC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
+  if (per_sm < 1) per_sm = 1;
+  const int64_t need = (a.C_pad + gpb - 1) / gpb;
+  const int64_t cap = (int64_t)sm_count() * per_sm;
+  const int blocks = (int)(need < cap ? need : cap);
+  kern<<<blocks, threads, smem, st>>>(a);
+  FMC_LAUNCH_CHECK();
+  return FMC_OK;
+}
+
+template <int KIND, int TGT>
+int launch_local_shape(const LocalArgs& a, Shape sh, cudaStream_t st) {
+#define FMC_SHAPE_CASE(g, v) \
+  if (sh.G == g && sh.V == v) return launch_local_t<KIND, TGT, g, v>(a, st);
+  FMC_SHAPE_CASE(4, 1) FMC_SHAPE_CASE(8, 1) FMC_SHAPE_CASE(4, 2) FMC_SHAPE_CASE(8, 2)
+  FMC_SHAPE_CASE(32, 1) FMC_SHAPE_CASE(8, 4) FMC_SHAPE_CASE(16, 2) FMC_SHAPE_CASE(32, 2)
+  FMC_SHAPE_CASE(16, 4) FMC_SHAPE_CASE(32, 4) FMC_SHAPE_CASE(16, 8) FMC_SHAPE_CASE(32, 8)
+#undef FMC_SHAPE_CASE
+  set_error("lanes_per_chain=%d with %d coordinates per lane is not instantiated", sh.G, sh.V);
+  return FMC_ERR_UNSUPPORTED;
+}
+
+template <int KIND>
+int launch_local_kind(const LocalArgs& a, Shape sh, cudaStream_t st) {
+  switch (a.tgt.kind) {
+    case FMC_TARGET_DIAG_GAUSSIAN: return launch_local_shape<KIND, FMC_TARGET_DIAG_GAUSSIAN>(a, sh, st);
+    case FMC_TARGET_DUAL_MOON: return launch_local_shape<KIND, FMC_TARGET_DUAL_MOON>(a, sh, st);
+    case FMC_TARGET_GAUSS_MIXTURE: return launch_local_shape<KIND, FMC_TARGET_GAUSS_MIXTURE>(a, sh, st);
+    case FMC_TARGET_ROSENBROCK: return launch_local_shape<KIND, FMC_TARGET_ROSENBROCK>(a, sh, st);
+    case FMC_TARGET_DENSE_GAUSSIAN: return launch_local_shape<KIND, FMC_TARGET_DENSE_GAUSSIAN>(a, sh, st);
+  }
+  set_error("unknown target kind %d", a.tgt.kind);
+  return FMC_ERR_INVALID_ARG;
+}
+
+int launch_local_mala(const LocalArgs& a, Shape sh, cudaStream_t st);
+int launch_local_hmc(const LocalArgs& a, Shape sh, cudaStream_t st);
+int launch_local_grw(const LocalArgs& a, Shape sh, cudaStream_t st);
+int check_target(const FmcTarget* t);
+
+}  // namespace fmc

@@ -1,0 +1,210 @@
+// targets.cuh -- registered target log-densities with hand-written adjoints.
+//
+// The reference takes an arbitrary JAX callable `logpdf(x, data)` and
+// differentiates it with jax.value_and_grad (resource/kernel/MALA.py:59,
+// resource/kernel/HMC.py:73-78). A fused device kernel cannot run Python, so
+// the sampler is given a target descriptor (FmcTarget) and evaluates the
+// value and its analytic gradient here.
+//
+// Work split: a chain is owned by a group of G lanes; lane `gl` holds the V
+// consecutive coordinates j = gl*V + v (v < V) of the position. Coordinates
+// j >= n_dim are padding: they hold 0, contribute 0 and get gradient 0.
+// Reductions over coordinates are butterfly shuffles inside the group, so
+// every lane of the group ends with the bitwise-same value.
+#pragma once
+#include "common.cuh"
+
+namespace fmc {
+
+constexpr int kMaxMixtureComponents = 16;
+
+template <int V>
+struct Vec { float v[V]; };
+
+__device__ __forceinline__ float ldg_or(const float* p, int64_t i, float dflt) {
+  return p ? __ldg(p + i) : dflt;
+}
+
+// --------------------------------------------------------------- diag Gaussian
+template <int G, int V, bool GRAD>
+__device__ __forceinline__ float tg_diag_gaussian(const FmcTarget& t, const float (&x)[V],
+                                                  float (&g)[V], int gl) {
+  const int d = t.n_dim;
+  float s = 0.f;
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    const int j = gl * V + v;
+    if (j < d) {
+      const float dx = x[v] - ldg_or(t.mean, j, 0.f);
+      const float iv = ldg_or(t.inv_var, j, 1.f);
+      s += dx * dx * iv;
+      if (GRAD) g[v] = -dx * iv;
+    } else if (GRAD) {
+      g[v] = 0.f;
+    }
+  }
+  return -0.5f * group_sum<G>(s) + t.scalars[0];
+}
+
+// --------------------------------------------------------------- dual moon
+// log p = -0.5((|x| - s0)/s1)^2 + logsumexp(-0.5((x0 + s2)/s3)^2, -0.5((x0 - s2)/s3)^2)
+template <int G, int V, bool GRAD>
+__device__ __forceinline__ float tg_dual_moon(const FmcTarget& t, const float (&x)[V],
+                                              float (&g)[V], int gl) {
+  const int d = t.n_dim;
+  const float s0 = t.scalars[0], s1 = t.scalars[1], s2 = t.scalars[2], s3 = t.scalars[3];
+  float r2 = 0.f;
+#pragma unroll
+  for (int v = 0; v < V; ++v) r2 += x[v] * x[v];  // padding holds 0
+  r2 = group_sum<G>(r2);
+  const float r = sqrtf(r2);
+  const float tt = (r - s0) / s1;
+  const float x0 = group_bcast<G>(x[0], 0);
+  const float za = (x0 + s2) / s3, zb = (x0 - s2) / s3;
+  const float a = -0.5f * za * za, b = -0.5f * zb * zb;
+  const float m = fmaxf(a, b);
+  const float lse = m + log1pf(expf(-fabsf(a - b)));
+  if (GRAD) {
+    const float cr = -(tt / s1) / r;
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const int j = gl * V + v;
+      g[v] = (j < d) ? cr * x[v] : 0.f;
+    }
+    if (gl == 0) {
+      const float wa = expf(a - lse), wb = expf(b - lse);
+      g[0] += wa * (-za / s3) + wb * (-zb / s3);
+    }
+  }
+  return -0.5f * tt * tt + lse;
+}
+
+// --------------------------------------------------------------- Gaussian mixture
+// log p = logsumexp_k( log_w[k] - 0.5 sum_j (x_j - mean[k,j])^2 inv_var[k,j] )
+template <int G, int V, bool GRAD>
+__device__ __forceinline__ float tg_mixture(const FmcTarget& t, const float (&x)[V],
+                                            float (&g)[V], int gl) {
+  const int d = t.n_dim, K = t.n_comp;
+  float e[kMaxMixtureComponents];
+  float emax = -INFINITY;
+#pragma unroll
+  for (int k = 0; k < kMaxMixtureComponents; ++k) {
+    if (k < K) {
+      float q = 0.f;
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        const int j = gl * V + v;
+        if (j < d) {
+          const float dx = x[v] - ldg_or(t.mean, (int64_t)k * d + j, 0.f);
+          q += dx * dx * ldg_or(t.inv_var, (int64_t)k * d + j, 1.f);
+        }
+      }
+      e[k] = ldg_or(t.log_w, k, 0.f) - 0.5f * group_sum<G>(q);
+      emax = fmaxf(emax, e[k]);
+    }
+  }
+  float ssum = 0.f;
+#pragma unroll
+  for (int k = 0; k < kMaxMixtureComponents; ++k)
+    if (k < K) ssum += expf(e[k] - emax);
+  const float lse = emax + logf(ssum);
+  if (GRAD) {
+#pragma unroll
+    for (int v = 0; v < V; ++v) g[v] = 0.f;
+#pragma unroll
+    for (int k = 0; k < kMaxMixtureComponents; ++k) {
+      if (k < K) {
+        const float w = expf(e[k] - lse);
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          const int j = gl * V + v;
+          if (j < d) {
+            const float dx = x[v] - ldg_or(t.mean, (int64_t)k * d + j, 0.f);
+            g[v] -= w * dx * ldg_or(t.inv_var, (int64_t)k * d + j, 1.f);
+          }
+        }
+      }
+    }
+  }
+  return lse;
+}
+
+// --------------------------------------------------------------- Rosenbrock chain
+// log p = -sum_{i=0}^{d-2} [ (s1 - x_i)^2 / s0 + s2 (x_{i+1} - x_i^2)^2 ]
+template <int G, int V, bool GRAD>
+__device__ __forceinline__ float tg_rosenbrock(const FmcTarget& t, const float (&x)[V],
+                                               float (&g)[V], int gl) {
+  const int d = t.n_dim;
+  const float s0 = t.scalars[0], s1 = t.scalars[1], s2 = t.scalars[2];
+  // neighbours across the lane boundary
+  const float next_first = __shfl_down_sync(0xffffffffu, x[0], 1, G);   // x_{gl*V+V}
+  const float prev_last = __shfl_up_sync(0xffffffffu, x[V - 1], 1, G);  // x_{gl*V-1}
+  float s = 0.f;
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    const int j = gl * V + v;
+    const float xn = (v + 1 < V) ? x[v + 1] : next_first;
+    const float xp = (v > 0) ? x[v - 1] : prev_last;
+    const bool has_next = (j + 1 < d);
+    const bool has_prev = (j >= 1) && (j < d);
+    const float a = s1 - x[v];
+    const float b = xn - x[v] * x[v];
+    if (has_next) s += a * a / s0 + s2 * b * b;
+    if (GRAD) {
+      float gv = 0.f;
+      if (has_next) gv += 2.f * a / s0 + 4.f * s2 * x[v] * b;
+      if (has_prev) gv -= 2.f * s2 * (x[v] - xp * xp);
+      g[v] = gv;
+    }
+  }
+  return -group_sum<G>(s);
+}
+
+// --------------------------------------------------------------- dense Gaussian
+// log p = -0.5 (x-m)^T P (x-m) + scalars[0], P symmetric (the host symmetrises).
+// The group stages dx in shared memory (`stage`, n_dim floats per group).
+template <int G, int V, bool GRAD>
+__device__ __forceinline__ float tg_dense_gaussian(const FmcTarget& t, const float (&x)[V],
+                                                   float (&g)[V], int gl, float* stage) {
+  const int d = t.n_dim;
+  float dx[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    const int j = gl * V + v;
+    dx[v] = (j < d) ? x[v] - ldg_or(t.mean, j, 0.f) : 0.f;
+    if (j < d) stage[j] = dx[v];
+  }
+  __syncwarp();
+  float acc[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) acc[v] = 0.f;
+  for (int k = 0; k < d; ++k) {
+    const float dk = stage[k];
+    const float* row = t.precision + (int64_t)k * d;
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const int j = gl * V + v;
+      if (j < d) acc[v] += __ldg(row + j) * dk;  // P[k, j] = P[j, k]
+    }
+  }
+  __syncwarp();
+  float s = 0.f;
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    s += dx[v] * acc[v];
+    if (GRAD) g[v] = -acc[v];
+  }
+  return -0.5f * group_sum<G>(s) + t.scalars[0];
+}
+
+template <int TGT, int G, int V, bool GRAD>
+__device__ __forceinline__ float target_eval(const FmcTarget& t, const float (&x)[V],
+                                             float (&g)[V], int gl, float* stage) {
+  if constexpr (TGT == FMC_TARGET_DIAG_GAUSSIAN) return tg_diag_gaussian<G, V, GRAD>(t, x, g, gl);
+  else if constexpr (TGT == FMC_TARGET_DUAL_MOON) return tg_dual_moon<G, V, GRAD>(t, x, g, gl);
+  else if constexpr (TGT == FMC_TARGET_GAUSS_MIXTURE) return tg_mixture<G, V, GRAD>(t, x, g, gl);
+  else if constexpr (TGT == FMC_TARGET_ROSENBROCK) return tg_rosenbrock<G, V, GRAD>(t, x, g, gl);
+  else return tg_dense_gaussian<G, V, GRAD>(t, x, g, gl, stage);
+}
+
+}  // namespace fmc
