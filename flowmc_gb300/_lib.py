@@ -60,6 +60,34 @@ class FmcLocalParams(ctypes.Structure):
     ]
 
 
+FMC_MAX_HIDDEN = 4
+PREC_FP32 = 0
+PREC_BF16 = 1
+
+
+class FmcFlow(ctypes.Structure):
+    _fields_ = [
+        ("n_dim", ctypes.c_int32),
+        ("n_layers", ctypes.c_int32),
+        ("n_hidden", ctypes.c_int32),
+        ("n_bins", ctypes.c_int32),
+        ("hidden", ctypes.c_int32 * FMC_MAX_HIDDEN),
+        ("range_min", ctypes.c_float),
+        ("range_max", ctypes.c_float),
+        ("min_bin_size", ctypes.c_float),
+        ("min_knot_slope", ctypes.c_float),
+        ("precision", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("theta", ctypes.c_void_p),
+        ("theta_bf16", ctypes.c_void_p),
+        ("aux", ctypes.c_void_p),
+    ]
+
+
+class FmcAdamParams(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_float) for n in ("lr", "b1", "b2", "eps", "weight_decay", "max_norm")]
+
+
 class FlowMCError(RuntimeError):
     """A libflowmc entry point returned a non-zero status."""
 
@@ -80,6 +108,47 @@ _SIGNATURES = {
     "fmc_target_value_grad": (ctypes.c_int, [
         ctypes.POINTER(FmcTarget), ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
         ctypes.c_void_p, ctypes.c_void_p]),
+    "fmc_flow_layout": (ctypes.c_int, [ctypes.POINTER(FmcFlow), ctypes.POINTER(ctypes.c_int64),
+                                       ctypes.POINTER(ctypes.c_int64)]),
+    "fmc_flow_workspace_size": (ctypes.c_int, [ctypes.POINTER(FmcFlow), ctypes.c_int64, ctypes.c_int32,
+                                               ctypes.POINTER(ctypes.c_size_t)]),
+    "fmc_flow_sync_bf16": (ctypes.c_int, [ctypes.POINTER(FmcFlow), ctypes.c_void_p]),
+    "fmc_flow_forward": (ctypes.c_int, [ctypes.POINTER(FmcFlow), ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "fmc_flow_inverse": (ctypes.c_int, [ctypes.POINTER(FmcFlow), ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "fmc_flow_log_prob": (ctypes.c_int, [ctypes.POINTER(FmcFlow), ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "fmc_flow_sample": (ctypes.c_int, [ctypes.POINTER(FmcFlow), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p,
+                                       ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                       ctypes.c_void_p]),
+    "fmc_flow_loss_grad": (ctypes.c_int, [ctypes.POINTER(FmcFlow), ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "fmc_nf_workspace_size": (ctypes.c_int, [ctypes.POINTER(FmcFlow), ctypes.c_int32, ctypes.c_int32,
+                                             ctypes.POINTER(ctypes.c_size_t)]),
+    "fmc_nf_global_steps": (ctypes.c_int, [
+        ctypes.POINTER(FmcFlow), ctypes.POINTER(FmcTarget), ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+        ctypes.c_int32, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+        ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "fmc_adamw_workspace_size": (ctypes.c_int, [ctypes.POINTER(ctypes.c_size_t)]),
+    "fmc_adamw_step": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+        ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.POINTER(FmcAdamParams), ctypes.c_void_p,
+        ctypes.c_size_t, ctypes.c_void_p]),
+    "fmc_flag_less": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "fmc_copy_if": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                   ctypes.c_void_p]),
+    "fmc_column_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_void_p]),
+    "fmc_permute_rows": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_uint64,
+                                        ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
+                                        ctypes.c_void_p]),
+    "fmc_select_workspace_size": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int64, ctypes.POINTER(ctypes.c_size_t)]),
+    "fmc_select_training_data": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int64,
+        ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+        ctypes.c_size_t, ctypes.c_void_p]),
     "fmc_last_error": (ctypes.c_char_p, []),
     "fmc_version": (ctypes.c_int, []),
     "fmc_device_sm_count": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int32)]),
@@ -151,3 +220,19 @@ def require_cuda_f32(t: torch.Tensor, name: str, shape: tuple | None = None) -> 
     if shape is not None and tuple(t.shape) != tuple(shape):
         raise ValueError(f"{name} has shape {tuple(t.shape)}, expected {tuple(shape)}")
     return t
+
+
+class Workspace:
+    """A growable, 256-byte aligned device scratch buffer owned by the caller
+    (the library never allocates)."""
+
+    def __init__(self):
+        self._buf = None
+
+    def get(self, nbytes: int, device) -> tuple[int, int]:
+        nbytes = max(int(nbytes), 256)
+        if self._buf is None or self._buf.numel() < nbytes or self._buf.device != torch.device(device):
+            self._buf = torch.empty(nbytes + 256, dtype=torch.uint8, device=device)
+        base = self._buf.data_ptr()
+        off = (-base) % 256
+        return base + off, self._buf.numel() - off

@@ -10,3 +10,9 @@ from .strategy.take_steps import TakeSerialSteps, TakeGroupSteps  # noqa: F401
 from .strategy.lambda_function import Lambda  # noqa: F401
 from .strategy.update_state import UpdateState  # noqa: F401
 from . import targets  # noqa: F401
+from .resource.kernel.NF_proposal import NFProposal  # noqa: F401
+from .resource.model.nf_model.rqSpline import MaskedCouplingRQSpline  # noqa: F401
+from .resource.optimizer import Optimizer  # noqa: F401
+from .strategy.train_model import TrainModel  # noqa: F401
+from .resource_strategy_bundle.RQSpline_MALA import RQSpline_MALA_Bundle  # noqa: F401
+from .Sampler import Sampler  # noqa: F401

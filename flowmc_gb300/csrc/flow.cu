@@ -1,0 +1,386 @@
+// flow.cu -- MaskedCouplingRQSpline inference: layout, forward, inverse,
+// log_prob and sample entry points (K3/K4).
+//
+// Per layer l (rqSpline.py:450-488, common.py:127-168, 211-240):
+//   k_affine        ScalarAffine (x + t) e^s (or its inverse) and the gather of
+//                   the conditioning coordinates into a dense [n, n_c] block
+//   conditioner     Linear+tanh ... Linear on the packed weights
+//                   (FP32: SIMT GEMMs with fused bias/tanh epilogues;
+//                    BF16: tcgen05 GEMMs, gemm_tc.cu)
+//   k_spline        RQ spline (or inverse) of the transformed coordinates,
+//                   log-determinants summed per row
+// Rows are processed in chunks sized to keep the conditioner outputs
+// (n_t * (3K+1) floats per row) within a bounded workspace.
+#include "flow.cuh"
+#include "gemm_simt.cuh"
+#include "gemm_tc.cuh"
+
+namespace fmc {
+
+int make_geom(const FmcFlow* f, FlowGeom& g) {
+  FMC_CHECK_ARG(f != nullptr, "flow is NULL");
+  FMC_CHECK_ARG(f->n_dim >= 2 && f->n_dim <= 4096, "flow n_dim=%d outside [2, 4096]", f->n_dim);
+  FMC_CHECK_ARG(f->n_layers >= 1 && f->n_layers <= FMC_MAX_LAYERS, "n_layers=%d outside [1, %d]", f->n_layers,
+                FMC_MAX_LAYERS);
+  FMC_CHECK_ARG(f->n_hidden >= 1 && f->n_hidden <= FMC_MAX_HIDDEN, "n_hidden=%d outside [1, %d]", f->n_hidden,
+                FMC_MAX_HIDDEN);
+  FMC_CHECK_ARG(f->n_bins >= 2 && f->n_bins <= 16, "n_bins=%d outside [2, 16]", f->n_bins);
+  FMC_CHECK_ARG(f->range_max > f->range_min, "empty spline range");
+  FMC_CHECK_ARG(f->min_bin_size > 0.f && f->min_bin_size * f->n_bins < f->range_max - f->range_min,
+                "min_bin_size incompatible with the range");
+  g.d = f->n_dim;
+  g.L = f->n_layers;
+  g.nh = f->n_hidden;
+  g.K = f->n_bins;
+  g.P = 3 * f->n_bins + 1;
+  for (int i = 0; i < FMC_MAX_HIDDEN; ++i) g.H[i] = i < g.nh ? f->hidden[i] : 0;
+  for (int i = 0; i < g.nh; ++i) FMC_CHECK_ARG(g.H[i] >= 1 && g.H[i] <= 8192, "hidden[%d]=%d invalid", i, g.H[i]);
+  g.cfg.rmin = f->range_min;
+  g.cfg.rmax = f->range_max;
+  g.cfg.min_bin = f->min_bin_size;
+  g.cfg.min_slope = f->min_knot_slope;
+  // rqSpline.py:37-38, in float32 as the reference's parameter dtype
+  g.cfg.slope_offset = logf(expf(1.0f - f->min_knot_slope) - 1.0f);
+  int64_t off = 0;
+  for (int l = 0; l < g.L; ++l) {
+    g.layer_off[l] = off;
+    off += g.lin_b(l, g.nh) + g.lin_out(l, g.nh);
+  }
+  g.layer_off[g.L] = off;
+  g.n_params = off;
+  return FMC_OK;
+}
+
+// ------------------------------------------------------------------ kernels
+__global__ void k_standardize(const float* __restrict__ x, int64_t n, int d, const float* __restrict__ aux,
+                              float* __restrict__ out) {
+  const int64_t tot = n * d;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
+    const int j = (int)(i % d);
+    out[i] = (x[i] - aux[j]) / sqrtf(aux[d + j]);
+  }
+}
+
+__global__ void k_destandardize(float* __restrict__ x, int64_t n, int d, const float* __restrict__ aux) {
+  const int64_t tot = n * d;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
+    const int j = (int)(i % d);
+    x[i] = x[i] * sqrtf(aux[d + j]) + aux[j];
+  }
+}
+
+__global__ void k_affine(const float* __restrict__ in, float* __restrict__ out, float* __restrict__ cond, int64_t n,
+                         int d, int nc, int cpar, const float* __restrict__ th_layer, int inverse,
+                         float* __restrict__ ld, int ld_init) {
+  const float s = th_layer[0], t = th_layer[1];
+  const float es = expf(inverse ? -s : s);
+  const int64_t tot = n * d;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / d;
+    const int j = (int)(i - r * d);
+    const float v = inverse ? in[i] * es - t : (in[i] + t) * es;   // common.py:229, 238
+    out[i] = v;
+    if (cond != nullptr && ((j & 1) == cpar)) cond[r * nc + (j >> 1)] = v;
+    if (ld != nullptr && j == 0) {
+      const float l = (float)d * (inverse ? -s : s);
+      ld[r] = ld_init ? l : ld[r] + l;
+    }
+  }
+}
+
+__global__ void k_base_logprob(const float* __restrict__ y, const float* __restrict__ ld, int64_t n, int d,
+                               const float* __restrict__ aux, float* __restrict__ logp) {
+  const int lane = threadIdx.x & 31;
+  const float c = aux[2 * d];
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < n; r += warps) {
+    float s = 0.f;
+    for (int j = lane; j < d; j += 32) {
+      const float v = y[r * d + j];
+      s += v * v;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+      // multivariate_normal.logpdf(y, 0, c I) (common.py:285-286)
+      logp[r] = ld[r] + (-0.5f * s / c - 0.5f * (float)d * logf(6.283185307179586f * c));
+    }
+  }
+}
+
+__global__ void k_base_sample(const float* __restrict__ z, Rng rng, int64_t n, int d, const float* __restrict__ aux,
+                              float* __restrict__ out) {
+  // jax.random.multivariate_normal(0, c I): mean + z @ cholesky(c I).T = sqrt(c) z
+  const float sc = sqrtf(aux[2 * d]);
+  const int64_t tot = n * d;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
+    float v;
+    if (z) {
+      v = z[i];
+    } else {
+      const int64_t r = i / d;
+      const int j = (int)(i - r * d);
+      const u32x4 b = rng.draw((uint64_t)r, 0, (uint32_t)(j >> 1), RNG_TAG_NF_NORMAL);
+      float z0, z1;
+      box_muller(b.x, b.y, z0, z1);
+      v = (j & 1) ? z1 : z0;
+    }
+    out[i] = v * sc;
+  }
+}
+
+static int ew_grid(int64_t tot) {
+  int64_t b = (tot + 255) / 256;
+  const int64_t cap = (int64_t)sm_count() * 32;
+  if (b > cap) b = cap;
+  return (int)(b < 1 ? 1 : b);
+}
+
+static int rows_grid(int64_t m) {
+  int64_t b = (m + 7) / 8;
+  const int64_t cap = (int64_t)sm_count() * 16;
+  if (b > cap) b = cap;
+  return (int)(b < 1 ? 1 : b);
+}
+
+// ------------------------------------------------------------------ workspace
+struct InferWs {
+  int64_t rows;   // chunk rows
+  float *xa, *cond, *h0, *h1, *raw, *ld;
+  uint16_t *cond16, *h16a, *h16b;  // BF16 operands
+};
+
+static int64_t align_up(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
+
+static int64_t infer_chunk_rows(const FlowGeom& g, int64_t n) {
+  const int64_t per_row = (int64_t)g.nt_max() * g.P + 2 * g.h_max() + g.nc_max() + g.d + 1;
+  int64_t rows = (int64_t)(512ll << 20) / (4 * per_row);   // ~512 MB of chunk buffers
+  rows = rows / 128 * 128;
+  if (rows < 128) rows = 128;
+  if (rows > 262144) rows = 262144;
+  if (n < rows) rows = align_up(n > 0 ? n : 1, 128);
+  return rows;
+}
+
+static size_t infer_ws_bytes(const FlowGeom& g, int64_t rows) {
+  const int64_t f = rows * ((int64_t)g.d + g.nc_max() + 2 * g.h_max() + (int64_t)g.nt_max() * g.P + 1);
+  const int64_t b16 = rows * (align_up(g.nc_max(), 64) + 2 * align_up(g.h_max(), 64));
+  return (size_t)(4 * f + 2 * b16 + 16 * 256);
+}
+
+static void carve_infer(const FlowGeom& g, int64_t rows, void* ws, InferWs& w) {
+  char* p = (char*)ws;
+  auto take = [&](int64_t bytes) {
+    char* r = p;
+    p += align_up(bytes, 256);
+    return r;
+  };
+  w.rows = rows;
+  w.xa = (float*)take(4 * rows * g.d);
+  w.cond = (float*)take(4 * rows * g.nc_max());
+  w.h0 = (float*)take(4 * rows * g.h_max());
+  w.h1 = (float*)take(4 * rows * g.h_max());
+  w.raw = (float*)take(4 * rows * (int64_t)g.nt_max() * g.P);
+  w.ld = (float*)take(4 * rows);
+  w.cond16 = (uint16_t*)take(2 * rows * align_up(g.nc_max(), 64));
+  w.h16a = (uint16_t*)take(2 * rows * align_up(g.h_max(), 64));
+  w.h16b = (uint16_t*)take(2 * rows * align_up(g.h_max(), 64));
+}
+
+// conditioner MLP of layer l on rows [0, m): cond (w.cond) -> raw (w.raw)
+static int conditioner(const FmcFlow* f, const FlowGeom& g, int l, int64_t m, InferWs& w, cudaStream_t st) {
+  const float* th = f->theta + g.layer_off[l];
+  if (f->precision == FMC_PREC_BF16) {
+    return conditioner_bf16(f, g, l, m, w.cond, w.cond16, w.h16a, w.h16b, w.raw, st);
+  }
+  const float* a = w.cond;
+  int in = g.nc(l);
+  float* bufs[2] = {w.h0, w.h1};
+  for (int i = 0; i <= g.nh; ++i) {
+    const int out = g.lin_out(l, i);
+    const float* W = th + g.lin_w(l, i);
+    const float* b = th + g.lin_b(l, i);
+    float* c = (i == g.nh) ? w.raw : bufs[i & 1];
+    int rc = (i == g.nh) ? sgemm<true, true, EPI_BIAS>(st, m, out, in, a, in, W, in, b, nullptr, 0, c, out, 0.f)
+                         : sgemm<true, true, EPI_BIAS_TANH>(st, m, out, in, a, in, W, in, b, nullptr, 0, c, out, 0.f);
+    if (rc) return rc;
+    a = c;
+    in = out;
+  }
+  return FMC_OK;
+}
+
+// one pass over all layers for rows x[0, m) -> y, ld (forward or inverse)
+static int flow_pass(const FmcFlow* f, const FlowGeom& g, const float* x, float* y, float* ld, int64_t m, bool inverse,
+                     InferWs& w, cudaStream_t st) {
+  const int grid = ew_grid(m * g.d);
+  for (int u = 0; u < g.L; ++u) {
+    const int l = inverse ? g.L - 1 - u : u;
+    const float* src = (u == 0) ? x : y;
+    k_affine<<<grid, 256, 0, st>>>(src, y, w.cond, m, g.d, g.nc(l), g.cpar(l), f->theta + g.layer_off[l],
+                                   inverse ? 1 : 0, ld, u == 0 ? 1 : 0);
+    FMC_LAUNCH_CHECK();
+    int rc = conditioner(f, g, l, m, w, st);
+    if (rc) return rc;
+    rc = launch_spline(g.K, inverse, st, w.raw, y, ld, m, g.d, g.nt(l), g.tpar(l), g.cfg);
+    if (rc) return rc;
+  }
+  return FMC_OK;
+}
+
+static int check_ws(const FlowGeom& g, int64_t n, void* ws, size_t ws_bytes, int64_t& rows) {
+  rows = infer_chunk_rows(g, n);
+  const size_t need = infer_ws_bytes(g, rows);
+  FMC_CHECK_ARG(ws != nullptr && ws_bytes >= need, "workspace of %zu bytes < %zu needed", ws_bytes, need);
+  FMC_CHECK_ARG(((uintptr_t)ws & 255) == 0, "workspace must be 256-byte aligned");
+  return FMC_OK;
+}
+
+static int check_flow_ptrs(const FmcFlow* f) {
+  FMC_CHECK_ARG(f->theta != nullptr && f->aux != nullptr, "flow theta/aux is NULL");
+  FMC_CHECK_ARG(f->precision == FMC_PREC_FP32 || f->precision == FMC_PREC_BF16, "unknown precision %d", f->precision);
+  if (f->precision == FMC_PREC_BF16) FMC_CHECK_ARG(f->theta_bf16 != nullptr, "BF16 mode needs theta_bf16");
+  return FMC_OK;
+}
+
+// forward/inverse/log_prob driver over row chunks
+enum PassKind { PASS_FORWARD, PASS_INVERSE, PASS_LOGPROB };
+
+int flow_apply(const FmcFlow* f, const float* x, int64_t n, float* out, float* out_ld, PassKind kind, void* ws,
+               size_t ws_bytes, cudaStream_t st) {
+  FlowGeom g;
+  int rc = make_geom(f, g);
+  if (rc) return rc;
+  if ((rc = check_flow_ptrs(f))) return rc;
+  FMC_CHECK_ARG(n >= 0, "n < 0");
+  if (n == 0) return FMC_OK;
+  FMC_CHECK_ARG(x != nullptr && out != nullptr, "NULL array");
+  int64_t rows;
+  if ((rc = check_ws(g, n, ws, ws_bytes, rows))) return rc;
+  InferWs w;
+  carve_infer(g, rows, ws, w);
+  for (int64_t r0 = 0; r0 < n; r0 += rows) {
+    const int64_t m = (n - r0 < rows) ? n - r0 : rows;
+    const float* xc = x + r0 * g.d;
+    if (kind == PASS_LOGPROB) {
+      k_standardize<<<ew_grid(m * g.d), 256, 0, st>>>(xc, m, g.d, f->aux, w.xa);
+      FMC_LAUNCH_CHECK();
+      if ((rc = flow_pass(f, g, w.xa, w.xa, w.ld, m, false, w, st))) return rc;
+      k_base_logprob<<<rows_grid(m), 256, 0, st>>>(w.xa, w.ld, m, g.d, f->aux, out + r0);
+      FMC_LAUNCH_CHECK();
+    } else {
+      float* yc = out + r0 * g.d;
+      float* ldc = out_ld ? out_ld + r0 : w.ld;
+      if ((rc = flow_pass(f, g, xc, yc, ldc, m, kind == PASS_INVERSE, w, st))) return rc;
+    }
+  }
+  return FMC_OK;
+}
+
+int flow_sample(const FmcFlow* f, uint64_t seed, uint64_t counter, const float* z, int64_t n, float* x, void* ws,
+                size_t ws_bytes, cudaStream_t st) {
+  FlowGeom g;
+  int rc = make_geom(f, g);
+  if (rc) return rc;
+  if ((rc = check_flow_ptrs(f))) return rc;
+  FMC_CHECK_ARG(n >= 0, "n < 0");
+  if (n == 0) return FMC_OK;
+  FMC_CHECK_ARG(x != nullptr, "NULL output");
+  int64_t rows;
+  if ((rc = check_ws(g, n, ws, ws_bytes, rows))) return rc;
+  InferWs w;
+  carve_infer(g, rows, ws, w);
+  const Rng rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter};
+  k_base_sample<<<ew_grid(n * g.d), 256, 0, st>>>(z, rng, n, g.d, f->aux, x);
+  FMC_LAUNCH_CHECK();
+  for (int64_t r0 = 0; r0 < n; r0 += rows) {
+    const int64_t m = (n - r0 < rows) ? n - r0 : rows;
+    float* xc = x + r0 * g.d;
+    if ((rc = flow_pass(f, g, xc, xc, w.ld, m, true, w, st))) return rc;
+  }
+  k_destandardize<<<ew_grid(n * g.d), 256, 0, st>>>(x, n, g.d, f->aux);
+  FMC_LAUNCH_CHECK();
+  return FMC_OK;
+}
+
+int flow_apply_logprob(const FmcFlow* f, const float* x, int64_t n, float* logp, void* ws, size_t ws_bytes,
+                       cudaStream_t st) {
+  return flow_apply(f, x, n, logp, nullptr, PASS_LOGPROB, ws, ws_bytes, st);
+}
+
+int flow_sample_rows(const FmcFlow* f, uint64_t seed, uint64_t counter, const float* z, int64_t n, float* x, void* ws,
+                     size_t ws_bytes, cudaStream_t st) {
+  return flow_sample(f, seed, counter, z, n, x, ws, ws_bytes, st);
+}
+
+size_t flow_infer_ws_bytes(const FmcFlow* f, int64_t n) {
+  FlowGeom g;
+  if (make_geom(f, g) != FMC_OK) return 0;
+  return infer_ws_bytes(g, infer_chunk_rows(g, n));
+}
+
+__global__ void k_f32_to_bf16(const float* __restrict__ a, uint16_t* __restrict__ b, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = f32_to_bf16_rn(a[i]);
+}
+
+}  // namespace fmc
+
+using namespace fmc;
+
+extern "C" int fmc_flow_layout(const FmcFlow* flow, int64_t* n_params, int64_t* layer_offsets) {
+  FlowGeom g;
+  int rc = make_geom(flow, g);
+  if (rc) return rc;
+  if (n_params) *n_params = g.n_params;
+  if (layer_offsets)
+    for (int l = 0; l <= g.L; ++l) layer_offsets[l] = g.layer_off[l];
+  return FMC_OK;
+}
+
+extern "C" int fmc_flow_workspace_size(const FmcFlow* flow, int64_t n, int32_t mode, size_t* bytes) {
+  FlowGeom g;
+  int rc = make_geom(flow, g);
+  if (rc) return rc;
+  FMC_CHECK_ARG(bytes != nullptr, "bytes is NULL");
+  FMC_CHECK_ARG(n >= 0, "n < 0");
+  if (mode == 0) {
+    *bytes = infer_ws_bytes(g, infer_chunk_rows(g, n));
+  } else if (mode == 1) {
+    *bytes = train_ws_bytes(g, n);
+  } else {
+    set_error("unknown workspace mode %d", mode);
+    return FMC_ERR_INVALID_ARG;
+  }
+  return FMC_OK;
+}
+
+extern "C" int fmc_flow_sync_bf16(const FmcFlow* flow, void* stream) {
+  FlowGeom g;
+  int rc = make_geom(flow, g);
+  if (rc) return rc;
+  FMC_CHECK_ARG(flow->theta && flow->theta_bf16, "theta/theta_bf16 NULL");
+  k_f32_to_bf16<<<ew_grid(g.n_params), 256, 0, (cudaStream_t)stream>>>(flow->theta, flow->theta_bf16, g.n_params);
+  FMC_LAUNCH_CHECK();
+  return FMC_OK;
+}
+
+extern "C" int fmc_flow_forward(const FmcFlow* flow, const float* x, int64_t n, float* y, float* logdet, void* ws,
+                                size_t ws_bytes, void* stream) {
+  return flow_apply(flow, x, n, y, logdet, PASS_FORWARD, ws, ws_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int fmc_flow_inverse(const FmcFlow* flow, const float* z, int64_t n, float* x, float* logdet, void* ws,
+                                size_t ws_bytes, void* stream) {
+  return flow_apply(flow, z, n, x, logdet, PASS_INVERSE, ws, ws_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int fmc_flow_log_prob(const FmcFlow* flow, const float* x, int64_t n, float* logp, void* ws,
+                                 size_t ws_bytes, void* stream) {
+  return flow_apply(flow, x, n, logp, nullptr, PASS_LOGPROB, ws, ws_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int fmc_flow_sample(const FmcFlow* flow, uint64_t seed, uint64_t counter, const float* z, int64_t n,
+                               float* x, void* ws, size_t ws_bytes, void* stream) {
+  return flow_sample(flow, seed, counter, z, n, x, ws, ws_bytes, (cudaStream_t)stream);
+}

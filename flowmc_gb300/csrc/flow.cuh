@@ -1,0 +1,59 @@
+// flow.cuh -- geometry of the packed MaskedCouplingRQSpline parameters and the
+// per-layer building blocks shared by the inference and training paths.
+#pragma once
+#include "common.cuh"
+#include "spline.cuh"
+
+namespace fmc {
+
+struct FlowGeom {
+  int d, L, nh, K, P;
+  int H[FMC_MAX_HIDDEN];
+  SplineCfg cfg;
+  int64_t n_params;
+  int64_t layer_off[FMC_MAX_LAYERS + 1];
+
+  // conditioning coordinates of layer l: j = 2k + cpar(l); transformed: j = 2k + tpar(l)
+  __host__ __device__ int cpar(int l) const { return 1 - (l & 1); }
+  __host__ __device__ int tpar(int l) const { return l & 1; }
+  __host__ __device__ int nc(int l) const { return (d - cpar(l) + 1) / 2; }
+  __host__ __device__ int nt(int l) const { return d - nc(l); }
+  int nc_max() const { return nc(0) > nc(1) ? nc(0) : nc(1); }
+  int nt_max() const { return nt(0) > nt(1) ? nt(0) : nt(1); }
+  int h_max() const {
+    int m = 0;
+    for (int i = 0; i < nh; ++i) m = H[i] > m ? H[i] : m;
+    return m;
+  }
+  // linear layer i of layer l: in/out sizes and offsets (relative to layer_off[l])
+  int lin_in(int l, int i) const { return i == 0 ? nc(l) : H[i - 1]; }
+  int lin_out(int l, int i) const { return i == nh ? nt(l) * P : H[i]; }
+  int64_t lin_w(int l, int i) const {
+    int64_t o = 2;
+    for (int u = 0; u < i; ++u) o += (int64_t)lin_out(l, u) * lin_in(l, u) + lin_out(l, u);
+    return o;
+  }
+  int64_t lin_b(int l, int i) const { return lin_w(l, i) + (int64_t)lin_out(l, i) * lin_in(l, i); }
+};
+
+int make_geom(const FmcFlow* f, FlowGeom& g);
+
+// --------------------------------------------------------------- kernels
+__global__ void k_standardize(const float* __restrict__ x, int64_t n, int d, const float* __restrict__ aux,
+                              float* __restrict__ out);
+__global__ void k_destandardize(float* __restrict__ x, int64_t n, int d, const float* __restrict__ aux);
+__global__ void k_affine(const float* __restrict__ in, float* __restrict__ out, float* __restrict__ cond,
+                         int64_t n, int d, int nc, int cpar, const float* __restrict__ th_layer, int inverse,
+                         float* __restrict__ ld, int ld_init);
+__global__ void k_base_logprob(const float* __restrict__ y, const float* __restrict__ ld, int64_t n, int d,
+                               const float* __restrict__ aux, float* __restrict__ logp);
+__global__ void k_base_sample(const float* __restrict__ z, Rng rng, int64_t n, int d,
+                              const float* __restrict__ aux, float* __restrict__ out);
+
+// spline kernels, one warp per row; instantiated for the supported bin counts
+int launch_spline(int K, bool inverse, cudaStream_t st, const float* raw, float* xa, float* ld, int64_t n, int d,
+                  int nt, int tpar, SplineCfg cfg);
+int launch_spline_bwd(int K, cudaStream_t st, const float* raw, const float* xa, const float* gy, float gld,
+                      float* graw, float* gxa, int64_t n, int d, int nt, int tpar, int cpar, SplineCfg cfg);
+
+}  // namespace fmc

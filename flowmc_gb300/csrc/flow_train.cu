@@ -1,0 +1,291 @@
+// flow_train.cu -- K6: loss and hand-written gradient of MaskedCouplingRQSpline
+// maximum-likelihood training (NFModel.loss_fn / train_step,
+// nf_model/base.py:98-125).
+//
+// Forward: the standardised batch runs through the layers; only each layer's
+// INPUT is kept ([L+1, n, d] floats). Backward, layer by layer in reverse:
+// the ScalarAffine output, the conditioning block and the conditioner's tanh
+// activations and outputs are recomputed from the saved input, then
+//   spline adjoint (spline.cuh)        -> d raw params, d x (transformed)
+//   conditioner adjoint (GEMMs)        -> d W, d b, d cond
+//   ScalarAffine adjoint               -> d x (layer input), d scale, d shift
+// All reductions (bias columns, scale/shift, loss) are two-stage with a fixed
+// order, so gradients are bitwise reproducible.
+#include "flow.cuh"
+#include "gemm_simt.cuh"
+#include "gemm_tc.cuh"
+
+namespace fmc {
+
+static int64_t a256(int64_t v) { return (v + 255) / 256 * 256; }
+
+struct TrainWs {
+  float *xs, *xa, *cond, *hs, *raw, *graw, *gh0, *gh1, *gcond, *gy, *gxa, *ld, *logp, *part;
+  int64_t part_floats;
+};
+
+static int colsum_blocks(int64_t n) {
+  int64_t rb = (n + 511) / 512;
+  if (rb > 128) rb = 128;
+  return (int)(rb < 1 ? 1 : rb);
+}
+
+static void carve_train(const FlowGeom& g, int64_t n, void* ws, TrainWs& w, size_t* total) {
+  char* p = (char*)ws;
+  int64_t used = 0;
+  auto take = [&](int64_t floats) {
+    float* r = (float*)(p + used);
+    used += a256(4 * floats);
+    return r;
+  };
+  const int64_t ntP = (int64_t)g.nt_max() * g.P;
+  w.xs = take((int64_t)(g.L + 1) * n * g.d);
+  w.xa = take(n * g.d);
+  w.cond = take(n * g.nc_max());
+  w.hs = take((int64_t)g.nh * n * g.h_max());
+  w.raw = take(n * ntP);
+  w.graw = take(n * ntP);
+  w.gh0 = take(n * g.h_max());
+  w.gh1 = take(n * g.h_max());
+  w.gcond = take(n * g.nc_max());
+  w.gy = take(n * g.d);
+  w.gxa = take(n * g.d);
+  w.ld = take(n);
+  w.logp = take(n);
+  int64_t m = ntP > g.h_max() ? ntP : g.h_max();
+  if (m < 4096) m = 4096;
+  w.part_floats = (int64_t)colsum_blocks(n) * m;
+  w.part = take(w.part_floats);
+  if (total) *total = (size_t)used;
+}
+
+size_t train_ws_bytes(const FlowGeom& g, int64_t n) {
+  TrainWs w;
+  size_t tot = 0;
+  carve_train(g, n, nullptr, w, &tot);
+  return tot;
+}
+
+// ------------------------------------------------------------------ kernels
+__global__ void k_colsum_partial(const float* __restrict__ gm, int64_t n, int m, int64_t rows_per,
+                                 float* __restrict__ part) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m) return;
+  const int64_t r0 = blockIdx.y * rows_per;
+  int64_t r1 = r0 + rows_per;
+  if (r1 > n) r1 = n;
+  float s = 0.f;
+  for (int64_t r = r0; r < r1; ++r) s += gm[r * m + j];
+  part[(int64_t)blockIdx.y * m + j] = s;
+}
+
+__global__ void k_colsum_final(const float* __restrict__ part, int rb, int m, float* __restrict__ out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m) return;
+  float s = 0.f;
+  for (int b = 0; b < rb; ++b) s += part[(int64_t)b * m + j];
+  out[j] = s;
+}
+
+static int colsum(cudaStream_t st, const float* gm, int64_t n, int m, float* part, float* out) {
+  const int rb = colsum_blocks(n);
+  const int64_t rows_per = (n + rb - 1) / rb;
+  dim3 grid((m + 255) / 256, rb);
+  k_colsum_partial<<<grid, 256, 0, st>>>(gm, n, m, rows_per, part);
+  FMC_LAUNCH_CHECK();
+  k_colsum_final<<<(m + 255) / 256, 256, 0, st>>>(part, rb, m, out);
+  FMC_LAUNCH_CHECK();
+  return FMC_OK;
+}
+
+template <int NT>
+__device__ __forceinline__ float block_sum(float v, float* sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  float r = 0.f;
+  if (threadIdx.x < 32) {
+    r = (lane < NT / 32) ? sh[lane] : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+  }
+  return r;  // valid in thread 0
+}
+
+// loss = -mean(logp): one block, fixed order
+__global__ void __launch_bounds__(1024) k_loss(const float* __restrict__ logp, int64_t n, float* __restrict__ loss) {
+  __shared__ float sh[32];
+  float s = 0.f;
+  for (int64_t i = threadIdx.x; i < n; i += 1024) s += logp[i];
+  s = block_sum<1024>(s, sh);
+  if (threadIdx.x == 0) *loss = -s / (float)n;
+}
+
+// gradient of the loss at the flow output: d/dy (-logN(y; 0, cI))/n = y / (c n)
+__global__ void k_init_gy(const float* __restrict__ y, int64_t tot, int d, const float* __restrict__ aux, float inv_n,
+                          float* __restrict__ gy) {
+  const float c = aux[2 * d];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x)
+    gy[i] = y[i] / c * inv_n;
+}
+
+// adjoint of xa = (x + t) e^s and of the conditioning gather;
+// writes d x and per-block partial sums of d t and (sum gxa * xa)
+__global__ void __launch_bounds__(256) k_affine_bwd(const float* __restrict__ gxa, const float* __restrict__ gcond,
+                                                    const float* __restrict__ xa, int64_t n, int d, int nc, int cpar,
+                                                    const float* __restrict__ th_layer, float* __restrict__ gx,
+                                                    float* __restrict__ part) {
+  __shared__ float sh[32];
+  const float es = expf(th_layer[0]);
+  const int64_t tot = n * d;
+  float st = 0.f, ss = 0.f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / d;
+    const int j = (int)(i - r * d);
+    float g = gxa[i];
+    if ((j & 1) == cpar) g += gcond[r * nc + (j >> 1)];
+    const float gv = g * es;
+    gx[i] = gv;
+    st += gv;
+    ss += g * xa[i];
+  }
+  st = block_sum<256>(st, sh);
+  ss = block_sum<256>(ss, sh);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = st;
+    part[2 * blockIdx.x + 1] = ss;
+  }
+}
+
+__global__ void k_affine_param_grad(const float* __restrict__ part, int nb, float ld_term, float* __restrict__ g_layer) {
+  if (threadIdx.x != 0) return;
+  float st = 0.f, ss = 0.f;
+  for (int b = 0; b < nb; ++b) {
+    st += part[2 * b];
+    ss += part[2 * b + 1];
+  }
+  g_layer[0] = ss + ld_term;  // d/d scale
+  g_layer[1] = st;            // d/d shift
+}
+
+static int ew_blocks(int64_t tot) {
+  int64_t b = (tot + 255) / 256;
+  const int64_t cap = (int64_t)sm_count() * 8;
+  if (b > cap) b = cap;
+  return (int)(b < 1 ? 1 : b);
+}
+
+// recompute layer l's conditioner on cond: hidden tanh activations into hs, output into raw
+static int recompute_mlp(const FmcFlow* f, const FlowGeom& g, int l, int64_t n, TrainWs& w, cudaStream_t st) {
+  const float* th = f->theta + g.layer_off[l];
+  const float* a = w.cond;
+  int in = g.nc(l);
+  for (int i = 0; i <= g.nh; ++i) {
+    const int out = g.lin_out(l, i);
+    float* c = (i == g.nh) ? w.raw : w.hs + (int64_t)i * n * g.h_max();
+    int rc = (i == g.nh)
+                 ? sgemm<true, true, EPI_BIAS>(st, n, out, in, a, in, th + g.lin_w(l, i), in, th + g.lin_b(l, i), nullptr, 0, c, out, 0.f)
+                 : sgemm<true, true, EPI_BIAS_TANH>(st, n, out, in, a, in, th + g.lin_w(l, i), in, th + g.lin_b(l, i), nullptr, 0, c, out, 0.f);
+    if (rc) return rc;
+    a = c;
+    in = out;
+  }
+  return FMC_OK;
+}
+
+int flow_loss_grad(const FmcFlow* f, const float* x, int64_t n, float* loss, float* grad, void* ws, size_t ws_bytes,
+                   cudaStream_t st) {
+  FlowGeom g;
+  int rc = make_geom(f, g);
+  if (rc) return rc;
+  FMC_CHECK_ARG(f->theta && f->aux, "flow theta/aux is NULL");
+  FMC_CHECK_ARG(n >= 1, "n=%lld < 1", (long long)n);
+  FMC_CHECK_ARG(x && loss && grad, "NULL array");
+  const size_t need = train_ws_bytes(g, n);
+  FMC_CHECK_ARG(ws && ws_bytes >= need, "workspace of %zu bytes < %zu needed", ws_bytes, need);
+  FMC_CHECK_ARG(((uintptr_t)ws & 255) == 0, "workspace must be 256-byte aligned");
+  TrainWs w;
+  carve_train(g, n, ws, w, nullptr);
+  const int d = g.d;
+  const int64_t nd = n * d;
+  const int eb = ew_blocks(nd);
+
+  // ---- forward, saving layer inputs
+  k_standardize<<<eb, 256, 0, st>>>(x, n, d, f->aux, w.xs);
+  FMC_LAUNCH_CHECK();
+  for (int l = 0; l < g.L; ++l) {
+    float* xin = w.xs + (int64_t)l * nd;
+    float* xout = w.xs + (int64_t)(l + 1) * nd;
+    k_affine<<<eb, 256, 0, st>>>(xin, xout, w.cond, n, d, g.nc(l), g.cpar(l), f->theta + g.layer_off[l], 0, w.ld,
+                                 l == 0 ? 1 : 0);
+    FMC_LAUNCH_CHECK();
+    if ((rc = recompute_mlp(f, g, l, n, w, st))) return rc;
+    if ((rc = launch_spline(g.K, false, st, w.raw, xout, w.ld, n, d, g.nt(l), g.tpar(l), g.cfg))) return rc;
+  }
+  const float* y = w.xs + (int64_t)g.L * nd;
+  {
+    int64_t blocks = (n + 7) / 8;
+    if (blocks > (int64_t)sm_count() * 16) blocks = (int64_t)sm_count() * 16;
+    k_base_logprob<<<(int)blocks, 256, 0, st>>>(y, w.ld, n, d, f->aux, w.logp);
+    FMC_LAUNCH_CHECK();
+  }
+  k_loss<<<1, 1024, 0, st>>>(w.logp, n, loss);
+  FMC_LAUNCH_CHECK();
+
+  // ---- backward
+  const float inv_n = 1.0f / (float)n;
+  const float gld = -inv_n;
+  k_init_gy<<<eb, 256, 0, st>>>(y, nd, d, f->aux, inv_n, w.gy);
+  FMC_LAUNCH_CHECK();
+  for (int l = g.L - 1; l >= 0; --l) {
+    const float* th = f->theta + g.layer_off[l];
+    float* gl = grad + g.layer_off[l];
+    const float* xin = w.xs + (int64_t)l * nd;
+    k_affine<<<eb, 256, 0, st>>>(xin, w.xa, w.cond, n, d, g.nc(l), g.cpar(l), th, 0, nullptr, 0);
+    FMC_LAUNCH_CHECK();
+    if ((rc = recompute_mlp(f, g, l, n, w, st))) return rc;
+    if ((rc = launch_spline_bwd(g.K, st, w.raw, w.xa, w.gy, gld, w.graw, w.gxa, n, d, g.nt(l), g.tpar(l), g.cpar(l),
+                                g.cfg)))
+      return rc;
+    // conditioner adjoint
+    const float* gcur = w.graw;
+    float* gbufs[2] = {w.gh0, w.gh1};
+    for (int i = g.nh; i >= 0; --i) {
+      const int out = g.lin_out(l, i), in = g.lin_in(l, i);
+      const float* a_in = (i == 0) ? w.cond : w.hs + (int64_t)(i - 1) * n * g.h_max();
+      // dW = g^T a_in  [out, in]
+      if ((rc = sgemm<false, false, EPI_NONE>(st, out, in, (int)n, gcur, out, a_in, in, nullptr, nullptr, 0,
+                                              gl + g.lin_w(l, i), in, 0.f)))
+        return rc;
+      if ((rc = colsum(st, gcur, n, out, w.part, gl + g.lin_b(l, i)))) return rc;
+      float* gnext = (i == 0) ? w.gcond : gbufs[i & 1];
+      if (i > 0) {
+        if ((rc = sgemm<true, false, EPI_DTANH>(st, n, in, out, gcur, out, th + g.lin_w(l, i), in, nullptr, a_in, in,
+                                                gnext, in, 0.f)))
+          return rc;
+      } else {
+        if ((rc = sgemm<true, false, EPI_NONE>(st, n, in, out, gcur, out, th + g.lin_w(l, i), in, nullptr, nullptr, 0,
+                                               gnext, in, 0.f)))
+          return rc;
+      }
+      gcur = gnext;
+    }
+    // ScalarAffine adjoint -> d(layer input) into gy
+    const int ab = eb < 1024 ? eb : 1024;
+    k_affine_bwd<<<ab, 256, 0, st>>>(w.gxa, w.gcond, w.xa, n, d, g.nc(l), g.cpar(l), th, w.gy, w.part);
+    FMC_LAUNCH_CHECK();
+    k_affine_param_grad<<<1, 32, 0, st>>>(w.part, ab, gld * (float)d * (float)n, gl);
+    FMC_LAUNCH_CHECK();
+  }
+  return FMC_OK;
+}
+
+}  // namespace fmc
+
+extern "C" int fmc_flow_loss_grad(const FmcFlow* flow, const float* x, int64_t n, float* loss, float* grad, void* ws,
+                                  size_t ws_bytes, void* stream) {
+  return fmc::flow_loss_grad(flow, x, n, loss, grad, ws, ws_bytes, (cudaStream_t)stream);
+}

@@ -70,8 +70,10 @@ extern "C" int fmc_local_steps(const FmcTarget* target, const FmcLocalParams* pa
   Shape sh = default_shape(a.d);
   if (params->lanes_per_chain > 0) {
     const int G = params->lanes_per_chain;
+    FMC_CHECK_SUPPORTED(G == 4 || G == 8 || G == 16 || G == 32, "lanes_per_chain=%d not in {4, 8, 16, 32}", G);
     int V = 1;
     while (G * V < a.d) V *= 2;
+    FMC_CHECK_SUPPORTED(V <= 8, "lanes_per_chain=%d too small for n_dim=%d", G, a.d);
     sh = Shape{G, V};
   }
   FMC_CHECK_SUPPORTED(sh.G * sh.V >= a.d, "shape too small for n_dim");

@@ -171,9 +171,11 @@ __global__ void __launch_bounds__(256) k_local_steps(const LocalArgs a) {
         }
         sa = group_sum<G>(sa);
         sb = group_sum<G>(sb);
-        // ratio = (lp1 - lp0) - (|prop - mean0|^2 - |x - mean1|^2) / (2 dt^2)
+        // ratio = (lp1 - lp0) - log q(prop | x) + log q(x | prop)
+        //       = (lp1 - lp0) + (|prop - mean0|^2 - |x - mean1|^2) / (2 dt^2)
+        // (the Gaussian normalisers cancel)
         const ff q = two_sum(sa, -sb);
-        const ff ratio = ff_add(two_sum(lp1, -lp), ff_neg(ff_mul_f(q, 0.5f / dt2)));
+        const ff ratio = ff_add(two_sum(lp1, -lp), ff_mul_f(q, 0.5f / dt2));
         acc = f_lt_ff(logu, ratio);
         if (acc) {
 #pragma unroll
@@ -334,9 +336,10 @@ template <int KIND, int TGT>
 int launch_local_shape(const LocalArgs& a, Shape sh, cudaStream_t st) {
 #define FMC_SHAPE_CASE(g, v) \
   if (sh.G == g && sh.V == v) return launch_local_t<KIND, TGT, g, v>(a, st);
-  FMC_SHAPE_CASE(4, 1) FMC_SHAPE_CASE(8, 1) FMC_SHAPE_CASE(4, 2) FMC_SHAPE_CASE(8, 2)
-  FMC_SHAPE_CASE(32, 1) FMC_SHAPE_CASE(8, 4) FMC_SHAPE_CASE(16, 2) FMC_SHAPE_CASE(32, 2)
-  FMC_SHAPE_CASE(16, 4) FMC_SHAPE_CASE(32, 4) FMC_SHAPE_CASE(16, 8) FMC_SHAPE_CASE(32, 8)
+  FMC_SHAPE_CASE(4, 1) FMC_SHAPE_CASE(4, 2) FMC_SHAPE_CASE(4, 4) FMC_SHAPE_CASE(4, 8)
+  FMC_SHAPE_CASE(8, 1) FMC_SHAPE_CASE(8, 2) FMC_SHAPE_CASE(8, 4) FMC_SHAPE_CASE(8, 8)
+  FMC_SHAPE_CASE(16, 1) FMC_SHAPE_CASE(16, 2) FMC_SHAPE_CASE(16, 4) FMC_SHAPE_CASE(16, 8)
+  FMC_SHAPE_CASE(32, 1) FMC_SHAPE_CASE(32, 2) FMC_SHAPE_CASE(32, 4) FMC_SHAPE_CASE(32, 8)
 #undef FMC_SHAPE_CASE
   set_error("lanes_per_chain=%d with %d coordinates per lane is not instantiated", sh.G, sh.V);
   return FMC_ERR_UNSUPPORTED;

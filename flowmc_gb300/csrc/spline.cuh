@@ -1,0 +1,242 @@
+// spline.cuh -- rational-quadratic spline (forward, inverse, adjoint) for one
+// coordinate, templated on the bin count K.
+//
+// Follows flowMC's rqSpline.py:
+//   knots     _normalize_bin_sizes / _normalize_knot_slopes / get_params  (:20-39, :310-338)
+//   forward   _rational_quadratic_spline_fwd (:42-128)
+//   inverse   _safe_quadratic_root + _rational_quadratic_spline_inv (:131-239)
+// The bin is picked with a one-hot predicate loop over compile-time knot
+// indices (as the reference does), so every array stays in registers.
+// The adjoint is written out by hand: through the spline formula, the
+// selected bin's knots, the cumulative sums, the two softmaxes and the
+// softplus slopes.
+#pragma once
+#include "common.cuh"
+
+namespace fmc {
+
+struct SplineCfg {
+  float rmin, rmax, min_bin, min_slope, slope_offset;
+};
+
+template <int K>
+struct Knots {
+  float xp[K + 1], yp[K + 1], sl[K + 1];
+  float pw[K], ph[K];  // softmax probabilities (kept for the adjoint)
+};
+
+__device__ __forceinline__ float softplus_f(float a) {
+  // jax.nn.softplus = logaddexp(a, 0)
+  return fmaxf(a, 0.f) + log1pf(expf(-fabsf(a)));
+}
+
+template <int K>
+__device__ __forceinline__ void softmax_k(const float* r, float (&p)[K]) {
+  float m = r[0];
+#pragma unroll
+  for (int k = 1; k < K; ++k) m = fmaxf(m, r[k]);
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    p[k] = expf(r[k] - m);
+    s += p[k];
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k) p[k] = p[k] / s;
+}
+
+// raw: the 3K+1 conditioner outputs of one coordinate
+template <int K>
+__device__ __forceinline__ void make_knots(const float* raw, const SplineCfg& c, Knots<K>& kn) {
+  const float R = c.rmax - c.rmin;
+  const float scale = R - (float)K * c.min_bin;
+  softmax_k<K>(raw, kn.pw);
+  softmax_k<K>(raw + K, kn.ph);
+  float cw = 0.f, ch = 0.f;
+  kn.xp[0] = c.rmin;
+  kn.yp[0] = c.rmin;
+#pragma unroll
+  for (int k = 0; k < K - 1; ++k) {
+    cw += kn.pw[k] * scale + c.min_bin;
+    ch += kn.ph[k] * scale + c.min_bin;
+    kn.xp[k + 1] = c.rmin + cw;
+    kn.yp[k + 1] = c.rmin + ch;
+  }
+  kn.xp[K] = c.rmax;
+  kn.yp[K] = c.rmax;
+#pragma unroll
+  for (int k = 0; k <= K; ++k) kn.sl[k] = softplus_f(raw[2 * K + k] + c.slope_offset) + c.min_slope;
+}
+
+struct Bin {
+  float x0, x1, y0, y1, d0, d1;
+  int k;
+};
+
+template <int K>
+__device__ __forceinline__ Bin select_bin(float v, const float (&pos)[K + 1], const Knots<K>& kn) {
+  Bin b{kn.xp[0], kn.xp[1], kn.yp[0], kn.yp[1], kn.sl[0], kn.sl[1], 0};
+#pragma unroll
+  for (int k = 1; k < K; ++k) {
+    if (v >= pos[k] && v < pos[k + 1]) b = Bin{kn.xp[k], kn.xp[k + 1], kn.yp[k], kn.yp[k + 1], kn.sl[k], kn.sl[k + 1], k};
+  }
+  return b;  // bin 0 also covers "no bin" (rqSpline.py:70-72)
+}
+
+template <int K>
+__device__ __forceinline__ void rqs_fwd(float x, const Knots<K>& kn, float& y, float& ld) {
+  const bool below = x <= kn.xp[0];
+  const bool above = x >= kn.xp[K];
+  const Bin b = select_bin<K>(x, kn.xp, kn);
+  const float w = b.x1 - b.x0, h = b.y1 - b.y0;
+  const float s = h / w;
+  float z = (x - b.x0) / w;
+  z = fminf(fmaxf(z, 0.f), 1.f);
+  const float sq = z * z;
+  const float q = z - sq;
+  const float om = 1.f - z;
+  const float sq1 = om * om;
+  const float st = b.d1 + b.d0 - 2.f * s;
+  const float num = h * (s * sq + b.d0 * q);
+  const float den = s + st * q;
+  y = b.y0 + num / den;
+  ld = 2.f * logf(s) + logf(b.d1 * sq + 2.f * s * q + b.d0 * sq1) - 2.f * logf(den);
+  if (below) { y = (x - kn.xp[0]) * kn.sl[0] + kn.yp[0]; ld = logf(kn.sl[0]); }
+  if (above) { y = (x - kn.xp[K]) * kn.sl[K] + kn.yp[K]; ld = logf(kn.sl[K]); }
+}
+
+template <int K>
+__device__ __forceinline__ void rqs_inv(float y, const Knots<K>& kn, float& x, float& ld) {
+  const bool below = y <= kn.yp[0];
+  const bool above = y >= kn.yp[K];
+  const Bin b = select_bin<K>(y, kn.yp, kn);
+  const float w = b.x1 - b.x0, h = b.y1 - b.y0;
+  const float s = h / w;
+  float ww = (y - b.y0) / h;
+  ww = fminf(fmaxf(ww, 0.f), 1.f);
+  const float st = b.d1 + b.d0 - 2.f * s;
+  const float c = -s * ww;
+  const float bb = b.d0 - st * ww;
+  const float a = s - bb;
+  // _safe_quadratic_root (rqSpline.py:131-155)
+  const float disc = bb * bb - 4.f * a * c;
+  float sqd = sqrtf(fmaxf(disc, 1.17549435e-38f));
+  if (!(disc > 0.f)) sqd = 0.f;
+  const float num = (bb >= 0.f) ? 2.f * c : -bb + sqd;
+  const float dnm = (bb >= 0.f) ? -bb - sqd : 2.f * a;
+  float z = num / dnm;
+  z = fminf(fmaxf(z, 0.f), 1.f);
+  x = w * z + b.x0;
+  const float sq = z * z;
+  const float q = z - sq;
+  const float om = 1.f - z;
+  const float sq1 = om * om;
+  const float den = s + st * q;
+  ld = -2.f * logf(s) - logf(b.d1 * sq + 2.f * s * q + b.d0 * sq1) + 2.f * logf(den);
+  if (below) { x = (y - kn.yp[0]) / kn.sl[0] + kn.xp[0]; ld = -logf(kn.sl[0]); }
+  if (above) { x = (y - kn.yp[K]) / kn.sl[K] + kn.xp[K]; ld = -logf(kn.sl[K]); }
+}
+
+// Adjoint of (y, ld) = rqs_fwd(x; raw): given gy = dL/dy and gl = dL/dld,
+// returns dL/dx and accumulates dL/draw[0..3K] into graw.
+template <int K>
+__device__ __forceinline__ float rqs_fwd_adjoint(float x, const float* raw, const SplineCfg& c, const Knots<K>& kn,
+                                                 float gy, float gl, float* graw) {
+  float gX[K + 1], gY[K + 1], gD[K + 1];
+#pragma unroll
+  for (int k = 0; k <= K; ++k) { gX[k] = 0.f; gY[k] = 0.f; gD[k] = 0.f; }
+  float gx = 0.f;
+  const bool below = x <= kn.xp[0];
+  const bool above = x >= kn.xp[K];
+  if (below) {
+    gx = gy * kn.sl[0];
+    gD[0] = gy * (x - kn.xp[0]) + gl / kn.sl[0];
+  } else if (above) {
+    gx = gy * kn.sl[K];
+    gD[K] = gy * (x - kn.xp[K]) + gl / kn.sl[K];
+  } else {
+    const Bin b = select_bin<K>(x, kn.xp, kn);
+    const float w = b.x1 - b.x0, h = b.y1 - b.y0;
+    const float s = h / w;
+    const float zr = (x - b.x0) / w;
+    const float z = fminf(fmaxf(zr, 0.f), 1.f);
+    const float sq = z * z, q = z - sq, om = 1.f - z, sq1 = om * om;
+    const float st = b.d1 + b.d0 - 2.f * s;
+    const float num = h * (s * sq + b.d0 * q);
+    const float den = s + st * q;
+    const float A = b.d1 * sq + 2.f * s * q + b.d0 * sq1;
+    // y = y0 + num/den ; ld = 2 log s + log A - 2 log den
+    const float g_num = gy / den;
+    const float g_den = -gy * num / (den * den) - 2.f * gl / den;
+    const float g_A = gl / A;
+    float g_s = 2.f * gl / s;
+    float g_h = g_num * (s * sq + b.d0 * q);
+    g_s += g_num * h * sq;
+    float g_sq = g_num * h * s;
+    float g_d0 = g_num * h * q;
+    float g_q = g_num * h * b.d0;
+    // den = s + (d1 + d0 - 2 s) q
+    g_s += g_den * (1.f - 2.f * q);
+    float g_d1 = g_den * q;
+    g_d0 += g_den * q;
+    g_q += g_den * st;
+    // A = d1 sq + 2 s q + d0 (1-z)^2
+    g_d1 += g_A * sq;
+    g_sq += g_A * b.d1;
+    g_s += g_A * 2.f * q;
+    g_q += g_A * 2.f * s;
+    g_d0 += g_A * sq1;
+    float g_z = -g_A * b.d0 * 2.f * om;
+    // q = z - z^2, sq = z^2
+    g_z += g_q * (1.f - 2.f * z) + g_sq * 2.f * z;
+    const float g_zr = (zr > 0.f && zr < 1.f) ? g_z : 0.f;
+    // zr = (x - x0)/w ; s = h/w
+    gx = g_zr / w;
+    float g_x0 = -g_zr / w;
+    float g_w = -g_zr * zr / w - g_s * s / w;
+    g_h += g_s / w;
+    // w = x1 - x0, h = y1 - y0
+    const float g_x1 = g_w;
+    g_x0 -= g_w;
+    const float g_y1 = g_h;
+    const float g_y0 = gy - g_h;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      if (k == b.k) {
+        gX[k] += g_x0; gX[k + 1] += g_x1;
+        gY[k] += g_y0; gY[k + 1] += g_y1;
+        gD[k] += g_d0; gD[k + 1] += g_d1;
+      }
+    }
+  }
+  // knots: X_k = rmin + sum_{i<k} w_i for 1 <= k <= K-1 (X_0, X_K constant)
+  const float scale = (c.rmax - c.rmin) - (float)K * c.min_bin;
+  float gpw[K], gph[K];
+  float accx = 0.f, accy = 0.f;
+#pragma unroll
+  for (int i = K - 1; i >= 0; --i) {
+    // g_w[i] = sum_{k=i+1}^{K-1} gX[k]
+    gpw[i] = accx * scale;
+    gph[i] = accy * scale;
+    if (i >= 1) { accx += gX[i]; accy += gY[i]; }
+  }
+  // softmax adjoint
+  float dw = 0.f, dh = 0.f;
+#pragma unroll
+  for (int i = 0; i < K; ++i) { dw += kn.pw[i] * gpw[i]; dh += kn.ph[i] * gph[i]; }
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    graw[i] = kn.pw[i] * (gpw[i] - dw);
+    graw[K + i] = kn.ph[i] * (gph[i] - dh);
+  }
+  // slopes: d_k = softplus(raw + off) + min_slope -> sigmoid
+#pragma unroll
+  for (int k = 0; k <= K; ++k) {
+    const float a = raw[2 * K + k] + c.slope_offset;
+    const float sg = 1.f / (1.f + expf(-a));
+    graw[2 * K + k] = gD[k] * sg;
+  }
+  return gx;
+}
+
+}  // namespace fmc

@@ -73,7 +73,7 @@ typedef struct FmcLocalParams {
   int32_t kind;               /* FMC_KERNEL_*                                    */
   int32_t n_leapfrog;         /* HMC: rows-2 of the leapfrog table (HMC.py:25-27) */
   float step_size;            /* MALA dt, HMC epsilon, GRW sigma                 */
-  int32_t lanes_per_chain;    /* 0 = choose; else 1,2,4,8,16,32 (autotuner)      */
+  int32_t lanes_per_chain;    /* 0 = default for n_dim; else 4, 8, 16 or 32 lanes  */
   const float* momentum_scale;/* HMC: [n_dim] = diag(cholesky(inv(M)))   or NULL = 1 */
   const float* metric_colsum; /* HMC: [n_dim] = sum_i M[i, j]            or NULL = 1 */
 } FmcLocalParams;
@@ -116,6 +116,147 @@ FMC_API int fmc_local_steps(const FmcTarget* target, const FmcLocalParams* param
  *   x [n, n_dim] -> logp [n], grad [n, n_dim] (grad may be NULL). */
 FMC_API int fmc_target_value_grad(const FmcTarget* target, const float* x, int64_t n,
                           float* logp, float* grad, void* stream);
+
+
+/* ---- MaskedCouplingRQSpline flow ------------------------------------- */
+/* Model of resource/model/nf_model/rqSpline.py:364-504. Layer l is
+ *   ScalarAffine(scale_l, shift_l) on all coordinates (common.py:211-240),
+ *   then an RQ-spline coupling whose mask is (j + l) % 2: coordinates with
+ *   (j + l) odd condition the MLP, the others are transformed
+ *   (rqSpline.py:427-440, common.py:127-168).
+ * Parameters live in ONE flat float32 vector `theta`; per layer, in order:
+ *   scale, shift,
+ *   W_0 [H_0, n_c(l)], b_0 [H_0],            (first Linear, conditioning columns only)
+ *   W_i [H_i, H_{i-1}], b_i [H_i]  (i < n_hidden),
+ *   W_o [n_t(l)*P, H_last], b_o [n_t(l)*P]   (last Linear, transformed-dim rows only)
+ * with P = 3*n_bins+1, n_c(l) = #{j < d : (j+l) odd}, n_t(l) = d - n_c(l).
+ * The reference's first-layer columns for transformed coordinates multiply
+ * zeros and its last-layer rows for conditioning coordinates are masked out
+ * (common.py:155-157), so they never influence a result; fmc_flow_layout
+ * gives the packing. `aux` holds the float leaves the reference keeps but
+ * never trains: aux[0:d] data_mean, aux[d:2d] diag(data_cov), aux[2d] the
+ * base Gaussian's covariance scale c (cov = c I), aux[2d+1] the product of
+ * weight-decay factors applied to the unused (packed-out) parameters. */
+enum { FMC_PREC_FP32 = 0, FMC_PREC_BF16 = 1 };
+
+#define FMC_MAX_HIDDEN 4
+#define FMC_MAX_LAYERS 64
+
+typedef struct FmcFlow {
+  int32_t n_dim;
+  int32_t n_layers;
+  int32_t n_hidden;                  /* number of hidden Linear+tanh layers (>= 1) */
+  int32_t n_bins;
+  int32_t hidden[FMC_MAX_HIDDEN];
+  float range_min, range_max;        /* spline range (-10, 10)            */
+  float min_bin_size, min_knot_slope;/* 1e-4, 1e-4 (rqSpline.py:299-300)   */
+  int32_t precision;                 /* FMC_PREC_FP32 or FMC_PREC_BF16      */
+  int32_t reserved;
+  float* theta;                      /* [n_params] float32 master weights   */
+  uint16_t* theta_bf16;              /* [n_params] bf16 shadow (BF16 mode)   */
+  float* aux;                        /* [2*n_dim + 2], see above             */
+} FmcFlow;
+
+/* Number of parameters and per-layer offsets into theta
+ * (layer_offsets[n_layers+1], host array). */
+FMC_API int fmc_flow_layout(const FmcFlow* flow, int64_t* n_params, int64_t* layer_offsets);
+
+/* Bytes of workspace the flow entry points need for n rows (host call).
+ * mode 0: log_prob / forward / inverse / sample;  1: loss + gradient. */
+FMC_API int fmc_flow_workspace_size(const FmcFlow* flow, int64_t n, int32_t mode, size_t* bytes);
+
+/* Refresh theta_bf16 from theta (after loading parameters). */
+FMC_API int fmc_flow_sync_bf16(const FmcFlow* flow, void* stream);
+
+/* MaskedCouplingRQSpline.forward for a batch (rqSpline.py:450-468):
+ * x [n, d] -> y [n, d], logdet [n]. No standardisation. */
+FMC_API int fmc_flow_forward(const FmcFlow* flow, const float* x, int64_t n, float* y, float* logdet,
+                             void* ws, size_t ws_bytes, void* stream);
+
+/* MaskedCouplingRQSpline.inverse (rqSpline.py:470-488), the reference's
+ * in-layer order: ScalarAffine inverse first, then the spline inverse. */
+FMC_API int fmc_flow_inverse(const FmcFlow* flow, const float* z, int64_t n, float* x, float* logdet,
+                             void* ws, size_t ws_bytes, void* stream);
+
+/* MaskedCouplingRQSpline.log_prob (rqSpline.py:498-504):
+ * x [n, d] (data space) -> logp [n]. */
+FMC_API int fmc_flow_log_prob(const FmcFlow* flow, const float* x, int64_t n, float* logp,
+                              void* ws, size_t ws_bytes, void* stream);
+
+/* MaskedCouplingRQSpline.sample (rqSpline.py:490-496): base normals from
+ * Philox(seed, counter) or from z [n, d] when non-NULL -> x [n, d]. */
+FMC_API int fmc_flow_sample(const FmcFlow* flow, uint64_t seed, uint64_t counter, const float* z,
+                            int64_t n, float* x, void* ws, size_t ws_bytes, void* stream);
+
+/* NFModel.loss_fn value and gradient (nf_model/base.py:98-100, 122):
+ * loss = -mean(log_prob(x)) over x [n, d]; grad [n_params] (overwritten)
+ * in theta's layout. Hand-written backward with the coupling activations
+ * recomputed; loss written to *loss (device scalar). */
+FMC_API int fmc_flow_loss_grad(const FmcFlow* flow, const float* x, int64_t n, float* loss, float* grad,
+                               void* ws, size_t ws_bytes, void* stream);
+
+/* ---- NFProposal global step ----------------------------------------------- */
+/* NFProposal.kernel (resource/kernel/NF_proposal.py:27-172) under
+ * TakeGroupSteps (strategy/take_steps.py:191-206) for every chain: n_steps
+ * flow proposals per chain (base normals from Philox or z [n_chains,
+ * n_steps, d]), their flow log_prob (forward pass) and target log-density,
+ * and the sequential independent-MH scan with uniforms from Philox or unif
+ * [n_chains, n_steps], writing thinned rows into the buffers like
+ * fmc_local_steps. x_last/lp_last: the last written row. */
+FMC_API int fmc_nf_workspace_size(const FmcFlow* flow, int32_t n_chains, int32_t n_steps, size_t* bytes);
+FMC_API int fmc_nf_global_steps(const FmcFlow* flow, const FmcTarget* target, const float* x0, int32_t n_chains,
+                                int32_t n_steps, int32_t thinning, uint64_t seed, uint64_t counter,
+                                const float* z, const float* unif, float* out_pos, float* out_logp,
+                                float* out_acc, int64_t buf_len, int64_t cursor, float* x_last, float* lp_last,
+                                void* ws, size_t ws_bytes, void* stream);
+
+/* ---- training (NFModel.train / TrainModel without host syncs) ---------- */
+/* optax.chain(clip_by_global_norm(max_norm), adamw(lr, b1, b2, eps,
+ * weight_decay)) then apply_updates (resource/optimizer.py:19-22,
+ * nf_model/base.py:123-124). Defaults of the reference: b1 = 0.9 (the
+ * Optimizer's momentum), b2 = 0.999, eps = 1e-8, weight_decay = 1e-4,
+ * max_norm = 1. */
+typedef struct FmcAdamParams {
+  float lr, b1, b2, eps, weight_decay, max_norm;
+} FmcAdamParams;
+
+FMC_API int fmc_adamw_workspace_size(size_t* bytes);
+/* One update of theta [n] (and its bf16 shadow when non-NULL) from grad [n]
+ * with moments m, v [n]; *count is optax's step count (device int32,
+ * incremented). aux [n_aux] are float leaves with zero gradient: they get the
+ * weight decay only. */
+FMC_API int fmc_adamw_step(float* theta, uint16_t* theta_bf16, const float* grad, float* m, float* v, int64_t n,
+                           float* aux, int32_t n_aux, int32_t* count, const FmcAdamParams* params, void* ws,
+                           size_t ws_bytes, void* stream);
+
+/* Best-epoch selection (nf_model/base.py:196-200) as device predicates:
+ * *flag = (*a < *best), and *best = *a when true; fmc_copy_if copies
+ * `bytes` from src to dst when *flag != 0. */
+FMC_API int fmc_flag_less(const float* a, float* best, int32_t* flag, void* stream);
+FMC_API int fmc_copy_if(const int32_t* flag, const void* src, void* dst, size_t bytes, void* stream);
+
+/* data_mean and diag(data_cov) of x [n, d] (nf_model/base.py:187-188):
+ * mean [d], unbiased variance [d]. */
+FMC_API int fmc_column_stats(const float* x, int64_t n, int32_t d, float* mean, float* var, void* stream);
+
+/* dst[r] = src[perm(first + r)] for r < m, perm a pseudo-random permutation of
+ * [0, n) keyed by (seed, counter): the epoch shuffle of NFModel.train_epoch
+ * (nf_model/base.py:139-146). */
+FMC_API int fmc_permute_rows(const float* src, int64_t n, int32_t d, uint64_t seed, uint64_t counter, int64_t first,
+                             int64_t m, float* dst, void* stream);
+
+/* TrainModel's data selection (strategy/train_model.py:66-80) from a chain
+ * buffer buf [n_chains, n_steps, d]: rows with all-finite coordinates in
+ * row-major order, reshaped to [n_chains, -1, d], the last history_window
+ * rows of each, then n_out rows drawn with replacement (indices idx [n_out]
+ * when non-NULL, else Philox(seed, counter)) -> out [n_out, d].
+ * *err (device int32) is set to 1 when the finite rows do not split evenly
+ * into n_chains (where the reference's reshape raises). */
+FMC_API int fmc_select_workspace_size(int32_t n_chains, int64_t n_steps, size_t* bytes);
+FMC_API int fmc_select_training_data(const float* buf, int32_t n_chains, int64_t n_steps, int32_t d,
+                                     int32_t history_window, int64_t n_out, uint64_t seed, uint64_t counter,
+                                     const int64_t* idx, float* out, int32_t* err, void* ws, size_t ws_bytes,
+                                     void* stream);
 
 /* ---- library --------------------------------------------------------- */
 FMC_API const char* fmc_last_error(void);

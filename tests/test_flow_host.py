@@ -1,0 +1,50 @@
+"""Host-side flow logic without a GPU: the packed parameter layout agrees
+with libflowmc's fmc_flow_layout, and reference-layout parameters round-trip
+through the packing."""
+import numpy as np
+import pytest
+import torch
+
+from flowmc_gb300 import _lib
+from flowmc_gb300.random import PRNGKey
+from flowmc_gb300.resource.model.nf_model.rqSpline import MaskedCouplingRQSpline
+
+needs_lib = pytest.mark.skipif(not _lib.LIB_PATH.exists(), reason="libflowmc.so not built")
+
+
+@needs_lib
+@pytest.mark.parametrize("d,L,hidden,nb", [(2, 3, [16, 16], 8), (5, 4, [32, 32], 8), (7, 2, [9], 4),
+                                           (128, 12, [512, 512], 12), (33, 5, [8, 8, 8], 3)])
+def test_layout_matches_library(d, L, hidden, nb):
+    m = MaskedCouplingRQSpline(d, L, hidden, nb, PRNGKey(0), device="cpu")
+    m.check_layout()
+
+
+def test_full_roundtrip_and_masks():
+    m = MaskedCouplingRQSpline(5, 3, [6, 7], 4, PRNGKey(3), device="cpu")
+    full = m.to_full()
+    assert full[0]["W"][0].shape == (6, 5) and full[0]["W"][-1].shape == (5 * 13, 7)
+    assert list(full[0]["mask"]) == [False, True, False, True, False]
+    assert list(full[1]["mask"]) == [True, False, True, False, True]
+    rng = np.random.default_rng(0)
+    for Lr in full:
+        Lr["W"] = [rng.normal(size=w.shape).astype(np.float32) for w in Lr["W"]]
+        Lr["b"] = [rng.normal(size=b.shape).astype(np.float32) for b in Lr["b"]]
+        Lr["scale"], Lr["shift"] = 0.25, -0.5
+    m.load_full(full)
+    back = m.to_full()
+    for a, b in zip(full, back):
+        for w1, w2 in zip(a["W"] + a["b"], b["W"] + b["b"]):
+            np.testing.assert_array_equal(w1, w2)
+        assert b["scale"] == 0.25 and b["shift"] == -0.5
+
+
+def test_reference_initialisation_statistics():
+    m = MaskedCouplingRQSpline(64, 2, [256, 256], 8, PRNGKey(1), device="cpu")
+    full = m.to_full()
+    W0 = full[0]["W"][0]
+    assert abs(W0.std() - np.sqrt(1e-2 / 64)) < 0.1 * np.sqrt(1e-2 / 64)   # N(0, scale/in), scale 1e-2
+    Wl = full[0]["W"][-1]
+    assert np.abs(Wl).max() <= 1 / np.sqrt(256) + 1e-7                     # Equinox U(-1/sqrt(in), ..)
+    assert float(m.aux[2 * 64]) == 1.0
+    assert torch.equal(m.data_mean, torch.zeros(64))
