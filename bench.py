@@ -1,0 +1,448 @@
+#!/usr/bin/env python
+"""Benchmark of the fused flowMC sampling path on one GB300 (per rank).
+
+Workload (default ``rosenbrock128``): the RQSpline bundle with an HMC local
+kernel on the 128-D Rosenbrock chain log p = -sum_i [(1-x_i)^2/20 +
+5 (x_{i+1}-x_i^2)^2], 16384 chains, HMC n_leapfrog=16 step 0.01 (identity
+mass), 40 local + 40 global NFProposal steps per loop, MaskedCouplingRQSpline
+12 layers x [512, 512] x 12 bins with BF16 conditioners, AdamW lr 5e-4,
+batch 65536, 5 epochs per training loop, n_max_examples 65536, x0 ~ N(0, I)
+(seed 4). ``mixture64`` is the 64-D 4-mode mixture bundle with MALA.
+
+A step is one loop of the bundle's schedule (local phase + global phase,
+plus flow training in training loops). The schedule has (W+K)//2 training
+loops then the rest production loops; the first W training loops are the
+untimed warm-up, the K timed loops follow. Defaults W=3, K=37 give the
+workload's 20 + 20 loops. value = chain-steps/s = n_chains * (n_local +
+n_global) * K / timed seconds (summed over ranks, which run independent
+replicas). The working set (chain buffers of several GB, flow weights) is
+far larger than L2, so L2 is not flushed between steps.
+
+``--impl reference`` times the CPU restatement of the same loop (the
+reference flowMC itself needs JAX, which this image does not have).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "min-ESS/s & chain-steps/s: fused BF16 vs plain FP32 on 1 GB300 at equal moment error"
+
+WORKLOADS = {
+    "rosenbrock128": dict(d=128, n_chains=16384, local="hmc", step=0.01, n_leapfrog=16, n_local=40, n_global=40,
+                          n_layers=12, hidden=[512, 512], n_bins=12, lr=5e-4, batch=65536, n_epochs=5,
+                          n_max=65536, seed=4),
+    "mixture64": dict(d=64, n_chains=4096, local="mala", step=0.05, n_leapfrog=0, n_local=50, n_global=50,
+                      n_layers=8, hidden=[256, 256], n_bins=8, lr=1e-3, batch=32768, n_epochs=5, n_max=32768,
+                      seed=3),
+}
+
+
+def make_target(name, w, device):
+    import numpy as np
+    from flowmc_gb300 import targets as TG
+    from flowmc_gb300.diagnostics import rosenbrock_chain_moments
+    if name == "rosenbrock128":
+        t = TG.Rosenbrock(w["d"], device=device)
+        mean, var = rosenbrock_chain_moments(w["d"])
+        return t, mean, var
+    rng = np.random.default_rng(3)
+    Q, R = np.linalg.qr(rng.normal(size=(64, 64)))
+    Q = Q * np.sign(np.diag(R))
+    u1, u2 = Q[:, 0], Q[:, 1]
+    means = np.stack([4 * u1, -4 * u1, 4 * u2, -4 * u2])
+    t = TG.GaussianMixture(means, 0.5, device=device)
+    mu, cov = t.mean_cov()
+    return t, mu, np.diag(cov)
+
+
+def useful_flow_flops(w):
+    """Useful conditioner FLOPs per sample per flow pass: the packed GEMMs
+    2(n_c H1 + H1 H2 + H2 n_t P) summed over layers."""
+    d, H, P = w["d"], w["hidden"], 3 * w["n_bins"] + 1
+    tot = 0
+    for l in range(w["n_layers"]):
+        nc = (d - (1 - (l & 1)) + 1) // 2
+        nt = d - nc
+        dims = [nc] + H + [nt * P]
+        tot += sum(2 * a * b for a, b in zip(dims[:-1], dims[1:]))
+    return tot
+
+
+def build_sampler(name, w, n_train, n_prod, precision, device):
+    import torch
+    from flowmc_gb300.random import PRNGKey, split
+    from flowmc_gb300.resource.kernel.HMC import HMC
+    from flowmc_gb300.resource.kernel.MALA import MALA
+    from flowmc_gb300.resource_strategy_bundle.RQSpline_MALA import RQSpline_MALA_Bundle
+    from flowmc_gb300.Sampler import Sampler
+    target, mean, var = make_target(name, w, device)
+    local = HMC(1, w["step"], w["n_leapfrog"]) if w["local"] == "hmc" else MALA(w["step"])
+    key = PRNGKey(w["seed"])
+    key, sub = split(key)
+    bundle = RQSpline_MALA_Bundle(sub, w["n_chains"], w["d"], target, w["n_local"], w["n_global"], n_train, n_prod,
+                                  w["n_epochs"], mala_step_size=w["step"], rq_spline_hidden_units=w["hidden"],
+                                  rq_spline_n_bins=w["n_bins"], rq_spline_n_layers=w["n_layers"],
+                                  learning_rate=w["lr"], batch_size=w["batch"], n_max_examples=w["n_max"],
+                                  local_sampler=local, precision=precision, device=device)
+    sampler = Sampler(w["d"], w["n_chains"], key, resource_strategy_bundles=bundle)
+    g = torch.Generator().manual_seed(w["seed"])
+    x0 = torch.randn(w["n_chains"], w["d"], generator=g)
+    return sampler, bundle, target, mean, var, x0
+
+
+def loop_segments(order, n_train):
+    segs = [order[6 * i:6 * i + 6] for i in range(n_train)]
+    rest = order[6 * n_train:]
+    assert rest[:2] == ["reset_steppers", "update_state"]
+    prod = rest[2:]
+    for i in range(0, len(prod), 4):
+        segs.append((rest[:2] if i == 0 else []) + prod[i:i + 4])
+    return segs
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, ValueError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) >= 9:
+                rows.append(p)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(v):
+            try:
+                return float(v)
+            except ValueError:
+                return float("nan")
+        sm = sorted(num(r[1]) for r in rows)
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": num(rows[0][2]), "samples": len(rows),
+                "power_w_max": max(num(r[3]) for r in rows), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), d.get("bf16_tflops_sustained", 1700.0), "measured"
+    return 6800.0, 1900.0, 1700.0, "fallback"
+
+
+# ---------------------------------------------------------------- CPU baseline
+def cpu_baseline(name, w, budget_s: float = 20.0):
+    """The oracle restatement (float64 NumPy, all host cores through BLAS)
+    timed on a bounded sample of the same loop, scaled to chain-steps/s of
+    the whole workload: one production loop (local + global phase) for a
+    few chains, and one training step on a small batch, extrapolated by
+    rows."""
+    import numpy as np
+    from oracle import flow as OF
+    from oracle import flow_torch as OFT
+    from oracle import kernels as OK
+    from flowmc_gb300.diagnostics import rosenbrock_chain_moments  # noqa: F401  (same package data)
+    rng = np.random.default_rng(0)
+    d = w["d"]
+    if name == "rosenbrock128":
+        t = {"kind": "rosenbrock", "n_dim": d, "a": 20.0, "b": 1.0, "c": 5.0}
+    else:
+        Q, R = np.linalg.qr(rng.normal(size=(64, 64)))
+        means = np.stack([4 * Q[:, 0], -4 * Q[:, 0], 4 * Q[:, 1], -4 * Q[:, 1]])
+        t = {"kind": "mixture", "mean": means, "inv_var": np.full((4, 64), 2.0),
+             "log_w": np.full(4, np.log(0.25) - 32 * np.log(2 * np.pi * 0.5))}
+    P = 3 * w["n_bins"] + 1
+    layers = []
+    for i in range(w["n_layers"]):
+        shape = [d] + w["hidden"] + [d * P]
+        layers.append({"W": [rng.normal(size=(b, a)) * 0.05 / np.sqrt(a) for a, b in zip(shape[:-1], shape[1:])],
+                       "b": [np.zeros(b) for b in shape[1:]], "scale": 0.0, "shift": 0.0,
+                       "mask": ((np.arange(d) + i) % 2).astype(bool)})
+    flow = OF.Flow(layers, w["n_bins"], np.zeros(d), np.eye(d))
+    C = 8
+    x = rng.normal(size=(C, d)) * 0.3 + 0.5
+    S1, S2 = w["n_local"], w["n_global"]
+    t0 = time.perf_counter()
+    OK.take_serial_steps(w["local"], t, x, S1, rng.normal(size=(C, S1, d)), rng.uniform(size=(C, S1)),
+                         step_size=w["step"], n_leapfrog=w["n_leapfrog"], M=np.eye(d))
+    t_local = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    OK.nf_proposal_kernel(flow, t, x, rng.normal(size=(C, S2, d)), rng.uniform(size=(C, S2)))
+    t_global = time.perf_counter() - t0
+    rows = 256
+    t0 = time.perf_counter()
+    OFT.loss_and_grad(flow, rng.normal(size=(rows, d)))
+    t_train_rows = time.perf_counter() - t0
+    n_loops = 40
+    n_train = 20
+    per_chain_loop = (t_local + t_global) / C
+    train_loop = t_train_rows / rows * w["n_epochs"] * w["n_max"]
+    total = n_loops * per_chain_loop * w["n_chains"] + n_train * train_loop
+    value = w["n_chains"] * (S1 + S2) * n_loops / total
+    try:
+        import threadpoolctl
+        cores = max(int(i.get("num_threads", 1)) for i in threadpoolctl.threadpool_info()) or os.cpu_count()
+    except Exception:
+        cores = os.cpu_count()
+    return {"value": value, "unit": "chain-steps/s", "cores": cores, "kind": "port",
+            "sample": (f"oracle float64 NumPy: one loop ({S1} local + {S2} global steps) for {C} chains "
+                       f"({t_local + t_global:.1f}s) and one flow loss+gradient on {rows} rows "
+                       f"({t_train_rows:.1f}s), scaled to {w['n_chains']} chains x 40 loops with 20 training "
+                       f"loops of {w['n_epochs']} x {w['n_max']} rows")}
+
+
+def reference_arm(args, w):
+    v = cpu_baseline(args.workload, w)
+    line = {"impl": "reference", "metric": METRIC, "value": v["value"], "unit": v["unit"], "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, **{k: w[k] for k in ("d", "n_chains", "n_local", "n_global")}},
+            "cpu_baseline": v,
+            "e2e": {"value": v["value"], "unit": v["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- main
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=37)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="fused", choices=["fused", "reference"])
+    ap.add_argument("--workload", default="rosenbrock128", choices=list(WORKLOADS))
+    ap.add_argument("--precision", default="bf16", choices=["bf16", "fp32"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-ess", action="store_true")
+    args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank == 0:
+            reference_arm(args, w)
+        return
+
+    import torch
+    import torch.distributed as dist
+    from flowmc_gb300 import _lib
+    from flowmc_gb300 import diagnostics as D
+    from flowmc_gb300 import profiling
+
+    if world > 1:
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl", rank=rank, world_size=world)
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    W, K = max(1, args.warmup), max(1, args.steps)
+    n_total = W + K
+    n_train = max(W, n_total // 2)
+    n_prod = n_total - n_train
+    precision = "bf16" if args.precision == "bf16" else "float32"
+    sampler, bundle, target, mean_ref, var_ref, x0 = build_sampler(args.workload, w, n_train, n_prod, precision, dev)
+    segs = loop_segments(bundle.strategy_order, n_train)
+    assert len(segs) == n_total
+
+    def run(segments, x, key):
+        for seg in segments:
+            for s in seg:
+                key, sampler.resources, x = sampler.strategies[s](key, sampler.resources, x, {})
+        return x, key
+
+    x = x0.to(dev)
+    key = sampler.rng_key
+    x, key = run(segs[:W], x, key)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    l0 = _lib.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    with profiling.Profiler() as prof:
+        e0.record()
+        x, key = run(segs[W:], x, key)
+        e1.record()
+        torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    launches = _lib.launch_count() - l0
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    secs = ms / 1e3
+    chain_steps = w["n_chains"] * (w["n_local"] + w["n_global"]) * K
+    value = chain_steps * world / secs
+
+    # ---- diagnostics on the production samples
+    pos = sampler.resources["positions_production"].data
+    extra = {}
+    if not args.no_ess:
+        ess = D.ess_bulk(pos)
+        extra["min_ess"] = float(ess.min())
+        extra["min_ess_per_s"] = float(ess.min()) * world / secs
+        extra["moment_error"] = D.moment_error(pos, mean_ref, var_ref)
+    acc_l = sampler.resources["local_accs_production"].data
+    acc_g = sampler.resources["global_accs_production"].data
+    # local rows are the first n_local of each 80-row loop block
+    blk = w["n_local"] + w["n_global"]
+    la = acc_l.reshape(w["n_chains"], -1, blk)[:, :, :w["n_local"]].mean().item()
+    ga = acc_g.reshape(w["n_chains"], -1, blk)[:, :, w["n_local"]:].mean().item()
+    extra["acceptance"] = {"local": la, "global": ga}
+
+    # ---- roofline per phase (device time from CUDA events inside the timed region)
+    hbm, bf16, bf16_s, src = measured_peaks()
+    tot = prof.totals_ms()
+    cnt = prof.counts()
+    kernels = {}
+    ff = useful_flow_flops(w)
+    if "local_steps" in tot:
+        n_cs = prof.units["local_steps"]
+        bytes_ = n_cs * (4 * w["d"] + 8)
+        t_s = tot["local_steps"] / 1e3
+        evals = (w["n_leapfrog"] + 1) if w["local"] == "hmc" else 1
+        flops = n_cs * evals * 15 * w["d"]
+        kernels["local_steps"] = {"ms": tot["local_steps"], "launches": cnt["local_steps"],
+                                  "achieved_gbs": bytes_ / t_s / 1e9, "frac_hbm": bytes_ / t_s / 1e9 / hbm,
+                                  "fp32_tflops": flops / t_s / 1e12,
+                                  "bytes_per_chain_step": 4 * w["d"] + 8}
+    if "nf_global" in tot:
+        props = prof.units["nf_global"]
+        flops = (2 * props + props / w["n_global"]) * ff
+        t_s = tot["nf_global"] / 1e3
+        kernels["nf_global"] = {"ms": tot["nf_global"], "launches": cnt["nf_global"],
+                                "achieved_tflops": flops / t_s / 1e12, "frac_bf16": flops / t_s / 1e12 / bf16,
+                                "useful_flops_per_sample_pass": ff}
+    if "train" in tot:
+        steps = prof.units["train"]
+        flops = steps * w["batch"] * 3 * ff
+        t_s = tot["train"] / 1e3
+        kernels["train"] = {"ms": tot["train"], "launches": cnt["train"], "achieved_tflops": flops / t_s / 1e12,
+                            "frac_bf16": flops / t_s / 1e12 / bf16}
+    dom = max(kernels, key=lambda k: kernels[k]["ms"])
+    dk = kernels[dom]
+    if dom == "local_steps":
+        roof = {"bound": "hbm", "kernel": "k_local_steps", "achieved": dk["achieved_gbs"], "peak": hbm,
+                "unit": "GB/s", "frac": dk["frac_hbm"], "traffic": None, "peak_source": src}
+    else:
+        peak = bf16 if args.precision == "bf16" else None
+        roof = {"bound": "tensor", "kernel": dom, "achieved": dk["achieved_tflops"], "peak": peak or bf16,
+                "unit": "TFLOP/s", "frac": dk["achieved_tflops"] / (peak or bf16), "traffic": None,
+                "peak_source": src if peak else f"{src} bf16 (this run used FP32 SIMT GEMMs)"}
+
+    # ---- end to end through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = end_to_end(sampler, bundle, w, dev, min(K, 4), x)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "chain-steps/s", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16" if args.precision == "bf16" else "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "n_dim": w["d"], "n_chains": w["n_chains"],
+                   "local_kernel": w["local"], "n_local_steps": w["n_local"], "n_global_steps": w["n_global"],
+                   "flow": f"{w['n_layers']}x{w['hidden']}x{w['n_bins']} bins", "n_training_loops": n_train,
+                   "n_production_loops": n_prod, "timed_loops": K, "batch_size": w["batch"],
+                   "n_epochs": w["n_epochs"], "parallelism": f"replicas{world}",
+                   "l2": "working set (chain buffers, flow weights) larger than L2; no flush"},
+        "roofline": roof, "kernels": kernels, "gpu_launches": launches, "clocks": clk,
+        "wall_s": wall, **extra,
+    }
+    if e2e is not None:
+        line["e2e"] = e2e
+    if rank == 0 and not args.no_cpu:
+        try:
+            line["cpu_baseline"] = cpu_baseline(args.workload, w)
+        except Exception as ex:  # the baseline must not sink the GPU line
+            line["cpu_baseline"] = {"value": None, "error": str(ex)[:200]}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def end_to_end(sampler, bundle, w, dev, n_loops, x_dev):
+    """Production loops driven through Sampler.sample with host buffers: each
+    step copies its starting positions host->device (pinned) and reads back
+    the rows it wrote plus the final positions (device->host, pinned)."""
+    import torch
+    prod = ["local_stepper", "update_global_step", "global_stepper", "update_local_step"]
+    sampler.strategy_order = prod
+    C, d = w["n_chains"], w["d"]
+    blk = w["n_local"] + w["n_global"]
+    x_host = torch.empty(C, d, pin_memory=True)
+    x_host.copy_(x_dev)
+    pos_h = torch.empty(C, blk, d, pin_memory=True)
+    lp_h = torch.empty(C, blk, pin_memory=True)
+    res = sampler.resources
+    steppers = [sampler.strategies["local_stepper"], sampler.strategies["global_stepper"]]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(n_loops):
+        for s in steppers:
+            s.set_current_position(0)
+        last = sampler.sample(x_host, {})                 # h2d inside Sampler.sample
+        pos_h.copy_(res["positions_production"].data[:, :blk], non_blocking=True)
+        lp_h.copy_(res["log_prob_production"].data[:, :blk], non_blocking=True)
+        x_host.copy_(last, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+    secs = time.perf_counter() - t0
+    h2d = C * d * 4
+    d2h = C * blk * d * 4 + C * blk * 4 + C * d * 4
+    return {"value": C * blk * n_loops / secs, "unit": "chain-steps/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "loops": n_loops}
+
+
+if __name__ == "__main__":
+    main()

@@ -152,6 +152,7 @@ _SIGNATURES = {
     "fmc_last_error": (ctypes.c_char_p, []),
     "fmc_version": (ctypes.c_int, []),
     "fmc_device_sm_count": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int32)]),
+    "fmc_launch_count": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint64)]),
 }
 
 EXPORTED = tuple(_SIGNATURES)
@@ -236,3 +237,10 @@ class Workspace:
         base = self._buf.data_ptr()
         off = (-base) % 256
         return base + off, self._buf.numel() - off
+
+
+def launch_count() -> int:
+    """Kernels launched by libflowmc so far in this process."""
+    v = ctypes.c_uint64()
+    check(lib().fmc_launch_count(ctypes.byref(v)))
+    return int(v.value)

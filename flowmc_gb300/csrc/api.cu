@@ -1,5 +1,6 @@
 // api.cu -- library plumbing: thread-local error text, version, device info.
 #include <stdarg.h>
+#include <atomic>
 #include "common.cuh"
 
 namespace fmc {
@@ -26,7 +27,16 @@ int sm_count() {
   return cached[dev];
 }
 
+static std::atomic<uint64_t> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
 }  // namespace fmc
+
+extern "C" int fmc_launch_count(uint64_t* out) {
+  FMC_CHECK_ARG(out != nullptr, "out is NULL");
+  *out = fmc::g_launches.load(std::memory_order_relaxed);
+  return FMC_OK;
+}
 
 extern "C" const char* fmc_last_error(void) { return fmc::g_err; }
 

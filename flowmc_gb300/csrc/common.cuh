@@ -47,6 +47,7 @@ void set_error(const char* fmt, ...);
 
 #define FMC_LAUNCH_CHECK()                                                   \
   do {                                                                       \
+    ::fmc::count_launch();                                                   \
     cudaError_t _e = cudaGetLastError();                                     \
     if (_e != cudaSuccess) {                                                 \
       ::fmc::set_error("kernel launch failed: %s (%s:%d)",                  \
@@ -56,6 +57,7 @@ void set_error(const char* fmt, ...);
   } while (0)
 
 int sm_count();  // cached per device
+void count_launch();  // process-wide tally of kernel launches (fmc_launch_count)
 
 // ---------------------------------------------------------------- Philox
 // Philox-4x32 with 10 rounds, constants from the SC'11 paper (Table 2 and

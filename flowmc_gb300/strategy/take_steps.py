@@ -16,6 +16,7 @@ from abc import abstractmethod
 
 import torch
 
+from ..profiling import region
 from ..random import split
 from ..resource.buffers import Buffer
 from ..resource.logPDF import as_target
@@ -87,8 +88,9 @@ class TakeSerialSteps(TakeSteps):
         if not isinstance(kernel, LocalKernel):
             raise TypeError(f"{type(kernel).__name__} is not a local kernel")
         pos, lp, acc = bufs
-        x_last, _ = run_local_steps(kernel, target, initial_position, self.n_steps, self.thinning, seed, 0,
-                                    pos.data, lp.data, acc.data, cursor, noise=noise, uniform=uniform)
+        with region("local_steps", units=initial_position.shape[0] * self.n_steps):
+            x_last, _ = run_local_steps(kernel, target, initial_position, self.n_steps, self.thinning, seed, 0,
+                                        pos.data, lp.data, acc.data, cursor, noise=noise, uniform=uniform)
         return x_last
 
 
@@ -98,5 +100,6 @@ class TakeGroupSteps(TakeSteps):
 
     def sample(self, kernel, seed, initial_position, target, bufs, cursor, data, noise=None, uniform=None):
         pos, lp, acc = bufs
-        return kernel.group_steps(seed, initial_position, target, self.n_steps, self.thinning,
-                                  pos.data, lp.data, acc.data, cursor, noise=noise, uniform=uniform)
+        with region("nf_global", units=initial_position.shape[0] * self.n_steps):
+            return kernel.group_steps(seed, initial_position, target, self.n_steps, self.thinning,
+                                      pos.data, lp.data, acc.data, cursor, noise=noise, uniform=uniform)

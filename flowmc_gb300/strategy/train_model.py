@@ -12,6 +12,7 @@ import ctypes
 import torch
 
 from .. import _lib
+from ..profiling import region
 from ..random import split
 from ..resource.buffers import Buffer
 from ..resource.model.nf_model.base import NFModel
@@ -76,8 +77,10 @@ class TrainModel(Strategy):
             print(f"n_epochs: {self.n_epochs}")
             print(f"batch_size: {self.batch_size}")
         # the key returned by NFModel.train replaces rng_key (train_model.py:369-377)
-        rng_key, model, state, loss_values = model.train(subkey, training_data, optimizer, optimizer.optim_state,
-                                                         self.n_epochs, self.batch_size, verbose=self.verbose)
+        with region("train", units=self.n_epochs * max(1, self.n_max_examples // self.batch_size)):
+            rng_key, model, state, loss_values = model.train(subkey, training_data, optimizer,
+                                                             optimizer.optim_state, self.n_epochs, self.batch_size,
+                                                             verbose=self.verbose)
         if self.loss_buffer_name != "":
             loss_buffer = resources[self.loss_buffer_name]
             assert isinstance(loss_buffer, Buffer), "Loss buffer resource must be a buffer"

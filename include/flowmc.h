@@ -263,6 +263,8 @@ FMC_API const char* fmc_last_error(void);
 FMC_API int fmc_version(void);               /* FMC_ABI_VERSION */
 /* Number of SMs of the current device (host call, synchronous). */
 FMC_API int fmc_device_sm_count(int32_t* out);
+/* Number of kernels this library has launched in the process (host counter). */
+FMC_API int fmc_launch_count(uint64_t* out);
 
 #ifdef __cplusplus
 }
