@@ -113,6 +113,12 @@ _SIGNATURES = {
     "fmc_flow_workspace_size": (ctypes.c_int, [ctypes.POINTER(FmcFlow), ctypes.c_int64, ctypes.c_int32,
                                                ctypes.POINTER(ctypes.c_size_t)]),
     "fmc_flow_sync_bf16": (ctypes.c_int, [ctypes.POINTER(FmcFlow), ctypes.c_void_p]),
+    "fmc_flow_bf16_size": (ctypes.c_int, [ctypes.POINTER(FmcFlow), ctypes.POINTER(ctypes.c_int64)]),
+    "fmc_tc_gemm_bf16": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
+        ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+        ctypes.c_void_p]),
+    "fmc_device_error": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int32), ctypes.c_int32]),
     "fmc_flow_forward": (ctypes.c_int, [ctypes.POINTER(FmcFlow), ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "fmc_flow_inverse": (ctypes.c_int, [ctypes.POINTER(FmcFlow), ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
@@ -243,4 +249,11 @@ def launch_count() -> int:
     """Kernels launched by libflowmc so far in this process."""
     v = ctypes.c_uint64()
     check(lib().fmc_launch_count(ctypes.byref(v)))
+    return int(v.value)
+
+
+def device_error(clear: bool = True) -> int:
+    """Error word of the tensor-core kernels (1 = a bounded wait expired); synchronous."""
+    v = ctypes.c_int32()
+    check(lib().fmc_device_error(ctypes.byref(v), 1 if clear else 0))
     return int(v.value)

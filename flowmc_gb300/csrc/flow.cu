@@ -48,6 +48,14 @@ int make_geom(const FmcFlow* f, FlowGeom& g) {
   }
   g.layer_off[g.L] = off;
   g.n_params = off;
+  int64_t o16 = 0;
+  for (int l = 0; l < g.L; ++l)
+    for (int i = 0; i <= g.nh; ++i) {
+      g.w16_off[l * (g.nh + 1) + i] = o16;
+      o16 += (int64_t)g.w16_rows(l, i) * g.w16_cols(l, i);
+    }
+  g.w16_off[g.L * (g.nh + 1)] = o16;
+  g.n_w16 = o16;
   return FMC_OK;
 }
 
@@ -319,10 +327,6 @@ size_t flow_infer_ws_bytes(const FmcFlow* f, int64_t n) {
   return infer_ws_bytes(g, infer_chunk_rows(g, n));
 }
 
-__global__ void k_f32_to_bf16(const float* __restrict__ a, uint16_t* __restrict__ b, int64_t n) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    b[i] = f32_to_bf16_rn(a[i]);
-}
 
 }  // namespace fmc
 
@@ -360,8 +364,15 @@ extern "C" int fmc_flow_sync_bf16(const FmcFlow* flow, void* stream) {
   int rc = make_geom(flow, g);
   if (rc) return rc;
   FMC_CHECK_ARG(flow->theta && flow->theta_bf16, "theta/theta_bf16 NULL");
-  k_f32_to_bf16<<<ew_grid(g.n_params), 256, 0, (cudaStream_t)stream>>>(flow->theta, flow->theta_bf16, g.n_params);
-  FMC_LAUNCH_CHECK();
+  return pack_bf16_weights(g, flow->theta, flow->theta_bf16, (cudaStream_t)stream);
+}
+
+extern "C" int fmc_flow_bf16_size(const FmcFlow* flow, int64_t* n_elems) {
+  FlowGeom g;
+  int rc = make_geom(flow, g);
+  if (rc) return rc;
+  FMC_CHECK_ARG(n_elems != nullptr, "n_elems is NULL");
+  *n_elems = g.n_w16;
   return FMC_OK;
 }
 

@@ -12,6 +12,10 @@ struct FlowGeom {
   SplineCfg cfg;
   int64_t n_params;
   int64_t layer_off[FMC_MAX_LAYERS + 1];
+  // padded bf16 copy of the Linear weights (BF16 path): segment l*(nh+1)+i is
+  // W_i of layer l as [round_up(out, 256), round_up(in, 64)], zero padded
+  int64_t w16_off[FMC_MAX_LAYERS * (FMC_MAX_HIDDEN + 1) + 1];
+  int64_t n_w16;
 
   // conditioning coordinates of layer l: j = 2k + cpar(l); transformed: j = 2k + tpar(l)
   __host__ __device__ int cpar(int l) const { return 1 - (l & 1); }
@@ -26,14 +30,17 @@ struct FlowGeom {
     return m;
   }
   // linear layer i of layer l: in/out sizes and offsets (relative to layer_off[l])
-  int lin_in(int l, int i) const { return i == 0 ? nc(l) : H[i - 1]; }
-  int lin_out(int l, int i) const { return i == nh ? nt(l) * P : H[i]; }
-  int64_t lin_w(int l, int i) const {
+  __host__ __device__ int lin_in(int l, int i) const { return i == 0 ? nc(l) : H[i - 1]; }
+  __host__ __device__ int lin_out(int l, int i) const { return i == nh ? nt(l) * P : H[i]; }
+  __host__ __device__ int64_t lin_w(int l, int i) const {
     int64_t o = 2;
     for (int u = 0; u < i; ++u) o += (int64_t)lin_out(l, u) * lin_in(l, u) + lin_out(l, u);
     return o;
   }
   int64_t lin_b(int l, int i) const { return lin_w(l, i) + (int64_t)lin_out(l, i) * lin_in(l, i); }
+  __host__ __device__ static int64_t rup(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
+  __host__ __device__ int w16_rows(int l, int i) const { return (int)rup(lin_out(l, i), 256); }
+  __host__ __device__ int w16_cols(int l, int i) const { return (int)rup(lin_in(l, i), 64); }
 };
 
 int make_geom(const FmcFlow* f, FlowGeom& g);

@@ -1,12 +1,176 @@
-// gemm_tc.cu -- BF16 conditioner GEMMs on the 5th-generation tensor cores.
+// gemm_tc.cu -- host side of the tcgen05 GEMM (tc_gemm.cuh) and the BF16
+// conditioner path of the flow: TMA tensor maps, the bf16 weight packing and
+// the conditioner MLP as a chain of tensor-core GEMMs with fused epilogues.
+#include <cudaTypedefs.h>
+#include <mutex>
 #include "gemm_tc.cuh"
+#include "tc_gemm.cuh"
 
 namespace fmc {
 
+__device__ int g_tc_error = 0;   // set by a tcgen05 kernel whose bounded wait expired
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  });
+  return fn;
+}
+
+// 2-D bf16 tensor [outer, inner] with row stride ld (elements), box {64, box_outer}, 128B swizzle
+static int make_map(CUtensorMap* m, const void* base, int64_t inner, int64_t outer, int64_t ld, int box_outer) {
+  auto fn = encode_fn();
+  FMC_CHECK_SUPPORTED(fn != nullptr, "cuTensorMapEncodeTiled is unavailable");
+  FMC_CHECK_ARG(((uintptr_t)base & 15) == 0, "TMA base address must be 16-byte aligned");
+  FMC_CHECK_ARG((ld * 2) % 16 == 0, "TMA row stride must be a multiple of 16 bytes");
+  FMC_CHECK_ARG(inner >= tc::BK && outer >= box_outer, "tensor smaller than one TMA box");
+  cuuint64_t dims[2] = {(cuuint64_t)inner, (cuuint64_t)outer};
+  cuuint64_t strides[1] = {(cuuint64_t)(ld * 2)};
+  cuuint32_t box[2] = {(cuuint32_t)tc::BK, (cuuint32_t)box_outer};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d): inner=%lld outer=%lld ld=%lld box=%d", (int)r, (long long)inner,
+              (long long)outer, (long long)ld, box_outer);
+    return FMC_ERR_CUDA;
+  }
+  return FMC_OK;
+}
+
+template <int BN, int STAGES, int EPI>
+static int launch_tc(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& mb, int64_t M, int N, int K,
+                     const float* bias, void* C, int64_t ldc, int n_store) {
+  using S = tc::Smem<BN, STAGES>;
+  auto kern = tc::k_tc_gemm<BN, STAGES, EPI>;
+  static bool attr_set = false;
+  if (!attr_set) {
+    FMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S::TOTAL));
+    attr_set = true;
+  }
+  int* err = nullptr;
+  FMC_CUDA_TRY(cudaGetSymbolAddress((void**)&err, g_tc_error));
+  const int64_t mt = (M + tc::BM - 1) / tc::BM;
+  FMC_CHECK_SUPPORTED(mt <= 65535, "too many row tiles (%lld)", (long long)mt);
+  dim3 grid((unsigned)((n_store + BN - 1) / BN), (unsigned)mt);
+  kern<<<grid, tc::kThreads, S::TOTAL, st>>>(ma, mb, (int)M, N, K, bias, C, ldc, n_store, err);
+  FMC_LAUNCH_CHECK();
+  return FMC_OK;
+}
+
+int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K, const uint16_t* B, int N,
+            int rows_b, const float* bias, void* C, int64_t ldc, int n_store, int epi) {
+  FMC_CHECK_ARG(K % tc::BK == 0 && K >= tc::BK, "K=%d must be a positive multiple of 64", K);
+  FMC_CHECK_ARG(rows_a % tc::BM == 0 && rows_a >= M, "A rows %lld must cover M and be a multiple of 128",
+                (long long)rows_a);
+  FMC_CHECK_ARG(rows_b % 256 == 0 && rows_b >= N, "B rows %d must cover N and be a multiple of 256", rows_b);
+  const int BN = (N > 128) ? 256 : 128;
+  CUtensorMap ma, mb;
+  int rc = make_map(&ma, A, K, rows_a, K, tc::BM);
+  if (rc) return rc;
+  if ((rc = make_map(&mb, B, K, rows_b, K, BN))) return rc;
+  if (epi == tc::TC_EPI_TANH_BF16) {
+    if (BN == 256) return launch_tc<256, 4, tc::TC_EPI_TANH_BF16>(st, ma, mb, M, N, K, bias, C, ldc, n_store);
+    return launch_tc<128, 4, tc::TC_EPI_TANH_BF16>(st, ma, mb, M, N, K, bias, C, ldc, n_store);
+  }
+  if (BN == 256) return launch_tc<256, 4, tc::TC_EPI_BIAS_F32>(st, ma, mb, M, N, K, bias, C, ldc, n_store);
+  return launch_tc<128, 4, tc::TC_EPI_BIAS_F32>(st, ma, mb, M, N, K, bias, C, ldc, n_store);
+}
+
+// ------------------------------------------------------------------ packing
+__global__ void k_pack_bf16(FlowGeom g, const float* __restrict__ theta, uint16_t* __restrict__ w16) {
+  const int seg = blockIdx.y;
+  const int l = seg / (g.nh + 1), i = seg % (g.nh + 1);
+  const int out = g.lin_out(l, i), in = g.lin_in(l, i);
+  const int rows = g.w16_rows(l, i), cols = g.w16_cols(l, i);
+  const float* W = theta + g.layer_off[l] + g.lin_w(l, i);
+  uint16_t* dst = w16 + g.w16_off[seg];
+  const int64_t tot = (int64_t)rows * cols;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(e / cols), c = (int)(e - (int64_t)r * cols);
+    const float v = (r < out && c < in) ? W[(int64_t)r * in + c] : 0.f;
+    dst[e] = f32_to_bf16_rn(v);
+  }
+}
+
+int pack_bf16_weights(const FlowGeom& g, const float* theta, uint16_t* w16, cudaStream_t st) {
+  const int segs = g.L * (g.nh + 1);
+  dim3 grid(64, segs);
+  k_pack_bf16<<<grid, 256, 0, st>>>(g, theta, w16);
+  FMC_LAUNCH_CHECK();
+  return FMC_OK;
+}
+
+// fp32 [m, n] -> bf16 [m, ld] zero padded (ld >= n)
+__global__ void k_to_bf16_pad(const float* __restrict__ a, int64_t m, int n, int ld, uint16_t* __restrict__ b) {
+  const int64_t tot = m * ld;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e / ld;
+    const int c = (int)(e - r * ld);
+    b[e] = (c < n) ? f32_to_bf16_rn(a[r * n + c]) : (uint16_t)0;
+  }
+}
+
 int conditioner_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t m, const float* cond, uint16_t* cond16,
                      uint16_t* h16a, uint16_t* h16b, float* raw, cudaStream_t st) {
-  set_error("BF16 conditioner path not available in this build");
-  return FMC_ERR_UNSUPPORTED;
+  const int64_t rows = (m + tc::BM - 1) / tc::BM * tc::BM;
+  const int nc = g.nc(l), ncp = g.w16_cols(l, 0);
+  {
+    int64_t blocks = (m * ncp + 255) / 256;
+    if (blocks > (int64_t)sm_count() * 16) blocks = (int64_t)sm_count() * 16;
+    k_to_bf16_pad<<<(int)blocks, 256, 0, st>>>(cond, m, nc, ncp, cond16);
+    FMC_LAUNCH_CHECK();
+  }
+  const float* th = f->theta + g.layer_off[l];
+  const uint16_t* a = cond16;
+  uint16_t* hbuf[2] = {h16a, h16b};
+  for (int i = 0; i <= g.nh; ++i) {
+    const int seg = l * (g.nh + 1) + i;
+    const int K = g.w16_cols(l, i), N = g.lin_out(l, i);
+    const uint16_t* B = f->theta_bf16 + g.w16_off[seg];
+    const float* bias = th + g.lin_b(l, i);
+    int rc;
+    if (i < g.nh) {
+      const int ldo = (int)FlowGeom::rup(N, 64);
+      rc = tc_gemm(st, a, m, rows, K, B, N, g.w16_rows(l, i), bias, hbuf[i & 1], ldo, ldo, tc::TC_EPI_TANH_BF16);
+      a = hbuf[i & 1];
+    } else {
+      rc = tc_gemm(st, a, m, rows, K, B, N, g.w16_rows(l, i), bias, raw, N, N, tc::TC_EPI_BIAS_F32);
+    }
+    if (rc) return rc;
+  }
+  return FMC_OK;
 }
 
 }  // namespace fmc
+
+using namespace fmc;
+
+extern "C" int fmc_tc_gemm_bf16(const uint16_t* A, int64_t M, int64_t rows_a, int32_t K, const uint16_t* B,
+                                int32_t N, int32_t rows_b, const float* bias, void* C, int64_t ldc, int32_t n_store,
+                                int32_t epilogue, void* stream) {
+  FMC_CHECK_ARG(A && B && bias && C, "NULL pointer");
+  FMC_CHECK_ARG(epilogue == 0 || epilogue == 1, "epilogue must be 0 (tanh, bf16 out) or 1 (bias, fp32 out)");
+  FMC_CHECK_ARG(n_store >= N && n_store <= ldc, "n_store must be in [N, ldc]");
+  return tc_gemm((cudaStream_t)stream, A, M, rows_a, K, B, N, rows_b, bias, C, ldc, n_store, epilogue);
+}
+
+extern "C" int fmc_device_error(int32_t* out, int32_t clear) {
+  FMC_CHECK_ARG(out != nullptr, "out is NULL");
+  int v = 0;
+  FMC_CUDA_TRY(cudaMemcpyFromSymbol(&v, g_tc_error, sizeof(int)));
+  if (clear) {
+    const int z = 0;
+    FMC_CUDA_TRY(cudaMemcpyToSymbol(g_tc_error, &z, sizeof(int)));
+  }
+  *out = v;
+  return FMC_OK;
+}

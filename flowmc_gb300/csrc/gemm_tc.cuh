@@ -17,4 +17,14 @@ int conditioner_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t m, cons
 
 size_t train_ws_bytes(const FlowGeom& g, int64_t n);
 
+// theta (fp32, packed) -> zero-padded bf16 weight segments (FlowGeom::w16_off)
+int pack_bf16_weights(const FlowGeom& g, const float* theta, uint16_t* w16, cudaStream_t st);
+
+// C = epi(A . B^T + bias) on tcgen05; A [M, lda] bf16 (K = lda valid columns,
+// lda multiple of 64), B [rows_b >= N, ldb] bf16 (ldb == lda, rows_b multiple
+// of 256), epi 0: tanh -> bf16 C [M, ldc] storing n_store columns (zeros
+// beyond N); epi 1: + bias -> fp32 C [M, ldc] storing n_store (= N) columns.
+int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K, const uint16_t* B, int N,
+            int rows_b, const float* bias, void* C, int64_t ldc, int n_store, int epi);
+
 }  // namespace fmc

@@ -1,0 +1,278 @@
+// tc_gemm.cuh -- BF16 GEMM on the sm_100-family 5th-generation tensor cores:
+//   C[M, N] = epilogue( A[M, K] . B[N, K]^T + bias )      (A, B bf16, K-major)
+// with FP32 accumulation in tensor memory (TMEM).
+//
+// One CTA computes one 128 x BN output tile:
+//   warp 0        TMA producer: cp.async.bulk.tensor loads of A and B
+//                 K-chunks (64 bf16 = one 128-byte swizzle atom) into a
+//                 STAGES-deep shared-memory ring (128B swizzle)
+//   warp 1        TMEM allocation owner and MMA issuer: one elected thread
+//                 issues tcgen05.mma.cta_group::1.kind::f16 (M=128, N=BN,
+//                 K=16 per instruction, 4 per chunk) and tcgen05.commit
+//                 frees each stage / signals the accumulator
+//   warps 2..5    epilogue: tcgen05.ld 32x32b (one accumulator row per
+//                 thread), bias, activation, conversion, global stores
+// Every mbarrier wait is bounded; on expiry the kernel records an error
+// code, skips the remaining work, still frees its TMEM and returns.
+//
+// Descriptor layouts (PTX ISA, tcgen05 "Matrix Descriptors" and
+// "Instruction descriptor"): shared-memory descriptor = start>>4 [0,14),
+// leading-byte-offset>>4 [16,30), stride-byte-offset>>4 [32,46), version 1
+// [46,48), swizzle mode [61,64) (2 = 128B); instruction descriptor for
+// kind::f16 = D format [4,6) (1 = f32), A format [7,10) and B format
+// [10,13) (1 = bf16), A/B major [15], [16] (0 = K-major), N>>3 [17,23),
+// M>>4 [24,29).
+#pragma once
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include "common.cuh"
+
+namespace fmc {
+namespace tc {
+
+constexpr int BM = 128;
+constexpr int BK = 64;                 // bf16 elements per 128-byte swizzle row
+constexpr int kEpiWarps = 4;
+constexpr int kThreads = 64 + 32 * kEpiWarps;
+
+enum Epi : int { TC_EPI_TANH_BF16 = 0, TC_EPI_BIAS_F32 = 1 };
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait: ~1 s at most, then false
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (uint32_t it = 0; it < (1u << 22); ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (it > 64) __nanosleep(256);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
+      ::"r"(smem_u32(dst)), "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(c0), "r"(c1)
+      : "memory");
+}
+
+__device__ __forceinline__ uint64_t smem_desc_sw128(const void* p) {
+  const uint64_t addr = smem_u32(p);
+  uint64_t d = 0;
+  d |= (addr >> 4) & 0x3FFFull;             // start address
+  d |= (uint64_t)1 << 16;                   // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;         // stride byte offset: 8 rows x 128 B
+  d |= (uint64_t)1 << 46;                   // descriptor version (sm_100 family)
+  d |= (uint64_t)2 << 61;                   // 128-byte swizzle
+  return d;
+}
+
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float tanh_fast(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+template <int BN, int STAGES>
+struct Smem {
+  static constexpr int A_BYTES = BM * BK * 2;
+  static constexpr int B_BYTES = BN * BK * 2;
+  static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+  static constexpr int TOTAL = STAGES * STAGE_BYTES + 1024 /*align slack*/ + 256 /*barriers*/;
+};
+
+// err: device word; 1 = a wait expired
+template <int BN, int STAGES, int EPI>
+__global__ void __launch_bounds__(kThreads, 1)
+    k_tc_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N, int K,
+              const float* __restrict__ bias, void* __restrict__ C, int64_t ldc, int n_store, int* err) {
+  extern __shared__ uint8_t smem_raw[];
+  using S = Smem<BN, STAGES>;
+  uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(base + STAGES * S::STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* acc_full = empty + STAGES;
+  uint32_t* tmem_slot = (uint32_t*)(acc_full + 1);
+  volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int nk = (K + BK - 1) / BK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(acc_full, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(BN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int issued = 0;
+      for (int k = 0; k < nk; ++k) {
+        const int s = k % STAGES;
+        const uint32_t ph = (uint32_t)(k / STAGES) & 1u;
+        if (k >= STAGES && !mbar_wait(&empty[s], ph ^ 1u)) {
+          *abort_flag = 1;
+          break;
+        }
+        if (*abort_flag) break;
+        uint8_t* sa = base + s * S::STAGE_BYTES;
+        uint8_t* sb = sa + S::A_BYTES;
+        mbar_expect_tx(&full[s], S::STAGE_BYTES);
+        tma_load_2d(sa, &tmA, &full[s], k * BK, m0);
+        tma_load_2d(sb, &tmB, &full[s], k * BK, n0);
+        issued = k + 1;
+      }
+      if (*abort_flag) {
+        // let the copies still in flight land before the CTA exits (bounded)
+        for (int k = issued > STAGES ? issued - STAGES : 0; k < issued; ++k)
+          mbar_wait(&full[k % STAGES], (uint32_t)(k / STAGES) & 1u);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16_f32(BN);
+      for (int k = 0; k < nk; ++k) {
+        const int s = k % STAGES;
+        const uint32_t ph = (uint32_t)(k / STAGES) & 1u;
+        if (!mbar_wait(&full[s], ph)) {
+          *abort_flag = 1;
+          break;
+        }
+        if (*abort_flag) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint8_t* sa = base + s * S::STAGE_BYTES;
+        const uint8_t* sb = sa + S::A_BYTES;
+        const uint64_t da = smem_desc_sw128(sa), db = smem_desc_sw128(sb);
+#pragma unroll
+        for (int kk = 0; kk < BK / 16; ++kk) {
+          // advance along K inside the swizzle atom: 16 bf16 = 32 bytes
+          mma_bf16(tmem, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, (k > 0 || kk > 0) ? 1u : 0u);
+        }
+        mma_commit(&empty[s]);
+      }
+      // always committed, also after an abort: it fires once every MMA issued
+      // so far has finished, so the TMEM can be released safely
+      mma_commit(acc_full);
+    }
+  } else {
+    // epilogue warps: TMEM lane quarter = warp % 4
+    const int q = warp & 3;
+    const int row = q * 32 + lane;
+    const int gm = m0 + row;
+    bool ok = mbar_wait(acc_full, 0);
+    if (!ok) *abort_flag = 1;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok && !*abort_flag) {
+#pragma unroll 1
+      for (int c0 = 0; c0 < BN; c0 += 32) {
+        float v[32];
+        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
+        const int gn0 = n0 + c0;
+        if (gm >= M || gn0 >= n_store) continue;
+        if (EPI == TC_EPI_TANH_BF16) {
+          __nv_bfloat16* out = (__nv_bfloat16*)C + (int64_t)gm * ldc + gn0;
+          uint32_t packed[16];
+#pragma unroll
+          for (int i = 0; i < 32; i += 2) {
+            const int j = gn0 + i;
+            const float b0 = (j < N) ? __ldg(bias + j) : 0.f;
+            const float b1 = (j + 1 < N) ? __ldg(bias + j + 1) : 0.f;
+            const float y0 = (j < N) ? tanh_fast(v[i] + b0) : 0.f;
+            const float y1 = (j + 1 < N) ? tanh_fast(v[i + 1] + b1) : 0.f;
+            const __nv_bfloat162 h = __floats2bfloat162_rn(y0, y1);
+            packed[i / 2] = *reinterpret_cast<const uint32_t*>(&h);
+          }
+          if (gn0 + 32 <= n_store) {
+            uint4* o4 = reinterpret_cast<uint4*>(out);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) o4[i] = make_uint4(packed[4 * i], packed[4 * i + 1], packed[4 * i + 2], packed[4 * i + 3]);
+          } else {
+            uint32_t* o = reinterpret_cast<uint32_t*>(out);
+            for (int i = 0; i < 16 && gn0 + 2 * i < n_store; ++i) o[i] = packed[i];
+          }
+        } else {
+          float* out = (float*)C + (int64_t)gm * ldc + gn0;
+          const int lim = n_store - gn0 < 32 ? n_store - gn0 : 32;
+#pragma unroll
+          for (int i = 0; i < 32; ++i)
+            if (i < lim) out[i] = v[i] + __ldg(bias + gn0 + i);
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN));
+  }
+  if (threadIdx.x == 0 && *abort_flag) atomicExch(err, 1);
+}
+
+}  // namespace tc
+}  // namespace fmc

@@ -82,7 +82,11 @@ class MaskedCouplingRQSpline(NFModel):
         aux[2 * d + 1] = 1.0   # decay of the packed-out entries
         self.theta = torch.zeros(self.n_params, dtype=torch.float32, device=self.device)
         self.aux = torch.tensor(aux, device=self.device)
-        self.theta_bf16 = torch.zeros(self.n_params, dtype=torch.bfloat16, device=self.device)
+        n16 = ctypes.c_int64(0)
+        if _lib.LIB_PATH.exists():
+            hs = self._host_struct()
+            _lib.check(_lib.lib().fmc_flow_bf16_size(ctypes.byref(hs), ctypes.byref(n16)))
+        self.theta_bf16 = torch.zeros(max(int(n16.value), 1), dtype=torch.bfloat16, device=self.device)
         self._ws = _lib.Workspace()
         self.load_full(full, sync=True)
 

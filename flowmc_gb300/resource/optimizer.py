@@ -41,11 +41,12 @@ class Optimizer(Resource):
         L = _lib.lib()
         _lib.check(L.fmc_adamw_workspace_size(ctypes.byref(nb)))
         ptr, size = self._ws.get(nb.value, model.device)
-        bf16 = model.theta_bf16.data_ptr() if model.precision in ("bf16", "bfloat16") else None
-        _lib.check(L.fmc_adamw_step(model.theta.data_ptr(), bf16, grad.data_ptr(), state.m.data_ptr(),
+        _lib.check(L.fmc_adamw_step(model.theta.data_ptr(), None, grad.data_ptr(), state.m.data_ptr(),
                                     state.v.data_ptr(), model.n_params, model.aux.data_ptr(), model.aux.numel(),
                                     state.count.data_ptr(), ctypes.byref(self.params), ptr, size,
                                     _lib.stream_handle(model.device)))
+        if model.precision in ("bf16", "bfloat16"):
+            model.sync_bf16()   # re-pack the padded bf16 weights the tensor-core GEMMs read
 
     def __call__(self, params, grads):
         raise NotImplementedError

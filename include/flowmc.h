@@ -165,7 +165,11 @@ FMC_API int fmc_flow_layout(const FmcFlow* flow, int64_t* n_params, int64_t* lay
  * mode 0: log_prob / forward / inverse / sample;  1: loss + gradient. */
 FMC_API int fmc_flow_workspace_size(const FmcFlow* flow, int64_t n, int32_t mode, size_t* bytes);
 
-/* Refresh theta_bf16 from theta (after loading parameters). */
+/* BF16 mode: theta_bf16 holds each Linear weight as a zero-padded bf16 block
+ * [round_up(out, 256), round_up(in, 64)], layer by layer (n_elems elements in
+ * total). fmc_flow_sync_bf16 refreshes it from theta (after loading or
+ * updating parameters). */
+FMC_API int fmc_flow_bf16_size(const FmcFlow* flow, int64_t* n_elems);
 FMC_API int fmc_flow_sync_bf16(const FmcFlow* flow, void* stream);
 
 /* MaskedCouplingRQSpline.forward for a batch (rqSpline.py:450-468):
@@ -257,6 +261,20 @@ FMC_API int fmc_select_training_data(const float* buf, int32_t n_chains, int64_t
                                      int32_t history_window, int64_t n_out, uint64_t seed, uint64_t counter,
                                      const int64_t* idx, float* out, int32_t* err, void* ws, size_t ws_bytes,
                                      void* stream);
+
+/* ---- tensor-core GEMM (the conditioner's building block) ---------------- */
+/* C = epilogue(A . B^T + bias) on tcgen05 with FP32 accumulation in TMEM.
+ * A [rows_a, K] and B [rows_b, K] bf16 row-major (K a multiple of 64, rows_a
+ * a multiple of 128 covering M, rows_b a multiple of 256 covering N).
+ * epilogue 0: tanh -> bf16 C [M, ldc] (n_store columns, zeros beyond N);
+ * epilogue 1: + bias -> fp32 C [M, ldc] (n_store = N columns). Replaces the
+ * Linear + tanh layers of MLP.__call__ (resource/model/common.py:109-112). */
+FMC_API int fmc_tc_gemm_bf16(const uint16_t* A, int64_t M, int64_t rows_a, int32_t K, const uint16_t* B,
+                             int32_t N, int32_t rows_b, const float* bias, void* C, int64_t ldc, int32_t n_store,
+                             int32_t epilogue, void* stream);
+/* Device error word of the tensor-core kernels: 1 after a bounded wait
+ * expired (synchronous read; clear != 0 resets it). */
+FMC_API int fmc_device_error(int32_t* out, int32_t clear);
 
 /* ---- library --------------------------------------------------------- */
 FMC_API const char* fmc_last_error(void);

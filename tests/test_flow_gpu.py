@@ -254,3 +254,30 @@ def gpu_grad_to_full_params(m):
     tmp = F.Flow([dict(Lr, mask=((np.arange(m.n_features) + i) % 2).astype(bool)) for i, Lr in enumerate(full)],
                  m.num_bins, np.zeros(m.n_features), np.eye(m.n_features))
     return F.flatten(tmp)
+
+
+BF16_CONFIGS = [(32, 4, (128, 128), 10), (128, 2, (512, 512), 12), (5, 2, (32, 32), 8), (64, 3, (256, 256), 8)]
+
+
+@pytest.mark.parametrize("d,L,hidden,nb", BF16_CONFIGS, ids=[f"d{c[0]}L{c[1]}K{c[3]}" for c in BF16_CONFIGS])
+def test_flow_bf16_conditioner_matches_oracle(cuda, d, L, hidden, nb):
+    """BF16 conditioner GEMMs (tcgen05) with FP32 spline: log-probs within 2e-2."""
+    from flowmc_gb300 import _lib
+    fl = to_f32(rand_flow(d, L, hidden, nb, seed=d + L, wscale=0.3))
+    m = gpu_model(fl, hidden, precision="bf16")
+    rng = np.random.default_rng(2)
+    x = (rng.normal(size=(1000, d)) * 1.5).astype(np.float32)
+    xt = torch.tensor(x, device="cuda")
+    lp = m.log_prob(xt).cpu().numpy()
+    olp = fl.log_prob(x.astype(np.float64))
+    assert _lib.device_error() == 0
+    err = np.abs(lp - olp) / np.maximum(1.0, np.abs(olp))
+    assert err.max() <= 2e-2, err.max()
+    y, ld = m.forward(xt)
+    oy, old = fl.forward(x.astype(np.float64))
+    assert np.abs(y.cpu().numpy() - oy).max() <= 2e-2 * max(1, np.abs(oy).max())
+    z = rng.normal(size=(500, d)).astype(np.float32)
+    from flowmc_gb300.random import PRNGKey
+    s = m.sample(PRNGKey(1), 500, z=torch.tensor(z, device="cuda")).cpu().numpy()
+    os_ = fl.sample(z.astype(np.float64))
+    assert np.abs(s - os_).max() <= 2e-2 * max(1, np.abs(os_).max())

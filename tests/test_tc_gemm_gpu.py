@@ -1,0 +1,52 @@
+"""tcgen05 BF16 GEMM (fmc_tc_gemm_bf16) against a plain PyTorch FP32
+reference of the same op: C = epi(A B^T + bias) on bf16-rounded A and B.
+Tolerance: 2e-3 relative to the largest |C| (FP32 accumulation order) for the
+fp32 epilogue; bf16 output rounding (2^-8) for the tanh epilogue."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def run(M, K, N, epi, seed=0):
+    from flowmc_gb300 import _lib
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    rows_a = -(-M // 128) * 128
+    rows_b = -(-N // 256) * 256
+    A = torch.zeros(rows_a, K, dtype=torch.bfloat16)
+    B = torch.zeros(rows_b, K, dtype=torch.bfloat16)
+    A[:M] = (torch.randn(M, K, generator=g) * 0.5).to(torch.bfloat16)
+    B[:N] = (torch.randn(N, K, generator=g) / np.sqrt(K)).to(torch.bfloat16)
+    bias = torch.randn(N, generator=g) * 0.1
+    A, B, bias = A.cuda(), B.cuda(), bias.cuda()
+    if epi == 0:
+        ldc = -(-N // 64) * 64
+        C = torch.full((M, ldc), float("nan"), dtype=torch.bfloat16, device="cuda")
+        n_store = ldc
+    else:
+        ldc = N
+        C = torch.full((M, ldc), float("nan"), dtype=torch.float32, device="cuda")
+        n_store = N
+    _lib.check(_lib.lib().fmc_tc_gemm_bf16(A.data_ptr(), M, rows_a, K, B.data_ptr(), N, rows_b, bias.data_ptr(),
+                                           C.data_ptr(), ldc, n_store, epi, _lib.stream_handle()))
+    torch.cuda.synchronize()
+    assert _lib.device_error() == 0
+    ref = A[:M].float() @ B[:N].float().T + bias
+    if epi == 0:
+        ref = torch.tanh(ref)
+        got = C.float()
+        assert torch.isfinite(got).all()
+        assert (got[:, N:] == 0).all()                      # padding columns are zero
+        err = (got[:, :N] - ref).abs().max().item()
+        assert err <= 2 ** -7, err
+    else:
+        err = (C - ref).abs().max().item()
+        assert err <= 2e-3 * ref.abs().max().item() + 1e-5, err
+
+
+@pytest.mark.parametrize("M,K,N", [(128, 64, 128), (300, 64, 256), (1000, 128, 512), (257, 512, 512),
+                                   (129, 64, 100), (4096, 512, 4736), (640, 192, 384)])
+@pytest.mark.parametrize("epi", [0, 1])
+def test_tc_gemm_matches_torch(cuda, M, K, N, epi):
+    run(M, K, N, epi, seed=M + K + N)
