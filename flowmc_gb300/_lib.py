@@ -155,6 +155,9 @@ _SIGNATURES = {
         ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int64,
         ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
         ctypes.c_size_t, ctypes.c_void_p]),
+    "fmc_select_training_data_noalloc": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int64,
+        ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "fmc_last_error": (ctypes.c_char_p, []),
     "fmc_version": (ctypes.c_int, []),
     "fmc_device_sm_count": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int32)]),

@@ -14,6 +14,7 @@
 //    "Ciphers with arbitrary finite domains", CT-RSA 2002).
 //  * fmc_select_training_data: TrainModel's finite-row filter, per-chain
 //    history window and with-replacement resampling (train_model.py:66-80).
+#include <mutex>
 #include "common.cuh"
 #include "gemm_tc.cuh"
 
@@ -389,4 +390,61 @@ extern "C" int fmc_select_training_data(const float* buf, int32_t n_chains, int6
                                                         n_out, out, err);
   FMC_LAUNCH_CHECK();
   return FMC_OK;
+}
+
+namespace fmc {
+
+// ---------------------------------------------------------------- allocation-free selection
+// fmc_select_training_data_noalloc: the training-data selection for callers that
+// cannot allocate device memory -- code running where cudaMalloc is off limits
+// (inside another framework's allocator or a memory pool it owns, under a
+// strict no-allocation policy in a serving process, or in a host callback).
+// Its scratch (row flags, tile offsets, compacted row ids, the row count) lives
+// in the file-scope array below, sized for at most kNoAllocSelectMaxRows =
+// n_chains * n_steps rows (about 12 MiB, held by every GPU that loads the
+// library until the process exits). Every call shares that array: calls that
+// overlap on the GPU (different streams, or different host threads) race on
+// it, so serialise them. No scratch word needs clearing between calls: each
+// call writes every word it later reads.
+constexpr int64_t kNoAllocSelectMaxRows = 1ll << 20;
+constexpr size_t kNoAllocSelectBytes =
+    (size_t)(kNoAllocSelectMaxRows * 4 + 256 + ((kNoAllocSelectMaxRows + kScanTile - 1) / kScanTile) * 4 + 256 +
+             kNoAllocSelectMaxRows * 8 + 256 + 64);
+static __device__ __align__(256) uint8_t g_noalloc_select_scratch[kNoAllocSelectBytes];
+
+static int noalloc_select_scratch(void** out) {
+  // the array's name is only a host-side handle; its device address comes from
+  // cudaGetSymbolAddress, looked up once per device with that device current
+  static std::mutex mu;
+  static void* addr[256] = {nullptr};
+  int dev = 0;
+  FMC_CUDA_TRY(cudaGetDevice(&dev));
+  FMC_CHECK_SUPPORTED(dev >= 0 && dev < 256, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lock(mu);
+  if (addr[dev] == nullptr) {
+    void* p = nullptr;
+    FMC_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_select_scratch));
+    addr[dev] = p;
+  }
+  *out = addr[dev];
+  return FMC_OK;
+}
+
+}  // namespace fmc
+
+extern "C" int fmc_select_training_data_noalloc(const float* buf, int32_t n_chains, int64_t n_steps, int32_t d,
+                                                int32_t history_window, int64_t n_out, uint64_t seed,
+                                                uint64_t counter, const int64_t* idx, float* out, int32_t* err,
+                                                void* stream) {
+  FMC_CHECK_ARG(n_chains >= 1 && n_steps >= 1, "bad sizes");
+  const int64_t rows = (int64_t)n_chains * n_steps;
+  FMC_CHECK_ARG(rows <= fmc::kNoAllocSelectMaxRows,
+                "n_chains * n_steps = %lld rows exceeds the %lld rows the static scratch of "
+                "fmc_select_training_data_noalloc holds; use fmc_select_training_data with a workspace",
+                (long long)rows, (long long)fmc::kNoAllocSelectMaxRows);
+  void* scratch = nullptr;
+  int rc = fmc::noalloc_select_scratch(&scratch);
+  if (rc) return rc;
+  return fmc_select_training_data(buf, n_chains, n_steps, d, history_window, n_out, seed, counter, idx, out, err,
+                                  scratch, fmc::kNoAllocSelectBytes, stream);
 }

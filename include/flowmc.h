@@ -261,6 +261,20 @@ FMC_API int fmc_select_training_data(const float* buf, int32_t n_chains, int64_t
                                      int32_t history_window, int64_t n_out, uint64_t seed, uint64_t counter,
                                      const int64_t* idx, float* out, int32_t* err, void* ws, size_t ws_bytes,
                                      void* stream);
+/* The same selection without a workspace argument and without any device
+ * allocation, for callers that cannot allocate device memory (code running
+ * inside another framework's allocator or memory pool, or under a
+ * no-allocation policy). No counterpart in the reference. Its scratch is a
+ * static device array of about 12 MiB held by every GPU that loads the
+ * library; it serves at most n_chains * n_steps = 1048576 rows and larger
+ * buffers are rejected with FMC_ERR_INVALID_ARG. The first call on each
+ * device looks the array's device address up (a synchronous runtime call), so
+ * make that first call before any stream capture. All calls share the array:
+ * calls that overlap on the GPU race, so serialise them. */
+FMC_API int fmc_select_training_data_noalloc(const float* buf, int32_t n_chains, int64_t n_steps, int32_t d,
+                                             int32_t history_window, int64_t n_out, uint64_t seed,
+                                             uint64_t counter, const int64_t* idx, float* out, int32_t* err,
+                                             void* stream);
 
 /* ---- tensor-core GEMM (the conditioner's building block) ---------------- */
 /* C = epilogue(A . B^T + bias) on tcgen05 with FP32 accumulation in TMEM.
