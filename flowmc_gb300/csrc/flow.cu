@@ -55,6 +55,12 @@ int make_geom(const FmcFlow* f, FlowGeom& g) {
       o16 += (int64_t)g.w16_rows(l, i) * g.w16_cols(l, i);
     }
   g.w16_off[g.L * (g.nh + 1)] = o16;
+  for (int l = 0; l < g.L; ++l)
+    for (int i = 0; i <= g.nh; ++i) {
+      g.w16t_off[l * (g.nh + 1) + i] = o16;
+      o16 += (int64_t)g.w16t_rows(l, i) * g.w16t_cols(l, i);
+    }
+  g.w16t_off[g.L * (g.nh + 1)] = o16;
   g.n_w16 = o16;
   return FMC_OK;
 }

@@ -15,6 +15,8 @@ struct FlowGeom {
   // padded bf16 copy of the Linear weights (BF16 path): segment l*(nh+1)+i is
   // W_i of layer l as [round_up(out, 256), round_up(in, 64)], zero padded
   int64_t w16_off[FMC_MAX_LAYERS * (FMC_MAX_HIDDEN + 1) + 1];
+  // transposed copies W_i^T as [round_up(in, 256), round_up(out, 64)] (training)
+  int64_t w16t_off[FMC_MAX_LAYERS * (FMC_MAX_HIDDEN + 1) + 1];
   int64_t n_w16;
 
   // conditioning coordinates of layer l: j = 2k + cpar(l); transformed: j = 2k + tpar(l)
@@ -41,6 +43,8 @@ struct FlowGeom {
   __host__ __device__ static int64_t rup(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
   __host__ __device__ int w16_rows(int l, int i) const { return (int)rup(lin_out(l, i), 256); }
   __host__ __device__ int w16_cols(int l, int i) const { return (int)rup(lin_in(l, i), 64); }
+  __host__ __device__ int w16t_rows(int l, int i) const { return (int)rup(lin_in(l, i), 256); }
+  __host__ __device__ int w16t_cols(int l, int i) const { return (int)rup(lin_out(l, i), 64); }
 };
 
 int make_geom(const FmcFlow* f, FlowGeom& g);

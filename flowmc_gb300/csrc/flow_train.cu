@@ -22,6 +22,9 @@ static int64_t a256(int64_t v) { return (v + 255) / 256 * 256; }
 struct TrainWs {
   float *xs, *xa, *cond, *hs, *raw, *graw, *gh0, *gh1, *gcond, *gy, *gxa, *ld, *logp, *part;
   int64_t part_floats;
+  // BF16 path (tensor-core GEMMs): activations, gradients and their transposes
+  uint16_t *cond16, *condT, *hs16, *hsT, *graw16, *grawT, *gz16[2], *gzT[2];
+  int64_t n128, n64, hld, htr, ncld, nctr, pld, ptr_rows;
 };
 
 static int colsum_blocks(int64_t n) {
@@ -30,12 +33,17 @@ static int colsum_blocks(int64_t n) {
   return (int)(rb < 1 ? 1 : rb);
 }
 
-static void carve_train(const FlowGeom& g, int64_t n, void* ws, TrainWs& w, size_t* total) {
+static void carve_train(const FlowGeom& g, int64_t n, bool bf16, void* ws, TrainWs& w, size_t* total) {
   char* p = (char*)ws;
   int64_t used = 0;
   auto take = [&](int64_t floats) {
     float* r = (float*)(p + used);
     used += a256(4 * floats);
+    return r;
+  };
+  auto take16 = [&](int64_t elems) {
+    uint16_t* r = (uint16_t*)(p + used);
+    used += a256(2 * elems);
     return r;
   };
   const int64_t ntP = (int64_t)g.nt_max() * g.P;
@@ -56,13 +64,35 @@ static void carve_train(const FlowGeom& g, int64_t n, void* ws, TrainWs& w, size
   if (m < 4096) m = 4096;
   w.part_floats = (int64_t)colsum_blocks(n) * m;
   w.part = take(w.part_floats);
+  w.cond16 = w.condT = w.hs16 = w.hsT = w.graw16 = w.grawT = nullptr;
+  w.gz16[0] = w.gz16[1] = w.gzT[0] = w.gzT[1] = nullptr;
+  if (bf16) {
+    w.n128 = FlowGeom::rup(n, 128);
+    w.n64 = FlowGeom::rup(n, 64);
+    w.hld = FlowGeom::rup(g.h_max(), 64);
+    w.htr = FlowGeom::rup(g.h_max(), 256);
+    w.ncld = FlowGeom::rup(g.nc_max(), 64);
+    w.nctr = FlowGeom::rup(g.nc_max(), 256);
+    w.pld = FlowGeom::rup(ntP, 64);
+    w.ptr_rows = FlowGeom::rup(ntP, 256);
+    w.cond16 = take16(w.n128 * w.ncld);
+    w.condT = take16(w.nctr * w.n64);
+    w.hs16 = take16((int64_t)g.nh * w.n128 * w.hld);
+    w.hsT = take16((int64_t)g.nh * w.htr * w.n64);
+    w.graw16 = take16(w.n128 * w.pld);
+    w.grawT = take16(w.ptr_rows * w.n64);
+    for (int k = 0; k < 2; ++k) {
+      w.gz16[k] = take16(w.n128 * w.hld);
+      w.gzT[k] = take16(w.htr * w.n64);
+    }
+  }
   if (total) *total = (size_t)used;
 }
 
 size_t train_ws_bytes(const FlowGeom& g, int64_t n) {
   TrainWs w;
   size_t tot = 0;
-  carve_train(g, n, nullptr, w, &tot);
+  carve_train(g, n, true, nullptr, w, &tot);   // sized for the BF16 path (a superset)
   return tot;
 }
 
@@ -92,6 +122,29 @@ static int colsum(cudaStream_t st, const float* gm, int64_t n, int m, float* par
   const int64_t rows_per = (n + rb - 1) / rb;
   dim3 grid((m + 255) / 256, rb);
   k_colsum_partial<<<grid, 256, 0, st>>>(gm, n, m, rows_per, part);
+  FMC_LAUNCH_CHECK();
+  k_colsum_final<<<(m + 255) / 256, 256, 0, st>>>(part, rb, m, out);
+  FMC_LAUNCH_CHECK();
+  return FMC_OK;
+}
+
+__global__ void k_colsum_partial_bf16(const uint16_t* __restrict__ gm, int64_t n, int m, int64_t ld,
+                                      int64_t rows_per, float* __restrict__ part) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m) return;
+  const int64_t r0 = blockIdx.y * rows_per;
+  int64_t r1 = r0 + rows_per;
+  if (r1 > n) r1 = n;
+  float s = 0.f;
+  for (int64_t r = r0; r < r1; ++r) s += __uint_as_float((uint32_t)gm[r * ld + j] << 16);
+  part[(int64_t)blockIdx.y * m + j] = s;
+}
+
+static int colsum_bf16(cudaStream_t st, const uint16_t* gm, int64_t n, int m, int64_t ld, float* part, float* out) {
+  const int rb = colsum_blocks(n);
+  const int64_t rows_per = (n + rb - 1) / rb;
+  dim3 grid((m + 255) / 256, rb);
+  k_colsum_partial_bf16<<<grid, 256, 0, st>>>(gm, n, m, ld, rows_per, part);
   FMC_LAUNCH_CHECK();
   k_colsum_final<<<(m + 255) / 256, 256, 0, st>>>(part, rb, m, out);
   FMC_LAUNCH_CHECK();
@@ -196,6 +249,84 @@ static int recompute_mlp(const FmcFlow* f, const FlowGeom& g, int l, int64_t n, 
   return FMC_OK;
 }
 
+// BF16 recompute of layer l's conditioner: tanh activations (and their
+// transposes for the weight gradients) in bf16, outputs in fp32
+static int recompute_mlp_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t n, TrainWs& w, cudaStream_t st) {
+  const float* th = f->theta + g.layer_off[l];
+  const int nc = g.nc(l);
+  int rc = to_bf16_pad_t(st, w.cond, n, nc, w.cond16, FlowGeom::rup(nc, 64), w.condT, w.n64, w.n64);
+  if (rc) return rc;
+  const uint16_t* a = w.cond16;
+  for (int i = 0; i <= g.nh; ++i) {
+    const int seg = l * (g.nh + 1) + i;
+    const int K = g.w16_cols(l, i), N = g.lin_out(l, i);
+    const uint16_t* B = f->theta_bf16 + g.w16_off[seg];
+    tc::EpiArgs ep{};
+    ep.bias = th + g.lin_b(l, i);
+    if (i < g.nh) {
+      uint16_t* h = w.hs16 + (int64_t)i * w.n128 * w.hld;
+      ep.ct = w.hsT + (int64_t)i * w.htr * w.n64;
+      ep.ldct = w.n64;
+      ep.ct_rows_pad = w.n64;
+      const int ldo = (int)FlowGeom::rup(N, 64);
+      rc = tc_gemm(st, a, n, w.n128, K, B, N, g.w16_rows(l, i), ep, h, ldo, ldo, tc::TC_EPI_TANH_BF16);
+      a = h;
+    } else {
+      rc = tc_gemm(st, a, n, w.n128, K, B, N, g.w16_rows(l, i), ep, w.raw, N, N, tc::TC_EPI_BIAS_F32);
+    }
+    if (rc) return rc;
+  }
+  return FMC_OK;
+}
+
+// BF16 adjoint of the conditioner: w.graw (fp32) -> weight/bias gradients into gl, d cond into w.gcond
+static int backward_mlp_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t n, TrainWs& w, float* gl,
+                             cudaStream_t st) {
+  const int ntP = g.lin_out(l, g.nh);
+  int rc = colsum(st, w.graw, n, ntP, w.part, gl + g.lin_b(l, g.nh));
+  if (rc) return rc;
+  if ((rc = to_bf16_pad_t(st, w.graw, n, ntP, w.graw16, FlowGeom::rup(ntP, 64), w.grawT, w.n64, w.n64))) return rc;
+  const uint16_t* gcur = w.graw16;
+  const uint16_t* gcurT = w.grawT;
+  int nxt = 0;
+  for (int i = g.nh; i >= 0; --i) {
+    const int out = g.lin_out(l, i), in = g.lin_in(l, i);
+    const int seg = l * (g.nh + 1) + i;
+    const uint16_t* aT = (i == 0) ? w.condT : w.hsT + (int64_t)(i - 1) * w.htr * w.n64;
+    // dW = g^T a  [out, in], reduced over the batch
+    tc::EpiArgs e0{};
+    if ((rc = tc_gemm(st, gcurT, out, FlowGeom::rup(out, 128), (int)w.n64, aT, in, (int)FlowGeom::rup(in, 256), e0,
+                      gl + g.lin_w(l, i), in, in, tc::TC_EPI_F32)))
+      return rc;
+    if (i < g.nh) {
+      if ((rc = colsum_bf16(st, gcur, n, out, FlowGeom::rup(out, 64), w.part, gl + g.lin_b(l, i)))) return rc;
+    }
+    const uint16_t* WT = f->theta_bf16 + g.w16t_off[seg];
+    if (i > 0) {
+      // d a = (g W) * (1 - a^2), a = the tanh activation feeding Linear i
+      tc::EpiArgs e1{};
+      e1.aux = w.hs16 + (int64_t)(i - 1) * w.n128 * w.hld;
+      e1.ldaux = FlowGeom::rup(in, 64);
+      e1.ct = w.gzT[nxt];
+      e1.ldct = w.n64;
+      e1.ct_rows_pad = w.n64;
+      const int ldo = (int)FlowGeom::rup(in, 64);
+      if ((rc = tc_gemm(st, gcur, n, w.n128, (int)FlowGeom::rup(out, 64), WT, in, g.w16t_rows(l, i), e1, w.gz16[nxt],
+                        ldo, ldo, tc::TC_EPI_DTANH_BF16)))
+        return rc;
+      gcur = w.gz16[nxt];
+      gcurT = w.gzT[nxt];
+      nxt ^= 1;
+    } else {
+      tc::EpiArgs e2{};
+      if ((rc = tc_gemm(st, gcur, n, w.n128, (int)FlowGeom::rup(out, 64), WT, in, g.w16t_rows(l, i), e2, w.gcond, in,
+                        in, tc::TC_EPI_F32)))
+        return rc;
+    }
+  }
+  return FMC_OK;
+}
+
 int flow_loss_grad(const FmcFlow* f, const float* x, int64_t n, float* loss, float* grad, void* ws, size_t ws_bytes,
                    cudaStream_t st) {
   FlowGeom g;
@@ -207,8 +338,10 @@ int flow_loss_grad(const FmcFlow* f, const float* x, int64_t n, float* loss, flo
   const size_t need = train_ws_bytes(g, n);
   FMC_CHECK_ARG(ws && ws_bytes >= need, "workspace of %zu bytes < %zu needed", ws_bytes, need);
   FMC_CHECK_ARG(((uintptr_t)ws & 255) == 0, "workspace must be 256-byte aligned");
+  const bool bf16 = f->precision == FMC_PREC_BF16;
+  if (bf16) FMC_CHECK_ARG(f->theta_bf16 != nullptr, "BF16 mode needs theta_bf16");
   TrainWs w;
-  carve_train(g, n, ws, w, nullptr);
+  carve_train(g, n, bf16, ws, w, nullptr);
   const int d = g.d;
   const int64_t nd = n * d;
   const int eb = ew_blocks(nd);
@@ -222,7 +355,7 @@ int flow_loss_grad(const FmcFlow* f, const float* x, int64_t n, float* loss, flo
     k_affine<<<eb, 256, 0, st>>>(xin, xout, w.cond, n, d, g.nc(l), g.cpar(l), f->theta + g.layer_off[l], 0, w.ld,
                                  l == 0 ? 1 : 0);
     FMC_LAUNCH_CHECK();
-    if ((rc = recompute_mlp(f, g, l, n, w, st))) return rc;
+    if ((rc = bf16 ? recompute_mlp_bf16(f, g, l, n, w, st) : recompute_mlp(f, g, l, n, w, st))) return rc;
     if ((rc = launch_spline(g.K, false, st, w.raw, xout, w.ld, n, d, g.nt(l), g.tpar(l), g.cfg))) return rc;
   }
   const float* y = w.xs + (int64_t)g.L * nd;
@@ -246,32 +379,36 @@ int flow_loss_grad(const FmcFlow* f, const float* x, int64_t n, float* loss, flo
     const float* xin = w.xs + (int64_t)l * nd;
     k_affine<<<eb, 256, 0, st>>>(xin, w.xa, w.cond, n, d, g.nc(l), g.cpar(l), th, 0, nullptr, 0);
     FMC_LAUNCH_CHECK();
-    if ((rc = recompute_mlp(f, g, l, n, w, st))) return rc;
+    if ((rc = bf16 ? recompute_mlp_bf16(f, g, l, n, w, st) : recompute_mlp(f, g, l, n, w, st))) return rc;
     if ((rc = launch_spline_bwd(g.K, st, w.raw, w.xa, w.gy, gld, w.graw, w.gxa, n, d, g.nt(l), g.tpar(l), g.cpar(l),
                                 g.cfg)))
       return rc;
-    // conditioner adjoint
-    const float* gcur = w.graw;
-    float* gbufs[2] = {w.gh0, w.gh1};
-    for (int i = g.nh; i >= 0; --i) {
-      const int out = g.lin_out(l, i), in = g.lin_in(l, i);
-      const float* a_in = (i == 0) ? w.cond : w.hs + (int64_t)(i - 1) * n * g.h_max();
-      // dW = g^T a_in  [out, in]
-      if ((rc = sgemm<false, false, EPI_NONE>(st, out, in, (int)n, gcur, out, a_in, in, nullptr, nullptr, 0,
-                                              gl + g.lin_w(l, i), in, 0.f)))
-        return rc;
-      if ((rc = colsum(st, gcur, n, out, w.part, gl + g.lin_b(l, i)))) return rc;
-      float* gnext = (i == 0) ? w.gcond : gbufs[i & 1];
-      if (i > 0) {
-        if ((rc = sgemm<true, false, EPI_DTANH>(st, n, in, out, gcur, out, th + g.lin_w(l, i), in, nullptr, a_in, in,
-                                                gnext, in, 0.f)))
+    if (bf16) {
+      if ((rc = backward_mlp_bf16(f, g, l, n, w, gl, st))) return rc;
+    } else {
+      // conditioner adjoint
+      const float* gcur = w.graw;
+      float* gbufs[2] = {w.gh0, w.gh1};
+      for (int i = g.nh; i >= 0; --i) {
+        const int out = g.lin_out(l, i), in = g.lin_in(l, i);
+        const float* a_in = (i == 0) ? w.cond : w.hs + (int64_t)(i - 1) * n * g.h_max();
+        // dW = g^T a_in  [out, in]
+        if ((rc = sgemm<false, false, EPI_NONE>(st, out, in, (int)n, gcur, out, a_in, in, nullptr, nullptr, 0,
+                                                gl + g.lin_w(l, i), in, 0.f)))
           return rc;
-      } else {
-        if ((rc = sgemm<true, false, EPI_NONE>(st, n, in, out, gcur, out, th + g.lin_w(l, i), in, nullptr, nullptr, 0,
-                                               gnext, in, 0.f)))
-          return rc;
+        if ((rc = colsum(st, gcur, n, out, w.part, gl + g.lin_b(l, i)))) return rc;
+        float* gnext = (i == 0) ? w.gcond : gbufs[i & 1];
+        if (i > 0) {
+          if ((rc = sgemm<true, false, EPI_DTANH>(st, n, in, out, gcur, out, th + g.lin_w(l, i), in, nullptr, a_in,
+                                                  in, gnext, in, 0.f)))
+            return rc;
+        } else {
+          if ((rc = sgemm<true, false, EPI_NONE>(st, n, in, out, gcur, out, th + g.lin_w(l, i), in, nullptr,
+                                                 nullptr, 0, gnext, in, 0.f)))
+            return rc;
+        }
+        gcur = gnext;
       }
-      gcur = gnext;
     }
     // ScalarAffine adjoint -> d(layer input) into gy
     const int ab = eb < 1024 ? eb : 1024;

@@ -48,7 +48,7 @@ static int make_map(CUtensorMap* m, const void* base, int64_t inner, int64_t out
 
 template <int BN, int STAGES, int EPI>
 static int launch_tc(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& mb, int64_t M, int N, int K,
-                     const float* bias, void* C, int64_t ldc, int n_store) {
+                     const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store) {
   using S = tc::Smem<BN, STAGES>;
   auto kern = tc::k_tc_gemm<BN, STAGES, EPI>;
   static bool attr_set = false;
@@ -61,50 +61,96 @@ static int launch_tc(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& 
   const int64_t mt = (M + tc::BM - 1) / tc::BM;
   FMC_CHECK_SUPPORTED(mt <= 65535, "too many row tiles (%lld)", (long long)mt);
   dim3 grid((unsigned)((n_store + BN - 1) / BN), (unsigned)mt);
-  kern<<<grid, tc::kThreads, S::TOTAL, st>>>(ma, mb, (int)M, N, K, bias, C, ldc, n_store, err);
+  kern<<<grid, tc::kThreads, S::TOTAL, st>>>(ma, mb, (int)M, N, K, ep, C, ldc, n_store, err);
   FMC_LAUNCH_CHECK();
   return FMC_OK;
 }
 
 int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K, const uint16_t* B, int N,
-            int rows_b, const float* bias, void* C, int64_t ldc, int n_store, int epi) {
+            int rows_b, const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store, int epi) {
   FMC_CHECK_ARG(K % tc::BK == 0 && K >= tc::BK, "K=%d must be a positive multiple of 64", K);
   FMC_CHECK_ARG(rows_a % tc::BM == 0 && rows_a >= M, "A rows %lld must cover M and be a multiple of 128",
                 (long long)rows_a);
   FMC_CHECK_ARG(rows_b % 256 == 0 && rows_b >= N, "B rows %d must cover N and be a multiple of 256", rows_b);
+  FMC_CHECK_ARG(n_store <= ldc, "n_store %d > ldc %lld", n_store, (long long)ldc);
+  if (epi == tc::TC_EPI_TANH_BF16 || epi == tc::TC_EPI_BIAS_F32) FMC_CHECK_ARG(ep.bias != nullptr, "bias is NULL");
+  if (epi == tc::TC_EPI_DTANH_BF16) FMC_CHECK_ARG(ep.aux != nullptr, "aux is NULL");
+  if (M <= 0) return FMC_OK;
   const int BN = (N > 128) ? 256 : 128;
   CUtensorMap ma, mb;
   int rc = make_map(&ma, A, K, rows_a, K, tc::BM);
   if (rc) return rc;
   if ((rc = make_map(&mb, B, K, rows_b, K, BN))) return rc;
-  if (epi == tc::TC_EPI_TANH_BF16) {
-    if (BN == 256) return launch_tc<256, 4, tc::TC_EPI_TANH_BF16>(st, ma, mb, M, N, K, bias, C, ldc, n_store);
-    return launch_tc<128, 4, tc::TC_EPI_TANH_BF16>(st, ma, mb, M, N, K, bias, C, ldc, n_store);
+#define TC_CASE(E)                                                                              \
+  if (epi == E) {                                                                               \
+    if (BN == 256) return launch_tc<256, 4, E>(st, ma, mb, M, N, K, ep, C, ldc, n_store);       \
+    return launch_tc<128, 4, E>(st, ma, mb, M, N, K, ep, C, ldc, n_store);                      \
   }
-  if (BN == 256) return launch_tc<256, 4, tc::TC_EPI_BIAS_F32>(st, ma, mb, M, N, K, bias, C, ldc, n_store);
-  return launch_tc<128, 4, tc::TC_EPI_BIAS_F32>(st, ma, mb, M, N, K, bias, C, ldc, n_store);
+  TC_CASE(tc::TC_EPI_TANH_BF16)
+  TC_CASE(tc::TC_EPI_BIAS_F32)
+  TC_CASE(tc::TC_EPI_DTANH_BF16)
+  TC_CASE(tc::TC_EPI_F32)
+#undef TC_CASE
+  set_error("unknown epilogue %d", epi);
+  return FMC_ERR_INVALID_ARG;
 }
 
 // ------------------------------------------------------------------ packing
 __global__ void k_pack_bf16(FlowGeom g, const float* __restrict__ theta, uint16_t* __restrict__ w16) {
-  const int seg = blockIdx.y;
+  const int nseg = g.L * (g.nh + 1);
+  const int seg = blockIdx.y % nseg;
+  const bool tr = blockIdx.y >= nseg;   // second half of the grid writes W^T
   const int l = seg / (g.nh + 1), i = seg % (g.nh + 1);
   const int out = g.lin_out(l, i), in = g.lin_in(l, i);
-  const int rows = g.w16_rows(l, i), cols = g.w16_cols(l, i);
+  const int rows = tr ? g.w16t_rows(l, i) : g.w16_rows(l, i);
+  const int cols = tr ? g.w16t_cols(l, i) : g.w16_cols(l, i);
   const float* W = theta + g.layer_off[l] + g.lin_w(l, i);
-  uint16_t* dst = w16 + g.w16_off[seg];
+  uint16_t* dst = w16 + (tr ? g.w16t_off[seg] : g.w16_off[seg]);
   const int64_t tot = (int64_t)rows * cols;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
     const int r = (int)(e / cols), c = (int)(e - (int64_t)r * cols);
-    const float v = (r < out && c < in) ? W[(int64_t)r * in + c] : 0.f;
+    float v = 0.f;
+    if (!tr && r < out && c < in) v = W[(int64_t)r * in + c];
+    if (tr && r < in && c < out) v = W[(int64_t)c * in + r];
     dst[e] = f32_to_bf16_rn(v);
   }
 }
 
 int pack_bf16_weights(const FlowGeom& g, const float* theta, uint16_t* w16, cudaStream_t st) {
   const int segs = g.L * (g.nh + 1);
-  dim3 grid(64, segs);
+  dim3 grid(64, 2 * segs);
   k_pack_bf16<<<grid, 256, 0, st>>>(g, theta, w16);
+  FMC_LAUNCH_CHECK();
+  return FMC_OK;
+}
+
+// fp32 [n, cols] -> bf16 [n, ldd] (zero padded) and/or transposed [ldd.., ldt]
+__global__ void k_to_bf16_pad_t(const float* __restrict__ src, int64_t n, int cols, uint16_t* __restrict__ dst,
+                                int64_t ldd, uint16_t* __restrict__ dstT, int64_t ldt, int64_t t_cols) {
+  __shared__ uint16_t tile[32][33];
+  const int64_t r0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8 threads
+  for (int k = ty; k < 32; k += 8) {
+    const int64_t r = r0 + k, c = c0 + tx;
+    const float v = (r < n && c < cols) ? src[r * cols + c] : 0.f;
+    const uint16_t b = f32_to_bf16_rn(v);
+    tile[k][tx] = b;
+    if (dst && r < n && c < ldd) dst[r * ldd + c] = b;
+  }
+  if (!dstT) return;
+  __syncthreads();
+  for (int k = ty; k < 32; k += 8) {
+    const int64_t c = c0 + k, r = r0 + tx;   // row c of dstT, column r
+    if (c < ldd && r < t_cols) dstT[c * ldt + r] = tile[tx][k];
+  }
+}
+
+int to_bf16_pad_t(cudaStream_t st, const float* src, int64_t n, int cols, uint16_t* dst, int64_t ldd, uint16_t* dstT,
+                  int64_t ldt, int64_t t_cols) {
+  const int64_t rows = dstT ? (t_cols > n ? t_cols : n) : n;
+  dim3 grid((unsigned)((ldd + 31) / 32), (unsigned)((rows + 31) / 32));
+  FMC_CHECK_SUPPORTED(grid.y <= 65535u, "too many rows for the conversion grid");
+  k_to_bf16_pad_t<<<grid, 256, 0, st>>>(src, n, cols, dst, ldd, dstT, ldt, t_cols);
   FMC_LAUNCH_CHECK();
   return FMC_OK;
 }
@@ -138,12 +184,14 @@ int conditioner_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t m, cons
     const uint16_t* B = f->theta_bf16 + g.w16_off[seg];
     const float* bias = th + g.lin_b(l, i);
     int rc;
+    tc::EpiArgs ep{};
+    ep.bias = bias;
     if (i < g.nh) {
       const int ldo = (int)FlowGeom::rup(N, 64);
-      rc = tc_gemm(st, a, m, rows, K, B, N, g.w16_rows(l, i), bias, hbuf[i & 1], ldo, ldo, tc::TC_EPI_TANH_BF16);
+      rc = tc_gemm(st, a, m, rows, K, B, N, g.w16_rows(l, i), ep, hbuf[i & 1], ldo, ldo, tc::TC_EPI_TANH_BF16);
       a = hbuf[i & 1];
     } else {
-      rc = tc_gemm(st, a, m, rows, K, B, N, g.w16_rows(l, i), bias, raw, N, N, tc::TC_EPI_BIAS_F32);
+      rc = tc_gemm(st, a, m, rows, K, B, N, g.w16_rows(l, i), ep, raw, N, N, tc::TC_EPI_BIAS_F32);
     }
     if (rc) return rc;
   }
@@ -160,7 +208,9 @@ extern "C" int fmc_tc_gemm_bf16(const uint16_t* A, int64_t M, int64_t rows_a, in
   FMC_CHECK_ARG(A && B && bias && C, "NULL pointer");
   FMC_CHECK_ARG(epilogue == 0 || epilogue == 1, "epilogue must be 0 (tanh, bf16 out) or 1 (bias, fp32 out)");
   FMC_CHECK_ARG(n_store >= N && n_store <= ldc, "n_store must be in [N, ldc]");
-  return tc_gemm((cudaStream_t)stream, A, M, rows_a, K, B, N, rows_b, bias, C, ldc, n_store, epilogue);
+  tc::EpiArgs ep{};
+  ep.bias = bias;
+  return tc_gemm((cudaStream_t)stream, A, M, rows_a, K, B, N, rows_b, ep, C, ldc, n_store, epilogue);
 }
 
 extern "C" int fmc_device_error(int32_t* out, int32_t clear) {

@@ -5,6 +5,23 @@
 
 namespace fmc {
 
+namespace tc {
+// epilogues of the tensor-core GEMM: 0 tanh(acc + bias) -> bf16;
+// 1 acc + bias -> fp32; 2 acc * (1 - aux^2) -> bf16 (tanh adjoint, aux = the
+// forward's tanh output); 3 acc -> fp32 (no bias). Modes 0 and 2 can also
+// store a transposed bf16 copy.
+enum Epi : int { TC_EPI_TANH_BF16 = 0, TC_EPI_BIAS_F32 = 1, TC_EPI_DTANH_BF16 = 2, TC_EPI_F32 = 3 };
+
+struct EpiArgs {
+  const float* bias;        // modes 0, 1
+  const uint16_t* aux;      // mode 2: bf16 [M, ldaux]
+  int64_t ldaux;
+  uint16_t* ct;             // optional transposed copy: ct[col * ldct + row]
+  int64_t ldct;
+  int64_t ct_rows_pad;      // rows in [M, ct_rows_pad) get zeros in the copy
+};
+}  // namespace tc
+
 __device__ __forceinline__ uint16_t f32_to_bf16_rn(float v) {
   return __bfloat16_as_ushort(__float2bfloat16_rn(v));
 }
@@ -18,13 +35,19 @@ int conditioner_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t m, cons
 size_t train_ws_bytes(const FlowGeom& g, int64_t n);
 
 // theta (fp32, packed) -> zero-padded bf16 weight segments (FlowGeom::w16_off)
+// and their transposes (FlowGeom::w16t_off)
 int pack_bf16_weights(const FlowGeom& g, const float* theta, uint16_t* w16, cudaStream_t st);
 
-// C = epi(A . B^T + bias) on tcgen05; A [M, lda] bf16 (K = lda valid columns,
-// lda multiple of 64), B [rows_b >= N, ldb] bf16 (ldb == lda, rows_b multiple
-// of 256), epi 0: tanh -> bf16 C [M, ldc] storing n_store columns (zeros
-// beyond N); epi 1: + bias -> fp32 C [M, ldc] storing n_store (= N) columns.
+// C = epi(A . B^T) on tcgen05; A [rows_a, K] bf16 (K a multiple of 64, rows_a
+// a multiple of 128 covering M), B [rows_b, K] bf16 (rows_b a multiple of 256
+// covering N). bf16 epilogues store n_store columns (zeros beyond N), fp32
+// epilogues n_store (= N) columns.
 int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K, const uint16_t* B, int N,
-            int rows_b, const float* bias, void* C, int64_t ldc, int n_store, int epi);
+            int rows_b, const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store, int epi);
+
+// fp32 src [n, cols] -> bf16 dst [>= n, ldd] (zero padded to ldd columns; may be
+// NULL) and/or its transpose dstT [>= ldd, ldt] (rows n..t_cols-1 zero)
+int to_bf16_pad_t(cudaStream_t st, const float* src, int64_t n, int cols, uint16_t* dst, int64_t ldd,
+                  uint16_t* dstT, int64_t ldt, int64_t t_cols);
 
 }  // namespace fmc

@@ -26,6 +26,7 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include "common.cuh"
+#include "gemm_tc.cuh"
 
 namespace fmc {
 namespace tc {
@@ -35,7 +36,7 @@ constexpr int BK = 64;                 // bf16 elements per 128-byte swizzle row
 constexpr int kEpiWarps = 4;
 constexpr int kThreads = 64 + 32 * kEpiWarps;
 
-enum Epi : int { TC_EPI_TANH_BF16 = 0, TC_EPI_BIAS_F32 = 1 };
+// epilogue modes and arguments: see gemm_tc.cuh
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -136,7 +137,7 @@ struct Smem {
 template <int BN, int STAGES, int EPI>
 __global__ void __launch_bounds__(kThreads, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N, int K,
-              const float* __restrict__ bias, void* __restrict__ C, int64_t ldc, int n_store, int* err) {
+              const EpiArgs ep, void* __restrict__ C, int64_t ldc, int n_store, int* err) {
   extern __shared__ uint8_t smem_raw[];
   using S = Smem<BN, STAGES>;
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -228,39 +229,69 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (!ok) *abort_flag = 1;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (ok && !*abort_flag) {
+      const bool row_ok = gm < M;
+      const bool ct_row = ep.ct != nullptr && gm < ep.ct_rows_pad;
 #pragma unroll 1
       for (int c0 = 0; c0 < BN; c0 += 32) {
         float v[32];
         tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
         const int gn0 = n0 + c0;
-        if (gm >= M || gn0 >= n_store) continue;
-        if (EPI == TC_EPI_TANH_BF16) {
-          __nv_bfloat16* out = (__nv_bfloat16*)C + (int64_t)gm * ldc + gn0;
+        if (gn0 >= n_store || !(row_ok || ct_row)) continue;
+        if (EPI == TC_EPI_TANH_BF16 || EPI == TC_EPI_DTANH_BF16) {
           uint32_t packed[16];
+          float y[32];
+          if (EPI == TC_EPI_TANH_BF16) {
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+              const int j = gn0 + i;
+              y[i] = (j < N && row_ok) ? tanh_fast(v[i] + __ldg(ep.bias + j)) : 0.f;
+            }
+          } else {
+            const uint16_t* ar = ep.aux + (int64_t)gm * ep.ldaux + gn0;
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+              const int j = gn0 + i;
+              float h = 0.f;
+              if (j < N && row_ok) h = __uint_as_float((uint32_t)ar[i] << 16);
+              y[i] = (j < N && row_ok) ? v[i] * (1.f - h * h) : 0.f;
+            }
+          }
 #pragma unroll
           for (int i = 0; i < 32; i += 2) {
-            const int j = gn0 + i;
-            const float b0 = (j < N) ? __ldg(bias + j) : 0.f;
-            const float b1 = (j + 1 < N) ? __ldg(bias + j + 1) : 0.f;
-            const float y0 = (j < N) ? tanh_fast(v[i] + b0) : 0.f;
-            const float y1 = (j + 1 < N) ? tanh_fast(v[i + 1] + b1) : 0.f;
-            const __nv_bfloat162 h = __floats2bfloat162_rn(y0, y1);
-            packed[i / 2] = *reinterpret_cast<const uint32_t*>(&h);
+            const __nv_bfloat162 hh = __floats2bfloat162_rn(y[i], y[i + 1]);
+            packed[i / 2] = *reinterpret_cast<const uint32_t*>(&hh);
           }
-          if (gn0 + 32 <= n_store) {
-            uint4* o4 = reinterpret_cast<uint4*>(out);
+          if (row_ok) {
+            __nv_bfloat16* out = (__nv_bfloat16*)C + (int64_t)gm * ldc + gn0;
+            if (gn0 + 32 <= n_store) {
+              uint4* o4 = reinterpret_cast<uint4*>(out);
 #pragma unroll
-            for (int i = 0; i < 4; ++i) o4[i] = make_uint4(packed[4 * i], packed[4 * i + 1], packed[4 * i + 2], packed[4 * i + 3]);
-          } else {
-            uint32_t* o = reinterpret_cast<uint32_t*>(out);
-            for (int i = 0; i < 16 && gn0 + 2 * i < n_store; ++i) o[i] = packed[i];
+              for (int i = 0; i < 4; ++i)
+                o4[i] = make_uint4(packed[4 * i], packed[4 * i + 1], packed[4 * i + 2], packed[4 * i + 3]);
+            } else {
+#pragma unroll
+              for (int i = 0; i < 16; ++i)
+                if (gn0 + 2 * i < n_store) reinterpret_cast<uint32_t*>(out)[i] = packed[i];
+            }
           }
-        } else {
+          if (ct_row) {
+            // transposed copy: column j of the tile becomes row j of ct; a warp's
+            // 32 rows give one contiguous 64-byte store per column
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+              if (gn0 + i < n_store) {
+                const uint32_t w = packed[i / 2];
+                const uint16_t hv = (i & 1) ? (uint16_t)(w >> 16) : (uint16_t)(w & 0xffffu);
+                ep.ct[(int64_t)(gn0 + i) * ep.ldct + gm] = hv;
+              }
+            }
+          }
+        } else if (row_ok) {
           float* out = (float*)C + (int64_t)gm * ldc + gn0;
           const int lim = n_store - gn0 < 32 ? n_store - gn0 : 32;
 #pragma unroll
           for (int i = 0; i < 32; ++i)
-            if (i < lim) out[i] = v[i] + __ldg(bias + gn0 + i);
+            if (i < lim) out[i] = (EPI == TC_EPI_BIAS_F32) ? v[i] + __ldg(ep.bias + gn0 + i) : v[i];
         }
       }
     }

@@ -166,9 +166,10 @@ FMC_API int fmc_flow_layout(const FmcFlow* flow, int64_t* n_params, int64_t* lay
 FMC_API int fmc_flow_workspace_size(const FmcFlow* flow, int64_t n, int32_t mode, size_t* bytes);
 
 /* BF16 mode: theta_bf16 holds each Linear weight as a zero-padded bf16 block
- * [round_up(out, 256), round_up(in, 64)], layer by layer (n_elems elements in
- * total). fmc_flow_sync_bf16 refreshes it from theta (after loading or
- * updating parameters). */
+ * [round_up(out, 256), round_up(in, 64)], layer by layer, followed by the
+ * transposed blocks [round_up(in, 256), round_up(out, 64)] the training
+ * backward reads (n_elems elements in total). fmc_flow_sync_bf16 refreshes it
+ * from theta (after loading or updating parameters). */
 FMC_API int fmc_flow_bf16_size(const FmcFlow* flow, int64_t* n_elems);
 FMC_API int fmc_flow_sync_bf16(const FmcFlow* flow, void* stream);
 
