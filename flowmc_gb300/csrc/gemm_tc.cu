@@ -59,9 +59,10 @@ static int launch_tc(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& 
   int* err = nullptr;
   FMC_CUDA_TRY(cudaGetSymbolAddress((void**)&err, g_tc_error));
   const int64_t mt = (M + tc::BM - 1) / tc::BM;
-  FMC_CHECK_SUPPORTED(mt <= 65535, "too many row tiles (%lld)", (long long)mt);
-  dim3 grid((unsigned)((n_store + BN - 1) / BN), (unsigned)mt);
-  kern<<<grid, tc::kThreads, S::TOTAL, st>>>(ma, mb, (int)M, N, K, ep, C, ldc, n_store, err);
+  const int64_t tiles = mt * ((n_store + BN - 1) / BN);
+  FMC_CHECK_SUPPORTED(tiles < (1ll << 31) && M < (1ll << 31), "GEMM too large (%lld tiles)", (long long)tiles);
+  const int64_t grid = tiles < sm_count() ? tiles : sm_count();   // persistent: one CTA per SM
+  kern<<<(unsigned)grid, tc::kThreads, S::TOTAL, st>>>(ma, mb, (int)M, N, K, ep, C, ldc, n_store, err);
   FMC_LAUNCH_CHECK();
   return FMC_OK;
 }

@@ -133,7 +133,14 @@ struct Smem {
   static constexpr int TOTAL = STAGES * STAGE_BYTES + 1024 /*align slack*/ + 256 /*barriers*/;
 };
 
-// err: device word; 1 = a wait expired
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Persistent GEMM: each CTA walks tiles t = blockIdx.x, +gridDim.x, ... (tile
+// t covers rows (t / n_tiles) * 128 and columns (t % n_tiles) * BN), with two
+// TMEM accumulators so the epilogue of one tile overlaps the MMAs of the next.
+// err: device word; 1 = a wait expired.
 template <int BN, int STAGES, int EPI>
 __global__ void __launch_bounds__(kThreads, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N, int K,
@@ -143,26 +150,34 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = (uint64_t*)(base + STAGES * S::STAGE_BYTES);
   uint64_t* empty = full + STAGES;
-  uint64_t* acc_full = empty + STAGES;
-  uint32_t* tmem_slot = (uint32_t*)(acc_full + 1);
+  uint64_t* acc_full = empty + STAGES;      // [2]
+  uint64_t* acc_empty = acc_full + 2;       // [2]
+  uint64_t* mma_done = acc_empty + 2;
+  uint32_t* tmem_slot = (uint32_t*)(mma_done + 1);
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
   const int nk = (K + BK - 1) / BK;
+  const int n_tiles = (n_store + BN - 1) / BN;
+  const int m_tiles = (M + BM - 1) / BM;
+  const int tiles = n_tiles * m_tiles;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(acc_full, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], kEpiWarps);
+    }
+    mbar_init(mma_done, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(BN));
+                 "r"(2 * BN));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -172,69 +187,94 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   if (warp == 0) {
     if (lane == 0) {
-      int issued = 0;
-      for (int k = 0; k < nk; ++k) {
-        const int s = k % STAGES;
-        const uint32_t ph = (uint32_t)(k / STAGES) & 1u;
-        if (k >= STAGES && !mbar_wait(&empty[s], ph ^ 1u)) {
-          *abort_flag = 1;
-          break;
+      uint32_t it = 0;
+      for (int t = blockIdx.x; t < tiles && !*abort_flag; t += gridDim.x) {
+        const int m0 = (t / n_tiles) * BM, n0 = (t % n_tiles) * BN;
+        for (int k = 0; k < nk; ++k, ++it) {
+          const int s = it % STAGES;
+          const uint32_t ph = (it / STAGES) & 1u;
+          if (it >= (uint32_t)STAGES && !mbar_wait(&empty[s], ph ^ 1u)) {
+            *abort_flag = 1;
+            break;
+          }
+          if (*abort_flag) break;
+          uint8_t* sa = base + s * S::STAGE_BYTES;
+          uint8_t* sb = sa + S::A_BYTES;
+          mbar_expect_tx(&full[s], S::STAGE_BYTES);
+          tma_load_2d(sa, &tmA, &full[s], k * BK, m0);
+          tma_load_2d(sb, &tmB, &full[s], k * BK, n0);
         }
-        if (*abort_flag) break;
-        uint8_t* sa = base + s * S::STAGE_BYTES;
-        uint8_t* sb = sa + S::A_BYTES;
-        mbar_expect_tx(&full[s], S::STAGE_BYTES);
-        tma_load_2d(sa, &tmA, &full[s], k * BK, m0);
-        tma_load_2d(sb, &tmB, &full[s], k * BK, n0);
-        issued = k + 1;
       }
       if (*abort_flag) {
         // let the copies still in flight land before the CTA exits (bounded)
-        for (int k = issued > STAGES ? issued - STAGES : 0; k < issued; ++k)
-          mbar_wait(&full[k % STAGES], (uint32_t)(k / STAGES) & 1u);
+        for (uint32_t j = it > (uint32_t)STAGES ? it - STAGES : 0; j < it; ++j)
+          mbar_wait(&full[j % STAGES], (j / STAGES) & 1u);
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
       const uint32_t idesc = idesc_bf16_f32(BN);
-      for (int k = 0; k < nk; ++k) {
-        const int s = k % STAGES;
-        const uint32_t ph = (uint32_t)(k / STAGES) & 1u;
-        if (!mbar_wait(&full[s], ph)) {
+      uint32_t it = 0;
+      int local = 0;
+      for (int t = blockIdx.x; t < tiles && !*abort_flag; t += gridDim.x, ++local) {
+        const int b = local & 1, use = local >> 1;
+        if (use > 0 && !mbar_wait(&acc_empty[b], (uint32_t)(use - 1) & 1u)) {
           *abort_flag = 1;
           break;
         }
-        if (*abort_flag) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint8_t* sa = base + s * S::STAGE_BYTES;
-        const uint8_t* sb = sa + S::A_BYTES;
-        const uint64_t da = smem_desc_sw128(sa), db = smem_desc_sw128(sb);
+        const uint32_t d = tmem + (uint32_t)(b * BN);
+        bool stop = false;
+        for (int k = 0; k < nk; ++k, ++it) {
+          const int s = it % STAGES;
+          const uint32_t ph = (it / STAGES) & 1u;
+          if (!mbar_wait(&full[s], ph) || *abort_flag) {
+            *abort_flag = 1;
+            stop = true;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint8_t* sa = base + s * S::STAGE_BYTES;
+          const uint8_t* sb = sa + S::A_BYTES;
+          const uint64_t da = smem_desc_sw128(sa), db = smem_desc_sw128(sb);
 #pragma unroll
-        for (int kk = 0; kk < BK / 16; ++kk) {
-          // advance along K inside the swizzle atom: 16 bf16 = 32 bytes
-          mma_bf16(tmem, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, (k > 0 || kk > 0) ? 1u : 0u);
+          for (int kk = 0; kk < BK / 16; ++kk) {
+            // advance along K inside the swizzle atom: 16 bf16 = 32 bytes
+            mma_bf16(d, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, (k > 0 || kk > 0) ? 1u : 0u);
+          }
+          mma_commit(&empty[s]);
         }
-        mma_commit(&empty[s]);
+        if (stop) break;
+        mma_commit(&acc_full[b]);
       }
-      // always committed, also after an abort: it fires once every MMA issued
-      // so far has finished, so the TMEM can be released safely
-      mma_commit(acc_full);
+      // fires once every MMA issued so far has finished (also after an abort),
+      // so the TMEM can be released safely
+      mma_commit(mma_done);
     }
   } else {
-    // epilogue warps: TMEM lane quarter = warp % 4
+    // epilogue warps: TMEM lane quarter = warp % 4, one accumulator row per thread
     const int q = warp & 3;
     const int row = q * 32 + lane;
-    const int gm = m0 + row;
-    bool ok = mbar_wait(acc_full, 0);
-    if (!ok) *abort_flag = 1;
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (ok && !*abort_flag) {
+    // vector stores only when every row start is 16-byte aligned
+    const int esz = (EPI == TC_EPI_TANH_BF16 || EPI == TC_EPI_DTANH_BF16) ? 2 : 4;
+    const bool vec_ok = (((uintptr_t)C & 15) == 0) && ((ldc * esz) % 16 == 0);
+    int local = 0;
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++local) {
+      const int b = local & 1, use = local >> 1;
+      const int m0 = (t / n_tiles) * BM, n0 = (t % n_tiles) * BN;
+      const int gm = m0 + row;
+      if (*abort_flag || !mbar_wait(&acc_full[b], (uint32_t)use & 1u)) {
+        *abort_flag = 1;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const bool row_ok = gm < M;
       const bool ct_row = ep.ct != nullptr && gm < ep.ct_rows_pad;
+      const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN);
 #pragma unroll 1
       for (int c0 = 0; c0 < BN; c0 += 32) {
         float v[32];
-        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
+        tmem_ld32(tbase + (uint32_t)c0, v);
         const int gn0 = n0 + c0;
         if (gn0 >= n_store || !(row_ok || ct_row)) continue;
         if (EPI == TC_EPI_TANH_BF16 || EPI == TC_EPI_DTANH_BF16) {
@@ -263,15 +303,16 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
           if (row_ok) {
             __nv_bfloat16* out = (__nv_bfloat16*)C + (int64_t)gm * ldc + gn0;
-            if (gn0 + 32 <= n_store) {
+            if (gn0 + 32 <= n_store && vec_ok) {
               uint4* o4 = reinterpret_cast<uint4*>(out);
 #pragma unroll
               for (int i = 0; i < 4; ++i)
                 o4[i] = make_uint4(packed[4 * i], packed[4 * i + 1], packed[4 * i + 2], packed[4 * i + 3]);
             } else {
+              uint16_t* o16 = reinterpret_cast<uint16_t*>(out);
 #pragma unroll
-              for (int i = 0; i < 16; ++i)
-                if (gn0 + 2 * i < n_store) reinterpret_cast<uint32_t*>(out)[i] = packed[i];
+              for (int i = 0; i < 32; ++i)
+                if (gn0 + i < n_store) o16[i] = (i & 1) ? (uint16_t)(packed[i / 2] >> 16) : (uint16_t)packed[i / 2];
             }
           }
           if (ct_row) {
@@ -288,19 +329,36 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         } else if (row_ok) {
           float* out = (float*)C + (int64_t)gm * ldc + gn0;
-          const int lim = n_store - gn0 < 32 ? n_store - gn0 : 32;
+          if (EPI == TC_EPI_BIAS_F32) {
 #pragma unroll
-          for (int i = 0; i < 32; ++i)
-            if (i < lim) out[i] = (EPI == TC_EPI_BIAS_F32) ? v[i] + __ldg(ep.bias + gn0 + i) : v[i];
+            for (int i = 0; i < 32; ++i)
+              if (gn0 + i < n_store) v[i] += __ldg(ep.bias + gn0 + i);
+          }
+          if (gn0 + 32 <= n_store && vec_ok) {
+            float4* o4 = reinterpret_cast<float4*>(out);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) o4[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+          } else {
+            const int lim = n_store - gn0 < 32 ? n_store - gn0 : 32;
+#pragma unroll
+            for (int i = 0; i < 32; ++i)
+              if (i < lim) out[i] = v[i];
+          }
         }
       }
+      // this warp's TMEM lanes of buffer b are read: release them to the MMA warp
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acc_empty[b]);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 1) {
+    if (lane == 0) mbar_wait(mma_done, 0);
+    __syncwarp();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN));
   }
   if (threadIdx.x == 0 && *abort_flag) atomicExch(err, 1);
 }
