@@ -174,6 +174,38 @@ def measured_peaks():
     return 6800.0, 1900.0, 1700.0, "fallback"
 
 
+# ---------------------------------------------------------------- plain FP32 form
+def plain_arm(name, w, dev, n_train, n_prod, timed_from, mean_ref, var_ref, ess=True):
+    """The plain FP32 PyTorch-eager form (flowmc_gb300.plain) on the same
+    workload: chain-steps/s over the loops from `timed_from` on, and (when
+    the production phase is long enough) its min-ESS/s and moment error."""
+    import torch
+    from flowmc_gb300 import diagnostics as D
+    from flowmc_gb300 import plain as PL
+    if name == "rosenbrock128":
+        vg = PL.rosenbrock_value_grad
+    else:
+        t, _, _ = make_target(name, w, dev)
+        means = torch.tensor(t.means, dtype=torch.float32, device=dev)
+        iv = torch.tensor(1.0 / t.var, dtype=torch.float32, device=dev)
+        lw = torch.tensor(t.log_w, dtype=torch.float32, device=dev)
+        vg = lambda x: PL.mixture_value_grad(x, means, iv, lw)
+    g = torch.Generator().manual_seed(w["seed"])
+    x0 = torch.randn(w["n_chains"], w["d"], generator=g).to(dev)
+    gen = torch.Generator(device=dev).manual_seed(w["seed"] + 100)
+    prod, secs, rates = PL.run_plain(w, vg, n_train, n_prod, x0, gen, timed_from=timed_from)
+    loops = n_train + n_prod - timed_from
+    out = {"value": w["n_chains"] * (w["n_local"] + w["n_global"]) * loops / secs, "unit": "chain-steps/s",
+           "loops_timed": loops, "n_training_loops": n_train, "n_production_loops": n_prod, "seconds": secs,
+           "acceptance": rates}
+    if ess and n_prod >= 2:
+        e = D.ess_bulk(prod)
+        out["min_ess"] = float(e.min())
+        out["min_ess_per_s"] = float(e.min()) / secs
+        out["moment_error"] = D.moment_error(prod, mean_ref, var_ref)
+    return out
+
+
 # ---------------------------------------------------------------- CPU baseline
 def cpu_baseline(name, w, budget_s: float = 20.0):
     """The oracle restatement (float64 NumPy, all host cores through BLAS)
@@ -259,6 +291,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ess", action="store_true")
     ap.add_argument("--chains", type=int, default=0, help="override n_chains (small profiling cases)")
+    ap.add_argument("--plain-loops", type=int, default=2,
+                    help="loops of the plain FP32 form timed for its chain-steps/s (0 = skip)")
+    ap.add_argument("--plain-full", action="store_true",
+                    help="run the plain FP32 form on the full schedule (min-ESS/s, moment error)")
     args = ap.parse_args()
     w = dict(WORKLOADS[args.workload])
     if args.chains > 0:
@@ -404,6 +440,18 @@ def main():
     }
     if e2e is not None:
         line["e2e"] = e2e
+    if rank == 0 and (args.plain_full or args.plain_loops > 0):
+        if args.plain_full:
+            pl = plain_arm(args.workload, w, dev, n_train, n_prod, W, mean_ref, var_ref)
+        else:
+            nt = max(1, args.plain_loops // 2)
+            pl = plain_arm(args.workload, w, dev, nt, args.plain_loops - nt, 0, mean_ref, var_ref, ess=False)
+        line["plain_fp32"] = pl
+        ratio = {"chain_steps_per_s": value / pl["value"]}
+        if "min_ess_per_s" in pl and "min_ess_per_s" in line:
+            ratio["min_ess_per_s"] = line["min_ess_per_s"] / pl["min_ess_per_s"]
+            ratio["moment_error_ratio"] = line["moment_error"] / pl["moment_error"]
+        line["fused_over_plain"] = ratio
     if rank == 0 and not args.no_cpu:
         try:
             line["cpu_baseline"] = cpu_baseline(args.workload, w)
