@@ -174,6 +174,49 @@ def measured_peaks():
     return 6800.0, 1900.0, 1700.0, "fallback"
 
 
+# ---------------------------------------------------------------- local-step HBM probe
+def local_hbm_probe(dev, chains=65536, steps=50, reps=5, lanes=(0,)):
+    """The local-step kernel alone on the cheap 64-D 4-mode mixture
+    (MALA and GRW, C chains x S steps, ~0.87 GB of buffer writes per launch):
+    algorithmic bytes 4d+8 per chain-step / CUDA-event time, against the HBM
+    peak. A derived probe of the mixture workload at a size the roofline can
+    resolve."""
+    import torch
+    from flowmc_gb300.resource.kernel.Gaussian_random_walk import GaussianRandomWalk
+    from flowmc_gb300.resource.kernel.MALA import MALA
+    from flowmc_gb300.resource.kernel.base import run_local_steps
+    t, _, _ = make_target("mixture64", WORKLOADS["mixture64"], dev)
+    d = t.n_dim
+    x0 = torch.randn(chains, d, device=dev)
+    pos = torch.empty(chains, steps, d, device=dev)
+    lp = torch.empty(chains, steps, device=dev)
+    acc = torch.empty(chains, steps, device=dev)
+    hbm = measured_peaks()[0]
+    out = {}
+    for name, k in (("mala", MALA(0.05)), ("grw", GaussianRandomWalk(0.05))):
+        best = None
+        for g in lanes:
+            k.lanes_per_chain = g
+            for _ in range(2):
+                run_local_steps(k, t, x0, steps, 1, 7, 0, pos, lp, acc, 0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            for r in range(reps):
+                run_local_steps(k, t, x0, steps, 1, 7, r + 1, pos, lp, acc, 0)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            gbs = chains * steps * (4 * d + 8) / (ms / 1e3) / 1e9
+            rec = {"lanes_per_chain": g, "ms_per_launch": ms, "achieved_gbs": gbs, "frac_hbm": gbs / hbm,
+                   "chain_steps_per_s": chains * steps / (ms / 1e3)}
+            if best is None or gbs > best["achieved_gbs"]:
+                best = rec
+        out[name] = best
+    out["config"] = f"64-D 4-mode mixture, {chains} chains x {steps} steps, bytes/chain-step {4 * d + 8}"
+    return out
+
+
 # ---------------------------------------------------------------- plain FP32 form
 def plain_arm(name, w, dev, n_train, n_prod, timed_from, mean_ref, var_ref, ess=True):
     """The plain FP32 PyTorch-eager form (flowmc_gb300.plain) on the same
@@ -293,6 +336,8 @@ def main():
     ap.add_argument("--chains", type=int, default=0, help="override n_chains (small profiling cases)")
     ap.add_argument("--plain-loops", type=int, default=2,
                     help="loops of the plain FP32 form timed for its chain-steps/s (0 = skip)")
+    ap.add_argument("--probe", default="", choices=["", "local"],
+                    help="run only the local-step HBM probe (a small profiling target)")
     ap.add_argument("--plain-full", action="store_true",
                     help="run the plain FP32 form on the full schedule (min-ESS/s, moment error)")
     args = ap.parse_args()
@@ -319,6 +364,10 @@ def main():
         dist.init_process_group("nccl", rank=rank, world_size=world)
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
+    if args.probe == "local":
+        print(json.dumps({"probe": "local_steps", **local_hbm_probe(dev, chains=w["n_chains"] if args.chains else 65536,
+                                                                     lanes=(0, 8, 16, 32))}), flush=True)
+        return
     W, K = max(1, args.warmup), max(1, args.steps)
     n_total = W + K
     n_train = max(W, n_total // 2)
@@ -419,6 +468,8 @@ def main():
         roof = {"bound": "tensor", "kernel": dom, "achieved": dk["achieved_tflops"], "peak": peak or bf16,
                 "unit": "TFLOP/s", "frac": dk["achieved_tflops"] / (peak or bf16), "traffic": None,
                 "peak_source": src if peak else f"{src} bf16 (this run used FP32 SIMT GEMMs)"}
+
+    kernels["local_steps_hbm_probe"] = local_hbm_probe(dev)
 
     # ---- end to end through the public API with host buffers
     e2e = None
