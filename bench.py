@@ -193,17 +193,20 @@ def local_hbm_probe(dev, chains=65536, steps=50, reps=5, lanes=(0,)):
     acc = torch.empty(chains, steps, device=dev)
     hbm = measured_peaks()[0]
     out = {}
-    for name, k in (("mala", MALA(0.05)), ("grw", GaussianRandomWalk(0.05))):
+    from flowmc_gb300 import targets as TG
+    diag = TG.DiagGaussian(d, device=dev)
+    for name, k, tt in (("mala", MALA(0.05), t), ("grw", GaussianRandomWalk(0.05), t),
+                        ("grw_diag_gaussian", GaussianRandomWalk(0.5), diag)):
         best = None
         for g in lanes:
             k.lanes_per_chain = g
             for _ in range(2):
-                run_local_steps(k, t, x0, steps, 1, 7, 0, pos, lp, acc, 0)
+                run_local_steps(k, tt, x0, steps, 1, 7, 0, pos, lp, acc, 0)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             torch.cuda.synchronize()
             e0.record()
             for r in range(reps):
-                run_local_steps(k, t, x0, steps, 1, 7, r + 1, pos, lp, acc, 0)
+                run_local_steps(k, tt, x0, steps, 1, 7, r + 1, pos, lp, acc, 0)
             e1.record()
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1) / reps
@@ -213,7 +216,8 @@ def local_hbm_probe(dev, chains=65536, steps=50, reps=5, lanes=(0,)):
             if best is None or gbs > best["achieved_gbs"]:
                 best = rec
         out[name] = best
-    out["config"] = f"64-D 4-mode mixture, {chains} chains x {steps} steps, bytes/chain-step {4 * d + 8}"
+    out["config"] = (f"64-D 4-mode mixture (mala, grw) and 64-D diagonal Gaussian (grw_diag_gaussian), "
+                     f"{chains} chains x {steps} steps, bytes/chain-step {4 * d + 8}")
     return out
 
 

@@ -64,21 +64,15 @@ void count_launch();  // process-wide tally of kernel launches (fmc_launch_count
 // the Weyl key schedule). counter = 4 x u32, key = 2 x u32.
 struct u32x4 { uint32_t x, y, z, w; };
 
-__host__ __device__ __forceinline__ uint32_t mulhi32(uint32_t a, uint32_t b) {
-#ifdef __CUDA_ARCH__
-  return __umulhi(a, b);
-#else
-  return (uint32_t)(((uint64_t)a * b) >> 32);
-#endif
-}
-
 __host__ __device__ __forceinline__ u32x4 philox4x32_10(u32x4 c, uint32_t k0, uint32_t k1) {
   const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
   const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
 #pragma unroll
   for (int r = 0; r < 10; ++r) {
-    const uint32_t hi0 = mulhi32(M0, c.x), lo0 = M0 * c.x;
-    const uint32_t hi1 = mulhi32(M1, c.z), lo1 = M1 * c.z;
+    // one 32x32 -> 64-bit multiply gives both halves of each product
+    const uint64_t p0 = (uint64_t)M0 * c.x, p1 = (uint64_t)M1 * c.z;
+    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
     c = u32x4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
     k0 += W0;
     k1 += W1;
@@ -95,7 +89,10 @@ __device__ __forceinline__ float u32_to_unit(uint32_t v) {
 __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float& z0, float& z1) {
   const float u1 = u32_to_unit(a);
   const float u2 = u32_to_unit(b);
-  const float r = sqrtf(-2.0f * __logf(u1));
+  // radius sqrt(-2 ln u1) as t * rsqrt(t) (two instructions instead of the
+  // IEEE square root); u1 = 1 gives t = 0 and r = 0
+  const float t = -2.0f * __logf(u1);
+  const float r = (t > 0.f) ? t * rsqrtf(t) : 0.f;
   float s, c;
   // angle 2*pi*u2 - pi keeps the argument inside [-pi, pi] for __sincosf
   __sincosf(6.28318530717958647692f * u2 - 3.14159265358979323846f, &s, &c);

@@ -61,6 +61,13 @@ int make_geom(const FmcFlow* f, FlowGeom& g) {
       o16 += (int64_t)g.w16t_rows(l, i) * g.w16t_cols(l, i);
     }
   g.w16t_off[g.L * (g.nh + 1)] = o16;
+  g.spl_dg = 256 / g.P;
+  g.spl_bn = ((g.spl_dg * g.P + 15) / 16) * 16;
+  for (int l = 0; l < g.L; ++l) {
+    g.w16g_off[l] = o16;
+    o16 += (int64_t)g.spl_groups(l) * g.spl_bn * g.w16_cols(l, g.nh);
+  }
+  g.w16g_off[g.L] = o16;
   g.n_w16 = o16;
   return FMC_OK;
 }
@@ -160,7 +167,7 @@ static int rows_grid(int64_t m) {
 // ------------------------------------------------------------------ workspace
 struct InferWs {
   int64_t rows;   // chunk rows
-  float *xa, *cond, *h0, *h1, *raw, *ld;
+  float *xa, *cond, *h0, *h1, *raw, *ld, *ldp;
   uint16_t *cond16, *h16a, *h16b;  // BF16 operands
 };
 
@@ -177,7 +184,8 @@ static int64_t infer_chunk_rows(const FlowGeom& g, int64_t n) {
 }
 
 static size_t infer_ws_bytes(const FlowGeom& g, int64_t rows) {
-  const int64_t f = rows * ((int64_t)g.d + g.nc_max() + 2 * g.h_max() + (int64_t)g.nt_max() * g.P + 1);
+  const int64_t ldp = 2 * (int64_t)((g.nt_max() + g.spl_dg - 1) / g.spl_dg);
+  const int64_t f = rows * ((int64_t)g.d + g.nc_max() + 2 * g.h_max() + (int64_t)g.nt_max() * g.P + 1 + ldp);
   const int64_t b16 = rows * (align_up(g.nc_max(), 64) + 2 * align_up(g.h_max(), 64));
   return (size_t)(4 * f + 2 * b16 + 16 * 256);
 }
@@ -196,6 +204,7 @@ static void carve_infer(const FlowGeom& g, int64_t rows, void* ws, InferWs& w) {
   w.h1 = (float*)take(4 * rows * g.h_max());
   w.raw = (float*)take(4 * rows * (int64_t)g.nt_max() * g.P);
   w.ld = (float*)take(4 * rows);
+  w.ldp = (float*)take(4 * rows * 2 * (int64_t)((g.nt_max() + g.spl_dg - 1) / g.spl_dg));
   w.cond16 = (uint16_t*)take(2 * rows * align_up(g.nc_max(), 64));
   w.h16a = (uint16_t*)take(2 * rows * align_up(g.h_max(), 64));
   w.h16b = (uint16_t*)take(2 * rows * align_up(g.h_max(), 64));
@@ -228,16 +237,24 @@ static int conditioner(const FmcFlow* f, const FlowGeom& g, int l, int64_t m, In
 static int flow_pass(const FmcFlow* f, const FlowGeom& g, const float* x, float* y, float* ld, int64_t m, bool inverse,
                      InferWs& w, cudaStream_t st) {
   const int grid = ew_grid(m * g.d);
+  const bool bf16 = f->precision == FMC_PREC_BF16;
   for (int u = 0; u < g.L; ++u) {
     const int l = inverse ? g.L - 1 - u : u;
     const float* src = (u == 0) ? x : y;
     k_affine<<<grid, 256, 0, st>>>(src, y, w.cond, m, g.d, g.nc(l), g.cpar(l), f->theta + g.layer_off[l],
                                    inverse ? 1 : 0, ld, u == 0 ? 1 : 0);
     FMC_LAUNCH_CHECK();
-    int rc = conditioner(f, g, l, m, w, st);
-    if (rc) return rc;
-    rc = launch_spline(g.K, inverse, st, w.raw, y, ld, m, g.d, g.nt(l), g.tpar(l), g.cfg);
-    if (rc) return rc;
+    int rc;
+    if (bf16) {
+      // hidden layers on tcgen05, then the last Linear fused with the spline
+      const uint16_t* h_last = nullptr;
+      if ((rc = conditioner_bf16_hidden(f, g, l, m, w.cond, w.cond16, w.h16a, w.h16b, &h_last, st))) return rc;
+      const int64_t rows = (m + 127) / 128 * 128;
+      if ((rc = tc_linear_spline(st, g, f, l, h_last, m, rows, inverse, y, ld, w.ldp))) return rc;
+    } else {
+      if ((rc = conditioner(f, g, l, m, w, st))) return rc;
+      if ((rc = launch_spline(g.K, inverse, st, w.raw, y, ld, m, g.d, g.nt(l), g.tpar(l), g.cfg))) return rc;
+    }
   }
   return FMC_OK;
 }

@@ -17,6 +17,11 @@ struct FlowGeom {
   int64_t w16_off[FMC_MAX_LAYERS * (FMC_MAX_HIDDEN + 1) + 1];
   // transposed copies W_i^T as [round_up(in, 256), round_up(out, 64)] (training)
   int64_t w16t_off[FMC_MAX_LAYERS * (FMC_MAX_HIDDEN + 1) + 1];
+  // the last Linear of each layer re-packed in spline groups (fused inference
+  // kernel, tc_spline.cu): group g = DG transformed coordinates x P rows,
+  // padded to BN rows; [n_groups(l) * BN, round_up(H_last, 64)]
+  int64_t w16g_off[FMC_MAX_LAYERS + 1];
+  int spl_dg, spl_bn;
   int64_t n_w16;
 
   // conditioning coordinates of layer l: j = 2k + cpar(l); transformed: j = 2k + tpar(l)
@@ -44,6 +49,7 @@ struct FlowGeom {
   __host__ __device__ int w16_rows(int l, int i) const { return (int)rup(lin_out(l, i), 256); }
   __host__ __device__ int w16_cols(int l, int i) const { return (int)rup(lin_in(l, i), 64); }
   __host__ __device__ int w16t_rows(int l, int i) const { return (int)rup(lin_in(l, i), 256); }
+  __host__ __device__ int spl_groups(int l) const { return (nt(l) + spl_dg - 1) / spl_dg; }
   __host__ __device__ int w16t_cols(int l, int i) const { return (int)rup(lin_out(l, i), 64); }
 };
 

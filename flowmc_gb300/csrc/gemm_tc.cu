@@ -25,7 +25,11 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 // 2-D bf16 tensor [outer, inner] with row stride ld (elements), box {64, box_outer}, 128B swizzle
+int make_tma_map_bf16(CUtensorMap* m, const void* base, int64_t inner, int64_t outer, int64_t ld, int box_outer);
 static int make_map(CUtensorMap* m, const void* base, int64_t inner, int64_t outer, int64_t ld, int box_outer) {
+  return make_tma_map_bf16(m, base, inner, outer, ld, box_outer);
+}
+int make_tma_map_bf16(CUtensorMap* m, const void* base, int64_t inner, int64_t outer, int64_t ld, int box_outer) {
   auto fn = encode_fn();
   FMC_CHECK_SUPPORTED(fn != nullptr, "cuTensorMapEncodeTiled is unavailable");
   FMC_CHECK_ARG(((uintptr_t)base & 15) == 0, "TMA base address must be 16-byte aligned");
@@ -99,8 +103,28 @@ int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K
 // ------------------------------------------------------------------ packing
 __global__ void k_pack_bf16(FlowGeom g, const float* __restrict__ theta, uint16_t* __restrict__ w16) {
   const int nseg = g.L * (g.nh + 1);
+  if ((int)blockIdx.y >= 2 * nseg) {
+    // grouped copy of layer l's last Linear for the fused spline kernel
+    const int l = blockIdx.y - 2 * nseg;
+    const int i = g.nh, in = g.lin_in(l, i), nt = g.nt(l);
+    const int cols = g.w16_cols(l, i), DG = g.spl_dg, BN = g.spl_bn;
+    const int rows = g.spl_groups(l) * BN;
+    const float* W = theta + g.layer_off[l] + g.lin_w(l, i);
+    uint16_t* dst = w16 + g.w16g_off[l];
+    const int64_t tot = (int64_t)rows * cols;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+      const int r = (int)(e / cols), c = (int)(e - (int64_t)r * cols);
+      const int grp = r / BN, rr = r - grp * BN;
+      const int u = rr / g.P, p = rr - u * g.P;
+      const int t = grp * DG + u;
+      float v = 0.f;
+      if (u < DG && t < nt && c < in) v = W[((int64_t)t * g.P + p) * in + c];
+      dst[e] = f32_to_bf16_rn(v);
+    }
+    return;
+  }
   const int seg = blockIdx.y % nseg;
-  const bool tr = blockIdx.y >= nseg;   // second half of the grid writes W^T
+  const bool tr = blockIdx.y >= nseg;   // second part of the grid writes W^T
   const int l = seg / (g.nh + 1), i = seg % (g.nh + 1);
   const int out = g.lin_out(l, i), in = g.lin_in(l, i);
   const int rows = tr ? g.w16t_rows(l, i) : g.w16_rows(l, i);
@@ -119,7 +143,7 @@ __global__ void k_pack_bf16(FlowGeom g, const float* __restrict__ theta, uint16_
 
 int pack_bf16_weights(const FlowGeom& g, const float* theta, uint16_t* w16, cudaStream_t st) {
   const int segs = g.L * (g.nh + 1);
-  dim3 grid(64, 2 * segs);
+  dim3 grid(64, 2 * segs + g.L);
   k_pack_bf16<<<grid, 256, 0, st>>>(g, theta, w16);
   FMC_LAUNCH_CHECK();
   return FMC_OK;
@@ -164,6 +188,35 @@ __global__ void k_to_bf16_pad(const float* __restrict__ a, int64_t m, int n, int
     const int c = (int)(e - r * ld);
     b[e] = (c < n) ? f32_to_bf16_rn(a[r * n + c]) : (uint16_t)0;
   }
+}
+
+int conditioner_bf16_hidden(const FmcFlow* f, const FlowGeom& g, int l, int64_t m, const float* cond,
+                            uint16_t* cond16, uint16_t* h16a, uint16_t* h16b, const uint16_t** h_last,
+                            cudaStream_t st) {
+  const int64_t rows = (m + tc::BM - 1) / tc::BM * tc::BM;
+  const int nc = g.nc(l), ncp = g.w16_cols(l, 0);
+  {
+    int64_t blocks = (m * ncp + 255) / 256;
+    if (blocks > (int64_t)sm_count() * 16) blocks = (int64_t)sm_count() * 16;
+    k_to_bf16_pad<<<(int)blocks, 256, 0, st>>>(cond, m, nc, ncp, cond16);
+    FMC_LAUNCH_CHECK();
+  }
+  const float* th = f->theta + g.layer_off[l];
+  const uint16_t* a = cond16;
+  uint16_t* hbuf[2] = {h16a, h16b};
+  for (int i = 0; i < g.nh; ++i) {
+    const int seg = l * (g.nh + 1) + i;
+    const int K = g.w16_cols(l, i), N = g.lin_out(l, i);
+    tc::EpiArgs ep{};
+    ep.bias = th + g.lin_b(l, i);
+    const int ldo = (int)FlowGeom::rup(N, 64);
+    int rc = tc_gemm(st, a, m, rows, K, f->theta_bf16 + g.w16_off[seg], N, g.w16_rows(l, i), ep, hbuf[i & 1], ldo, ldo,
+                     tc::TC_EPI_TANH_BF16);
+    if (rc) return rc;
+    a = hbuf[i & 1];
+  }
+  *h_last = a;
+  return FMC_OK;
 }
 
 int conditioner_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t m, const float* cond, uint16_t* cond16,

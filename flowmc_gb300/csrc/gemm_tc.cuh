@@ -34,6 +34,16 @@ int conditioner_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t m, cons
 
 size_t train_ws_bytes(const FlowGeom& g, int64_t n);
 
+// the conditioner's hidden layers only (conversion + tanh GEMMs); *h_last is
+// the last tanh activation (bf16 [round_up(m, 128), round_up(H_last, 64)])
+int conditioner_bf16_hidden(const FmcFlow* f, const FlowGeom& g, int l, int64_t m, const float* cond,
+                            uint16_t* cond16, uint16_t* h16a, uint16_t* h16b, const uint16_t** h_last,
+                            cudaStream_t st);
+
+// the last Linear of layer l fused with the spline (tc_spline.cu)
+int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l, const uint16_t* A, int64_t M,
+                     int64_t rows_a, bool inverse, float* xa, float* ld, float* ldp);
+
 // theta (fp32, packed) -> zero-padded bf16 weight segments (FlowGeom::w16_off)
 // and their transposes (FlowGeom::w16t_off)
 int pack_bf16_weights(const FlowGeom& g, const float* theta, uint16_t* w16, cudaStream_t st);

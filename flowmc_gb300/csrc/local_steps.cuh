@@ -86,9 +86,14 @@ __device__ __forceinline__ void draw_normals(const LocalArgs& a, int64_t c, int 
     if (gl * V + v >= d) xi[v] = 0.f;
 }
 
-__device__ __forceinline__ float draw_uniform(const LocalArgs& a, int64_t c, int s) {
+// Uniforms come four steps per Philox call: draws are refreshed on steps
+// s = 0 mod 4 (every lane of the group computes the same call, so the group
+// agrees on u) and consumed from `ub`.
+__device__ __forceinline__ float draw_uniform(const LocalArgs& a, int64_t c, int s, u32x4& ub) {
   if (a.unif) return __ldcs(a.unif + (int64_t)c * a.S + s);
-  return u32_to_unit(a.rng.draw(c, s, 0u, RNG_TAG_LOCAL_UNIFORM).x);
+  if ((s & 3) == 0) ub = a.rng.draw(c, (uint64_t)(s >> 2), 0u, RNG_TAG_LOCAL_UNIFORM);
+  const int r = s & 3;
+  return u32_to_unit(r == 0 ? ub.x : r == 1 ? ub.y : r == 2 ? ub.z : ub.w);
 }
 
 template <int G, int V>
@@ -147,10 +152,11 @@ __global__ void __launch_bounds__(256) k_local_steps(const LocalArgs a) {
 #pragma unroll
     for (int v = 0; v < V; ++v) xr[v] = x[v];
 
+    u32x4 ub{0u, 0u, 0u, 0u};
     for (int s = 0; s < a.S; ++s) {
       float xi[V];
       draw_normals<V>(a, cc, s, gl, xi);
-      const float logu = logf(draw_uniform(a, cc, s));
+      const float logu = logf(draw_uniform(a, cc, s, ub));
       bool acc;
       if constexpr (KIND == FMC_KERNEL_MALA) {
         const float dt2 = dt * dt;

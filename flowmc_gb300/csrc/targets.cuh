@@ -81,52 +81,58 @@ __device__ __forceinline__ float tg_dual_moon(const FmcTarget& t, const float (&
 
 // --------------------------------------------------------------- Gaussian mixture
 // log p = logsumexp_k( log_w[k] - 0.5 sum_j (x_j - mean[k,j])^2 inv_var[k,j] )
+// One pass over the components with an online log-sum-exp: running max m,
+// running sum S = sum_k exp(e_k - m) and the running weighted gradient
+// Gr = sum_k exp(e_k - m) * (-(x - mean_k) inv_var_k), rescaled whenever m
+// grows; at the end lp = m + log S and grad = Gr / S. No per-component
+// arrays, so the loop stays rolled and register use stays flat in K.
 template <int G, int V, bool GRAD>
 __device__ __forceinline__ float tg_mixture(const FmcTarget& t, const float (&x)[V],
                                             float (&g)[V], int gl) {
   const int d = t.n_dim, K = t.n_comp;
-  float e[kMaxMixtureComponents];
-  float emax = -INFINITY;
+  float m = -INFINITY, S = 0.f;
+  float Gr[V];
 #pragma unroll
-  for (int k = 0; k < kMaxMixtureComponents; ++k) {
-    if (k < K) {
-      float q = 0.f;
+  for (int v = 0; v < V; ++v) Gr[v] = 0.f;
+#pragma unroll 1
+  for (int k = 0; k < K; ++k) {
+    float q = 0.f;
+    float gk[V];
 #pragma unroll
-      for (int v = 0; v < V; ++v) {
-        const int j = gl * V + v;
-        if (j < d) {
-          const float dx = x[v] - ldg_or(t.mean, (int64_t)k * d + j, 0.f);
-          q += dx * dx * ldg_or(t.inv_var, (int64_t)k * d + j, 1.f);
-        }
+    for (int v = 0; v < V; ++v) {
+      const int j = gl * V + v;
+      gk[v] = 0.f;
+      if (j < d) {
+        const float dx = x[v] - ldg_or(t.mean, (int64_t)k * d + j, 0.f);
+        const float iv = ldg_or(t.inv_var, (int64_t)k * d + j, 1.f);
+        q += dx * dx * iv;
+        gk[v] = -dx * iv;
       }
-      e[k] = ldg_or(t.log_w, k, 0.f) - 0.5f * group_sum<G>(q);
-      emax = fmaxf(emax, e[k]);
+    }
+    const float e = ldg_or(t.log_w, k, 0.f) - 0.5f * group_sum<G>(q);
+    if (e > m) {
+      const float r = expf(m - e);   // 0 on the first component (m = -inf)
+      S = S * r + 1.f;
+      if (GRAD) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) Gr[v] = Gr[v] * r + gk[v];
+      }
+      m = e;
+    } else {
+      const float w = expf(e - m);
+      S += w;
+      if (GRAD) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) Gr[v] += w * gk[v];
+      }
     }
   }
-  float ssum = 0.f;
-#pragma unroll
-  for (int k = 0; k < kMaxMixtureComponents; ++k)
-    if (k < K) ssum += expf(e[k] - emax);
-  const float lse = emax + logf(ssum);
   if (GRAD) {
+    const float inv = 1.f / S;
 #pragma unroll
-    for (int v = 0; v < V; ++v) g[v] = 0.f;
-#pragma unroll
-    for (int k = 0; k < kMaxMixtureComponents; ++k) {
-      if (k < K) {
-        const float w = expf(e[k] - lse);
-#pragma unroll
-        for (int v = 0; v < V; ++v) {
-          const int j = gl * V + v;
-          if (j < d) {
-            const float dx = x[v] - ldg_or(t.mean, (int64_t)k * d + j, 0.f);
-            g[v] -= w * dx * ldg_or(t.inv_var, (int64_t)k * d + j, 1.f);
-          }
-        }
-      }
-    }
+    for (int v = 0; v < V; ++v) g[v] = Gr[v] * inv;
   }
-  return lse;
+  return m + logf(S);
 }
 
 // --------------------------------------------------------------- Rosenbrock chain

@@ -116,7 +116,10 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
       : "r"(taddr));
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+  for (int i = 0; i < 32; ++i) {
+    asm volatile("" : "+r"(r[i]));   // keep every use after the wait
+    v[i] = __uint_as_float(r[i]);
+  }
 }
 
 __device__ __forceinline__ float tanh_fast(float x) {
