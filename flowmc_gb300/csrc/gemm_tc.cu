@@ -10,6 +10,12 @@ namespace fmc {
 
 __device__ int g_tc_error = 0;   // set by a tcgen05 kernel whose bounded wait expired
 
+// device address of g_tc_error (kernels of other files get it through this)
+int tc_error_word(int** out) {
+  FMC_CUDA_TRY(cudaGetSymbolAddress((void**)out, g_tc_error));
+  return FMC_OK;
+}
+
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   static std::once_flag once;

@@ -220,7 +220,7 @@ __global__ void k_ld_reduce(const float* __restrict__ ldp, int n_part, int64_t m
   }
 }
 
-extern __device__ int g_tc_error;
+int tc_error_word(int** out);
 int make_tma_map_bf16(CUtensorMap* m, const void* base, int64_t inner, int64_t outer, int64_t ld, int box_outer);
 
 int spline_groups(int K_bins, int nt, int* dg, int* bn) {
@@ -243,7 +243,8 @@ static int launch_spl(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap&
     attr = true;
   }
   int* err = nullptr;
-  FMC_CUDA_TRY(cudaGetSymbolAddress((void**)&err, g_tc_error));
+  int rc = tc_error_word(&err);
+  if (rc) return rc;
   const int64_t tiles = (M + tc::BM - 1) / tc::BM * n_groups;
   const int64_t grid = tiles < sm_count() ? tiles : sm_count();
   kern<<<(unsigned)grid, tc::kSplThreads, S::TOTAL, st>>>(ma, mb, (int)M, n_groups, nt, K, bias, xa, d, tpar, ldp,
