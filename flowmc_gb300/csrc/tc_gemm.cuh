@@ -33,7 +33,7 @@ namespace tc {
 
 constexpr int BM = 128;
 constexpr int BK = 64;                 // bf16 elements per 128-byte swizzle row
-constexpr int kEpiWarps = 4;
+constexpr int kEpiWarps = 8;   // two per TMEM lane quarter
 constexpr int kThreads = 64 + 32 * kEpiWarps;
 
 // epilogue modes and arguments: see gemm_tc.cuh
@@ -61,11 +61,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// bounded wait: ~1 s at most, then false
+// bounded wait: try_wait itself suspends the thread for a short hardware
+// window, so spin on it first; after 2^16 tries back off with short sleeps.
+// Gives up after roughly one second and returns false.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (uint32_t it = 0; it < (1u << 22); ++it) {
+  for (uint32_t it = 0; it < (1u << 16); ++it)
     if (mbar_try_wait(bar, parity)) return true;
-    if (it > 64) __nanosleep(256);
+  for (uint32_t it = 0; it < (1u << 23); ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    __nanosleep(128);
   }
   return false;
 }
@@ -255,12 +259,15 @@ __global__ void __launch_bounds__(kThreads, 1)
       mma_commit(mma_done);
     }
   } else {
-    // epilogue warps: TMEM lane quarter = warp % 4, one accumulator row per thread
+    // epilogue warps: TMEM lane quarter = warp % 4, one accumulator row per
+    // thread; the two warps of a quarter take alternate 32-column chunks
     const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
     const int row = q * 32 + lane;
     // vector stores only when every row start is 16-byte aligned
     const int esz = (EPI == TC_EPI_TANH_BF16 || EPI == TC_EPI_DTANH_BF16) ? 2 : 4;
     const bool vec_ok = (((uintptr_t)C & 15) == 0) && ((ldc * esz) % 16 == 0);
+    const bool aux_vec = (((uintptr_t)ep.aux & 15) == 0) && ((ep.ldaux * 2) % 16 == 0);
     int local = 0;
     for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++local) {
       const int b = local & 1, use = local >> 1;
@@ -275,7 +282,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       const bool ct_row = ep.ct != nullptr && gm < ep.ct_rows_pad;
       const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN);
 #pragma unroll 1
-      for (int c0 = 0; c0 < BN; c0 += 32) {
+      for (int c0 = half * 32; c0 < BN; c0 += 64) {
         float v[32];
         tmem_ld32(tbase + (uint32_t)c0, v);
         const int gn0 = n0 + c0;
@@ -291,11 +298,19 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
           } else {
             const uint16_t* ar = ep.aux + (int64_t)gm * ep.ldaux + gn0;
+            uint16_t hv[32];
+            if (row_ok && aux_vec && gn0 + 32 <= N) {
+              const uint4* a4 = reinterpret_cast<const uint4*>(ar);
+#pragma unroll
+              for (int i = 0; i < 4; ++i) *reinterpret_cast<uint4*>(&hv[8 * i]) = __ldg(a4 + i);
+            } else {
+#pragma unroll
+              for (int i = 0; i < 32; ++i) hv[i] = (row_ok && gn0 + i < N) ? ar[i] : (uint16_t)0;
+            }
 #pragma unroll
             for (int i = 0; i < 32; ++i) {
               const int j = gn0 + i;
-              float h = 0.f;
-              if (j < N && row_ok) h = __uint_as_float((uint32_t)ar[i] << 16);
+              const float h = __uint_as_float((uint32_t)hv[i] << 16);
               y[i] = (j < N && row_ok) ? v[i] * (1.f - h * h) : 0.f;
             }
           }
