@@ -16,3 +16,4 @@ from .resource.optimizer import Optimizer  # noqa: F401
 from .strategy.train_model import TrainModel  # noqa: F401
 from .resource_strategy_bundle.RQSpline_MALA import RQSpline_MALA_Bundle  # noqa: F401
 from .Sampler import Sampler  # noqa: F401
+from . import batched  # noqa: F401

@@ -111,6 +111,26 @@ FMC_API int fmc_local_steps(const FmcTarget* target, const FmcLocalParams* param
                     int64_t buf_len, int64_t cursor,
                     float* x_last, float* lp_last, void* stream);
 
+/* Many dense-Gaussian targets of uneven dimension (1..256) in ONE persistent
+ * launch: n_steps of MALA or HMC (identity mass) for every chain of every
+ * target, chain tiles pulled by CTAs from an atomic work counter. The local
+ * steps of TakeSerialSteps (strategy/take_steps.py:156-180) with MALA.kernel /
+ * HMC.kernel (resource/kernel/MALA.py:26-89, HMC.py:98-151), batched across
+ * targets. Host arrays (length n_targets): targets, n_chains, step_sizes,
+ * noise/unif (device pointers, each may be NULL; or the array pointer NULL
+ * for Philox), out_pos/out_logp/out_acc (device pointers to each target's
+ * buffers [n_chains_t, buf_len, d_t] / [n_chains_t, buf_len]).
+ * x0, x_last: [sum_t n_chains_t, 256] (row stride 256, target t's chains
+ * from row sum_{u<t} n_chains_u); lp_last [sum_t n_chains_t]. */
+FMC_API int fmc_batched_workspace_size(int32_t n_targets, int64_t total_chains, size_t* bytes);
+FMC_API int fmc_batched_dense_local_steps(const FmcTarget* targets, int32_t n_targets, const int32_t* n_chains,
+                                          const FmcLocalParams* params, const float* step_sizes, const float* x0,
+                                          int32_t n_steps, int32_t thinning, uint64_t seed, uint64_t counter,
+                                          const float* const* noise, const float* const* unif,
+                                          float* const* out_pos, float* const* out_logp, float* const* out_acc,
+                                          int64_t buf_len, int64_t cursor, float* x_last, float* lp_last,
+                                          void* ws, size_t ws_bytes, void* stream);
+
 /* Evaluate a registered target (value and gradient) on a batch.
  * Replaces jax.vmap(jax.value_and_grad(LogPDF)) (resource/logPDF.py:225-226).
  *   x [n, n_dim] -> logp [n], grad [n, n_dim] (grad may be NULL). */
