@@ -94,7 +94,7 @@ def build_sampler(name, w, n_train, n_prod, precision, device):
                                   w["n_epochs"], mala_step_size=w["step"], rq_spline_hidden_units=w["hidden"],
                                   rq_spline_n_bins=w["n_bins"], rq_spline_n_layers=w["n_layers"],
                                   learning_rate=w["lr"], batch_size=w["batch"], n_max_examples=w["n_max"],
-                                  local_sampler=local, precision=precision, device=device)
+                                  local_sampler=local, precision=precision, device=device, autotune=True)
     sampler = Sampler(w["d"], w["n_chains"], key, resource_strategy_bundles=bundle)
     g = torch.Generator().manual_seed(w["seed"])
     x0 = torch.randn(w["n_chains"], w["d"], generator=g)

@@ -1,0 +1,59 @@
+"""Autotuner for the chain-block shape of the fused local-step kernel.
+
+The local-step kernel assigns each chain to a group of G lanes (4, 8, 16 or
+32) holding V = next_pow2(d / G) coordinates each. Which G is fastest depends
+on the kernel kind, the target's cost per coordinate and the number of
+chains (occupancy versus shuffle depth), so it is measured: each candidate
+runs a short probe of the real launch (same target, chain count and kernel,
+a few steps into a scratch buffer), timed with CUDA events, and the fastest
+is cached per (kernel kind, target kind, dimension, chain count) and written
+to ``kernel.lanes_per_chain``.
+"""
+from __future__ import annotations
+
+import torch
+
+_cache: dict = {}
+
+
+def candidates(d: int) -> list[int]:
+    out = []
+    for g in (4, 8, 16, 32):
+        v = 1
+        while g * v < d:
+            v *= 2
+        if v <= 8:
+            out.append(g)
+    return out
+
+
+def tune_local_kernel(kernel, target, n_chains: int, probe_steps: int = 8, reps: int = 3) -> int:
+    """Pick lanes_per_chain for (kernel, target, n_chains); returns it."""
+    from .resource.kernel.base import run_local_steps
+    d = target.n_dim
+    key = (type(kernel).__name__, target.kind, d, n_chains, getattr(kernel, "n_leapfrog", 0))
+    if key in _cache:
+        kernel.lanes_per_chain = _cache[key]
+        return _cache[key]
+    dev = target.device if target.device.type == "cuda" else torch.device("cuda")
+    x0 = torch.randn(n_chains, d, device=dev) * 0.1
+    pos = torch.empty(n_chains, probe_steps, d, device=dev)
+    lp = torch.empty(n_chains, probe_steps, device=dev)
+    acc = torch.empty(n_chains, probe_steps, device=dev)
+    saved = kernel.lanes_per_chain
+    best, best_ms = saved, float("inf")
+    for g in candidates(d):
+        kernel.lanes_per_chain = g
+        run_local_steps(kernel, target, x0, probe_steps, 1, 1, 0, pos, lp, acc, 0)   # warm
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for r in range(reps):
+            run_local_steps(kernel, target, x0, probe_steps, 1, 1, r, pos, lp, acc, 0)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        if ms < best_ms:
+            best, best_ms = g, ms
+    kernel.lanes_per_chain = best
+    _cache[key] = best
+    return best

@@ -68,17 +68,28 @@ __device__ __forceinline__ void draw_normals(const LocalArgs& a, int64_t c, int 
     }
     return;
   }
+  // Coordinate j takes component (j & 3) of the Philox block keyed by j & ~3:
+  // (x, y) -> Box-Muller -> j&3 = 0, 1 and (z, w) -> j&3 = 2, 3. The stream
+  // depends on (chain, step, coordinate) only, never on the lane-group shape,
+  // so every (G, V) choice samples the same chains.
+  if constexpr (V >= 4) {
 #pragma unroll
-  for (int q = 0; q < V; q += 4) {
-    const u32x4 r = a.rng.draw(c, s, (uint32_t)(gl * V + q), RNG_TAG_LOCAL_NORMAL);
-    float z0, z1, z2, z3;
-    box_muller(r.x, r.y, z0, z1);
-    xi[q] = z0;
-    if (q + 1 < V) xi[q + 1] = z1;
-    if (q + 2 < V) {
-      box_muller(r.z, r.w, z2, z3);
-      xi[q + 2] = z2;
-      if (q + 3 < V) xi[q + 3] = z3;
+    for (int q = 0; q < V; q += 4) {
+      const u32x4 r = a.rng.draw(c, s, (uint32_t)(gl * V + q), RNG_TAG_LOCAL_NORMAL);
+      box_muller(r.x, r.y, xi[q], xi[q + 1]);
+      box_muller(r.z, r.w, xi[q + 2], xi[q + 3]);
+    }
+  } else {
+    const int j = gl * V;   // V = 2: j is even
+    const u32x4 r = a.rng.draw(c, s, (uint32_t)(j & ~3), RNG_TAG_LOCAL_NORMAL);
+    const bool hi = (j & 2) != 0;
+    float z0, z1;
+    box_muller(hi ? r.z : r.x, hi ? r.w : r.y, z0, z1);
+    if constexpr (V == 1) {
+      xi[0] = (j & 1) ? z1 : z0;
+    } else {
+      xi[0] = z0;
+      xi[1] = z1;
     }
   }
 #pragma unroll

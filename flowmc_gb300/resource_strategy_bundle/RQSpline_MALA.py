@@ -8,6 +8,7 @@ reference's behaviour):
   precision          "float32" (default) or "bf16" conditioner GEMMs
   history_window     TrainModel's per-chain window (the reference fixes 100)
   device             where buffers and the flow live
+  autotune           measure the local kernel's chain-block shape on first use
 """
 from __future__ import annotations
 
@@ -39,7 +40,7 @@ class RQSpline_MALA_Bundle(ResourceStrategyBundle):
                  rq_spline_n_layers: int = 4, learning_rate: float = 1e-3, batch_size: int = 10000,
                  n_max_examples: int = 10000, local_thinning: int = 1, global_thinning: int = 1,
                  n_NFproposal_batch_size: int = 10000, verbose: bool = False, local_sampler=None,
-                 precision: str = "float32", history_window: int = 100, device=None):
+                 precision: str = "float32", history_window: int = 100, device=None, autotune: bool = False):
         n_training_steps = (n_local_steps // local_thinning * n_training_loops
                             + n_global_steps // global_thinning * n_training_loops)
         n_production_steps = (n_local_steps // local_thinning * n_production_loops
@@ -93,7 +94,8 @@ class RQSpline_MALA_Bundle(ResourceStrategyBundle):
 
         local_stepper = TakeSerialSteps("logpdf", "local_sampler", "sampler_state",
                                         ["target_positions", "target_log_prob", "target_local_accs"], n_local_steps,
-                                        thinning=local_thinning, chain_batch_size=chain_batch_size, verbose=verbose)
+                                        thinning=local_thinning, chain_batch_size=chain_batch_size, verbose=verbose,
+                                        autotune=autotune)
         global_stepper = TakeGroupSteps("logpdf", "global_sampler", "sampler_state",
                                         ["target_positions", "target_log_prob", "target_global_accs"],
                                         n_global_steps, thinning=global_thinning, chain_batch_size=chain_batch_size,

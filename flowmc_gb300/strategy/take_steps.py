@@ -36,7 +36,8 @@ class TakeSteps(Strategy):
     verbose: bool
 
     def __init__(self, logpdf_name: str, kernel_name: str, state_name: str, buffer_names: list,
-                 n_steps: int, thinning: int = 1, chain_batch_size: int = 0, verbose: bool = False):
+                 n_steps: int, thinning: int = 1, chain_batch_size: int = 0, verbose: bool = False,
+                 autotune: bool = False):
         self.logpdf_name = logpdf_name
         self.kernel_name = kernel_name
         self.state_name = state_name
@@ -46,6 +47,8 @@ class TakeSteps(Strategy):
         self.thinning = thinning
         self.chain_batch_size = chain_batch_size
         self.verbose = verbose
+        # measure the local kernel's chain-block shape on the first call
+        self.autotune = autotune
 
     def set_current_position(self, current_position: int):
         self.current_position = current_position
@@ -88,6 +91,10 @@ class TakeSerialSteps(TakeSteps):
         if not isinstance(kernel, LocalKernel):
             raise TypeError(f"{type(kernel).__name__} is not a local kernel")
         pos, lp, acc = bufs
+        if getattr(self, "autotune", False) and not getattr(kernel, "_tuned", False):
+            from ..autotune import tune_local_kernel
+            tune_local_kernel(kernel, target, initial_position.shape[0])
+            kernel._tuned = True
         with region("local_steps", units=initial_position.shape[0] * self.n_steps):
             x_last, _ = run_local_steps(kernel, target, initial_position, self.n_steps, self.thinning, seed, 0,
                                         pos.data, lp.data, acc.data, cursor, noise=noise, uniform=uniform)

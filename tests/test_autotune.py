@@ -1,0 +1,51 @@
+"""Chain-block autotuner: candidate shapes and that every tuned shape samples the same chains."""
+import pytest
+import torch
+
+from flowmc_gb300 import autotune
+
+
+def test_candidates_cover_valid_shapes():
+    assert autotune.candidates(2) == [4, 8, 16, 32]
+    assert autotune.candidates(64) == [8, 16, 32]
+    assert autotune.candidates(128) == [16, 32]
+    assert autotune.candidates(256) == [32]
+    for d in (3, 17, 100, 200):
+        for g in autotune.candidates(d):
+            v = 1
+            while g * v < d:
+                v *= 2
+            assert v <= 8
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kname", ["MALA", "GRW", "HMC"])
+def test_tuned_shape_matches_default_shape(cuda, kname):
+    from flowmc_gb300.resource.kernel.base import run_local_steps
+    from flowmc_gb300.resource.kernel.MALA import MALA
+    from flowmc_gb300.resource.kernel.HMC import HMC
+    from flowmc_gb300.resource.kernel.Gaussian_random_walk import GaussianRandomWalk
+    from flowmc_gb300.targets import GaussianMixture
+    d, C, S = 48, 1024, 6
+    g = torch.Generator().manual_seed(3)
+    tgt = GaussianMixture(torch.randn(4, d, generator=g), torch.full((4, d), 0.5), torch.ones(4) / 4, device="cuda")
+    kern = {"MALA": lambda: MALA(step_size=0.05), "GRW": lambda: GaussianRandomWalk(step_size=0.1),
+            "HMC": lambda: HMC(step_size=0.05, n_leapfrog=4)}[kname]()
+    best = autotune.tune_local_kernel(kern, tgt, C, probe_steps=4, reps=1)
+    assert best in autotune.candidates(d)
+    x0 = torch.randn(C, d, generator=g).cuda()
+    outs = []
+    for lanes in autotune.candidates(d):
+        kern.lanes_per_chain = lanes
+        pos = torch.empty(C, S, d, device="cuda")
+        lp = torch.empty(C, S, device="cuda")
+        acc = torch.empty(C, S, device="cuda")
+        run_local_steps(kern, tgt, x0, S, 1, 11, 0, pos, lp, acc, 0)
+        outs.append((pos, lp, acc))
+    # the noise is indexed by (chain, step, coordinate), so shapes differ only in reduction order
+    for pos, lp, acc in outs[1:]:
+        same = (acc == outs[0][2]).float().mean().item()
+        assert same > 0.99
+        ok = (acc == outs[0][2]).all(dim=1)
+        torch.testing.assert_close(pos[ok], outs[0][0][ok], rtol=1e-3, atol=1e-3)
+        torch.testing.assert_close(lp[ok], outs[0][1][ok], rtol=1e-3, atol=1e-3)
