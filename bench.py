@@ -326,6 +326,40 @@ def reference_arm(args, w):
 
 
 # ---------------------------------------------------------------- main
+def kernel_trace(path, fn, cmd):
+    """Per-kernel launch list of fn() from CUPTI activity records (torch.profiler):
+    launches, total device time and share per kernel name, written as text."""
+    import torch
+    from torch.profiler import profile, ProfilerActivity
+    import tempfile
+    with profile(activities=[ProfilerActivity.CUDA]) as p:
+        fn()
+        torch.cuda.synchronize()
+    # kernels launched outside torch ops only appear in the raw activity trace
+    with tempfile.TemporaryDirectory() as td:
+        tp = os.path.join(td, "trace.json")
+        p.export_chrome_trace(tp)
+        with open(tp) as f:
+            events = json.load(f).get("traceEvents", [])
+    rows = {}
+    for ev in events:
+        cat = ev.get("cat", "")
+        if cat not in ("kernel", "gpu_memcpy", "gpu_memset"):
+            continue
+        name = ev.get("name", "")
+        key = name.split("(")[0].replace("void ", "") if cat == "kernel" else cat + " " + name.split(" ")[0]
+        n, t = rows.get(key, (0, 0.0))
+        rows[key] = (n + 1, t + float(ev.get("dur", 0.0)) / 1e3)
+    total = sum(t for _, t in rows.values())
+    with open(path, "w") as f:
+        f.write(f"# {cmd} --kernel-trace {os.path.basename(path)}\n")
+        f.write("# per kernel: launches, device ms (sum over launches), share of device time\n")
+        for k, (n, t) in sorted(rows.items(), key=lambda kv: -kv[1][1]):
+            f.write(f"{k:60s} {n:8d} {t:12.3f} {100 * t / total:7.2f}%\n")
+        f.write(f"{'total':60s} {sum(n for n, _ in rows.values()):8d} {total:12.3f}\n")
+    print(json.dumps({"kernel_trace": path, "device_ms": total, "kernels": len(rows)}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -342,6 +376,9 @@ def main():
                     help="loops of the plain FP32 form timed for its chain-steps/s (0 = skip)")
     ap.add_argument("--probe", default="", choices=["", "local"],
                     help="run only the local-step HBM probe (a small profiling target)")
+    ap.add_argument("--kernel-trace", default="",
+                    help="write a per-kernel launch list (CUPTI activity timestamps) of the K loops to this "
+                         "file instead of the bench line; its times are not bench values")
     ap.add_argument("--plain-full", action="store_true",
                     help="run the plain FP32 form on the full schedule (min-ESS/s, moment error)")
     args = ap.parse_args()
@@ -391,6 +428,11 @@ def main():
     key = sampler.rng_key
     x, key = run(segs[:W], x, key)
     torch.cuda.synchronize()
+    if args.kernel_trace:
+        kernel_trace(args.kernel_trace, lambda: run(segs[W:], x, key),
+                     f"python bench.py --steps {K} --warmup {W} --workload {args.workload} "
+                     f"--precision {args.precision}" + (f" --chains {args.chains}" if args.chains else ""))
+        return
     if world > 1:
         dist.barrier()
     clocks = ClockSampler(local_rank)

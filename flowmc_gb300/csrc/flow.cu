@@ -184,7 +184,7 @@ static int64_t infer_chunk_rows(const FlowGeom& g, int64_t n) {
 }
 
 static size_t infer_ws_bytes(const FlowGeom& g, int64_t rows) {
-  const int64_t ldp = 2 * (int64_t)((g.nt_max() + g.spl_dg - 1) / g.spl_dg);
+  const int64_t ldp = kSplineEpiPerQuarter * (int64_t)((g.nt_max() + g.spl_dg - 1) / g.spl_dg);
   const int64_t f = rows * ((int64_t)g.d + g.nc_max() + 2 * g.h_max() + (int64_t)g.nt_max() * g.P + 1 + ldp);
   const int64_t b16 = rows * (align_up(g.nc_max(), 64) + 2 * align_up(g.h_max(), 64));
   return (size_t)(4 * f + 2 * b16 + 16 * 256);
@@ -204,7 +204,7 @@ static void carve_infer(const FlowGeom& g, int64_t rows, void* ws, InferWs& w) {
   w.h1 = (float*)take(4 * rows * g.h_max());
   w.raw = (float*)take(4 * rows * (int64_t)g.nt_max() * g.P);
   w.ld = (float*)take(4 * rows);
-  w.ldp = (float*)take(4 * rows * 2 * (int64_t)((g.nt_max() + g.spl_dg - 1) / g.spl_dg));
+  w.ldp = (float*)take(4 * rows * kSplineEpiPerQuarter * (int64_t)((g.nt_max() + g.spl_dg - 1) / g.spl_dg));
   w.cond16 = (uint16_t*)take(2 * rows * align_up(g.nc_max(), 64));
   w.h16a = (uint16_t*)take(2 * rows * align_up(g.h_max(), 64));
   w.h16b = (uint16_t*)take(2 * rows * align_up(g.h_max(), 64));

@@ -40,7 +40,12 @@ int conditioner_bf16_hidden(const FmcFlow* f, const FlowGeom& g, int l, int64_t 
                             uint16_t* cond16, uint16_t* h16a, uint16_t* h16b, const uint16_t** h_last,
                             cudaStream_t st);
 
-// the last Linear of layer l fused with the spline (tc_spline.cu)
+// epilogue warps per TMEM lane quarter in the fused spline kernel; each
+// leaves one log-determinant partial per row and coordinate group
+constexpr int kSplineEpiPerQuarter = 3;
+
+// the last Linear of layer l fused with the spline (tc_spline.cu); ldp holds
+// kSplineEpiPerQuarter * n_groups floats per row
 int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l, const uint16_t* A, int64_t M,
                      int64_t rows_a, bool inverse, float* xa, float* ld, float* ldp);
 

@@ -239,4 +239,89 @@ __device__ __forceinline__ float rqs_fwd_adjoint(float x, const float* raw, cons
   return gx;
 }
 
+// ---------------------------------------------------------------- inference, one bin
+// Inference-only spline for the BF16 path: the same function as make_knots +
+// rqs_fwd / rqs_inv, but only the bin that holds v is built. Both softmax
+// normalisers are still needed (every knot depends on them), the knot
+// positions are running sums whose last value at or below v picks the bin
+// (identical to the one-hot selection: knots increase, so exactly one k has
+// knot_k <= v < knot_{k+1}), and only that bin's two slopes go through the
+// softplus. Exponentials, logarithms and divisions use the fast hardware
+// approximations; with bf16 conditioner weights their error is far below the
+// inputs' own rounding. raw: the 3K+1 conditioner outputs with bias added.
+__device__ __forceinline__ float softplus_fast(float a) {
+  return fmaxf(a, 0.f) + log1pf(__expf(-fabsf(a)));
+}
+
+template <int K, bool INV>
+__device__ __forceinline__ void rqs_apply_fast(const float (&raw)[3 * K + 1], float v, const SplineCfg& c, float& out,
+                                               float& ld) {
+  float mw = raw[0], mh = raw[K];
+#pragma unroll
+  for (int k = 1; k < K; ++k) {
+    mw = fmaxf(mw, raw[k]);
+    mh = fmaxf(mh, raw[K + k]);
+  }
+  float ew[K], eh[K], sw = 0.f, sh = 0.f;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    ew[k] = __expf(raw[k] - mw);
+    eh[k] = __expf(raw[K + k] - mh);
+    sw += ew[k];
+    sh += eh[k];
+  }
+  const float scale = (c.rmax - c.rmin) - (float)K * c.min_bin;
+  const float fw = __fdividef(scale, sw), fh = __fdividef(scale, sh);
+  // bin 0 by default (also covers v below the range)
+  float cw = 0.f, ch = 0.f;
+  float x0 = c.rmin, y0 = c.rmin, x1 = c.rmax, y1 = c.rmax, r0 = raw[2 * K], r1 = raw[2 * K + 1];
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const float xk = c.rmin + cw, yk = c.rmin + ch;
+    cw += ew[k] * fw + c.min_bin;
+    ch += eh[k] * fh + c.min_bin;
+    const float xk1 = (k == K - 1) ? c.rmax : c.rmin + cw;
+    const float yk1 = (k == K - 1) ? c.rmax : c.rmin + ch;
+    if (k == 0 || v >= (INV ? yk : xk)) {
+      x0 = xk; x1 = xk1; y0 = yk; y1 = yk1;
+      r0 = raw[2 * K + k];
+      r1 = raw[2 * K + k + 1];
+    }
+  }
+  const float d0 = softplus_fast(r0 + c.slope_offset) + c.min_slope;
+  const float d1 = softplus_fast(r1 + c.slope_offset) + c.min_slope;
+  const float w = x1 - x0, h = y1 - y0;
+  const float s = __fdividef(h, w);
+  const float st = d1 + d0 - 2.f * s;
+  float z;
+  if (!INV) {
+    z = fminf(fmaxf(__fdividef(v - x0, w), 0.f), 1.f);
+  } else {
+    const float ww = fminf(fmaxf(__fdividef(v - y0, h), 0.f), 1.f);
+    const float cq = -s * ww;
+    const float bq = d0 - st * ww;
+    const float aq = s - bq;
+    const float disc = bq * bq - 4.f * aq * cq;
+    const float sqd = (disc > 0.f) ? sqrtf(disc) : 0.f;
+    const float num = (bq >= 0.f) ? 2.f * cq : -bq + sqd;
+    const float dnm = (bq >= 0.f) ? -bq - sqd : 2.f * aq;
+    z = fminf(fmaxf(__fdividef(num, dnm), 0.f), 1.f);
+  }
+  const float sq = z * z, q = z - sq, om = 1.f - z;
+  const float den = s + st * q;
+  const float A = d1 * sq + 2.f * s * q + d0 * om * om;
+  const float lg = 2.f * __logf(s) + __logf(A) - 2.f * __logf(den);
+  if (!INV) {
+    out = y0 + __fdividef(h * (s * sq + d0 * q), den);
+    ld = lg;
+    if (v <= c.rmin) { out = (v - c.rmin) * d0 + c.rmin; ld = __logf(d0); }
+    if (v >= c.rmax) { out = (v - c.rmax) * d1 + c.rmax; ld = __logf(d1); }
+  } else {
+    out = w * z + x0;
+    ld = -lg;
+    if (v <= c.rmin) { out = __fdividef(v - c.rmin, d0) + c.rmin; ld = -__logf(d0); }
+    if (v >= c.rmax) { out = __fdividef(v - c.rmax, d1) + c.rmax; ld = -__logf(d1); }
+  }
+}
+
 }  // namespace fmc

@@ -13,16 +13,17 @@
 // ldp[row, 2g + half]. The conditioner outputs never reach global memory.
 //
 // Structure as k_tc_gemm (tc_gemm.cuh): persistent CTAs, TMA producer warp,
-// MMA warp, two TMEM accumulators; here eight epilogue warps (two per TMEM
-// lane quarter, each taking every other coordinate of the group). All waits
-// are bounded.
+// MMA warp, two TMEM accumulators; here kSplineEpiPerQuarter epilogue warps
+// per TMEM lane quarter, warp h of a quarter taking coordinates h, h + E, ...
+// of the group. Only the bin that holds each input is built
+// (rqs_apply_fast). All waits are bounded.
 #include "flow.cuh"
 #include "tc_gemm.cuh"
 
 namespace fmc {
 namespace tc {
 
-constexpr int kSplEpiWarps = 8;
+constexpr int kSplEpiWarps = 4 * kSplineEpiPerQuarter;
 constexpr int kSplThreads = 64 + 32 * kSplEpiWarps;
 
 template <int K>
@@ -156,9 +157,10 @@ __global__ void __launch_bounds__(kSplThreads, 1)
       mma_commit(mma_done);
     }
   } else {
+    constexpr int E = kSplineEpiPerQuarter;
     const int ew = warp - 2;
     const int q = warp & 3;          // TMEM lane quarter
-    const int half = ew >> 2;        // which alternate coordinates of the group
+    const int half = ew >> 2;        // coordinates half, half + E, ... of the group
     const int row = q * 32 + lane;
     int local = 0;
     for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++local) {
@@ -173,26 +175,24 @@ __global__ void __launch_bounds__(kSplThreads, 1)
       const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * 256);
       float ldsum = 0.f;
 #pragma unroll 1
-      for (int u = half; u < DG; u += 2) {
+      for (int u = half; u < DG; u += E) {
         const int tcoord = g * DG + u;
         if (tcoord >= nt) break;
         float raw[P];
         tmem_ld_cols<P>(tb + (uint32_t)(u * P), raw);   // warp-collective: every lane loads
         if (gm < M) {
+          float* xp = xa + (int64_t)gm * d + 2 * tcoord + tpar;
+          const float xv = *xp;
           const float* bb = bias + (int64_t)tcoord * P;
 #pragma unroll
           for (int p = 0; p < P; ++p) raw[p] += __ldg(bb + p);
-          Knots<KB> kn;
-          make_knots<KB>(raw, cfg, kn);
-          float* xp = xa + (int64_t)gm * d + 2 * tcoord + tpar;
           float y, l;
-          if (INV) rqs_inv<KB>(*xp, kn, y, l);
-          else rqs_fwd<KB>(*xp, kn, y, l);
+          rqs_apply_fast<KB, INV>(raw, xv, cfg, y, l);
           *xp = y;
           ldsum += l;
         }
       }
-      if (gm < M) ldp[(int64_t)gm * (2 * n_groups) + 2 * g + half] = ldsum;
+      if (gm < M) ldp[(int64_t)gm * (E * n_groups) + E * g + half] = ldsum;
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncwarp();
       if (lane == 0) mbar_arrive(&acc_empty[b]);
@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(kSplThreads, 1)
 
 }  // namespace tc
 
-// ld[r] += sum of the row's 2 * n_groups partials (fixed order)
+// ld[r] += sum of the row's kSplineEpiPerQuarter * n_groups partials (fixed order)
 __global__ void k_ld_reduce(const float* __restrict__ ldp, int n_part, int64_t m, float* __restrict__ ld) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < m; r += (int64_t)gridDim.x * blockDim.x) {
     float s = 0.f;
@@ -281,7 +281,7 @@ int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l
   if (rc) return rc;
   int64_t blocks = (M + 255) / 256;
   if (blocks > (int64_t)sm_count() * 8) blocks = (int64_t)sm_count() * 8;
-  k_ld_reduce<<<(int)(blocks < 1 ? 1 : blocks), 256, 0, st>>>(ldp, 2 * n_groups, M, ld);
+  k_ld_reduce<<<(int)(blocks < 1 ? 1 : blocks), 256, 0, st>>>(ldp, kSplineEpiPerQuarter * n_groups, M, ld);
   FMC_LAUNCH_CHECK();
   return FMC_OK;
 }
