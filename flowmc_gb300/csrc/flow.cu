@@ -173,24 +173,38 @@ struct InferWs {
 
 static int64_t align_up(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
 
-static int64_t infer_chunk_rows(const FlowGeom& g, int64_t n) {
-  const int64_t per_row = (int64_t)g.nt_max() * g.P + 2 * g.h_max() + g.nc_max() + g.d + 1;
-  int64_t rows = (int64_t)(512ll << 20) / (4 * per_row);   // ~512 MB of chunk buffers
-  rows = rows / 128 * 128;
-  if (rows < 128) rows = 128;
-  if (rows > 262144) rows = 262144;
+// BF16 chunks: the three bf16 activation buffers of a chunk (cond16, h16a,
+// h16b) at this many rows stay within about twice the 129 MB L2 for the
+// 512-wide conditioners
+constexpr int64_t kBf16ChunkRows = 65536;
+
+static int64_t infer_floats_per_row(const FlowGeom& g, bool bf16) {
+  const int64_t ldp = kSplineEpiPerQuarter * (int64_t)((g.nt_max() + g.spl_dg - 1) / g.spl_dg);
+  // xa, cond, ld (+ the fused kernel's log-det partials, or the fp32 conditioner buffers)
+  return (int64_t)g.d + g.nc_max() + 1 + (bf16 ? ldp : 2 * g.h_max() + (int64_t)g.nt_max() * g.P);
+}
+
+static int64_t infer_chunk_rows(const FlowGeom& g, int64_t n, bool bf16) {
+  int64_t rows;
+  if (bf16) {
+    rows = kBf16ChunkRows;
+  } else {
+    rows = (int64_t)(512ll << 20) / (4 * infer_floats_per_row(g, false));   // ~512 MB of chunk buffers
+    rows = rows / 128 * 128;
+    if (rows < 128) rows = 128;
+    if (rows > 262144) rows = 262144;
+  }
   if (n < rows) rows = align_up(n > 0 ? n : 1, 128);
   return rows;
 }
 
-static size_t infer_ws_bytes(const FlowGeom& g, int64_t rows) {
-  const int64_t ldp = kSplineEpiPerQuarter * (int64_t)((g.nt_max() + g.spl_dg - 1) / g.spl_dg);
-  const int64_t f = rows * ((int64_t)g.d + g.nc_max() + 2 * g.h_max() + (int64_t)g.nt_max() * g.P + 1 + ldp);
-  const int64_t b16 = rows * (align_up(g.nc_max(), 64) + 2 * align_up(g.h_max(), 64));
+static size_t infer_ws_bytes(const FlowGeom& g, int64_t rows, bool bf16) {
+  const int64_t f = rows * infer_floats_per_row(g, bf16);
+  const int64_t b16 = bf16 ? rows * (align_up(g.nc_max(), 64) + 2 * align_up(g.h_max(), 64)) : 0;
   return (size_t)(4 * f + 2 * b16 + 16 * 256);
 }
 
-static void carve_infer(const FlowGeom& g, int64_t rows, void* ws, InferWs& w) {
+static void carve_infer(const FlowGeom& g, int64_t rows, bool bf16, void* ws, InferWs& w) {
   char* p = (char*)ws;
   auto take = [&](int64_t bytes) {
     char* r = p;
@@ -200,22 +214,24 @@ static void carve_infer(const FlowGeom& g, int64_t rows, void* ws, InferWs& w) {
   w.rows = rows;
   w.xa = (float*)take(4 * rows * g.d);
   w.cond = (float*)take(4 * rows * g.nc_max());
-  w.h0 = (float*)take(4 * rows * g.h_max());
-  w.h1 = (float*)take(4 * rows * g.h_max());
-  w.raw = (float*)take(4 * rows * (int64_t)g.nt_max() * g.P);
   w.ld = (float*)take(4 * rows);
-  w.ldp = (float*)take(4 * rows * kSplineEpiPerQuarter * (int64_t)((g.nt_max() + g.spl_dg - 1) / g.spl_dg));
-  w.cond16 = (uint16_t*)take(2 * rows * align_up(g.nc_max(), 64));
-  w.h16a = (uint16_t*)take(2 * rows * align_up(g.h_max(), 64));
-  w.h16b = (uint16_t*)take(2 * rows * align_up(g.h_max(), 64));
+  w.h0 = w.h1 = w.raw = w.ldp = nullptr;
+  w.cond16 = w.h16a = w.h16b = nullptr;
+  if (bf16) {
+    w.ldp = (float*)take(4 * rows * kSplineEpiPerQuarter * (int64_t)((g.nt_max() + g.spl_dg - 1) / g.spl_dg));
+    w.cond16 = (uint16_t*)take(2 * rows * align_up(g.nc_max(), 64));
+    w.h16a = (uint16_t*)take(2 * rows * align_up(g.h_max(), 64));
+    w.h16b = (uint16_t*)take(2 * rows * align_up(g.h_max(), 64));
+  } else {
+    w.h0 = (float*)take(4 * rows * g.h_max());
+    w.h1 = (float*)take(4 * rows * g.h_max());
+    w.raw = (float*)take(4 * rows * (int64_t)g.nt_max() * g.P);
+  }
 }
 
 // conditioner MLP of layer l on rows [0, m): cond (w.cond) -> raw (w.raw)
 static int conditioner(const FmcFlow* f, const FlowGeom& g, int l, int64_t m, InferWs& w, cudaStream_t st) {
   const float* th = f->theta + g.layer_off[l];
-  if (f->precision == FMC_PREC_BF16) {
-    return conditioner_bf16(f, g, l, m, w.cond, w.cond16, w.h16a, w.h16b, w.raw, st);
-  }
   const float* a = w.cond;
   int in = g.nc(l);
   float* bufs[2] = {w.h0, w.h1};
@@ -259,9 +275,9 @@ static int flow_pass(const FmcFlow* f, const FlowGeom& g, const float* x, float*
   return FMC_OK;
 }
 
-static int check_ws(const FlowGeom& g, int64_t n, void* ws, size_t ws_bytes, int64_t& rows) {
-  rows = infer_chunk_rows(g, n);
-  const size_t need = infer_ws_bytes(g, rows);
+static int check_ws(const FlowGeom& g, int64_t n, bool bf16, void* ws, size_t ws_bytes, int64_t& rows) {
+  rows = infer_chunk_rows(g, n, bf16);
+  const size_t need = infer_ws_bytes(g, rows, bf16);
   FMC_CHECK_ARG(ws != nullptr && ws_bytes >= need, "workspace of %zu bytes < %zu needed", ws_bytes, need);
   FMC_CHECK_ARG(((uintptr_t)ws & 255) == 0, "workspace must be 256-byte aligned");
   return FMC_OK;
@@ -287,9 +303,10 @@ int flow_apply(const FmcFlow* f, const float* x, int64_t n, float* out, float* o
   if (n == 0) return FMC_OK;
   FMC_CHECK_ARG(x != nullptr && out != nullptr, "NULL array");
   int64_t rows;
-  if ((rc = check_ws(g, n, ws, ws_bytes, rows))) return rc;
+  const bool bf16 = f->precision == FMC_PREC_BF16;
+  if ((rc = check_ws(g, n, bf16, ws, ws_bytes, rows))) return rc;
   InferWs w;
-  carve_infer(g, rows, ws, w);
+  carve_infer(g, rows, bf16, ws, w);
   for (int64_t r0 = 0; r0 < n; r0 += rows) {
     const int64_t m = (n - r0 < rows) ? n - r0 : rows;
     const float* xc = x + r0 * g.d;
@@ -318,9 +335,10 @@ int flow_sample(const FmcFlow* f, uint64_t seed, uint64_t counter, const float* 
   if (n == 0) return FMC_OK;
   FMC_CHECK_ARG(x != nullptr, "NULL output");
   int64_t rows;
-  if ((rc = check_ws(g, n, ws, ws_bytes, rows))) return rc;
+  const bool bf16 = f->precision == FMC_PREC_BF16;
+  if ((rc = check_ws(g, n, bf16, ws, ws_bytes, rows))) return rc;
   InferWs w;
-  carve_infer(g, rows, ws, w);
+  carve_infer(g, rows, bf16, ws, w);
   const Rng rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter};
   k_base_sample<<<ew_grid(n * g.d), 256, 0, st>>>(z, rng, n, g.d, f->aux, x);
   FMC_LAUNCH_CHECK();
@@ -347,7 +365,8 @@ int flow_sample_rows(const FmcFlow* f, uint64_t seed, uint64_t counter, const fl
 size_t flow_infer_ws_bytes(const FmcFlow* f, int64_t n) {
   FlowGeom g;
   if (make_geom(f, g) != FMC_OK) return 0;
-  return infer_ws_bytes(g, infer_chunk_rows(g, n));
+  const bool bf16 = f->precision == FMC_PREC_BF16;
+  return infer_ws_bytes(g, infer_chunk_rows(g, n, bf16), bf16);
 }
 
 
@@ -372,9 +391,10 @@ extern "C" int fmc_flow_workspace_size(const FmcFlow* flow, int64_t n, int32_t m
   FMC_CHECK_ARG(bytes != nullptr, "bytes is NULL");
   FMC_CHECK_ARG(n >= 0, "n < 0");
   if (mode == 0) {
-    *bytes = infer_ws_bytes(g, infer_chunk_rows(g, n));
+    const bool bf16 = flow->precision == FMC_PREC_BF16;
+    *bytes = infer_ws_bytes(g, infer_chunk_rows(g, n, bf16), bf16);
   } else if (mode == 1) {
-    *bytes = train_ws_bytes(g, n);
+    *bytes = train_ws_bytes(g, n, flow->precision == FMC_PREC_BF16);
   } else {
     set_error("unknown workspace mode %d", mode);
     return FMC_ERR_INVALID_ARG;

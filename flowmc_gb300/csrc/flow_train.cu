@@ -22,6 +22,11 @@ static int64_t a256(int64_t v) { return (v + 255) / 256 * 256; }
 struct TrainWs {
   float *xs, *xa, *cond, *hs, *raw, *graw, *gh0, *gh1, *gcond, *gy, *gxa, *ld, *logp, *part;
   int64_t part_floats;
+  // fused last-Linear + spline kernels (BF16 path): log-det partials and
+  // per-128-row-tile bias-gradient partials; split-K partials of the
+  // weight-gradient GEMMs (K = the batch)
+  float *ldp, *bpart, *kpart;
+  int64_t kpart_floats;
   // BF16 path (tensor-core GEMMs): activations, gradients and their transposes
   uint16_t *cond16, *condT, *hs16, *hsT, *graw16, *grawT, *gz16[2], *gzT[2];
   int64_t n128, n64, hld, htr, ncld, nctr, pld, ptr_rows;
@@ -50,11 +55,12 @@ static void carve_train(const FlowGeom& g, int64_t n, bool bf16, void* ws, Train
   w.xs = take((int64_t)(g.L + 1) * n * g.d);
   w.xa = take(n * g.d);
   w.cond = take(n * g.nc_max());
-  w.hs = take((int64_t)g.nh * n * g.h_max());
-  w.raw = take(n * ntP);
-  w.graw = take(n * ntP);
-  w.gh0 = take(n * g.h_max());
-  w.gh1 = take(n * g.h_max());
+  // fp32 conditioner activations and gradients: the FP32 path only
+  w.hs = bf16 ? nullptr : take((int64_t)g.nh * n * g.h_max());
+  w.raw = bf16 ? nullptr : take(n * ntP);
+  w.graw = bf16 ? nullptr : take(n * ntP);
+  w.gh0 = bf16 ? nullptr : take(n * g.h_max());
+  w.gh1 = bf16 ? nullptr : take(n * g.h_max());
   w.gcond = take(n * g.nc_max());
   w.gy = take(n * g.d);
   w.gxa = take(n * g.d);
@@ -64,6 +70,8 @@ static void carve_train(const FlowGeom& g, int64_t n, bool bf16, void* ws, Train
   if (m < 4096) m = 4096;
   w.part_floats = (int64_t)colsum_blocks(n) * m;
   w.part = take(w.part_floats);
+  w.ldp = w.bpart = w.kpart = nullptr;
+  w.kpart_floats = 0;
   w.cond16 = w.condT = w.hs16 = w.hsT = w.graw16 = w.grawT = nullptr;
   w.gz16[0] = w.gz16[1] = w.gzT[0] = w.gzT[1] = nullptr;
   if (bf16) {
@@ -85,14 +93,23 @@ static void carve_train(const FlowGeom& g, int64_t n, bool bf16, void* ws, Train
       w.gz16[k] = take16(w.n128 * w.hld);
       w.gzT[k] = take16(w.htr * w.n64);
     }
+    const int64_t groups = (g.nt_max() + g.spl_dg - 1) / g.spl_dg;
+    w.ldp = take(n * kSplineEpiPerQuarter * groups);
+    w.bpart = take((w.n128 / 128) * ntP);
+    for (int l = 0; l < g.L; ++l)
+      for (int i = 0; i <= g.nh; ++i) {
+        const int64_t f = (int64_t)splitk_scratch_floats(g.lin_out(l, i), g.lin_in(l, i), (int)w.n64);
+        if (f > w.kpart_floats) w.kpart_floats = f;
+      }
+    w.kpart = w.kpart_floats > 0 ? take(w.kpart_floats) : nullptr;
   }
   if (total) *total = (size_t)used;
 }
 
-size_t train_ws_bytes(const FlowGeom& g, int64_t n) {
+size_t train_ws_bytes(const FlowGeom& g, int64_t n, bool bf16) {
   TrainWs w;
   size_t tot = 0;
-  carve_train(g, n, true, nullptr, w, &tot);   // sized for the BF16 path (a superset)
+  carve_train(g, n, bf16, nullptr, w, &tot);
   return tot;
 }
 
@@ -249,43 +266,39 @@ static int recompute_mlp(const FmcFlow* f, const FlowGeom& g, int l, int64_t n, 
   return FMC_OK;
 }
 
-// BF16 recompute of layer l's conditioner: tanh activations (and their
-// transposes for the weight gradients) in bf16, outputs in fp32
-static int recompute_mlp_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t n, TrainWs& w, cudaStream_t st) {
+// BF16 recompute of layer l's conditioner hidden layers: tanh activations
+// (and their transposes for the weight gradients) in bf16; the last Linear is
+// recomputed inside the fused spline adjoint
+static int recompute_hidden_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t n, TrainWs& w, cudaStream_t st) {
   const float* th = f->theta + g.layer_off[l];
   const int nc = g.nc(l);
   int rc = to_bf16_pad_t(st, w.cond, n, nc, w.cond16, FlowGeom::rup(nc, 64), w.condT, w.n64, w.n64);
   if (rc) return rc;
   const uint16_t* a = w.cond16;
-  for (int i = 0; i <= g.nh; ++i) {
+  for (int i = 0; i < g.nh; ++i) {
     const int seg = l * (g.nh + 1) + i;
     const int K = g.w16_cols(l, i), N = g.lin_out(l, i);
-    const uint16_t* B = f->theta_bf16 + g.w16_off[seg];
     tc::EpiArgs ep{};
     ep.bias = th + g.lin_b(l, i);
-    if (i < g.nh) {
-      uint16_t* h = w.hs16 + (int64_t)i * w.n128 * w.hld;
-      ep.ct = w.hsT + (int64_t)i * w.htr * w.n64;
-      ep.ldct = w.n64;
-      ep.ct_rows_pad = w.n64;
-      const int ldo = (int)FlowGeom::rup(N, 64);
-      rc = tc_gemm(st, a, n, w.n128, K, B, N, g.w16_rows(l, i), ep, h, ldo, ldo, tc::TC_EPI_TANH_BF16);
-      a = h;
-    } else {
-      rc = tc_gemm(st, a, n, w.n128, K, B, N, g.w16_rows(l, i), ep, w.raw, N, N, tc::TC_EPI_BIAS_F32);
-    }
-    if (rc) return rc;
+    uint16_t* h = w.hs16 + (int64_t)i * w.n128 * w.hld;
+    ep.ct = w.hsT + (int64_t)i * w.htr * w.n64;
+    ep.ldct = w.n64;
+    ep.ct_rows_pad = w.n64;
+    const int ldo = (int)FlowGeom::rup(N, 64);
+    if ((rc = tc_gemm(st, a, n, w.n128, K, f->theta_bf16 + g.w16_off[seg], N, g.w16_rows(l, i), ep, h, ldo, ldo,
+                      tc::TC_EPI_TANH_BF16)))
+      return rc;
+    a = h;
   }
   return FMC_OK;
 }
 
-// BF16 adjoint of the conditioner: w.graw (fp32) -> weight/bias gradients into gl, d cond into w.gcond
+// BF16 adjoint of the conditioner: d raw (w.graw16 / w.grawT, bf16, with the
+// last bias gradient already reduced) -> weight/bias gradients into gl, d cond
+// into w.gcond
 static int backward_mlp_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t n, TrainWs& w, float* gl,
                              cudaStream_t st) {
-  const int ntP = g.lin_out(l, g.nh);
-  int rc = colsum(st, w.graw, n, ntP, w.part, gl + g.lin_b(l, g.nh));
-  if (rc) return rc;
-  if ((rc = to_bf16_pad_t(st, w.graw, n, ntP, w.graw16, FlowGeom::rup(ntP, 64), w.grawT, w.n64, w.n64))) return rc;
+  int rc = FMC_OK;
   const uint16_t* gcur = w.graw16;
   const uint16_t* gcurT = w.grawT;
   int nxt = 0;
@@ -293,8 +306,11 @@ static int backward_mlp_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t
     const int out = g.lin_out(l, i), in = g.lin_in(l, i);
     const int seg = l * (g.nh + 1) + i;
     const uint16_t* aT = (i == 0) ? w.condT : w.hsT + (int64_t)(i - 1) * w.htr * w.n64;
-    // dW = g^T a  [out, in], reduced over the batch
+    // dW = g^T a  [out, in], reduced over the batch (split along it when the
+    // [out, in] tile grid is small)
     tc::EpiArgs e0{};
+    e0.kpart = w.kpart;
+    e0.kpart_floats = w.kpart_floats;
     if ((rc = tc_gemm(st, gcurT, out, FlowGeom::rup(out, 128), (int)w.n64, aT, in, (int)FlowGeom::rup(in, 256), e0,
                       gl + g.lin_w(l, i), in, in, tc::TC_EPI_F32)))
       return rc;
@@ -335,10 +351,10 @@ int flow_loss_grad(const FmcFlow* f, const float* x, int64_t n, float* loss, flo
   FMC_CHECK_ARG(f->theta && f->aux, "flow theta/aux is NULL");
   FMC_CHECK_ARG(n >= 1, "n=%lld < 1", (long long)n);
   FMC_CHECK_ARG(x && loss && grad, "NULL array");
-  const size_t need = train_ws_bytes(g, n);
+  const bool bf16 = f->precision == FMC_PREC_BF16;
+  const size_t need = train_ws_bytes(g, n, bf16);
   FMC_CHECK_ARG(ws && ws_bytes >= need, "workspace of %zu bytes < %zu needed", ws_bytes, need);
   FMC_CHECK_ARG(((uintptr_t)ws & 255) == 0, "workspace must be 256-byte aligned");
-  const bool bf16 = f->precision == FMC_PREC_BF16;
   if (bf16) FMC_CHECK_ARG(f->theta_bf16 != nullptr, "BF16 mode needs theta_bf16");
   TrainWs w;
   carve_train(g, n, bf16, ws, w, nullptr);
@@ -355,8 +371,15 @@ int flow_loss_grad(const FmcFlow* f, const float* x, int64_t n, float* loss, flo
     k_affine<<<eb, 256, 0, st>>>(xin, xout, w.cond, n, d, g.nc(l), g.cpar(l), f->theta + g.layer_off[l], 0, w.ld,
                                  l == 0 ? 1 : 0);
     FMC_LAUNCH_CHECK();
-    if ((rc = bf16 ? recompute_mlp_bf16(f, g, l, n, w, st) : recompute_mlp(f, g, l, n, w, st))) return rc;
-    if ((rc = launch_spline(g.K, false, st, w.raw, xout, w.ld, n, d, g.nt(l), g.tpar(l), g.cfg))) return rc;
+    if (bf16) {
+      // the inference path: hidden layers, then the last Linear fused with the spline
+      const uint16_t* h_last = nullptr;
+      if ((rc = conditioner_bf16_hidden(f, g, l, n, w.cond, w.cond16, w.gz16[0], w.gz16[1], &h_last, st))) return rc;
+      if ((rc = tc_linear_spline(st, g, f, l, h_last, n, w.n128, false, xout, w.ld, w.ldp))) return rc;
+    } else {
+      if ((rc = recompute_mlp(f, g, l, n, w, st))) return rc;
+      if ((rc = launch_spline(g.K, false, st, w.raw, xout, w.ld, n, d, g.nt(l), g.tpar(l), g.cfg))) return rc;
+    }
   }
   const float* y = w.xs + (int64_t)g.L * nd;
   {
@@ -379,13 +402,23 @@ int flow_loss_grad(const FmcFlow* f, const float* x, int64_t n, float* loss, flo
     const float* xin = w.xs + (int64_t)l * nd;
     k_affine<<<eb, 256, 0, st>>>(xin, w.xa, w.cond, n, d, g.nc(l), g.cpar(l), th, 0, nullptr, 0);
     FMC_LAUNCH_CHECK();
-    if ((rc = bf16 ? recompute_mlp_bf16(f, g, l, n, w, st) : recompute_mlp(f, g, l, n, w, st))) return rc;
-    if ((rc = launch_spline_bwd(g.K, st, w.raw, w.xa, w.gy, gld, w.graw, w.gxa, n, d, g.nt(l), g.tpar(l), g.cpar(l),
-                                g.cfg)))
-      return rc;
     if (bf16) {
+      // hidden activations, then the last Linear recomputed inside the fused
+      // spline adjoint, which leaves d raw in both bf16 operand layouts
+      if ((rc = recompute_hidden_bf16(f, g, l, n, w, st))) return rc;
+      const uint16_t* h_last = g.nh > 0 ? w.hs16 + (int64_t)(g.nh - 1) * w.n128 * w.hld : w.cond16;
+      if ((rc = tc_linear_spline_bwd(st, g, f, l, h_last, n, w.n128, w.xa, w.gy, gld, w.gxa, w.graw16, w.pld,
+                                     w.grawT, w.n64, w.bpart)))
+        return rc;
+      const int ntP = g.lin_out(l, g.nh);
+      k_colsum_final<<<(ntP + 255) / 256, 256, 0, st>>>(w.bpart, (int)(w.n128 / 128), ntP, gl + g.lin_b(l, g.nh));
+      FMC_LAUNCH_CHECK();
       if ((rc = backward_mlp_bf16(f, g, l, n, w, gl, st))) return rc;
     } else {
+      if ((rc = recompute_mlp(f, g, l, n, w, st))) return rc;
+      if ((rc = launch_spline_bwd(g.K, st, w.raw, w.xa, w.gy, gld, w.graw, w.gxa, n, d, g.nt(l), g.tpar(l), g.cpar(l),
+                                  g.cfg)))
+        return rc;
       // conditioner adjoint
       const float* gcur = w.graw;
       float* gbufs[2] = {w.gh0, w.gh1};

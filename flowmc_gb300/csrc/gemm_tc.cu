@@ -56,6 +56,38 @@ int make_tma_map_bf16(CUtensorMap* m, const void* base, int64_t inner, int64_t o
   return FMC_OK;
 }
 
+// C[m, n] = sum over the split-K slices of part[s * stride + m * ldc + n] (fixed order)
+__global__ void k_splitk_reduce(const float* __restrict__ part, int splits, int64_t stride, int64_t M, int n_store,
+                                int64_t ldc, float* __restrict__ C) {
+  const int64_t tot = M * n_store;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t m = e / n_store, n = e - m * n_store;
+    const int64_t o = m * ldc + n;
+    float v = 0.f;
+    for (int s = 0; s < splits; ++s) v += part[s * stride + o];
+    C[o] = v;
+  }
+}
+
+// K-slices for an fp32 GEMM whose tile grid would leave SMs idle: enough to
+// fill the SMs, at most 32, at least 4 K-chunks each, never an empty slice
+static int splitk_count(int64_t tiles, int K) {
+  const int nk = K / tc::BK;
+  int64_t s = sm_count() / (tiles > 0 ? tiles : 1);
+  if (s > 32) s = 32;
+  if (s > nk / 4) s = nk / 4;
+  if (s < 2) return 1;
+  const int nks = (nk + (int)s - 1) / (int)s;
+  return (nk + nks - 1) / nks;
+}
+
+size_t splitk_scratch_floats(int64_t M, int N, int K) {
+  const int BN = (N > 128) ? 256 : 128;
+  const int64_t tiles = (M + tc::BM - 1) / tc::BM * ((N + BN - 1) / BN);
+  const int s = splitk_count(tiles, K);
+  return s > 1 ? (size_t)s * (size_t)M * (size_t)N : 0;
+}
+
 template <int BN, int STAGES, int EPI>
 static int launch_tc(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& mb, int64_t M, int N, int K,
                      const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store) {
@@ -70,10 +102,24 @@ static int launch_tc(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& 
   FMC_CUDA_TRY(cudaGetSymbolAddress((void**)&err, g_tc_error));
   const int64_t mt = (M + tc::BM - 1) / tc::BM;
   const int64_t tiles = mt * ((n_store + BN - 1) / BN);
-  FMC_CHECK_SUPPORTED(tiles < (1ll << 31) && M < (1ll << 31), "GEMM too large (%lld tiles)", (long long)tiles);
-  const int64_t grid = tiles < sm_count() ? tiles : sm_count();   // persistent: one CTA per SM
-  kern<<<(unsigned)grid, tc::kThreads, S::TOTAL, st>>>(ma, mb, (int)M, N, K, ep, C, ldc, n_store, err);
+  FMC_CHECK_SUPPORTED(tiles < (1ll << 26) && M < (1ll << 31), "GEMM too large (%lld tiles)", (long long)tiles);
+  int splits = 1;
+  if (EPI == tc::TC_EPI_F32 && ep.kpart != nullptr) {
+    splits = splitk_count(tiles, K);
+    if ((int64_t)splits * M * ldc > ep.kpart_floats) splits = 1;
+  }
+  const int64_t items = tiles * splits;
+  const int64_t grid = items < sm_count() ? items : sm_count();   // persistent: one CTA per SM
+  void* out = splits > 1 ? (void*)ep.kpart : C;
+  kern<<<(unsigned)grid, tc::kThreads, S::TOTAL, st>>>(ma, mb, (int)M, N, K, ep, out, ldc, n_store, splits, M * ldc,
+                                                      err);
   FMC_LAUNCH_CHECK();
+  if (splits > 1) {
+    int64_t blocks = (M * n_store + 255) / 256;
+    if (blocks > (int64_t)sm_count() * 8) blocks = (int64_t)sm_count() * 8;
+    k_splitk_reduce<<<(int)blocks, 256, 0, st>>>(ep.kpart, splits, M * ldc, M, n_store, ldc, (float*)C);
+    FMC_LAUNCH_CHECK();
+  }
   return FMC_OK;
 }
 
@@ -222,39 +268,6 @@ int conditioner_bf16_hidden(const FmcFlow* f, const FlowGeom& g, int l, int64_t 
     a = hbuf[i & 1];
   }
   *h_last = a;
-  return FMC_OK;
-}
-
-int conditioner_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t m, const float* cond, uint16_t* cond16,
-                     uint16_t* h16a, uint16_t* h16b, float* raw, cudaStream_t st) {
-  const int64_t rows = (m + tc::BM - 1) / tc::BM * tc::BM;
-  const int nc = g.nc(l), ncp = g.w16_cols(l, 0);
-  {
-    int64_t blocks = (m * ncp + 255) / 256;
-    if (blocks > (int64_t)sm_count() * 16) blocks = (int64_t)sm_count() * 16;
-    k_to_bf16_pad<<<(int)blocks, 256, 0, st>>>(cond, m, nc, ncp, cond16);
-    FMC_LAUNCH_CHECK();
-  }
-  const float* th = f->theta + g.layer_off[l];
-  const uint16_t* a = cond16;
-  uint16_t* hbuf[2] = {h16a, h16b};
-  for (int i = 0; i <= g.nh; ++i) {
-    const int seg = l * (g.nh + 1) + i;
-    const int K = g.w16_cols(l, i), N = g.lin_out(l, i);
-    const uint16_t* B = f->theta_bf16 + g.w16_off[seg];
-    const float* bias = th + g.lin_b(l, i);
-    int rc;
-    tc::EpiArgs ep{};
-    ep.bias = bias;
-    if (i < g.nh) {
-      const int ldo = (int)FlowGeom::rup(N, 64);
-      rc = tc_gemm(st, a, m, rows, K, B, N, g.w16_rows(l, i), ep, hbuf[i & 1], ldo, ldo, tc::TC_EPI_TANH_BF16);
-      a = hbuf[i & 1];
-    } else {
-      rc = tc_gemm(st, a, m, rows, K, B, N, g.w16_rows(l, i), ep, raw, N, N, tc::TC_EPI_BIAS_F32);
-    }
-    if (rc) return rc;
-  }
   return FMC_OK;
 }
 

@@ -19,6 +19,8 @@ struct EpiArgs {
   uint16_t* ct;             // optional transposed copy: ct[col * ldct + row]
   int64_t ldct;
   int64_t ct_rows_pad;      // rows in [M, ct_rows_pad) get zeros in the copy
+  float* kpart;             // mode 3: optional scratch for split-K partial products
+  int64_t kpart_floats;     //   (the GEMM splits K when the tile grid leaves SMs idle)
 };
 }  // namespace tc
 
@@ -26,13 +28,7 @@ __device__ __forceinline__ uint16_t f32_to_bf16_rn(float v) {
   return __bfloat16_as_ushort(__float2bfloat16_rn(v));
 }
 
-// Conditioner MLP of layer l for rows [0, m) in BF16 with FP32 accumulation:
-// cond (fp32 [m, n_c]) -> raw (fp32 [m, n_t*P]); cond16/h16a/h16b are bf16
-// staging buffers with rows padded to 64 elements.
-int conditioner_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t m, const float* cond, uint16_t* cond16,
-                     uint16_t* h16a, uint16_t* h16b, float* raw, cudaStream_t st);
-
-size_t train_ws_bytes(const FlowGeom& g, int64_t n);
+size_t train_ws_bytes(const FlowGeom& g, int64_t n, bool bf16);
 
 // the conditioner's hidden layers only (conversion + tanh GEMMs); *h_last is
 // the last tanh activation (bf16 [round_up(m, 128), round_up(H_last, 64)])
@@ -49,6 +45,15 @@ constexpr int kSplineEpiPerQuarter = 3;
 int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l, const uint16_t* A, int64_t M,
                      int64_t rows_a, bool inverse, float* xa, float* ld, float* ldp);
 
+// adjoint of layer l's last Linear + spline (tc_spline.cu), recomputing the
+// Linear from A: dL/dx into gxa (every coordinate), dL/draw in bf16 into graw
+// [>= M, ldg] (columns t*P + p, padding up to ldg zeroed) and grawT [t*P + p,
+// ldt] (rows M..ldt zeroed), and per-128-row-tile column sums of dL/draw into
+// bpart [ceil(M / 128), nt * P]
+int tc_linear_spline_bwd(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l, const uint16_t* A, int64_t M,
+                         int64_t rows_a, const float* xa, const float* gy, float gld, float* gxa, uint16_t* graw,
+                         int64_t ldg, uint16_t* grawT, int64_t ldt, float* bpart);
+
 // theta (fp32, packed) -> zero-padded bf16 weight segments (FlowGeom::w16_off)
 // and their transposes (FlowGeom::w16t_off)
 int pack_bf16_weights(const FlowGeom& g, const float* theta, uint16_t* w16, cudaStream_t st);
@@ -59,6 +64,10 @@ int pack_bf16_weights(const FlowGeom& g, const float* theta, uint16_t* w16, cuda
 // epilogues n_store (= N) columns.
 int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K, const uint16_t* B, int N,
             int rows_b, const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store, int epi);
+
+// scratch (floats) that tc_gemm's fp32 mode uses for split-K partials of an
+// M x N x K product when EpiArgs::kpart is given (0: it would not split)
+size_t splitk_scratch_floats(int64_t M, int N, int K);
 
 // fp32 src [n, cols] -> bf16 dst [>= n, ldd] (zero padded to ldd columns; may be
 // NULL) and/or its transpose dstT [>= ldd, ldt] (rows n..t_cols-1 zero)

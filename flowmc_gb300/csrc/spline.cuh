@@ -11,6 +11,7 @@
 // selected bin's knots, the cumulative sums, the two softmaxes and the
 // softplus slopes.
 #pragma once
+#include <cuda_bf16.h>
 #include "common.cuh"
 
 namespace fmc {
@@ -322,6 +323,135 @@ __device__ __forceinline__ void rqs_apply_fast(const float (&raw)[3 * K + 1], fl
     if (v <= c.rmin) { out = __fdividef(v - c.rmin, d0) + c.rmin; ld = -__logf(d0); }
     if (v >= c.rmax) { out = __fdividef(v - c.rmax, d1) + c.rmax; ld = -__logf(d1); }
   }
+}
+
+// Adjoint of rqs_apply_fast<K, false> for the BF16 training path: given
+// gy = dL/dy and gl = dL/dlogdet, returns dL/dx and writes dL/draw[0..3K] as
+// bf16 to out. Same derivative as rqs_fwd_adjoint, organised around the one
+// bin that holds x: only its two knots carry gradient into the cumulative
+// widths/heights (so dL/dw_i is a two-term prefix rule) and only its two
+// slopes go through the softplus derivative; the rest of the slope
+// gradients are exactly zero.
+template <int K>
+__device__ __forceinline__ float rqs_fwd_adjoint_fast(const float (&raw)[3 * K + 1], float x, float gy, float gl,
+                                                      const SplineCfg& c, uint16_t* __restrict__ out) {
+  float mw = raw[0], mh = raw[K];
+#pragma unroll
+  for (int k = 1; k < K; ++k) {
+    mw = fmaxf(mw, raw[k]);
+    mh = fmaxf(mh, raw[K + k]);
+  }
+  float pw[K], ph[K], sw = 0.f, sh = 0.f;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    pw[k] = __expf(raw[k] - mw);
+    ph[k] = __expf(raw[K + k] - mh);
+    sw += pw[k];
+    sh += ph[k];
+  }
+  const float iw = __fdividef(1.f, sw), ih = __fdividef(1.f, sh);
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    pw[k] *= iw;
+    ph[k] *= ih;
+  }
+  const float scale = (c.rmax - c.rmin) - (float)K * c.min_bin;
+  float cw = 0.f, ch = 0.f;
+  float x0 = c.rmin, y0 = c.rmin, x1 = c.rmax, y1 = c.rmax, r0 = raw[2 * K], r1 = raw[2 * K + 1];
+  int kb = 0;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const float xk = c.rmin + cw, yk = c.rmin + ch;
+    cw += pw[k] * scale + c.min_bin;
+    ch += ph[k] * scale + c.min_bin;
+    const float xk1 = (k == K - 1) ? c.rmax : c.rmin + cw;
+    const float yk1 = (k == K - 1) ? c.rmax : c.rmin + ch;
+    if (k == 0 || x >= xk) {
+      x0 = xk; x1 = xk1; y0 = yk; y1 = yk1;
+      r0 = raw[2 * K + k];
+      r1 = raw[2 * K + k + 1];
+      kb = k;
+    }
+  }
+  const float a0 = r0 + c.slope_offset, a1 = r1 + c.slope_offset;
+  const float d0 = softplus_fast(a0) + c.min_slope, d1 = softplus_fast(a1) + c.min_slope;
+  float gx, g_x0 = 0.f, g_x1 = 0.f, g_y0 = 0.f, g_y1 = 0.f, g_d0 = 0.f, g_d1 = 0.f;
+  if (x <= c.rmin) {
+    gx = gy * d0;
+    g_d0 = gy * (x - c.rmin) + __fdividef(gl, d0);
+  } else if (x >= c.rmax) {
+    gx = gy * d1;
+    g_d1 = gy * (x - c.rmax) + __fdividef(gl, d1);
+  } else {
+    const float w = x1 - x0, h = y1 - y0;
+    const float iwd = __fdividef(1.f, w);
+    const float s = h * iwd;
+    const float zr = (x - x0) * iwd;
+    const float z = fminf(fmaxf(zr, 0.f), 1.f);
+    const float sq = z * z, q = z - sq, om = 1.f - z, sq1 = om * om;
+    const float st = d1 + d0 - 2.f * s;
+    const float num = h * (s * sq + d0 * q);
+    const float den = s + st * q;
+    const float A = d1 * sq + 2.f * s * q + d0 * sq1;
+    const float iden = __fdividef(1.f, den);
+    // y = y0 + num/den ; ld = 2 log s + log A - 2 log den
+    const float g_num = gy * iden;
+    const float g_den = -(gy * num * iden + 2.f * gl) * iden;
+    const float g_A = __fdividef(gl, A);
+    float g_s = __fdividef(2.f * gl, s);
+    float g_h = g_num * (s * sq + d0 * q);
+    g_s += g_num * h * sq;
+    float g_sq = g_num * h * s;
+    g_d0 = g_num * h * q;
+    float g_q = g_num * h * d0;
+    g_s += g_den * (1.f - 2.f * q);
+    g_d1 = g_den * q;
+    g_d0 += g_den * q;
+    g_q += g_den * st;
+    g_d1 += g_A * sq;
+    g_sq += g_A * d1;
+    g_s += g_A * 2.f * q;
+    g_q += g_A * 2.f * s;
+    g_d0 += g_A * sq1;
+    float g_z = -g_A * d0 * 2.f * om;
+    g_z += g_q * (1.f - 2.f * z) + g_sq * 2.f * z;
+    const float g_zr = (zr > 0.f && zr < 1.f) ? g_z : 0.f;
+    gx = g_zr * iwd;
+    const float g_w = -(g_zr * zr + g_s * s) * iwd;
+    g_h += g_s * iwd;
+    g_x0 = -g_zr * iwd - g_w;
+    g_x1 = g_w;
+    g_y1 = g_h;
+    g_y0 = gy - g_h;
+  }
+  // interior knot k (1 <= k <= K-1) is rmin + sum_{i<k} width_i: dL/dwidth_i
+  // collects the gradients of the bin's two knots that lie beyond i
+  const float ax0 = (kb >= 1) ? g_x0 : 0.f, ax1 = (kb + 1 <= K - 1) ? g_x1 : 0.f;
+  const float ay0 = (kb >= 1) ? g_y0 : 0.f, ay1 = (kb + 1 <= K - 1) ? g_y1 : 0.f;
+  float dw = 0.f, dh = 0.f;
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    const float gwi = scale * ((i < kb ? ax0 : 0.f) + (i <= kb ? ax1 : 0.f));
+    const float ghi = scale * ((i < kb ? ay0 : 0.f) + (i <= kb ? ay1 : 0.f));
+    dw += pw[i] * gwi;
+    dh += ph[i] * ghi;
+  }
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    const float gwi = scale * ((i < kb ? ax0 : 0.f) + (i <= kb ? ax1 : 0.f));
+    const float ghi = scale * ((i < kb ? ay0 : 0.f) + (i <= kb ? ay1 : 0.f));
+    out[i] = __bfloat16_as_ushort(__float2bfloat16_rn(pw[i] * (gwi - dw)));
+    out[K + i] = __bfloat16_as_ushort(__float2bfloat16_rn(ph[i] * (ghi - dh)));
+  }
+  // slopes: d = softplus(raw + offset) + min_slope, d' = sigmoid(raw + offset)
+  const float gs0 = g_d0 * __fdividef(1.f, 1.f + __expf(-a0));
+  const float gs1 = g_d1 * __fdividef(1.f, 1.f + __expf(-a1));
+#pragma unroll
+  for (int k = 0; k <= K; ++k) {
+    const float v = (k == kb ? gs0 : 0.f) + (k == kb + 1 ? gs1 : 0.f);
+    out[2 * K + k] = __bfloat16_as_ushort(__float2bfloat16_rn(v));
+  }
+  return gx;
 }
 
 }  // namespace fmc

@@ -144,14 +144,17 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// Persistent GEMM: each CTA walks tiles t = blockIdx.x, +gridDim.x, ... (tile
-// t covers rows (t / n_tiles) * 128 and columns (t % n_tiles) * BN), with two
-// TMEM accumulators so the epilogue of one tile overlaps the MMAs of the next.
-// err: device word; 1 = a wait expired.
+// Persistent GEMM: each CTA walks work items t = blockIdx.x, +gridDim.x, ...
+// Item t is K-slice s = t % splits of tile t / splits (tile u covers rows
+// (u / n_tiles) * 128 and columns (u % n_tiles) * BN); with splits > 1 the
+// slices write their fp32 partial products to C + s * split_stride and the
+// host reduces them. Two TMEM accumulators let the epilogue of one item
+// overlap the MMAs of the next. err: device word; 1 = a wait expired.
 template <int BN, int STAGES, int EPI>
 __global__ void __launch_bounds__(kThreads, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N, int K,
-              const EpiArgs ep, void* __restrict__ C, int64_t ldc, int n_store, int* err) {
+              const EpiArgs ep, void* __restrict__ C, int64_t ldc, int n_store, int splits, int64_t split_stride,
+              int* err) {
   extern __shared__ uint8_t smem_raw[];
   using S = Smem<BN, STAGES>;
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -165,9 +168,10 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nk = (K + BK - 1) / BK;
+  const int nks = (nk + splits - 1) / splits;   // K chunks per slice
   const int n_tiles = (n_store + BN - 1) / BN;
   const int m_tiles = (M + BM - 1) / BM;
-  const int tiles = n_tiles * m_tiles;
+  const int tiles = n_tiles * m_tiles * splits;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -196,8 +200,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (lane == 0) {
       uint32_t it = 0;
       for (int t = blockIdx.x; t < tiles && !*abort_flag; t += gridDim.x) {
-        const int m0 = (t / n_tiles) * BM, n0 = (t % n_tiles) * BN;
-        for (int k = 0; k < nk; ++k, ++it) {
+        const int u = t / splits, sl = t - u * splits;
+        const int m0 = (u / n_tiles) * BM, n0 = (u % n_tiles) * BN;
+        const int kb = sl * nks, ke = (kb + nks < nk) ? kb + nks : nk;
+        for (int k = kb; k < ke; ++k, ++it) {
           const int s = it % STAGES;
           const uint32_t ph = (it / STAGES) & 1u;
           if (it >= (uint32_t)STAGES && !mbar_wait(&empty[s], ph ^ 1u)) {
@@ -231,8 +237,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t d = tmem + (uint32_t)(b * BN);
+        const int sl = t % splits;
+        const int kb = sl * nks, ke = (kb + nks < nk) ? kb + nks : nk;
         bool stop = false;
-        for (int k = 0; k < nk; ++k, ++it) {
+        for (int k = kb; k < ke; ++k, ++it) {
           const int s = it % STAGES;
           const uint32_t ph = (it / STAGES) & 1u;
           if (!mbar_wait(&full[s], ph) || *abort_flag) {
@@ -247,7 +255,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
           for (int kk = 0; kk < BK / 16; ++kk) {
             // advance along K inside the swizzle atom: 16 bf16 = 32 bytes
-            mma_bf16(d, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, (k > 0 || kk > 0) ? 1u : 0u);
+            mma_bf16(d, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, (k > kb || kk > 0) ? 1u : 0u);
           }
           mma_commit(&empty[s]);
         }
@@ -271,7 +279,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     int local = 0;
     for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++local) {
       const int b = local & 1, use = local >> 1;
-      const int m0 = (t / n_tiles) * BM, n0 = (t % n_tiles) * BN;
+      const int u = t / splits, sl = t - u * splits;
+      const int m0 = (u / n_tiles) * BM, n0 = (u % n_tiles) * BN;
       const int gm = m0 + row;
       if (*abort_flag || !mbar_wait(&acc_full[b], (uint32_t)use & 1u)) {
         *abort_flag = 1;
@@ -346,7 +355,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
           }
         } else if (row_ok) {
-          float* out = (float*)C + (int64_t)gm * ldc + gn0;
+          float* out = (float*)C + sl * split_stride + (int64_t)gm * ldc + gn0;
           if (EPI == TC_EPI_BIAS_F32) {
 #pragma unroll
             for (int i = 0; i < 32; ++i)

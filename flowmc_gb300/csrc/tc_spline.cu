@@ -1,22 +1,35 @@
 // tc_spline.cu -- the last conditioner Linear fused with the rational-quadratic
-// spline (forward or inverse) on the tensor cores.
+// spline on the tensor cores: the forward/inverse pass (inference and the
+// training forward) and the spline adjoint (training backward).
 //
 // For one coupling layer, rows [0, M) of the previous tanh activation A (bf16)
 // are multiplied by the last Linear's weights, re-packed in groups: group g
 // holds the DG = floor(256 / P) transformed coordinates t = g*DG .. g*DG+DG-1,
 // each as its P = 3K+1 consecutive weight rows, padded to BN rows (a multiple
 // of 16). The accumulator of a (128-row, group) tile therefore holds, for
-// every row, the complete raw spline parameters of DG coordinates. The
-// epilogue threads (one accumulator row each) add the bias, build the knots,
-// evaluate the spline (rqSpline.py:42-239) on x = xa[row, 2t + tpar], write
-// the result back into xa and leave the row's log-determinant partial sum in
-// ldp[row, 2g + half]. The conditioner outputs never reach global memory.
+// every row, the complete raw spline parameters of DG coordinates, and the
+// conditioner outputs never reach global memory.
 //
-// Structure as k_tc_gemm (tc_gemm.cuh): persistent CTAs, TMA producer warp,
-// MMA warp, two TMEM accumulators; here kSplineEpiPerQuarter epilogue warps
-// per TMEM lane quarter, warp h of a quarter taking coordinates h, h + E, ...
-// of the group. Only the bin that holds each input is built
-// (rqs_apply_fast). All waits are bounded.
+//   k_tc_spline      epilogue: bias, knots of the selected bin only, the
+//                    spline (rqSpline.py:42-239) on x = xa[row, 2t + tpar]
+//                    written back into xa; per-row log-determinant partials
+//                    into ldp[row, E*g + h]
+//   k_tc_spline_bwd  epilogue: bias, knots, the spline adjoint of the
+//                    selected bin (rqs_fwd_adjoint_fast) given dL/dy = gy[row, 2t + tpar] and
+//                    dL/dlogdet = gld; dL/dx into gxa, dL/draw as bf16 staged
+//                    in shared memory and written out twice, row-major
+//                    [row, t*P + p] and transposed [t*P + p, row] (the two
+//                    operand layouts of the conditioner's backward GEMMs),
+//                    plus per-tile column sums for the bias gradient
+//
+// Both kernels are persistent (tile t = blockIdx.x, +gridDim.x, ...): warp 0
+// issues the TMA loads of a STAGES-deep ring, warp 1 owns the TMEM and issues
+// tcgen05.mma into two accumulators (the epilogue of one tile overlaps the
+// MMAs of the next), and kSplineEpiPerQuarter warps per TMEM lane quarter run
+// the epilogue, warp h of a quarter taking coordinates h, h + E, ... of the
+// group. Every mbarrier wait is bounded; on expiry the kernel raises the
+// device error word, skips the remaining work, still frees its TMEM and
+// returns.
 #include "flow.cuh"
 #include "tc_gemm.cuh"
 
@@ -24,13 +37,19 @@ namespace fmc {
 namespace tc {
 
 constexpr int kSplEpiWarps = 4 * kSplineEpiPerQuarter;
-constexpr int kSplThreads = 64 + 32 * kSplEpiWarps;
+constexpr int kSplEpiThreads = 32 * kSplEpiWarps;
+constexpr int kSplThreads = 64 + kSplEpiThreads;
 
 template <int K>
 struct SplineTile {
   static constexpr int P = 3 * K + 1;
   static constexpr int DG = 256 / P;
-  static constexpr int BN = ((DG * P + 15) / 16) * 16;
+  static constexpr int DGP = DG * P;
+  static constexpr int BN = ((DGP + 15) / 16) * 16;
+  // bf16 row pitch of the adjoint staging tile: an even count whose half is
+  // odd, so the 32 rows a warp touches in one column fall in 32 banks
+  static constexpr int SP = ((DGP + 1) / 2 % 2 == 1) ? ((DGP + 1) / 2) * 2 : ((DGP + 1) / 2 + 1) * 2;
+  static constexpr int STG_BYTES = BM * SP * 2;
 };
 
 // N consecutive accumulator columns of this thread's lane; every register is
@@ -49,133 +68,194 @@ __device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, float (&v)[N]) {
   }
 }
 
-template <int KB, bool INV, int STAGES>
-__global__ void __launch_bounds__(kSplThreads, 1)
-    k_tc_spline(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int n_groups,
-                int nt, int K, const float* __restrict__ bias, float* __restrict__ xa, int d, int tpar,
-                float* __restrict__ ldp, SplineCfg cfg, int* err) {
-  using T = SplineTile<KB>;
-  constexpr int P = T::P, DG = T::DG, BN = T::BN;
+// barriers and TMEM of one CTA of the fused kernels
+struct Pipe {
+  uint8_t* base;
+  uint64_t *full, *empty, *acc_full, *acc_empty, *mma_done;
+  uint32_t* tmem_slot;
+  volatile int* abort_flag;
+  uint32_t tmem;
+};
+
+template <int BN, int STAGES>
+__device__ __forceinline__ Pipe pipe_setup(uint8_t* base, int warp) {
   using S = Smem<BN, STAGES>;
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = (uint64_t*)(base + STAGES * S::STAGE_BYTES);
-  uint64_t* empty = full + STAGES;
-  uint64_t* acc_full = empty + STAGES;
-  uint64_t* acc_empty = acc_full + 2;
-  uint64_t* mma_done = acc_empty + 2;
-  uint32_t* tmem_slot = (uint32_t*)(mma_done + 1);
-  volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
-
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nk = (K + BK - 1) / BK;
-  const int m_tiles = (M + BM - 1) / BM;
-  const int tiles = m_tiles * n_groups;
-
+  Pipe p;
+  p.base = base;
+  p.full = (uint64_t*)(base + STAGES * S::STAGE_BYTES);
+  p.empty = p.full + STAGES;
+  p.acc_full = p.empty + STAGES;
+  p.acc_empty = p.acc_full + 2;
+  p.mma_done = p.acc_empty + 2;
+  p.tmem_slot = (uint32_t*)(p.mma_done + 1);
+  p.abort_flag = (volatile int*)(p.tmem_slot + 1);
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
-      mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
+      mbar_init(&p.full[s], 1);
+      mbar_init(&p.empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
-      mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_empty[b], kSplEpiWarps);
+      mbar_init(&p.acc_full[b], 1);
+      mbar_init(&p.acc_empty[b], kSplEpiWarps);
     }
-    mbar_init(mma_done, 1);
-    *abort_flag = 0;
+    mbar_init(p.mma_done, 1);
+    *p.abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(p.tmem_slot)),
                  "r"(512));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const uint32_t tmem = *tmem_slot;
+  p.tmem = *p.tmem_slot;
+  return p;
+}
+
+// warp 0, one lane: A and B K-chunks of every tile of this CTA into the ring
+template <int BN, int STAGES>
+__device__ __forceinline__ void producer(const Pipe& p, const CUtensorMap* tmA, const CUtensorMap* tmB, int tiles,
+                                         int n_groups, int nk) {
+  using S = Smem<BN, STAGES>;
+  uint32_t it = 0;
+  for (int t = blockIdx.x; t < tiles && !*p.abort_flag; t += gridDim.x) {
+    const int m0 = (t / n_groups) * BM, n0 = (t % n_groups) * BN;
+    for (int k = 0; k < nk; ++k, ++it) {
+      const int s = it % STAGES;
+      const uint32_t ph = (it / STAGES) & 1u;
+      if (it >= (uint32_t)STAGES && !mbar_wait(&p.empty[s], ph ^ 1u)) {
+        *p.abort_flag = 1;
+        break;
+      }
+      if (*p.abort_flag) break;
+      uint8_t* sa = p.base + s * S::STAGE_BYTES;
+      uint8_t* sb = sa + S::A_BYTES;
+      mbar_expect_tx(&p.full[s], S::STAGE_BYTES);
+      tma_load_2d(sa, tmA, &p.full[s], k * BK, m0);
+      tma_load_2d(sb, tmB, &p.full[s], k * BK, n0);
+    }
+  }
+  if (*p.abort_flag) {
+    // let the copies still in flight land before the CTA exits (bounded)
+    for (uint32_t j = it > (uint32_t)STAGES ? it - STAGES : 0; j < it; ++j)
+      mbar_wait(&p.full[j % STAGES], (j / STAGES) & 1u);
+  }
+}
+
+// warp 1, one lane: the MMAs of every tile into accumulator (local & 1)
+template <int BN, int STAGES>
+__device__ __forceinline__ void mma_issuer(const Pipe& p, int tiles, int nk) {
+  using S = Smem<BN, STAGES>;
+  const uint32_t idesc = idesc_bf16_f32(BN);
+  uint32_t it = 0;
+  int local = 0;
+  for (int t = blockIdx.x; t < tiles && !*p.abort_flag; t += gridDim.x, ++local) {
+    const int b = local & 1, use = local >> 1;
+    if (use > 0 && !mbar_wait(&p.acc_empty[b], (uint32_t)(use - 1) & 1u)) {
+      *p.abort_flag = 1;
+      break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t dcol = p.tmem + (uint32_t)(b * 256);
+    bool stop = false;
+    for (int k = 0; k < nk; ++k, ++it) {
+      const int s = it % STAGES;
+      const uint32_t ph = (it / STAGES) & 1u;
+      if (!mbar_wait(&p.full[s], ph) || *p.abort_flag) {
+        *p.abort_flag = 1;
+        stop = true;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint8_t* sa = p.base + s * S::STAGE_BYTES;
+      const uint8_t* sb = sa + S::A_BYTES;
+      const uint64_t da = smem_desc_sw128(sa), db = smem_desc_sw128(sb);
+#pragma unroll
+      for (int kk = 0; kk < BK / 16; ++kk)
+        mma_bf16(dcol, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, (k > 0 || kk > 0) ? 1u : 0u);
+      mma_commit(&p.empty[s]);
+    }
+    if (stop) break;
+    mma_commit(&p.acc_full[b]);
+  }
+  // fires once every MMA issued so far has finished (also after an abort)
+  mma_commit(p.mma_done);
+}
+
+__device__ __forceinline__ void pipe_teardown(const Pipe& p, int warp, int lane, int* err) {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    if (lane == 0) mbar_wait(p.mma_done, 0);
+    __syncwarp();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(p.tmem), "r"(512));
+  }
+  if (threadIdx.x == 0 && *p.abort_flag) atomicExch(err, 1);
+}
+
+// this warp's TMEM lanes of accumulator b are read: hand them back to the MMA warp
+__device__ __forceinline__ void release_acc(const Pipe& p, int b, int lane) {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncwarp();
+  if (lane == 0) mbar_arrive(&p.acc_empty[b]);
+}
+
+// named barrier over the epilogue warps only (id 0 is __syncthreads)
+__device__ __forceinline__ void epi_sync(int id) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(kSplEpiThreads) : "memory");
+}
+
+// OR of v over the epilogue warps (barrier 3 with a predicate reduction), so
+// that every epilogue warp takes the same branch before a named barrier
+__device__ __forceinline__ bool epi_any(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n barrier.red.or.pred p, 3, %2, q;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(kSplEpiThreads)
+      : "memory");
+  return r != 0;
+}
+
+template <int KB, bool INV, int STAGES>
+__global__ void __launch_bounds__(kSplThreads, 1)
+    k_tc_spline(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int n_groups,
+                int nt, int K, const float* __restrict__ bias, float* __restrict__ xa, int d, int tpar,
+                float* __restrict__ ldp, SplineCfg cfg, int* err) {
+  using T = SplineTile<KB>;
+  constexpr int P = T::P, DG = T::DG, BN = T::BN, E = kSplineEpiPerQuarter;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nk = (K + BK - 1) / BK;
+  const int tiles = (M + BM - 1) / BM * n_groups;
+  const Pipe p = pipe_setup<BN, STAGES>(base, warp);
 
   if (warp == 0) {
-    if (lane == 0) {
-      uint32_t it = 0;
-      for (int t = blockIdx.x; t < tiles && !*abort_flag; t += gridDim.x) {
-        const int m0 = (t / n_groups) * BM, n0 = (t % n_groups) * BN;
-        for (int k = 0; k < nk; ++k, ++it) {
-          const int s = it % STAGES;
-          const uint32_t ph = (it / STAGES) & 1u;
-          if (it >= (uint32_t)STAGES && !mbar_wait(&empty[s], ph ^ 1u)) {
-            *abort_flag = 1;
-            break;
-          }
-          if (*abort_flag) break;
-          uint8_t* sa = base + s * S::STAGE_BYTES;
-          uint8_t* sb = sa + S::A_BYTES;
-          mbar_expect_tx(&full[s], S::STAGE_BYTES);
-          tma_load_2d(sa, &tmA, &full[s], k * BK, m0);
-          tma_load_2d(sb, &tmB, &full[s], k * BK, n0);
-        }
-      }
-      if (*abort_flag) {
-        for (uint32_t j = it > (uint32_t)STAGES ? it - STAGES : 0; j < it; ++j)
-          mbar_wait(&full[j % STAGES], (j / STAGES) & 1u);
-      }
-    }
+    if (lane == 0) producer<BN, STAGES>(p, &tmA, &tmB, tiles, n_groups, nk);
   } else if (warp == 1) {
-    if (lane == 0) {
-      const uint32_t idesc = idesc_bf16_f32(BN);
-      uint32_t it = 0;
-      int local = 0;
-      for (int t = blockIdx.x; t < tiles && !*abort_flag; t += gridDim.x, ++local) {
-        const int b = local & 1, use = local >> 1;
-        if (use > 0 && !mbar_wait(&acc_empty[b], (uint32_t)(use - 1) & 1u)) {
-          *abort_flag = 1;
-          break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t dcol = tmem + (uint32_t)(b * 256);
-        bool stop = false;
-        for (int k = 0; k < nk; ++k, ++it) {
-          const int s = it % STAGES;
-          const uint32_t ph = (it / STAGES) & 1u;
-          if (!mbar_wait(&full[s], ph) || *abort_flag) {
-            *abort_flag = 1;
-            stop = true;
-            break;
-          }
-          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          const uint8_t* sa = base + s * S::STAGE_BYTES;
-          const uint8_t* sb = sa + S::A_BYTES;
-          const uint64_t da = smem_desc_sw128(sa), db = smem_desc_sw128(sb);
-#pragma unroll
-          for (int kk = 0; kk < BK / 16; ++kk)
-            mma_bf16(dcol, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, (k > 0 || kk > 0) ? 1u : 0u);
-          mma_commit(&empty[s]);
-        }
-        if (stop) break;
-        mma_commit(&acc_full[b]);
-      }
-      mma_commit(mma_done);
-    }
+    if (lane == 0) mma_issuer<BN, STAGES>(p, tiles, nk);
   } else {
-    constexpr int E = kSplineEpiPerQuarter;
-    const int ew = warp - 2;
     const int q = warp & 3;          // TMEM lane quarter
-    const int half = ew >> 2;        // coordinates half, half + E, ... of the group
+    const int h = (warp - 2) >> 2;   // coordinates h, h + E, ... of the group
     const int row = q * 32 + lane;
     int local = 0;
     for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++local) {
       const int b = local & 1, use = local >> 1;
       const int m0 = (t / n_groups) * BM, g = t % n_groups;
       const int gm = m0 + row;
-      if (*abort_flag || !mbar_wait(&acc_full[b], (uint32_t)use & 1u)) {
-        *abort_flag = 1;
+      if (*p.abort_flag || !mbar_wait(&p.acc_full[b], (uint32_t)use & 1u)) {
+        *p.abort_flag = 1;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * 256);
+      const uint32_t tb = p.tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * 256);
       float ldsum = 0.f;
 #pragma unroll 1
-      for (int u = half; u < DG; u += E) {
+      for (int u = h; u < DG; u += E) {
         const int tcoord = g * DG + u;
         if (tcoord >= nt) break;
         float raw[P];
@@ -185,28 +265,135 @@ __global__ void __launch_bounds__(kSplThreads, 1)
           const float xv = *xp;
           const float* bb = bias + (int64_t)tcoord * P;
 #pragma unroll
-          for (int p = 0; p < P; ++p) raw[p] += __ldg(bb + p);
+          for (int i = 0; i < P; ++i) raw[i] += __ldg(bb + i);
           float y, l;
           rqs_apply_fast<KB, INV>(raw, xv, cfg, y, l);
           *xp = y;
           ldsum += l;
         }
       }
-      if (gm < M) ldp[(int64_t)gm * (E * n_groups) + E * g + half] = ldsum;
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&acc_empty[b]);
+      if (gm < M) ldp[(int64_t)gm * (E * n_groups) + E * g + h] = ldsum;
+      release_acc(p, b, lane);
     }
   }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  if (warp == 1) {
-    if (lane == 0) mbar_wait(mma_done, 0);
-    __syncwarp();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+  pipe_teardown(p, warp, lane, err);
+}
+
+// Arguments of the adjoint epilogue.
+struct SplineBwdArgs {
+  const float* bias;   // the last Linear's bias, [nt * P]
+  const float* xa;     // spline inputs (the ScalarAffine output), [M, d]
+  const float* gy;     // dL/d(layer output), [M, d]
+  float gld;           // dL/d(log-determinant), the same for every row
+  float* gxa;          // dL/d(spline input), [M, d]; conditioning coordinates copied from gy
+  uint16_t* graw;      // bf16 [>= M, ldg] row-major; columns [nt*P, ldg) are zeroed
+  int64_t ldg;
+  uint16_t* grawT;     // bf16 [>= nt*P, ldt] transposed; rows in [M, ldt) get zeros
+  int64_t ldt;
+  float* bpart;        // [m_tiles, nt*P] column sums of each 128-row tile
+  int d, nt, tpar, cpar;
+};
+
+template <int KB, int STAGES>
+__global__ void __launch_bounds__(kSplThreads, 1)
+    k_tc_spline_bwd(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M,
+                    int n_groups, int K, const SplineBwdArgs a, SplineCfg cfg, int* err) {
+  using T = SplineTile<KB>;
+  constexpr int P = T::P, DG = T::DG, DGP = T::DGP, BN = T::BN, SP = T::SP, E = kSplineEpiPerQuarter;
+  using S = Smem<BN, STAGES>;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  // staging tile after the ring and its barriers
+  uint16_t* stg = (uint16_t*)(base + STAGES * S::STAGE_BYTES + 256);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nk = (K + BK - 1) / BK;
+  const int tiles = (M + BM - 1) / BM * n_groups;
+  const int ntP = a.nt * P;
+  const Pipe p = pipe_setup<BN, STAGES>(base, warp);
+
+  if (warp == 0) {
+    if (lane == 0) producer<BN, STAGES>(p, &tmA, &tmB, tiles, n_groups, nk);
+  } else if (warp == 1) {
+    if (lane == 0) mma_issuer<BN, STAGES>(p, tiles, nk);
+  } else {
+    const int q = warp & 3;
+    const int h = (warp - 2) >> 2;
+    const int row = q * 32 + lane;
+    const int et = threadIdx.x - 64;   // 0 .. kSplEpiThreads-1
+    const int ew = et >> 5;
+    int local = 0;
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++local) {
+      const int b = local & 1, use = local >> 1;
+      const int mt = t / n_groups, g = t % n_groups;
+      const int m0 = mt * BM;
+      const int gm = m0 + row;
+      const bool row_ok = gm < M;
+      // the tile loop has named barriers: all epilogue warps leave it together
+      const bool bad = *p.abort_flag || !mbar_wait(&p.acc_full[b], (uint32_t)use & 1u);
+      if (epi_any(bad)) {
+        *p.abort_flag = 1;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t tb = p.tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * 256);
+      const int nu = (a.nt - g * DG) < DG ? (a.nt - g * DG) : DG;   // coordinates in this group
+      const int vc = nu * P;                                         // valid staged columns
+#pragma unroll 1
+      for (int u = h; u < nu; u += E) {
+        const int tcoord = g * DG + u;
+        float raw[P];
+        tmem_ld_cols<P>(tb + (uint32_t)(u * P), raw);
+        uint16_t* srow = stg + row * SP + u * P;
+        if (row_ok) {
+          const float* bb = a.bias + (int64_t)tcoord * P;
+#pragma unroll
+          for (int i = 0; i < P; ++i) raw[i] += __ldg(bb + i);
+          const int64_t j = (int64_t)gm * a.d + 2 * tcoord + a.tpar;
+          a.gxa[j] = rqs_fwd_adjoint_fast<KB>(raw, a.xa[j], a.gy[j], a.gld, cfg, srow);
+        } else {
+#pragma unroll
+          for (int i = 0; i < P; ++i) srow[i] = 0;
+        }
+      }
+      release_acc(p, b, lane);
+      if (g == 0 && row_ok) {
+        const int ncond = a.d - a.nt;
+        for (int k = h; k < ncond; k += E) {
+          const int64_t j = (int64_t)gm * a.d + 2 * k + a.cpar;
+          a.gxa[j] = a.gy[j];
+        }
+      }
+      epi_sync(1);
+      // row-major copy: the group's columns are contiguous in [t*P + p] order;
+      // the last group also zeroes the padding columns up to ldg
+      {
+        const int64_t c0 = (int64_t)g * DGP;
+        const int width = (g == n_groups - 1) ? (int)(a.ldg - c0) : vc;
+        for (int r = ew; r < BM && m0 + r < M; r += kSplEpiWarps) {
+          uint16_t* dst = a.graw + (int64_t)(m0 + r) * a.ldg + c0;
+          for (int c = lane; c < width; c += 32) dst[c] = (c < vc) ? stg[r * SP + c] : (uint16_t)0;
+        }
+      }
+      // transposed copy and the column sums, one column per warp at a time:
+      // lane l holds rows l, l+32, l+64, l+96 (64 contiguous bytes per store)
+      for (int c = ew; c < vc; c += kSplEpiWarps) {
+        const int64_t col = (int64_t)g * DGP + c;
+        float s = 0.f;
+#pragma unroll
+        for (int k = 0; k < BM / 32; ++k) {
+          const int r = lane + 32 * k;
+          const uint16_t v = stg[r * SP + c];
+          if (m0 + r < a.ldt) a.grawT[col * a.ldt + m0 + r] = v;
+          s += __uint_as_float((uint32_t)v << 16);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) a.bpart[(int64_t)mt * ntP + col] = s;
+      }
+      epi_sync(2);   // the staging tile is free again
+    }
   }
-  if (threadIdx.x == 0 && *abort_flag) atomicExch(err, 1);
+  pipe_teardown(p, warp, lane, err);
 }
 
 }  // namespace tc
@@ -253,6 +440,32 @@ static int launch_spl(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap&
   return FMC_OK;
 }
 
+template <int KB>
+static int launch_spl_bwd(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& mb, int64_t M, int n_groups,
+                          int K, const tc::SplineBwdArgs& a, SplineCfg cfg) {
+  constexpr int STAGES = 3;
+  using T = tc::SplineTile<KB>;
+  using S = tc::Smem<T::BN, STAGES>;
+  constexpr int TOTAL = S::TOTAL + T::STG_BYTES;
+  static_assert(TOTAL <= 227 * 1024, "fused spline adjoint: shared memory over the per-CTA limit");
+  auto kern = tc::k_tc_spline_bwd<KB, STAGES>;
+  static bool attr = false;
+  if (!attr) {
+    FMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, TOTAL));
+    attr = true;
+  }
+  int* err = nullptr;
+  int rc = tc_error_word(&err);
+  if (rc) return rc;
+  const int64_t tiles = (M + tc::BM - 1) / tc::BM * n_groups;
+  const int64_t grid = tiles < sm_count() ? tiles : sm_count();
+  kern<<<(unsigned)grid, tc::kSplThreads, TOTAL, st>>>(ma, mb, (int)M, n_groups, K, a, cfg, err);
+  FMC_LAUNCH_CHECK();
+  return FMC_OK;
+}
+
+#define FMC_SPLINE_BINS(X) X(2) X(3) X(4) X(5) X(6) X(8) X(10) X(12) X(16)
+
 // The last Linear of layer l fused with its spline: A = the last tanh
 // activation (bf16 [rows_a, K]), Bg = the grouped weights, xa updated in place,
 // ld[r] accumulated.
@@ -273,7 +486,7 @@ int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l
     rc = inverse ? launch_spl<k, true>(st, ma, mb, M, n_groups, nt, Kd, bias, xa, g.d, g.tpar(l), ldp, g.cfg)    \
                  : launch_spl<k, false>(st, ma, mb, M, n_groups, nt, Kd, bias, xa, g.d, g.tpar(l), ldp, g.cfg);  \
   } else
-  SPL_CASE(2) SPL_CASE(3) SPL_CASE(4) SPL_CASE(5) SPL_CASE(6) SPL_CASE(8) SPL_CASE(10) SPL_CASE(12) SPL_CASE(16) {
+  FMC_SPLINE_BINS(SPL_CASE) {
     set_error("n_bins=%d is not instantiated for the fused spline", g.K);
     return FMC_ERR_UNSUPPORTED;
   }
@@ -284,6 +497,47 @@ int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l
   k_ld_reduce<<<(int)(blocks < 1 ? 1 : blocks), 256, 0, st>>>(ldp, kSplineEpiPerQuarter * n_groups, M, ld);
   FMC_LAUNCH_CHECK();
   return FMC_OK;
+}
+
+// Adjoint of layer l's last Linear + spline, recomputing the Linear from A
+// (the last tanh activation, bf16 [rows_a, K]).
+int tc_linear_spline_bwd(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l, const uint16_t* A, int64_t M,
+                         int64_t rows_a, const float* xa, const float* gy, float gld, float* gxa, uint16_t* graw,
+                         int64_t ldg, uint16_t* grawT, int64_t ldt, float* bpart) {
+  const int nt = g.nt(l);
+  int dg, bn;
+  const int n_groups = spline_groups(g.K, nt, &dg, &bn);
+  const int Kd = g.w16_cols(l, g.nh);
+  FMC_CHECK_ARG(ldg >= (int64_t)nt * g.P && ldt >= M, "graw leading dimensions too small");
+  CUtensorMap ma, mb;
+  int rc = make_tma_map_bf16(&ma, A, Kd, rows_a, Kd, tc::BM);
+  if (rc) return rc;
+  if ((rc = make_tma_map_bf16(&mb, f->theta_bf16 + g.w16g_off[l], Kd, (int64_t)n_groups * bn, Kd, bn))) return rc;
+  tc::SplineBwdArgs a;
+  a.bias = f->theta + g.layer_off[l] + g.lin_b(l, g.nh);
+  a.xa = xa;
+  a.gy = gy;
+  a.gld = gld;
+  a.gxa = gxa;
+  a.graw = graw;
+  a.ldg = ldg;
+  a.grawT = grawT;
+  a.ldt = ldt;
+  a.bpart = bpart;
+  a.d = g.d;
+  a.nt = nt;
+  a.tpar = g.tpar(l);
+  a.cpar = g.cpar(l);
+#define SPL_CASE(k)                                                  \
+  if (g.K == k) {                                                    \
+    rc = launch_spl_bwd<k>(st, ma, mb, M, n_groups, Kd, a, g.cfg);   \
+  } else
+  FMC_SPLINE_BINS(SPL_CASE) {
+    set_error("n_bins=%d is not instantiated for the fused spline", g.K);
+    return FMC_ERR_UNSUPPORTED;
+  }
+#undef SPL_CASE
+  return rc;
 }
 
 }  // namespace fmc
