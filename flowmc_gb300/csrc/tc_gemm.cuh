@@ -126,6 +126,26 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   }
 }
 
+// issue a 32-column TMEM load without waiting; the registers must not be
+// read before tmem_wait_pin
+__device__ __forceinline__ void tmem_ld32_issue(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+
+// wait for this thread's TMEM loads; every register is pinned after the wait
+__device__ __forceinline__ void tmem_wait_pin(uint32_t (&r)[32]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) asm volatile("" : "+r"(r[i]));
+}
+
 __device__ __forceinline__ float tanh_fast(float x) {
   float y;
   asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
@@ -290,37 +310,32 @@ __global__ void __launch_bounds__(kThreads, 1)
       const bool row_ok = gm < M;
       const bool ct_row = ep.ct != nullptr && gm < ep.ct_rows_pad;
       const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN);
-#pragma unroll 1
-      for (int c0 = half * 32; c0 < BN; c0 += 64) {
-        float v[32];
-        tmem_ld32(tbase + (uint32_t)c0, v);
+      // One 32-column chunk: v = accumulator row segment, bl = bias of column
+      // n0 + c0 + lane (lane-distributed, broadcast with shuffles before any
+      // lane-dependent branch), av = the row's tanh activations (mode 2).
+      auto chunk = [&](const uint32_t (&r)[32], int c0, float bl, const uint4 (&av)[4]) {
         const int gn0 = n0 + c0;
-        if (gn0 >= n_store || !(row_ok || ct_row)) continue;
+        if (gn0 >= n_store) return;   // uniform across the warp
+        float v[32];
+#pragma unroll
+        for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+        if (EPI == TC_EPI_TANH_BF16 || EPI == TC_EPI_BIAS_F32) {
+#pragma unroll
+          for (int i = 0; i < 32; ++i) v[i] += __shfl_sync(0xffffffffu, bl, i);
+        }
+        if (!(row_ok || ct_row)) return;
         if (EPI == TC_EPI_TANH_BF16 || EPI == TC_EPI_DTANH_BF16) {
           uint32_t packed[16];
           float y[32];
           if (EPI == TC_EPI_TANH_BF16) {
 #pragma unroll
-            for (int i = 0; i < 32; ++i) {
-              const int j = gn0 + i;
-              y[i] = (j < N && row_ok) ? tanh_fast(v[i] + __ldg(ep.bias + j)) : 0.f;
-            }
+            for (int i = 0; i < 32; ++i) y[i] = (gn0 + i < N && row_ok) ? tanh_fast(v[i]) : 0.f;
           } else {
-            const uint16_t* ar = ep.aux + (int64_t)gm * ep.ldaux + gn0;
-            uint16_t hv[32];
-            if (row_ok && aux_vec && gn0 + 32 <= N) {
-              const uint4* a4 = reinterpret_cast<const uint4*>(ar);
-#pragma unroll
-              for (int i = 0; i < 4; ++i) *reinterpret_cast<uint4*>(&hv[8 * i]) = __ldg(a4 + i);
-            } else {
-#pragma unroll
-              for (int i = 0; i < 32; ++i) hv[i] = (row_ok && gn0 + i < N) ? ar[i] : (uint16_t)0;
-            }
+            const uint16_t* hv = reinterpret_cast<const uint16_t*>(av);
 #pragma unroll
             for (int i = 0; i < 32; ++i) {
-              const int j = gn0 + i;
               const float h = __uint_as_float((uint32_t)hv[i] << 16);
-              y[i] = (j < N && row_ok) ? v[i] * (1.f - h * h) : 0.f;
+              y[i] = (gn0 + i < N && row_ok) ? v[i] * (1.f - h * h) : 0.f;
             }
           }
 #pragma unroll
@@ -356,11 +371,6 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         } else if (row_ok) {
           float* out = (float*)C + sl * split_stride + (int64_t)gm * ldc + gn0;
-          if (EPI == TC_EPI_BIAS_F32) {
-#pragma unroll
-            for (int i = 0; i < 32; ++i)
-              if (gn0 + i < n_store) v[i] += __ldg(ep.bias + gn0 + i);
-          }
           if (gn0 + 32 <= n_store && vec_ok) {
             float4* o4 = reinterpret_cast<float4*>(out);
 #pragma unroll
@@ -372,11 +382,55 @@ __global__ void __launch_bounds__(kThreads, 1)
               if (i < lim) out[i] = v[i];
           }
         }
+      };
+      // operands of chunk c0 that come from global memory, loaded ahead
+      auto prefetch = [&](int c0, float& bl, uint4 (&av)[4]) {
+        const int j = n0 + c0 + lane;
+        if (EPI == TC_EPI_TANH_BF16 || EPI == TC_EPI_BIAS_F32) bl = (j < N) ? __ldg(ep.bias + j) : 0.f;
+        if (EPI == TC_EPI_DTANH_BF16) {
+          const int gn0 = n0 + c0;
+          const uint16_t* ar = ep.aux + (int64_t)gm * ep.ldaux + gn0;
+          if (row_ok && aux_vec && gn0 + 32 <= N) {
+            const uint4* a4 = reinterpret_cast<const uint4*>(ar);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) av[i] = __ldg(a4 + i);
+          } else {
+            uint16_t* hv = reinterpret_cast<uint16_t*>(av);
+#pragma unroll
+            for (int i = 0; i < 32; ++i) hv[i] = (row_ok && gn0 + i < N) ? ar[i] : (uint16_t)0;
+          }
+        }
+      };
+      // software pipeline over this warp's chunks c0 = half*32 + 64*i: the
+      // TMEM load and global operands of chunk i+1 are in flight while chunk i
+      // is processed; the accumulator goes back to the MMA warp as soon as
+      // its last chunk is in registers
+      constexpr int NCH = BN / 64;
+      uint32_t ra[32], rb[32];
+      float bl_cur = 0.f, bl_nxt = 0.f;
+      uint4 av_cur[4], av_nxt[4];
+      tmem_ld32_issue(tbase + (uint32_t)(half * 32), ra);
+      prefetch(half * 32, bl_nxt, av_nxt);
+#pragma unroll
+      for (int i = 0; i < NCH; ++i) {
+        const int c0 = half * 32 + 64 * i;
+        uint32_t(&cur)[32] = (i & 1) ? rb : ra;
+        uint32_t(&nxt)[32] = (i & 1) ? ra : rb;
+        bl_cur = bl_nxt;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) av_cur[k] = av_nxt[k];
+        tmem_wait_pin(cur);
+        if (i + 1 < NCH) {
+          tmem_ld32_issue(tbase + (uint32_t)(c0 + 64), nxt);
+          prefetch(c0 + 64, bl_nxt, av_nxt);
+        } else {
+          // this warp's TMEM lanes of buffer b are read: release them to the MMA warp
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&acc_empty[b]);
+        }
+        chunk(cur, c0, bl_cur, av_cur);
       }
-      // this warp's TMEM lanes of buffer b are read: release them to the MMA warp
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&acc_empty[b]);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
