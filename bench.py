@@ -18,6 +18,11 @@ n_global) * K / timed seconds (summed over ranks, which run independent
 replicas). The working set (chain buffers of several GB, flow weights) is
 far larger than L2, so L2 is not flushed between steps.
 
+``e2e`` repeats the timed region's loop mix through ``Sampler.sample`` (one
+call per loop) with pinned host buffers: each loop copies its starting
+positions host->device and reads the rows it wrote and its final positions
+back, all inside the wall-clock timed region.
+
 ``--impl reference`` times the CPU restatement of the same loop (the
 reference flowMC itself needs JAX, which this image does not have).
 """
@@ -332,6 +337,11 @@ def kernel_trace(path, fn, cmd):
     import torch
     from torch.profiler import profile, ProfilerActivity
     import tempfile
+    # the first activity session of a process can come back empty: open one
+    # on a trivial op first
+    with profile(activities=[ProfilerActivity.CUDA]):
+        torch.ones(1, device="cuda").add_(1)
+        torch.cuda.synchronize()
     with profile(activities=[ProfilerActivity.CUDA]) as p:
         fn()
         torch.cuda.synchronize()
@@ -342,15 +352,21 @@ def kernel_trace(path, fn, cmd):
         with open(tp) as f:
             events = json.load(f).get("traceEvents", [])
     rows = {}
+    cats = {}
     for ev in events:
         cat = ev.get("cat", "")
-        if cat not in ("kernel", "gpu_memcpy", "gpu_memset"):
+        cats[cat] = cats.get(cat, 0) + 1
+        if cat.lower() not in ("kernel", "gpu_memcpy", "gpu_memset"):
             continue
         name = ev.get("name", "")
         key = name.split("(")[0].replace("void ", "") if cat == "kernel" else cat + " " + name.split(" ")[0]
         n, t = rows.get(key, (0, 0.0))
         rows[key] = (n + 1, t + float(ev.get("dur", 0.0)) / 1e3)
     total = sum(t for _, t in rows.values())
+    if not rows:
+        print(json.dumps({"kernel_trace": path, "error": "no device activity records", "categories": cats}),
+              flush=True)
+        return
     with open(path, "w") as f:
         f.write(f"# {cmd} --kernel-trace {os.path.basename(path)}\n")
         f.write("# per kernel: launches, device ms (sum over launches), share of device time\n")
@@ -520,7 +536,7 @@ def main():
     # ---- end to end through the public API with host buffers
     e2e = None
     if not args.no_e2e:
-        e2e = end_to_end(sampler, bundle, w, dev, min(K, 4), x)
+        e2e = end_to_end(sampler, bundle, w, dev, n_train - W, n_prod, x)
 
     line = {
         "metric": METRIC, "value": value, "unit": "chain-steps/s", "n_gpus": world, "steps": K, "warmup": W,
@@ -560,13 +576,16 @@ def main():
         dist.destroy_process_group()
 
 
-def end_to_end(sampler, bundle, w, dev, n_loops, x_dev):
-    """Production loops driven through Sampler.sample with host buffers: each
-    step copies its starting positions host->device (pinned) and reads back
-    the rows it wrote plus the final positions (device->host, pinned)."""
+def end_to_end(sampler, bundle, w, dev, n_train_loops, n_prod_loops, x_dev):
+    """The timed region's loop mix (n_train_loops training loops, then
+    n_prod_loops production loops) driven through Sampler.sample with host
+    buffers: every loop copies its starting positions host->device (pinned,
+    inside Sampler.sample) and reads back the rows it wrote plus the final
+    positions (device->host, pinned)."""
     import torch
+    train = ["local_stepper", "update_global_step", "model_trainer", "update_model", "global_stepper",
+             "update_local_step"]
     prod = ["local_stepper", "update_global_step", "global_stepper", "update_local_step"]
-    sampler.strategy_order = prod
     C, d = w["n_chains"], w["d"]
     blk = w["n_local"] + w["n_global"]
     x_host = torch.empty(C, d, pin_memory=True)
@@ -574,22 +593,25 @@ def end_to_end(sampler, bundle, w, dev, n_loops, x_dev):
     pos_h = torch.empty(C, blk, d, pin_memory=True)
     lp_h = torch.empty(C, blk, pin_memory=True)
     res = sampler.resources
+    state = res["sampler_state"]
     steppers = [sampler.strategies["local_stepper"], sampler.strategies["global_stepper"]]
+    plan = [train] * n_train_loops + [prod] * n_prod_loops
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(n_loops):
+    for order in plan:
+        sampler.strategy_order = order
         for s in steppers:
             s.set_current_position(0)
         last = sampler.sample(x_host, {})                 # h2d inside Sampler.sample
-        pos_h.copy_(res["positions_production"].data[:, :blk], non_blocking=True)
-        lp_h.copy_(res["log_prob_production"].data[:, :blk], non_blocking=True)
+        pos_h.copy_(res[state.data["target_positions"]].data[:, :blk], non_blocking=True)
+        lp_h.copy_(res[state.data["target_log_prob"]].data[:, :blk], non_blocking=True)
         x_host.copy_(last, non_blocking=True)
         torch.cuda.current_stream().synchronize()
     secs = time.perf_counter() - t0
     h2d = C * d * 4
     d2h = C * blk * d * 4 + C * blk * 4 + C * d * 4
-    return {"value": C * blk * n_loops / secs, "unit": "chain-steps/s", "h2d_bytes_per_step": h2d,
-            "d2h_bytes_per_step": d2h, "loops": n_loops}
+    return {"value": C * blk * len(plan) / secs, "unit": "chain-steps/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "training_loops": n_train_loops, "production_loops": n_prod_loops}
 
 
 if __name__ == "__main__":

@@ -90,19 +90,30 @@ __global__ void k_destandardize(float* __restrict__ x, int64_t n, int d, const f
   }
 }
 
-__global__ void k_affine(const float* __restrict__ in, float* __restrict__ out, float* __restrict__ cond, int64_t n,
-                         int d, int nc, int cpar, const float* __restrict__ th_layer, int inverse,
-                         float* __restrict__ ld, int ld_init) {
+// one warp per row: ScalarAffine of every coordinate, the conditioning
+// coordinates gathered into cond (fp32 [n, nc]) and/or cond16 (bf16 [n, ldc16],
+// columns nc..ldc16 zeroed: the operand of the first tensor-core GEMM)
+__global__ void k_affine(const float* __restrict__ in, float* __restrict__ out, float* __restrict__ cond,
+                         uint16_t* __restrict__ cond16, int ldc16, int64_t n, int d, int nc, int cpar,
+                         const float* __restrict__ th_layer, int inverse, float* __restrict__ ld, int ld_init) {
   const float s = th_layer[0], t = th_layer[1];
   const float es = expf(inverse ? -s : s);
-  const int64_t tot = n * d;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = i / d;
-    const int j = (int)(i - r * d);
-    const float v = inverse ? in[i] * es - t : (in[i] + t) * es;   // common.py:229, 238
-    out[i] = v;
-    if (cond != nullptr && ((j & 1) == cpar)) cond[r * nc + (j >> 1)] = v;
-    if (ld != nullptr && j == 0) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < n; r += warps) {
+    const float* ir = in + r * d;
+    float* orow = out + r * d;
+    for (int j = lane; j < d; j += 32) {
+      const float v = inverse ? ir[j] * es - t : (ir[j] + t) * es;   // common.py:229, 238
+      orow[j] = v;
+      if ((j & 1) == cpar) {
+        if (cond != nullptr) cond[r * nc + (j >> 1)] = v;
+        if (cond16 != nullptr) cond16[r * ldc16 + (j >> 1)] = f32_to_bf16_rn(v);
+      }
+    }
+    if (cond16 != nullptr)
+      for (int c = nc + lane; c < ldc16; c += 32) cond16[r * ldc16 + c] = 0;
+    if (ld != nullptr && lane == 0) {
       const float l = (float)d * (inverse ? -s : s);
       ld[r] = ld_init ? l : ld[r] + l;
     }
@@ -252,19 +263,21 @@ static int conditioner(const FmcFlow* f, const FlowGeom& g, int l, int64_t m, In
 // one pass over all layers for rows x[0, m) -> y, ld (forward or inverse)
 static int flow_pass(const FmcFlow* f, const FlowGeom& g, const float* x, float* y, float* ld, int64_t m, bool inverse,
                      InferWs& w, cudaStream_t st) {
-  const int grid = ew_grid(m * g.d);
+  const int grid = rows_grid(m);
   const bool bf16 = f->precision == FMC_PREC_BF16;
   for (int u = 0; u < g.L; ++u) {
     const int l = inverse ? g.L - 1 - u : u;
     const float* src = (u == 0) ? x : y;
-    k_affine<<<grid, 256, 0, st>>>(src, y, w.cond, m, g.d, g.nc(l), g.cpar(l), f->theta + g.layer_off[l],
-                                   inverse ? 1 : 0, ld, u == 0 ? 1 : 0);
+    // BF16: the conditioning block goes straight to the bf16 GEMM operand
+    k_affine<<<grid, 256, 0, st>>>(src, y, bf16 ? nullptr : w.cond, bf16 ? w.cond16 : nullptr, g.w16_cols(l, 0), m,
+                                   g.d, g.nc(l), g.cpar(l), f->theta + g.layer_off[l], inverse ? 1 : 0, ld,
+                                   u == 0 ? 1 : 0);
     FMC_LAUNCH_CHECK();
     int rc;
     if (bf16) {
       // hidden layers on tcgen05, then the last Linear fused with the spline
       const uint16_t* h_last = nullptr;
-      if ((rc = conditioner_bf16_hidden(f, g, l, m, w.cond, w.cond16, w.h16a, w.h16b, &h_last, st))) return rc;
+      if ((rc = conditioner_bf16_hidden(f, g, l, m, nullptr, w.cond16, w.h16a, w.h16b, &h_last, st))) return rc;
       const int64_t rows = (m + 127) / 128 * 128;
       if ((rc = tc_linear_spline(st, g, f, l, h_last, m, rows, inverse, y, ld, w.ldp))) return rc;
     } else {

@@ -247,7 +247,7 @@ int conditioner_bf16_hidden(const FmcFlow* f, const FlowGeom& g, int l, int64_t 
                             cudaStream_t st) {
   const int64_t rows = (m + tc::BM - 1) / tc::BM * tc::BM;
   const int nc = g.nc(l), ncp = g.w16_cols(l, 0);
-  {
+  if (cond != nullptr) {
     int64_t blocks = (m * ncp + 255) / 256;
     if (blocks > (int64_t)sm_count() * 16) blocks = (int64_t)sm_count() * 16;
     k_to_bf16_pad<<<(int)blocks, 256, 0, st>>>(cond, m, nc, ncp, cond16);

@@ -31,7 +31,8 @@ __device__ __forceinline__ uint16_t f32_to_bf16_rn(float v) {
 size_t train_ws_bytes(const FlowGeom& g, int64_t n, bool bf16);
 
 // the conditioner's hidden layers only (conversion + tanh GEMMs); *h_last is
-// the last tanh activation (bf16 [round_up(m, 128), round_up(H_last, 64)])
+// the last tanh activation (bf16 [round_up(m, 128), round_up(H_last, 64)]);
+// with cond == NULL, cond16 already holds the bf16 conditioning block
 int conditioner_bf16_hidden(const FmcFlow* f, const FlowGeom& g, int l, int64_t m, const float* cond,
                             uint16_t* cond16, uint16_t* h16a, uint16_t* h16b, const uint16_t** h_last,
                             cudaStream_t st);

@@ -108,21 +108,55 @@ __global__ void k_copy_if(const int32_t* __restrict__ flag, const uint4* __restr
   if (blockIdx.x == 0 && threadIdx.x < tail) dst_tail[threadIdx.x] = src_tail[threadIdx.x];
 }
 
-// column mean and unbiased variance of x [n, d] (two passes, fixed order)
-__global__ void k_column_stats(const float* __restrict__ x, int64_t n, int d, float* __restrict__ mean,
-                               float* __restrict__ var) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= d) return;
+// Column mean and unbiased variance of x [n, d] in two deterministic stages:
+// row block b (rows [b*rows_per, ...)) computes, per column, its own mean and
+// sum of squared deviations (two passes over its rows, coalesced across the
+// column); the final kernel merges the blocks in index order with the
+// pairwise update of Chan, Golub and LeVeque (1979):
+//   n = na + nb, delta = mb - ma, m = ma + delta nb / n, M2 = M2a + M2b + delta^2 na nb / n.
+// Partials live in a static device buffer (one column tile at a time), so
+// concurrent calls on different streams of one device must not overlap.
+constexpr int kColStatBlocks = 512;
+constexpr int kColStatCols = 512;
+__device__ float g_colstat_scratch[2 * kColStatBlocks * kColStatCols];
+
+// x points at the tile's first column; row stride d, tile width dc
+__global__ void k_colstat_partial(const float* __restrict__ x, int64_t n, int d, int dc, int64_t rows_per,
+                                  float* __restrict__ pmean, float* __restrict__ pm2) {
+  const int j = blockIdx.y * blockDim.x + threadIdx.x;
+  if (j >= dc) return;
+  const int64_t r0 = blockIdx.x * rows_per;
+  const int64_t r1 = (r0 + rows_per < n) ? r0 + rows_per : n;
   float s = 0.f;
-  for (int64_t r = 0; r < n; ++r) s += x[r * d + j];
-  const float mu = s / (float)n;
+  for (int64_t r = r0; r < r1; ++r) s += x[r * d + j];
+  const float mu = r1 > r0 ? s / (float)(r1 - r0) : 0.f;
   float q = 0.f;
-  for (int64_t r = 0; r < n; ++r) {
+  for (int64_t r = r0; r < r1; ++r) {
     const float e = x[r * d + j] - mu;
     q += e * e;
   }
-  mean[j] = mu;
-  var[j] = q / (float)(n - 1);
+  pmean[(int64_t)blockIdx.x * dc + j] = mu;
+  pm2[(int64_t)blockIdx.x * dc + j] = q;
+}
+
+__global__ void k_colstat_final(const float* __restrict__ pmean, const float* __restrict__ pm2, int rb, int64_t n,
+                                int d, int64_t rows_per, float* __restrict__ mean, float* __restrict__ var) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= d) return;
+  double na = 0.0, ma = 0.0, m2 = 0.0;
+  for (int b = 0; b < rb; ++b) {
+    const int64_t r0 = b * rows_per;
+    const int64_t r1 = (r0 + rows_per < n) ? r0 + rows_per : n;
+    const double nb = (double)(r1 - r0);
+    if (nb <= 0.0) continue;
+    const double mb = pmean[(int64_t)b * d + j], qb = pm2[(int64_t)b * d + j];
+    const double nn = na + nb, delta = mb - ma;
+    ma += delta * nb / nn;
+    m2 += qb + delta * delta * na * nb / nn;
+    na = nn;
+  }
+  mean[j] = (float)ma;
+  var[j] = (float)(m2 / (double)(n - 1));
 }
 
 // ---------------------------------------------------------------- Feistel permutation
@@ -326,8 +360,26 @@ extern "C" int fmc_copy_if(const int32_t* flag, const void* src, void* dst, size
 extern "C" int fmc_column_stats(const float* x, int64_t n, int32_t d, float* mean, float* var, void* stream) {
   FMC_CHECK_ARG(x && mean && var, "NULL pointer");
   FMC_CHECK_ARG(n >= 2 && d >= 1, "need n >= 2 rows and d >= 1");
-  k_column_stats<<<(d + 127) / 128, 128, 0, (cudaStream_t)stream>>>(x, n, d, mean, var);
-  FMC_LAUNCH_CHECK();
+  cudaStream_t st = (cudaStream_t)stream;
+  float* part = nullptr;
+  FMC_CUDA_TRY(cudaGetSymbolAddress((void**)&part, g_colstat_scratch));
+  // column tiles of at most kColStatCols; per tile enough row blocks to cover
+  // the SMs a few times over (at most kColStatBlocks, at least 64 rows each)
+  for (int c0 = 0; c0 < d; c0 += kColStatCols) {
+    const int dc = (d - c0 < kColStatCols) ? d - c0 : kColStatCols;
+    int64_t rb = (int64_t)sm_count() * 4 * 128 / (dc < 128 ? 128 : dc);
+    if (rb > kColStatBlocks) rb = kColStatBlocks;
+    if (rb > (n + 63) / 64) rb = (n + 63) / 64;
+    if (rb < 1) rb = 1;
+    const int64_t rows_per = (n + rb - 1) / rb;
+    rb = (n + rows_per - 1) / rows_per;
+    dim3 grid((unsigned)rb, (unsigned)((dc + 127) / 128));
+    k_colstat_partial<<<grid, 128, 0, st>>>(x + c0, n, d, dc, rows_per, part, part + rb * dc);
+    FMC_LAUNCH_CHECK();
+    k_colstat_final<<<(dc + 127) / 128, 128, 0, st>>>(part, part + rb * dc, (int)rb, n, dc, rows_per, mean + c0,
+                                                       var + c0);
+    FMC_LAUNCH_CHECK();
+  }
   return FMC_OK;
 }
 

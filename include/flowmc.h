@@ -261,7 +261,9 @@ FMC_API int fmc_flag_less(const float* a, float* best, int32_t* flag, void* stre
 FMC_API int fmc_copy_if(const int32_t* flag, const void* src, void* dst, size_t bytes, void* stream);
 
 /* data_mean and diag(data_cov) of x [n, d] (nf_model/base.py:187-188):
- * mean [d], unbiased variance [d]. */
+ * mean [d], unbiased variance [d]. Deterministic two-stage reduction whose
+ * partials live in a static device buffer: calls on different streams of
+ * one device must not run concurrently. */
 FMC_API int fmc_column_stats(const float* x, int64_t n, int32_t d, float* mean, float* var, void* stream);
 
 /* dst[r] = src[perm(first + r)] for r < m, perm a pseudo-random permutation of

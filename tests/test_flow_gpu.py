@@ -319,3 +319,21 @@ def test_training_bf16_reduces_loss(cuda):
     losses = losses.cpu().numpy()
     assert np.isfinite(losses).all()
     assert losses[-1] < losses[0] - 0.3, losses
+
+
+@pytest.mark.parametrize("n,d", [(2, 1), (1000, 7), (300000, 128), (5000, 1500)])
+def test_column_stats_matches_numpy(cuda, n, d):
+    """fmc_column_stats (data standardisation before training, nf_model/base.py:
+    data mean and variance): two-stage block merge against float64 numpy,
+    on columns with a large offset and a small spread."""
+    from flowmc_gb300 import _lib
+    rng = np.random.default_rng(n + d)
+    x = (rng.normal(size=(n, d)) * rng.uniform(1e-2, 3.0, size=d) + rng.uniform(-100, 100, size=d)).astype(np.float32)
+    xt = torch.tensor(x, device="cuda")
+    mean = torch.empty(d, device="cuda")
+    var = torch.empty(d, device="cuda")
+    _lib.check(_lib.lib().fmc_column_stats(xt.data_ptr(), n, d, mean.data_ptr(), var.data_ptr(),
+                                           _lib.stream_handle()))
+    x64 = x.astype(np.float64)
+    np.testing.assert_allclose(mean.cpu().numpy(), x64.mean(0), rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(var.cpu().numpy(), x64.var(0, ddof=1), rtol=2e-4, atol=1e-6)
