@@ -53,6 +53,7 @@ struct LocalArgs {
   float* x_last;
   float* lp_last;
   int64_t C_pad;
+  int32_t tab_smem;   // diag Gaussian / mixture: tables staged in shared memory
 };
 
 template <int V>
@@ -109,24 +110,23 @@ __device__ __forceinline__ float draw_uniform(const LocalArgs& a, int64_t c, int
 
 template <int G, int V>
 __device__ __forceinline__ void store_row(float* dst, const float (&x)[V], int gl, int d) {
-  // dst points at element 0 of the row
+  // dst points at element 0 of the row. With d a multiple of the vector
+  // width, each vector chunk of a lane's coordinates is wholly inside the row
+  // or wholly padding, so the guard is per chunk (a lane may straddle d).
   if constexpr (V % 4 == 0) {
     if (d % 4 == 0) {
-      if (gl * V < d) {
 #pragma unroll
-        for (int q = 0; q < V; q += 4)
+      for (int q = 0; q < V; q += 4)
+        if (gl * V + q < d)
           __stcs(reinterpret_cast<float4*>(dst + gl * V + q), make_float4(x[q], x[q + 1], x[q + 2], x[q + 3]));
-      }
       return;
     }
   }
   if constexpr (V % 2 == 0) {
     if (d % 2 == 0) {
-      if (gl * V < d) {
 #pragma unroll
-        for (int q = 0; q < V; q += 2)
-          __stcs(reinterpret_cast<float2*>(dst + gl * V + q), make_float2(x[q], x[q + 1]));
-      }
+      for (int q = 0; q < V; q += 2)
+        if (gl * V + q < d) __stcs(reinterpret_cast<float2*>(dst + gl * V + q), make_float2(x[q], x[q + 1]));
       return;
     }
   }
@@ -145,6 +145,13 @@ __global__ void __launch_bounds__(256) k_local_steps(const LocalArgs a) {
   const int64_t gib = threadIdx.x / G;
   const int d = a.d;
   float* stage = (TGT == FMC_TARGET_DENSE_GAUSSIAN) ? smem + gib * d : nullptr;
+  if constexpr (TGT == FMC_TARGET_DIAG_GAUSSIAN || TGT == FMC_TARGET_GAUSS_MIXTURE) {
+    if (a.tab_smem) {
+      stage_target_table(a.tgt, smem);
+      __syncthreads();
+      stage = smem;
+    }
+  }
   const float dt = a.step;
 
   for (int64_t c = blockIdx.x * groups_per_block + gib; c < a.C_pad;
@@ -164,6 +171,12 @@ __global__ void __launch_bounds__(256) k_local_steps(const LocalArgs a) {
     for (int v = 0; v < V; ++v) xr[v] = x[v];
 
     u32x4 ub{0u, 0u, 0u, 0u};
+    // next stored row (every thin-th step, from row `start`)
+    const int64_t row0 = cc * a.buf_len + a.start;
+    float* prow = a.out_pos + row0 * d;
+    float* plp = a.out_logp + row0;
+    float* pacc = a.out_acc + row0;
+    int tcount = 0;
     for (int s = 0; s < a.S; ++s) {
       float xi[V];
       draw_normals<V>(a, cc, s, gl, xi);
@@ -252,19 +265,22 @@ __global__ void __launch_bounds__(256) k_local_steps(const LocalArgs a) {
           lp = lpp;
         }
       }
-      if (s % a.thin == 0) {
+      if (tcount == 0) {
         if (active) {
-          const int64_t row = cc * a.buf_len + a.start + s / a.thin;
-          store_row<G, V>(a.out_pos + row * d, x, gl, d);
+          store_row<G, V>(prow, x, gl, d);
           if (gl == 0) {
-            __stcs(a.out_logp + row, lp);
-            __stcs(a.out_acc + row, acc ? 1.f : 0.f);
+            __stcs(plp, lp);
+            __stcs(pacc, acc ? 1.f : 0.f);
           }
         }
+        prow += d;
+        ++plp;
+        ++pacc;
 #pragma unroll
         for (int v = 0; v < V; ++v) xr[v] = x[v];
         lpr = lp;
       }
+      if (++tcount == a.thin) tcount = 0;
     }
     if (active) {
 #pragma unroll
@@ -333,7 +349,16 @@ int launch_local_t(const LocalArgs& a0, cudaStream_t st) {
   const int gpb = threads / G;
   const int gpw = 32 / G;
   a.C_pad = ((int64_t)a.C + gpw - 1) / gpw * gpw;
-  const size_t smem = (TGT == FMC_TARGET_DENSE_GAUSSIAN) ? (size_t)gpb * a.d * sizeof(float) : 0;
+  size_t smem = (TGT == FMC_TARGET_DENSE_GAUSSIAN) ? (size_t)gpb * a.d * sizeof(float) : 0;
+  a.tab_smem = 0;
+  if (TGT == FMC_TARGET_DIAG_GAUSSIAN || TGT == FMC_TARGET_GAUSS_MIXTURE) {
+    const int K = (TGT == FMC_TARGET_GAUSS_MIXTURE) ? a.tgt.n_comp : 1;
+    const size_t tab = (size_t)2 * K * a.d * sizeof(float);
+    if (tab <= 32 * 1024) {   // small tables only: keeps several blocks per SM
+      smem = tab;
+      a.tab_smem = 1;
+    }
+  }
   auto kern = k_local_steps<KIND, TGT, G, V>;
   if (smem > 48 * 1024) {
     FMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

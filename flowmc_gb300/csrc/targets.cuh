@@ -25,12 +25,61 @@ __device__ __forceinline__ float ldg_or(const float* p, int64_t i, float dflt) {
   return p ? __ldg(p + i) : dflt;
 }
 
+// The V entries of this lane's coordinates from one row of a shared-memory
+// table (a lane's coordinates are fixed for the whole kernel); padding
+// coordinates read 0. float4 loads when the rows are 16-byte aligned.
+template <int V>
+__device__ __forceinline__ void tab_row(const float* row, int gl, int d, float (&out)[V]) {
+  const int j0 = gl * V;
+  if constexpr (V % 4 == 0) {
+    if ((d & 3) == 0) {
+#pragma unroll
+      for (int q = 0; q < V; q += 4) {
+        // d % 4 == 0: a 4-coordinate chunk is either wholly inside the row or wholly padding
+        const float4 t =
+            (j0 + q < d) ? *reinterpret_cast<const float4*>(row + j0 + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+        out[q] = t.x; out[q + 1] = t.y; out[q + 2] = t.z; out[q + 3] = t.w;
+      }
+      return;
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < V; ++v) out[v] = (j0 + v < d) ? row[j0 + v] : 0.f;
+}
+
+// Shared-memory copy of the diagonal-Gaussian / mixture tables: means
+// [K * d] then inverse variances [K * d] (missing tables get 0 and 1).
+__device__ __forceinline__ int target_table_floats(const FmcTarget& t) {
+  const int K = (t.kind == FMC_TARGET_GAUSS_MIXTURE) ? t.n_comp : 1;
+  return 2 * K * t.n_dim;
+}
+__device__ __forceinline__ void stage_target_table(const FmcTarget& t, float* tab) {
+  const int n = target_table_floats(t) / 2;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    tab[i] = t.mean ? __ldg(t.mean + i) : 0.f;
+    tab[n + i] = t.inv_var ? __ldg(t.inv_var + i) : 1.f;
+  }
+}
+
 // --------------------------------------------------------------- diag Gaussian
+// tab: the shared-memory table (stage_target_table) or NULL for global loads
 template <int G, int V, bool GRAD>
 __device__ __forceinline__ float tg_diag_gaussian(const FmcTarget& t, const float (&x)[V],
-                                                  float (&g)[V], int gl) {
+                                                  float (&g)[V], int gl, const float* tab) {
   const int d = t.n_dim;
   float s = 0.f;
+  if (tab != nullptr) {
+    float mu[V], iv[V];
+    tab_row<V>(tab, gl, d, mu);
+    tab_row<V>(tab + d, gl, d, iv);   // 0 on padding coordinates: no contribution
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const float dx = x[v] - mu[v];
+      s += dx * dx * iv[v];
+      if (GRAD) g[v] = -dx * iv[v];
+    }
+    return -0.5f * group_sum<G>(s) + t.scalars[0];
+  }
 #pragma unroll
   for (int v = 0; v < V; ++v) {
     const int j = gl * V + v;
@@ -88,7 +137,7 @@ __device__ __forceinline__ float tg_dual_moon(const FmcTarget& t, const float (&
 // arrays, so the loop stays rolled and register use stays flat in K.
 template <int G, int V, bool GRAD>
 __device__ __forceinline__ float tg_mixture(const FmcTarget& t, const float (&x)[V],
-                                            float (&g)[V], int gl) {
+                                            float (&g)[V], int gl, const float* tab) {
   const int d = t.n_dim, K = t.n_comp;
   float m = -INFINITY, S = 0.f;
   float Gr[V];
@@ -98,15 +147,27 @@ __device__ __forceinline__ float tg_mixture(const FmcTarget& t, const float (&x)
   for (int k = 0; k < K; ++k) {
     float q = 0.f;
     float gk[V];
+    if (tab != nullptr) {
+      float mu[V], iv[V];
+      tab_row<V>(tab + k * d, gl, d, mu);
+      tab_row<V>(tab + (K + k) * d, gl, d, iv);   // 0 on padding coordinates
 #pragma unroll
-    for (int v = 0; v < V; ++v) {
-      const int j = gl * V + v;
-      gk[v] = 0.f;
-      if (j < d) {
-        const float dx = x[v] - ldg_or(t.mean, (int64_t)k * d + j, 0.f);
-        const float iv = ldg_or(t.inv_var, (int64_t)k * d + j, 1.f);
-        q += dx * dx * iv;
-        gk[v] = -dx * iv;
+      for (int v = 0; v < V; ++v) {
+        const float dx = x[v] - mu[v];
+        q += dx * dx * iv[v];
+        gk[v] = -dx * iv[v];
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        const int j = gl * V + v;
+        gk[v] = 0.f;
+        if (j < d) {
+          const float dx = x[v] - ldg_or(t.mean, (int64_t)k * d + j, 0.f);
+          const float iv = ldg_or(t.inv_var, (int64_t)k * d + j, 1.f);
+          q += dx * dx * iv;
+          gk[v] = -dx * iv;
+        }
       }
     }
     const float e = ldg_or(t.log_w, k, 0.f) - 0.5f * group_sum<G>(q);
@@ -203,12 +264,15 @@ __device__ __forceinline__ float tg_dense_gaussian(const FmcTarget& t, const flo
   return -0.5f * group_sum<G>(s) + t.scalars[0];
 }
 
+// stage: the dense Gaussian's per-group scratch (n_dim floats), or for the
+// diagonal Gaussian and the mixture the block's shared-memory table copy
+// (stage_target_table; NULL = read the tables from global memory)
 template <int TGT, int G, int V, bool GRAD>
 __device__ __forceinline__ float target_eval(const FmcTarget& t, const float (&x)[V],
                                              float (&g)[V], int gl, float* stage) {
-  if constexpr (TGT == FMC_TARGET_DIAG_GAUSSIAN) return tg_diag_gaussian<G, V, GRAD>(t, x, g, gl);
+  if constexpr (TGT == FMC_TARGET_DIAG_GAUSSIAN) return tg_diag_gaussian<G, V, GRAD>(t, x, g, gl, stage);
   else if constexpr (TGT == FMC_TARGET_DUAL_MOON) return tg_dual_moon<G, V, GRAD>(t, x, g, gl);
-  else if constexpr (TGT == FMC_TARGET_GAUSS_MIXTURE) return tg_mixture<G, V, GRAD>(t, x, g, gl);
+  else if constexpr (TGT == FMC_TARGET_GAUSS_MIXTURE) return tg_mixture<G, V, GRAD>(t, x, g, gl, stage);
   else if constexpr (TGT == FMC_TARGET_ROSENBROCK) return tg_rosenbrock<G, V, GRAD>(t, x, g, gl);
   else return tg_dense_gaussian<G, V, GRAD>(t, x, g, gl, stage);
 }

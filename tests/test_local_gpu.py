@@ -36,6 +36,14 @@ def make_targets():
         "rosenbrock128": TG.Rosenbrock(128),
         "dense": TG.DenseGaussian(P, mean=rng.normal(size=6)),
         "mixture64": TG.GaussianMixture(rng.normal(size=(4, 64)), 0.5),
+        # d % 4 == 0 with d < lanes x coordinates: the shared-memory tables are read as
+        # float4 and the last lane's chunks straddle the end of the row
+        "mixture20": TG.GaussianMixture(rng.normal(size=(3, 20)), rng.uniform(0.3, 1.0, size=(3, 20))),
+        "diag20": TG.DiagGaussian(20, mean=rng.normal(size=20), inv_var=rng.uniform(0.5, 2.0, size=20)),
+        # default chain blocks whose last lane straddles d: d = 18 with 8 lanes x 4
+        # (float2 row stores) and d = 132 with 32 lanes x 8 (float4 row stores)
+        "diag18": TG.DiagGaussian(18, mean=rng.normal(size=18), inv_var=rng.uniform(0.5, 2.0, size=18)),
+        "mixture132": TG.GaussianMixture(rng.normal(size=(2, 132)), 0.7),
     }
 
 
@@ -98,6 +106,8 @@ CASES = [
     ("hmc", "rosenbrock", 0.01, 10), ("hmc", "dense", 0.1, 5), ("hmc", "rosenbrock128", 0.01, 16),
     ("grw", "std2", 1.0, 0), ("grw", "dual_moon", 0.05, 0), ("grw", "mixture", 0.5, 0),
     ("grw", "rosenbrock", 0.05, 0), ("grw", "mixture64", 0.1, 0),
+    ("mala", "mixture20", 0.2, 0), ("grw", "diag20", 0.3, 0), ("hmc", "diag20", 0.1, 3),
+    ("grw", "diag18", 0.3, 0), ("mala", "mixture132", 0.05, 0),
 ]
 
 
@@ -145,9 +155,10 @@ def test_trajectory_parity(tgts, kind, tname, step, nlf):
     assert 0 < acc.mean() <= 1
 
 
+@pytest.mark.parametrize("tname", ["mixture", "mixture20"])
 @pytest.mark.parametrize("lanes", [4, 8, 16, 32])
-def test_lane_shapes_agree(tgts, lanes):
-    tgt = tgts["mixture"]
+def test_lane_shapes_agree(tgts, lanes, tname):
+    tgt = tgts[tname]
     C, S, d = 6, 12, tgt.n_dim
     rng = np.random.default_rng(5)
     x0 = rng.normal(size=(C, d)).astype(np.float32)
