@@ -2,6 +2,7 @@
 // conditioner path of the flow: TMA tensor maps, the bf16 weight packing and
 // the conditioner MLP as a chain of tensor-core GEMMs with fused epilogues.
 #include <cudaTypedefs.h>
+#include <cstring>
 #include <mutex>
 #include "gemm_tc.cuh"
 #include "tc_gemm.cuh"
@@ -88,14 +89,17 @@ size_t splitk_scratch_floats(int64_t M, int N, int K) {
   return s > 1 ? (size_t)s * (size_t)M * (size_t)N : 0;
 }
 
-template <int BN, int STAGES, int EPI>
-static int launch_tc(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& mb, int64_t M, int N, int K,
-                     const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store) {
+template <int BN, int STAGES, int EPI, bool TSTORE>
+static int launch_tc(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap& mc, int64_t M,
+                     int N, int K, const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store) {
   using S = tc::Smem<BN, STAGES>;
-  auto kern = tc::k_tc_gemm<BN, STAGES, EPI>;
+  // ring + alignment slack + barrier block (1024 with TSTORE, so the staging stays 1024-aligned) + staging
+  constexpr int TOTAL = TSTORE ? S::TOTAL + 768 + tc::kStagingBytes : S::TOTAL;
+  static_assert(TOTAL <= 227 * 1024, "tcgen05 GEMM: shared memory over the per-CTA limit");
+  auto kern = tc::k_tc_gemm<BN, STAGES, EPI, TSTORE>;
   static bool attr_set = false;
   if (!attr_set) {
-    FMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S::TOTAL));
+    FMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, TOTAL));
     attr_set = true;
   }
   int* err = nullptr;
@@ -111,8 +115,8 @@ static int launch_tc(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& 
   const int64_t items = tiles * splits;
   const int64_t grid = items < sm_count() ? items : sm_count();   // persistent: one CTA per SM
   void* out = splits > 1 ? (void*)ep.kpart : C;
-  kern<<<(unsigned)grid, tc::kThreads, S::TOTAL, st>>>(ma, mb, (int)M, N, K, ep, out, ldc, n_store, splits, M * ldc,
-                                                      err);
+  kern<<<(unsigned)grid, tc::kThreads, TOTAL, st>>>(ma, mb, mc, (int)M, N, K, ep, out, ldc, n_store, splits, M * ldc,
+                                                   err);
   FMC_LAUNCH_CHECK();
   if (splits > 1) {
     int64_t blocks = (M * n_store + 255) / 256;
@@ -134,20 +138,34 @@ int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K
   if (epi == tc::TC_EPI_DTANH_BF16) FMC_CHECK_ARG(ep.aux != nullptr, "aux is NULL");
   if (M <= 0) return FMC_OK;
   const int BN = (N > 128) ? 256 : 128;
-  CUtensorMap ma, mb;
+  CUtensorMap ma, mb, mc;
   int rc = make_map(&ma, A, K, rows_a, K, tc::BM);
   if (rc) return rc;
   if ((rc = make_map(&mb, B, K, rows_b, K, BN))) return rc;
-#define TC_CASE(E)                                                                              \
-  if (epi == E) {                                                                               \
-    if (BN == 256) return launch_tc<256, 4, E>(st, ma, mb, M, N, K, ep, C, ldc, n_store);       \
-    return launch_tc<128, 4, E>(st, ma, mb, M, N, K, ep, C, ldc, n_store);                      \
+  // bf16 outputs go out through TMA stores when C can carry a tensor map
+  // (16-byte aligned rows, at least one 64 x 32 box)
+  const bool bf16_out = epi == tc::TC_EPI_TANH_BF16 || epi == tc::TC_EPI_DTANH_BF16;
+  const bool tstore = bf16_out && ((uintptr_t)C & 15) == 0 && (ldc * 2) % 16 == 0 && n_store >= 64 && M >= 32;
+  memset(&mc, 0, sizeof(mc));
+  if (tstore && (rc = make_map(&mc, C, n_store, M, ldc, 32))) return rc;
+#define TC_CASE(E)                                                                                            \
+  if (epi == E) {                                                                                             \
+    if (BN == 256) return launch_tc<256, 4, E, false>(st, ma, mb, mc, M, N, K, ep, C, ldc, n_store);          \
+    return launch_tc<128, 4, E, false>(st, ma, mb, mc, M, N, K, ep, C, ldc, n_store);                         \
   }
+#define TC_CASE_TS(E)                                                                                         \
+  if (epi == E && tstore) {                                                                                   \
+    if (BN == 256) return launch_tc<256, 3, E, true>(st, ma, mb, mc, M, N, K, ep, C, ldc, n_store);           \
+    return launch_tc<128, 4, E, true>(st, ma, mb, mc, M, N, K, ep, C, ldc, n_store);                          \
+  }
+  TC_CASE_TS(tc::TC_EPI_TANH_BF16)
+  TC_CASE_TS(tc::TC_EPI_DTANH_BF16)
   TC_CASE(tc::TC_EPI_TANH_BF16)
   TC_CASE(tc::TC_EPI_BIAS_F32)
   TC_CASE(tc::TC_EPI_DTANH_BF16)
   TC_CASE(tc::TC_EPI_F32)
 #undef TC_CASE
+#undef TC_CASE_TS
   set_error("unknown epilogue %d", epi);
   return FMC_ERR_INVALID_ARG;
 }

@@ -164,20 +164,49 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
+// ---- TMA store of the bf16 epilogues: each epilogue warp stages a 32-row x
+// 64-column block (4 KB, the 128-byte swizzle of the output tensor map: the
+// 16-byte chunk c of row r sits at r*128 + ((c ^ (r & 7)) * 16)) and one lane
+// stores it with cp.async.bulk.tensor; two staging buffers per warp.
+constexpr int kStageBlockBytes = 32 * 128;
+constexpr int kStagingBytes = kEpiWarps * 2 * kStageBlockBytes;
+
+__device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
+  asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
+}
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, uint32_t src, int c0, int c1) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];"
+               ::"l"((uint64_t)map), "r"(src), "r"(c0), "r"(c1)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// at most one committed store group may still be reading shared memory
+__device__ __forceinline__ void bulk_wait_read_1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 // Persistent GEMM: each CTA walks work items t = blockIdx.x, +gridDim.x, ...
 // Item t is K-slice s = t % splits of tile t / splits (tile u covers rows
 // (u / n_tiles) * 128 and columns (u % n_tiles) * BN); with splits > 1 the
 // slices write their fp32 partial products to C + s * split_stride and the
 // host reduces them. Two TMEM accumulators let the epilogue of one item
 // overlap the MMAs of the next. err: device word; 1 = a wait expired.
-template <int BN, int STAGES, int EPI>
+// TSTORE (bf16 modes only): the row-major output goes through per-warp
+// shared-memory staging and TMA stores on tmC ([M, n_store] bf16, box 64 x 32);
+// the shared memory then holds the ring, its barriers, 768 bytes of padding
+// and the staging buffers (kStagingBytes, 1024-byte aligned).
+template <int BN, int STAGES, int EPI, bool TSTORE>
 __global__ void __launch_bounds__(kThreads, 1)
-    k_tc_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N, int K,
-              const EpiArgs ep, void* __restrict__ C, int64_t ldc, int n_store, int splits, int64_t split_stride,
-              int* err) {
+    k_tc_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+              const __grid_constant__ CUtensorMap tmC, int M, int N, int K, const EpiArgs ep, void* __restrict__ C,
+              int64_t ldc, int n_store, int splits, int64_t split_stride, int* err) {
+  static_assert(!TSTORE || EPI == TC_EPI_TANH_BF16 || EPI == TC_EPI_DTANH_BF16, "TMA store: bf16 epilogues only");
   extern __shared__ uint8_t smem_raw[];
   using S = Smem<BN, STAGES>;
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t* staging = base + STAGES * S::STAGE_BYTES + 1024;
   uint64_t* full = (uint64_t*)(base + STAGES * S::STAGE_BYTES);
   uint64_t* empty = full + STAGES;
   uint64_t* acc_full = empty + STAGES;      // [2]
@@ -296,6 +325,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int esz = (EPI == TC_EPI_TANH_BF16 || EPI == TC_EPI_DTANH_BF16) ? 2 : 4;
     const bool vec_ok = (((uintptr_t)C & 15) == 0) && ((ldc * esz) % 16 == 0);
     const bool aux_vec = (((uintptr_t)ep.aux & 15) == 0) && ((ep.ldaux * 2) % 16 == 0);
+    int blkno = 0;   // staged blocks so far (selects the staging buffer)
     int local = 0;
     for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++local) {
       const int b = local & 1, use = local >> 1;
@@ -313,7 +343,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       // One 32-column chunk: v = accumulator row segment, bl = bias of column
       // n0 + c0 + lane (lane-distributed, broadcast with shuffles before any
       // lane-dependent branch), av = the row's tanh activations (mode 2).
-      auto chunk = [&](const uint32_t (&r)[32], int c0, float bl, const uint4 (&av)[4]) {
+      auto chunk = [&](const uint32_t (&r)[32], int c0, float bl, const uint4 (&av)[4], int sub) {
         const int gn0 = n0 + c0;
         if (gn0 >= n_store) return;   // uniform across the warp
         float v[32];
@@ -323,7 +353,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
           for (int i = 0; i < 32; ++i) v[i] += __shfl_sync(0xffffffffu, bl, i);
         }
-        if (!(row_ok || ct_row)) return;
+        if (!TSTORE && !(row_ok || ct_row)) return;
         if (EPI == TC_EPI_TANH_BF16 || EPI == TC_EPI_DTANH_BF16) {
           uint32_t packed[16];
           float y[32];
@@ -343,7 +373,16 @@ __global__ void __launch_bounds__(kThreads, 1)
             const __nv_bfloat162 hh = __floats2bfloat162_rn(y[i], y[i + 1]);
             packed[i / 2] = *reinterpret_cast<const uint32_t*>(&hh);
           }
-          if (row_ok) {
+          if (TSTORE) {
+            // half `sub` of this warp's current 64-column block (zeros in rows >= M are clipped by the store)
+            const uint32_t buf = smem_u32(staging) + (uint32_t)(((warp - 2) * 2 + (blkno & 1)) * kStageBlockBytes);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const int cc = sub * 4 + k;
+              st_shared_v4(buf + (uint32_t)(lane * 128 + ((cc ^ (lane & 7)) << 4)), packed[4 * k], packed[4 * k + 1],
+                           packed[4 * k + 2], packed[4 * k + 3]);
+            }
+          } else if (row_ok) {
             __nv_bfloat16* out = (__nv_bfloat16*)C + (int64_t)gm * ldc + gn0;
             if (gn0 + 32 <= n_store && vec_ok) {
               uint4* o4 = reinterpret_cast<uint4*>(out);
@@ -401,19 +440,22 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         }
       };
-      // software pipeline over this warp's chunks c0 = half*32 + 64*i: the
-      // TMEM load and global operands of chunk i+1 are in flight while chunk i
-      // is processed; the accumulator goes back to the MMA warp as soon as
-      // its last chunk is in registers
+      // software pipeline over this warp's NCH 32-column chunks: the TMEM
+      // load and global operands of chunk i+1 are in flight while chunk i is
+      // processed; the accumulator goes back to the MMA warp as soon as its
+      // last chunk is in registers. Chunk order: alternate 32-column chunks of
+      // the two warps of a quarter, or with TSTORE whole 64-column blocks
+      // (warp `half` takes blocks half, half + 2, ...).
       constexpr int NCH = BN / 64;
+      auto col_of = [&](int i) { return TSTORE ? (half + 2 * (i >> 1)) * 64 + 32 * (i & 1) : half * 32 + 64 * i; };
       uint32_t ra[32], rb[32];
       float bl_cur = 0.f, bl_nxt = 0.f;
       uint4 av_cur[4], av_nxt[4];
-      tmem_ld32_issue(tbase + (uint32_t)(half * 32), ra);
-      prefetch(half * 32, bl_nxt, av_nxt);
+      tmem_ld32_issue(tbase + (uint32_t)col_of(0), ra);
+      prefetch(col_of(0), bl_nxt, av_nxt);
 #pragma unroll
       for (int i = 0; i < NCH; ++i) {
-        const int c0 = half * 32 + 64 * i;
+        const int c0 = col_of(i);
         uint32_t(&cur)[32] = (i & 1) ? rb : ra;
         uint32_t(&nxt)[32] = (i & 1) ? ra : rb;
         bl_cur = bl_nxt;
@@ -421,18 +463,36 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int k = 0; k < 4; ++k) av_cur[k] = av_nxt[k];
         tmem_wait_pin(cur);
         if (i + 1 < NCH) {
-          tmem_ld32_issue(tbase + (uint32_t)(c0 + 64), nxt);
-          prefetch(c0 + 64, bl_nxt, av_nxt);
+          tmem_ld32_issue(tbase + (uint32_t)col_of(i + 1), nxt);
+          prefetch(col_of(i + 1), bl_nxt, av_nxt);
         } else {
           // this warp's TMEM lanes of buffer b are read: release them to the MMA warp
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
           __syncwarp();
           if (lane == 0) mbar_arrive(&acc_empty[b]);
         }
-        chunk(cur, c0, bl_cur, av_cur);
+        const bool blk_live = n0 + (c0 & ~63) < n_store;   // uniform
+        if (TSTORE && (i & 1) == 0 && blk_live) {
+          // the staging buffer about to be filled was last used two blocks ago
+          if (lane == 0) bulk_wait_read_1();
+          __syncwarp();
+        }
+        chunk(cur, c0, bl_cur, av_cur, i & 1);
+        if (TSTORE && (i & 1) == 1 && blk_live) {
+          fence_proxy_async_smem();
+          __syncwarp();
+          if (lane == 0) {
+            tma_store_2d(&tmC, smem_u32(staging) + (uint32_t)(((warp - 2) * 2 + (blkno & 1)) * kStageBlockBytes),
+                         n0 + (c0 & ~63), m0 + q * 32);
+            bulk_commit();
+          }
+          ++blkno;
+        }
       }
     }
   }
+  // staged stores must finish reading shared memory before the CTA exits
+  if (TSTORE && warp >= 2 && lane == 0) bulk_wait_all();
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 1) {
