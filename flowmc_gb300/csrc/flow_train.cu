@@ -371,17 +371,21 @@ int flow_loss_grad(const FmcFlow* f, const float* x, int64_t n, float* loss, flo
   // ---- forward, saving layer inputs
   k_standardize<<<eb, 256, 0, st>>>(x, n, d, f->aux, w.xs);
   FMC_LAUNCH_CHECK();
+  int parts = 0;   // log-det partials of the previous fused spline layer, folded in by k_affine
   for (int l = 0; l < g.L; ++l) {
     float* xin = w.xs + (int64_t)l * nd;
     float* xout = w.xs + (int64_t)(l + 1) * nd;
     k_affine<<<rb, 256, 0, st>>>(xin, xout, bf16 ? nullptr : w.cond, bf16 ? w.cond16 : nullptr, g.w16_cols(l, 0),
-                                 n, d, g.nc(l), g.cpar(l), f->theta + g.layer_off[l], 0, w.ld, l == 0 ? 1 : 0);
+                                 n, d, g.nc(l), g.cpar(l), f->theta + g.layer_off[l], 0, w.ld, l == 0 ? 1 : 0,
+                                 parts ? w.ldp : nullptr, parts);
     FMC_LAUNCH_CHECK();
     if (bf16) {
       // the inference path: hidden layers, then the last Linear fused with the spline
       const uint16_t* h_last = nullptr;
       if ((rc = conditioner_bf16_hidden(f, g, l, n, nullptr, w.cond16, w.gz16[0], w.gz16[1], &h_last, st))) return rc;
-      if ((rc = tc_linear_spline(st, g, f, l, h_last, n, w.n128, false, xout, w.ld, w.ldp))) return rc;
+      if ((rc = tc_linear_spline(st, g, f, l, h_last, n, w.n128, false, xout, nullptr, w.ldp))) return rc;
+      parts = spline_ld_parts(g, l);
+      if (l == g.L - 1 && (rc = ld_reduce(st, w.ldp, parts, n, w.ld))) return rc;
     } else {
       if ((rc = recompute_mlp(f, g, l, n, w, st))) return rc;
       if ((rc = launch_spline(g.K, false, st, w.raw, xout, w.ld, n, d, g.nt(l), g.tpar(l), g.cfg))) return rc;
@@ -406,7 +410,8 @@ int flow_loss_grad(const FmcFlow* f, const float* x, int64_t n, float* loss, flo
     const float* th = f->theta + g.layer_off[l];
     float* gl = grad + g.layer_off[l];
     const float* xin = w.xs + (int64_t)l * nd;
-    k_affine<<<rb, 256, 0, st>>>(xin, w.xa, w.cond, nullptr, 0, n, d, g.nc(l), g.cpar(l), th, 0, nullptr, 0);
+    k_affine<<<rb, 256, 0, st>>>(xin, w.xa, w.cond, nullptr, 0, n, d, g.nc(l), g.cpar(l), th, 0, nullptr, 0, nullptr,
+                                 0);
     FMC_LAUNCH_CHECK();
     if (bf16) {
       // hidden activations, then the last Linear recomputed inside the fused

@@ -42,9 +42,14 @@ int conditioner_bf16_hidden(const FmcFlow* f, const FlowGeom& g, int l, int64_t 
 constexpr int kSplineEpiPerQuarter = 3;
 
 // the last Linear of layer l fused with the spline (tc_spline.cu); ldp holds
-// kSplineEpiPerQuarter * n_groups floats per row
+// spline_ld_parts(g, l) = kSplineEpiPerQuarter * n_groups floats per row,
+// which are added to ld (ld_reduce) unless ld is NULL (the caller folds them
+// into its next pass over the rows)
 int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l, const uint16_t* A, int64_t M,
                      int64_t rows_a, bool inverse, float* xa, float* ld, float* ldp);
+int spline_ld_parts(const FlowGeom& g, int l);
+// ld[r] += sum of the row's n_part partials (fixed order)
+int ld_reduce(cudaStream_t st, const float* ldp, int n_part, int64_t m, float* ld);
 
 // adjoint of layer l's last Linear + spline (tc_spline.cu), recomputing the
 // Linear from A: dL/dx into gxa (every coordinate), dL/draw in bf16 into graw
