@@ -258,6 +258,41 @@ def plain_arm(name, w, dev, n_train, n_prod, timed_from, mean_ref, var_ref, ess=
     return out
 
 
+def compare_arms(name, w, dev, T, P, precision):
+    """Equal-work comparison: the fused bundle and the plain FP32 form each run
+    T training + P production loops from the same seed. Wall clock covers the
+    whole schedule (training included, as ESS/s is defined); the fused arm is
+    timed on a second sampler after a warm-up run of the first (one-time
+    set-up, autotuning and workspace growth excluded), the plain arm from its
+    first loop. min-ESS: rank-normalised bulk ESS over the production samples;
+    moment error against the workload's reference moments."""
+    import torch
+    from flowmc_gb300 import diagnostics as D
+    prec = "bf16" if precision == "bf16" else "float32"
+    out = {"workload": name, "training_loops": T, "production_loops": P}
+    for rep in range(2):
+        sampler, bundle, target, mean_ref, var_ref, x0 = build_sampler(name, w, T, P, prec, dev)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sampler.sample(x0, {})
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+    pos = sampler.resources["positions_production"].data
+    ess = D.ess_bulk(pos)
+    out["fused"] = {"seconds": secs, "min_ess": float(ess.min()), "min_ess_per_s": float(ess.min()) / secs,
+                    "moment_error": D.moment_error(pos, mean_ref, var_ref),
+                    "chain_steps_per_s": w["n_chains"] * (w["n_local"] + w["n_global"]) * (T + P) / secs}
+    pl = plain_arm(name, w, dev, T, P, 0, mean_ref, var_ref)
+    out["plain_fp32"] = {"seconds": pl["seconds"], "min_ess": pl.get("min_ess"),
+                         "min_ess_per_s": pl.get("min_ess_per_s"), "moment_error": pl.get("moment_error"),
+                         "chain_steps_per_s": pl["value"]}
+    f, q = out["fused"], out["plain_fp32"]
+    if q.get("min_ess_per_s"):
+        out["ratio_min_ess_per_s"] = f["min_ess_per_s"] / q["min_ess_per_s"]
+        out["ratio_moment_error"] = f["moment_error"] / q["moment_error"]
+    return out
+
+
 # ---------------------------------------------------------------- CPU baseline
 def cpu_baseline(name, w, budget_s: float = 20.0):
     """The oracle restatement (float64 NumPy, all host cores through BLAS)
@@ -395,6 +430,9 @@ def main():
     ap.add_argument("--kernel-trace", default="",
                     help="write a per-kernel launch list (CUPTI activity timestamps) of the K loops to this "
                          "file instead of the bench line; its times are not bench values")
+    ap.add_argument("--compare", default="",
+                    help="T,P: fused bundle and plain FP32 form on the same workload and seed with T training + P "
+                         "production loops each; prints their min-ESS/s and moment errors instead of the bench line")
     ap.add_argument("--plain-full", action="store_true",
                     help="run the plain FP32 form on the full schedule (min-ESS/s, moment error)")
     args = ap.parse_args()
@@ -424,6 +462,10 @@ def main():
     if args.probe == "local":
         print(json.dumps({"probe": "local_steps", **local_hbm_probe(dev, chains=w["n_chains"] if args.chains else 65536,
                                                                      lanes=(0, 8, 16, 32))}), flush=True)
+        return
+    if args.compare:
+        T, P = (int(v) for v in args.compare.split(","))
+        print(json.dumps({"compare": compare_arms(args.workload, w, dev, T, P, args.precision)}), flush=True)
         return
     W, K = max(1, args.warmup), max(1, args.steps)
     n_total = W + K
