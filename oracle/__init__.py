@@ -12,13 +12,10 @@ baseline); the product path (``flowmc_gb300``) never does.
 Pinning: the reference's own tests hold no numeric golden vectors, only
 known-answer/statistical pins (acceptance -> 1 at tiny steps, N(0, I)
 moments, leapfrog reversibility, determinism, shapes); the oracle is checked
-against all of them in ``tests/test_oracle.py``. In addition the golden
-fixtures under ``tests/golden/`` were produced by running the reference's
-own source files (MALA/HMC/GRW kernels, the RQ-spline functions and
-MaskedCouplingRQSpline, NFProposal) on a NumPy-backed stand-in for the JAX
-API with scripted noise (``tests/golden/make_golden.py``), and the oracle
-must reproduce them. JAX's threefry key streams, Equinox's Linear init and
-optax's AdamW are third-party code absent from the reference tree: the
-oracle restates them from their published definitions (parity on RNG
+against all of them in ``tests/test_oracle.py``, and its gradients against
+central finite differences. The reference itself cannot run here (it needs
+JAX, which is not installed). JAX's threefry key streams, Equinox's Linear
+init and optax's AdamW are third-party code absent from the reference tree:
+the oracle restates them from their published definitions (parity on RNG
 streams is therefore not claimed; explicit noise replaces it).
 """
