@@ -226,6 +226,121 @@ def local_hbm_probe(dev, chains=65536, steps=50, reps=5, lanes=(0,)):
     return out
 
 
+# ---------------------------------------------------------------- batched dense targets
+def batched_probe(dev, kind="mala", steps=2000, thin=20, seed=1):
+    """48 dense Gaussians sampled in one persistent launch: d_t ~ U{8..256},
+    Sigma = Q diag(lambda) Q^T with Q Haar (QR of a Gaussian matrix, signs
+    fixed) and lambda ~ logU[1e-2, 10]^d, chains per target round(exp(U[ln 512,
+    ln 8192])), x0 ~ N(0, I); MALA step 0.5 sqrt(lambda_min) d^(-1/3), HMC 10
+    leapfrog steps with step 0.2 sqrt(lambda_min). `steps` steps, every
+    `thin`-th stored. Reports chain-steps/s, the FP32 rate of the target
+    evaluations (2d^2 + 4d FLOPs each; MALA 1, HMC n_leapfrog + 1 per step)
+    against the nominal FP32 peak (SMs x 128 lanes x 2 FLOPs x max clock), and
+    the worst mean / covariance error over the targets (second half of the
+    stored rows)."""
+    import numpy as np
+    import torch
+    from flowmc_gb300 import targets as TG
+    from flowmc_gb300 import _lib
+    from flowmc_gb300.batched import BatchedDenseLocalSteps
+    rng = np.random.default_rng(seed)
+    dims = rng.integers(8, 257, size=48)
+    chains = [int(round(math.exp(rng.uniform(math.log(512), math.log(8192))))) for _ in dims]
+    ts, covs, lmins = [], [], []
+    for d in dims:
+        Q, R = np.linalg.qr(rng.normal(size=(d, d)))
+        Q = Q * np.sign(np.diag(R))
+        lam = np.exp(rng.uniform(math.log(1e-2), math.log(10.0), size=d))
+        cov = Q @ np.diag(lam) @ Q.T
+        ts.append(TG.DenseGaussian(Q @ np.diag(1.0 / lam) @ Q.T, device=dev))
+        covs.append(cov)
+        lmins.append(lam.min())
+    nlf = 10
+    step = [0.5 * math.sqrt(lm) * d ** (-1 / 3) if kind == "mala" else 0.2 * math.sqrt(lm) for lm, d in zip(lmins, dims)]
+    b = BatchedDenseLocalSteps(ts, chains, step, kind=kind, n_leapfrog=nlf)
+    g = torch.Generator(device=dev).manual_seed(seed)
+    xs = [torch.randn(c, int(d), device=dev, generator=g) for c, d in zip(chains, dims)]
+    b.run(xs, 4, seed=seed)   # warm-up
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    outs, _, _ = b.run(xs, steps, thinning=thin, seed=seed + 1)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    C = sum(chains)
+    evals = 1 if kind == "mala" else nlf + 1
+    flops = sum(c * steps * evals * (2.0 * d * d + 4.0 * d) for c, d in zip(chains, dims))
+    sms = ctypes_sm_count()
+    fp32_peak = sms * 128 * 2 * measured_peaks_raw().get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+    worst_mean = worst_cov = 0.0
+    for t, cov in enumerate(covs):
+        pos = outs[t][0][:, outs[t][0].shape[1] // 2:].reshape(-1, int(dims[t])).double()
+        mu = pos.mean(0).cpu().numpy()
+        emp = torch.cov(pos.T).cpu().numpy()
+        worst_mean = max(worst_mean, float(np.max(np.abs(mu) / np.sqrt(np.diag(cov)))))
+        worst_cov = max(worst_cov, float(np.linalg.norm(emp - cov) / np.linalg.norm(cov)))
+    return {"kind": kind, "targets": 48, "chains": C, "dims": [int(dims.min()), int(dims.max())],
+            "mean_d": float(dims.mean()), "steps": steps, "thinning": thin, "ms": ms,
+            "chain_steps_per_s": C * steps / (ms / 1e3), "fp32_tflops": flops / (ms / 1e3) / 1e12,
+            "fp32_peak_nominal_tflops": fp32_peak, "frac_fp32": flops / (ms / 1e3) / 1e12 / fp32_peak,
+            "worst_mean_error_sd": worst_mean, "worst_cov_rel_frobenius": worst_cov}
+
+
+def ctypes_sm_count():
+    import ctypes
+    from flowmc_gb300 import _lib
+    n = ctypes.c_int32()
+    _lib.check(_lib.lib().fmc_device_sm_count(ctypes.byref(n)))
+    return n.value
+
+
+def measured_peaks_raw():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def train_probe(dev, precision="bf16", seed=2):
+    """Flow maximum-likelihood training on an 8-mode 32-D mixture: 262144
+    samples, MaskedCouplingRQSpline 8 x [128, 128] x 10 bins, AdamW lr 1e-3,
+    batch 16384, 20 epochs. Reports samples/s, useful TFLOP/s (3 x the
+    forward's 2(n_c H1 + H1 H2 + H2 n_t P) per sample and layer) and the
+    final loss."""
+    import numpy as np
+    import torch
+    from flowmc_gb300.random import PRNGKey
+    from flowmc_gb300.resource.model.nf_model.rqSpline import MaskedCouplingRQSpline
+    from flowmc_gb300.resource.optimizer import Optimizer
+    rng = np.random.default_rng(seed)
+    d, N = 32, 262144
+    means = rng.uniform(-5, 5, size=(8, d))
+    scales = rng.uniform(0.3, 1.0, size=(8, d))
+    lab = rng.integers(0, 8, size=N)
+    data = torch.tensor(means[lab] + scales[lab] * rng.normal(size=(N, d)), dtype=torch.float32, device=dev)
+    prec = "bf16" if precision == "bf16" else "float32"
+    m = MaskedCouplingRQSpline(d, 8, [128, 128], 10, PRNGKey(seed), precision=prec, device=dev)
+    opt = Optimizer(m, learning_rate=1e-3)
+    m.train(PRNGKey(1), data, opt, opt.optim_state, 1, 16384, verbose=False)   # warm-up epoch
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    _, m, st, losses = m.train(PRNGKey(2), data, opt, opt.optim_state, 20, 16384, verbose=False)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    H, P = 128, 31
+    nc, nt = d // 2, d // 2
+    per_layer = 2 * (nc * H + H * H + H * nt * P)
+    flops = 3.0 * per_layer * 8 * N * 20
+    bf16 = measured_peaks()[1]
+    return {"precision": precision, "samples": N, "epochs": 20, "batch": 16384, "ms": ms,
+            "samples_per_s": N * 20 / (ms / 1e3), "useful_tflops": flops / (ms / 1e3) / 1e12,
+            "frac_bf16": flops / (ms / 1e3) / 1e12 / bf16, "final_loss": float(losses[-1])}
+
+
 # ---------------------------------------------------------------- plain FP32 form
 def plain_arm(name, w, dev, n_train, n_prod, timed_from, mean_ref, var_ref, ess=True):
     """The plain FP32 PyTorch-eager form (flowmc_gb300.plain) on the same
@@ -425,7 +540,7 @@ def main():
     ap.add_argument("--chains", type=int, default=0, help="override n_chains (small profiling cases)")
     ap.add_argument("--plain-loops", type=int, default=2,
                     help="loops of the plain FP32 form timed for its chain-steps/s (0 = skip)")
-    ap.add_argument("--probe", default="", choices=["", "local"],
+    ap.add_argument("--probe", default="", choices=["", "local", "batched", "train"],
                     help="run only the local-step HBM probe (a small profiling target)")
     ap.add_argument("--kernel-trace", default="",
                     help="write a per-kernel launch list (CUPTI activity timestamps) of the K loops to this "
@@ -459,6 +574,14 @@ def main():
         dist.init_process_group("nccl", rank=rank, world_size=world)
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
+    if args.probe == "batched":
+        print(json.dumps({"probe": "batched_dense", "mala": batched_probe(dev, "mala"),
+                          "hmc": batched_probe(dev, "hmc")}), flush=True)
+        return
+    if args.probe == "train":
+        print(json.dumps({"probe": "flow_training_d32", "bf16": train_probe(dev, "bf16"),
+                          "fp32": train_probe(dev, "fp32")}), flush=True)
+        return
     if args.probe == "local":
         print(json.dumps({"probe": "local_steps", **local_hbm_probe(dev, chains=w["n_chains"] if args.chains else 65536,
                                                                      lanes=(0, 8, 16, 32))}), flush=True)
