@@ -373,7 +373,7 @@ def plain_arm(name, w, dev, n_train, n_prod, timed_from, mean_ref, var_ref, ess=
     return out
 
 
-def compare_arms(name, w, dev, T, P, precision):
+def compare_arms(name, w, dev, T, P, precision, plain=True):
     """Equal-work comparison: the fused bundle and the plain FP32 form each run
     T training + P production loops from the same seed. Wall clock covers the
     whole schedule (training included, as ESS/s is defined); the fused arm is
@@ -384,7 +384,7 @@ def compare_arms(name, w, dev, T, P, precision):
     import torch
     from flowmc_gb300 import diagnostics as D
     prec = "bf16" if precision == "bf16" else "float32"
-    out = {"workload": name, "training_loops": T, "production_loops": P}
+    out = {"workload": name, "seed": w["seed"], "training_loops": T, "production_loops": P}
     for rep in range(2):
         sampler, bundle, target, mean_ref, var_ref, x0 = build_sampler(name, w, T, P, prec, dev)
         torch.cuda.synchronize()
@@ -397,6 +397,8 @@ def compare_arms(name, w, dev, T, P, precision):
     out["fused"] = {"seconds": secs, "min_ess": float(ess.min()), "min_ess_per_s": float(ess.min()) / secs,
                     "moment_error": D.moment_error(pos, mean_ref, var_ref),
                     "chain_steps_per_s": w["n_chains"] * (w["n_local"] + w["n_global"]) * (T + P) / secs}
+    if not plain:
+        return out
     pl = plain_arm(name, w, dev, T, P, 0, mean_ref, var_ref)
     out["plain_fp32"] = {"seconds": pl["seconds"], "min_ess": pl.get("min_ess"),
                          "min_ess_per_s": pl.get("min_ess_per_s"), "moment_error": pl.get("moment_error"),
@@ -545,6 +547,8 @@ def main():
     ap.add_argument("--kernel-trace", default="",
                     help="write a per-kernel launch list (CUPTI activity timestamps) of the K loops to this "
                          "file instead of the bench line; its times are not bench values")
+    ap.add_argument("--seeds", default="",
+                    help="with --compare: comma-separated workload seeds; the fused arm runs each, the plain arm the first")
     ap.add_argument("--compare", default="",
                     help="T,P: fused bundle and plain FP32 form on the same workload and seed with T training + P "
                          "production loops each; prints their min-ESS/s and moment errors instead of the bench line")
@@ -588,7 +592,12 @@ def main():
         return
     if args.compare:
         T, P = (int(v) for v in args.compare.split(","))
-        print(json.dumps({"compare": compare_arms(args.workload, w, dev, T, P, args.precision)}), flush=True)
+        seeds = [int(v) for v in args.seeds.split(",")] if args.seeds else [w["seed"]]
+        res = []
+        for i, sd in enumerate(seeds):
+            ws = dict(w, seed=sd)
+            res.append(compare_arms(args.workload, ws, dev, T, P, args.precision, plain=(i == 0)))
+        print(json.dumps({"compare": res[0] if len(res) == 1 else res}), flush=True)
         return
     W, K = max(1, args.warmup), max(1, args.steps)
     n_total = W + K

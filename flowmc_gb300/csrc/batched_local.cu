@@ -52,29 +52,61 @@ struct BatchArgs {
 };
 
 // Y[c][j] = sum_k DX[c][k] P[k][j] for the tile; also lp_c = -0.5 sum_j DX Y + const.
-// Thread (cg, jg): chains cg*8..cg*8+7, columns jg*4..jg*4+3.
+// Thread (cg, jg): chains cg*8..cg*8+7, columns jg*4..jg*4+3. The k loop runs
+// in chunks of 4 rows of P with the next two chunks' P values already in
+// registers (the rows stream from L2 with only 8 warps per SM to hide their
+// latency); the 8 chains' dx for a chunk are one float4 shared-memory load each.
+__device__ __forceinline__ void load_p4(const float* __restrict__ P, int d, int k0, int j0, float (&p)[4][4]) {
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int k = k0 + r;
+    const float* row = P + (int64_t)k * d + j0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) p[r][u] = (k < d && j0 + u < d) ? __ldg(row + u) : 0.f;
+  }
+}
+
 __device__ void dense_eval(const BatchTarget& T, const float* X, float* DX, float* G, float* lp, float* red) {
   const int tid = threadIdx.x, jg = tid & 63, cg = tid >> 6;
   const int d = T.d;
-  for (int e = tid; e < kBT * d; e += kBThreads) {
-    const int c = e / d, j = e - c * d;
-    DX[c * kBDMax + j] = X[c * kBDMax + j] - (T.mean ? __ldg(T.mean + j) : 0.f);
+  {
+    // dx = x - mean, zero beyond d up to the next multiple of 4 (read by the float4 loads)
+    const int c = tid >> 3, sub = tid & 7;
+    const int d4 = (d + 3) & ~3;
+    for (int j = sub; j < d4; j += 8)
+      DX[c * kBDMax + j] = (j < d) ? X[c * kBDMax + j] - (T.mean ? __ldg(T.mean + j) : 0.f) : 0.f;
   }
   __syncthreads();
   float acc[8][4] = {};
   const int j0 = jg * 4;
   if (j0 < d) {
-    for (int k = 0; k < d; ++k) {
-      const float* prow = T.precision + (int64_t)k * d + j0;
-      float p[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) p[u] = (j0 + u < d) ? __ldg(prow + u) : 0.f;
+    // three register buffers in fixed roles over an unrolled group of three
+    // chunks, so no buffer is ever copied; rows >= d read as zeros
+    float pa[4][4], pb[4][4], pc[4][4];
+    auto fma_chunk = [&](int k0, const float (&p)[4][4]) {
 #pragma unroll
       for (int c = 0; c < 8; ++c) {
-        const float xv = DX[(cg * 8 + c) * kBDMax + k];
+        const float4 xv = *reinterpret_cast<const float4*>(DX + (cg * 8 + c) * kBDMax + k0);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) acc[c][u] = fmaf(xv, p[u], acc[c][u]);
+        for (int u = 0; u < 4; ++u) {
+          acc[c][u] = fmaf(xv.x, p[0][u], acc[c][u]);
+          acc[c][u] = fmaf(xv.y, p[1][u], acc[c][u]);
+          acc[c][u] = fmaf(xv.z, p[2][u], acc[c][u]);
+          acc[c][u] = fmaf(xv.w, p[3][u], acc[c][u]);
+        }
       }
+    };
+    load_p4(T.precision, d, 0, j0, pa);
+    load_p4(T.precision, d, 4, j0, pb);
+    for (int k0 = 0; k0 < d; k0 += 12) {
+      load_p4(T.precision, d, k0 + 8, j0, pc);
+      fma_chunk(k0, pa);
+      if (k0 + 4 >= d) break;
+      load_p4(T.precision, d, k0 + 12, j0, pa);
+      fma_chunk(k0 + 4, pb);
+      if (k0 + 8 >= d) break;
+      load_p4(T.precision, d, k0 + 16, j0, pb);
+      fma_chunk(k0 + 8, pc);
     }
   }
   // gradient -P dx and the per-chain partial of dx . P dx
@@ -104,6 +136,9 @@ __device__ void dense_eval(const BatchTarget& T, const float* X, float* DX, floa
   __syncthreads();
 }
 
+// Elementwise passes over a tile use the same mapping: 8 threads per chain
+// (256 threads = 32 chains), thread tid on chain tid >> 3 and coordinates
+// (tid & 7) + 8i.
 // per-chain sum over j < d of f(c, j) in a fixed order: 8 threads per chain
 // (256 threads = 32 chains), strided over j, then a 3-level shuffle
 template <typename F>
@@ -164,8 +199,7 @@ __global__ void __launch_bounds__(kBThreads) k_batched_dense(const BatchArgs a) 
       // ---- proposal (MALA) or leapfrog trajectory (HMC) into Y / Gy / lpy
       if (a.kind == FMC_KERNEL_MALA) {
         const float dt2 = dt * dt;
-        for (int e = tid; e < kBT * d; e += kBThreads) {
-          const int c = e / d, j = e - c * d;
+        for (int j = tid & 7, c = tid >> 3; j < d; j += 8) {
           const float xi = draw_normal(a, T, c0 + c, s, j);
           const int i = c * kBDMax + j;
           Y[i] = (X[i] + dt2 * Gx[i] / 2.0f) + dt * xi;
@@ -186,8 +220,7 @@ __global__ void __launch_bounds__(kBThreads) k_batched_dense(const BatchArgs a) 
         if ((tid & 7) == 0) { sA[tid >> 3] = va; sB[tid >> 3] = vb; }
         __syncthreads();
       } else {
-        for (int e = tid; e < kBT * d; e += kBThreads) {
-          const int c = e / d, j = e - c * d;
+        for (int j = tid & 7, c = tid >> 3; j < d; j += 8) {
           const int i = c * kBDMax + j;
           Pm[i] = draw_normal(a, T, c0 + c, s, j);
           Y[i] = X[i];
@@ -203,23 +236,20 @@ __global__ void __launch_bounds__(kBThreads) k_batched_dense(const BatchArgs a) 
         }
         __syncthreads();
         // row 0: half kick with the gradient at x
-        for (int e = tid; e < kBT * d; e += kBThreads) {
-          const int c = e / d, j = e - c * d;
+        for (int j = tid & 7, c = tid >> 3; j < d; j += 8) {
           const int i = c * kBDMax + j;
           Pm[i] = Pm[i] + (dt * 0.5f) * Gy[i];
         }
         __syncthreads();
         for (int r = 1; r <= a.n_leapfrog + 1; ++r) {
           const float ek = (r == a.n_leapfrog + 1) ? dt * 0.5f : dt;
-          for (int e = tid; e < kBT * d; e += kBThreads) {
-            const int c = e / d, j = e - c * d;
+          for (int j = tid & 7, c = tid >> 3; j < d; j += 8) {
             const int i = c * kBDMax + j;
             Y[i] = Y[i] + dt * Pm[i];
           }
           __syncthreads();
           dense_eval(T, Y, DX, Gy, lpy, red);
-          for (int e = tid; e < kBT * d; e += kBThreads) {
-            const int c = e / d, j = e - c * d;
+          for (int j = tid & 7, c = tid >> 3; j < d; j += 8) {
             const int i = c * kBDMax + j;
             Pm[i] = Pm[i] + ek * Gy[i];
           }
@@ -253,8 +283,7 @@ __global__ void __launch_bounds__(kBThreads) k_batched_dense(const BatchArgs a) 
         acc_s[c] = (c < nc) && f_lt_ff(logu, ratio) ? 1 : 0;
       }
       __syncthreads();
-      for (int e = tid; e < kBT * d; e += kBThreads) {
-        const int c = e / d, j = e - c * d;
+      for (int j = tid & 7, c = tid >> 3; j < d; j += 8) {
         if (acc_s[c]) {
           const int i = c * kBDMax + j;
           X[i] = Y[i];
@@ -265,8 +294,7 @@ __global__ void __launch_bounds__(kBThreads) k_batched_dense(const BatchArgs a) 
       __syncthreads();
       if (s % a.thin == 0) {
         const int64_t row = a.start + s / a.thin;
-        for (int e = tid; e < nc * d; e += kBThreads) {
-          const int c = e / d, j = e - c * d;
+        for (int j = tid & 7, c = tid >> 3; c < nc && j < d; j += 8) {
           __stcs(T.out_pos + ((int64_t)(c0 + c) * a.buf_len + row) * d + j, X[c * kBDMax + j]);
         }
         if (tid < nc) {
@@ -274,8 +302,7 @@ __global__ void __launch_bounds__(kBThreads) k_batched_dense(const BatchArgs a) 
           __stcs(T.out_acc + (int64_t)(c0 + tid) * a.buf_len + row, acc_s[tid] ? 1.f : 0.f);
           xr_lp[tid] = lpx[tid];
         }
-        for (int e = tid; e < nc * d; e += kBThreads) {
-          const int c = e / d, j = e - c * d;
+        for (int j = tid & 7, c = tid >> 3; c < nc && j < d; j += 8) {
           a.x_last[(int64_t)(T.chain_offset + c0 + c) * kBDMax + j] = X[c * kBDMax + j];
         }
       }
