@@ -23,7 +23,7 @@ def _iso_normal_logpdf(a: np.ndarray, mean: np.ndarray, var: float) -> np.ndarra
     return -0.5 * np.sum(r * r, axis=-1) / var - 0.5 * d * np.log(2.0 * np.pi * var)
 
 
-def mala_kernel(t, x, dt, xi, u):
+def mala_kernel(t, x, dt, xi, u, return_ratio=False):
     """One MALA step for every chain (MALA.py:26-89).
 
     x [C, d], xi [C, d] standard normals (the key1 draw), u [C] uniforms
@@ -40,7 +40,7 @@ def mala_kernel(t, x, dt, xi, u):
     acc = np.log(u) < ratio                                # MALA.py:83-84
     x_new = np.where(acc[:, None], prop, x)
     lp_new = np.where(acc, lp1, lp0)
-    return x_new, lp_new, acc
+    return (x_new, lp_new, acc, ratio) if return_ratio else (x_new, lp_new, acc)
 
 
 def leapfrog_coefs(n_leapfrog: int) -> np.ndarray:
@@ -75,7 +75,7 @@ def leapfrog(t, x, p, eps, n_leapfrog, M):
     return x, p
 
 
-def hmc_kernel(t, x, lp, eps, n_leapfrog, M, xi, u):
+def hmc_kernel(t, x, lp, eps, n_leapfrog, M, xi, u, return_ratio=False):
     """One HMC step (HMC.py:98-151); H uses the incoming log_prob (HMC.py:137)."""
     M = np.asarray(M, np.float64)
     Mm = M if M.ndim == 2 else np.diag(M)
@@ -86,15 +86,39 @@ def hmc_kernel(t, x, lp, eps, n_leapfrog, M, xi, u):
     lpq = T.value(t, xq)
     Hq = -lpq + kinetic(pq, M)
     acc = np.log(u) < H - Hq                              # HMC.py:141-145
-    return np.where(acc[:, None], xq, x), np.where(acc, lpq, lp), acc
+    out = (np.where(acc[:, None], xq, x), np.where(acc, lpq, lp), acc)
+    return out + (H - Hq,) if return_ratio else out
 
 
-def grw_kernel(t, x, lp, sigma, xi, u):
+def grw_kernel(t, x, lp, sigma, xi, u, return_ratio=False):
     """Gaussian_random_walk.py:48-61."""
     prop = x + xi * sigma
     lpp = T.value(t, prop)
     acc = np.log(u) < lpp - lp
-    return np.where(acc[:, None], prop, x), np.where(acc, lpp, lp), acc
+    out = (np.where(acc[:, None], prop, x), np.where(acc, lpp, lp), acc)
+    return out + (lpp - lp,) if return_ratio else out
+
+
+def accept_margins(kind, t, x0, noise, unif, *, step_size, n_leapfrog=10, M=None):
+    """Per chain and step, |log u - log ratio| / (1 + |log ratio|) along the
+    oracle trajectory: small values mark near-ties, where a float32 kernel
+    may legitimately decide the other way."""
+    x = np.asarray(x0, np.float64)
+    lp = T.value(t, x)
+    C, d = x.shape
+    M = np.eye(d) if M is None else M
+    S = noise.shape[1]
+    out = np.zeros((C, S))
+    for s in range(S):
+        xi, u = np.asarray(noise[:, s], np.float64), np.asarray(unif[:, s], np.float64)
+        if kind == "mala":
+            x, lp, _, r = mala_kernel(t, x, step_size, xi, u, return_ratio=True)
+        elif kind == "hmc":
+            x, lp, _, r = hmc_kernel(t, x, lp, step_size, n_leapfrog, M, xi, u, return_ratio=True)
+        else:
+            x, lp, _, r = grw_kernel(t, x, lp, step_size, xi, u, return_ratio=True)
+        out[:, s] = np.abs(np.log(u) - r) / (1.0 + np.abs(r))
+    return out
 
 
 def take_serial_steps(kind, t, x0, n_steps, noise, unif, *, step_size, n_leapfrog=10, M=None,

@@ -1,0 +1,24 @@
+import torch
+
+
+def _stack(ys):
+    y0 = ys[0]
+    if y0 is None:
+        return None
+    if isinstance(y0, tuple):
+        return tuple(_stack([y[k] for y in ys]) for k in range(len(y0)))
+    return torch.stack([torch.as_tensor(y, dtype=torch.float64) for y in ys])
+
+
+def scan(f, init, xs=None, length=None):
+    carry = init
+    ys = []
+    it = xs if xs is not None else range(length)
+    for x in it:
+        carry, y = f(carry, x)
+        ys.append(y)
+    return carry, _stack(ys) if ys else None
+
+
+def stop_gradient(x):
+    return x.detach() if isinstance(x, torch.Tensor) else x

@@ -1,0 +1,111 @@
+"""Golden vectors produced by the reference's own source (tests/golden/make_golden.py:
+flowMC's MALA, HMC and GaussianRandomWalk kernels and its RQSpline, run on
+scripted normals and uniforms). The oracle must reproduce them in float64;
+the CUDA kernels, fed the same draws, must reproduce them within the float32
+trajectory tolerance (1e-5 relative) with identical accept decisions up to
+the first near-tie."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import flow as F
+from oracle import kernels as K
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "reference_vectors.npz")
+
+
+def _load():
+    z = np.load(GOLD)
+    return z, json.loads(str(z["cases"]))
+
+
+def _kernel_cases():
+    _, cases = _load()
+    return [c for c in cases if c["kind"] in ("mala", "hmc", "grw")]
+
+
+def _spline_cases():
+    _, cases = _load()
+    return [c for c in cases if c["kind"] == "rqspline"]
+
+
+@pytest.mark.parametrize("case", _kernel_cases(), ids=lambda c: c["name"])
+def test_oracle_kernels_match_reference_source(case):
+    z, _ = _load()
+    n = case["name"]
+    x0, noise, unif = z[f"{n}/x0"], z[f"{n}/noise"], z[f"{n}/unif"]
+    M = z[f"{n}/M"] if f"{n}/M" in z else None
+    pos, lps, accs, _ = K.take_serial_steps(case["kind"], case["target"], x0, noise.shape[1], noise, unif,
+                                            step_size=case["step_size"], n_leapfrog=case["n_leapfrog"], M=M)
+    np.testing.assert_array_equal(accs, z[f"{n}/acc"])
+    np.testing.assert_allclose(pos, z[f"{n}/pos"], rtol=1e-9, atol=1e-10)
+    np.testing.assert_allclose(lps, z[f"{n}/logp"], rtol=1e-9, atol=1e-10)
+    assert 0 < z[f"{n}/acc"].mean() < 1 or case["kind"] == "hmc"
+
+
+@pytest.mark.parametrize("case", _spline_cases(), ids=lambda c: c["name"])
+def test_oracle_spline_matches_reference_source(case):
+    z, _ = _load()
+    n = case["name"]
+    raw, x = z[f"{n}/raw"], z[f"{n}/x"]
+    xp, yp, sl = F.spline_params(raw, case["n_bins"])
+    y, ld = F.rqs_forward(x, xp, yp, sl)
+    np.testing.assert_allclose(y, z[f"{n}/fwd_y"], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(ld, z[f"{n}/fwd_logdet"], rtol=1e-12, atol=1e-12)
+    xi, ldi = F.rqs_inverse(x, xp, yp, sl)
+    np.testing.assert_allclose(xi, z[f"{n}/inv_x"], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(ldi, z[f"{n}/inv_logdet"], rtol=1e-12, atol=1e-12)
+    # the fixture covers both linear tails and the interior
+    assert (x < -10).any() and (x > 10).any() and (np.abs(x) < 10).any()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", _kernel_cases(), ids=lambda c: c["name"])
+def test_cuda_kernels_match_reference_source(cuda, case):
+    import torch
+    from flowmc_gb300 import targets as TG
+    from flowmc_gb300.resource.kernel.Gaussian_random_walk import GaussianRandomWalk
+    from flowmc_gb300.resource.kernel.HMC import HMC
+    from flowmc_gb300.resource.kernel.MALA import MALA
+    from flowmc_gb300.resource.kernel.base import run_local_steps
+    z, _ = _load()
+    n, t = case["name"], case["target"]
+    x0, noise, unif = z[f"{n}/x0"], z[f"{n}/noise"], z[f"{n}/unif"]
+    if t["kind"] == "dual_moon":
+        tgt = TG.DualMoon(t["n_dim"], r0=t["r0"], sr=t["sr"], mu=t["mu"], s0=t["s0"])
+    elif t["kind"] == "rosenbrock":
+        tgt = TG.Rosenbrock(t["n_dim"], a=t["a"], b=t["b"], c=t["c"])
+    else:
+        tgt = TG.DiagGaussian(t["n_dim"], mean=t["mean"], inv_var=t["inv_var"], const=t["const"])
+    if case["kind"] == "mala":
+        kern = MALA(case["step_size"])
+    elif case["kind"] == "hmc":
+        kern = HMC(condition_matrix=z[f"{n}/M"], step_size=case["step_size"], n_leapfrog=case["n_leapfrog"])
+    else:
+        kern = GaussianRandomWalk(case["step_size"])
+    C, S, d = noise.shape
+    dev = torch.device("cuda")
+    if case["kind"] == "hmc" and np.count_nonzero(z[f"{n}/M"] - np.diag(np.diag(z[f"{n}/M"]))):
+        # the fused HMC kernel takes diagonal mass matrices only and says so
+        with pytest.raises(NotImplementedError):
+            kern.local_params(d, dev)
+        return
+    pos = torch.full((C, S, d), -np.inf, device=dev)
+    lp = torch.full((C, S), -np.inf, device=dev)
+    acc = torch.full((C, S), -np.inf, device=dev)
+    f32 = lambda a: torch.tensor(a, dtype=torch.float32, device=dev)
+    run_local_steps(kern, tgt, f32(x0), S, 1, 1, 0, pos, lp, acc, 0, noise=f32(noise), uniform=f32(unif))
+    torch.cuda.synchronize()
+    pos, lp, acc = pos.cpu().numpy(), lp.cpu().numpy(), acc.cpu().numpy()
+    # near-ties: where the float64 reference's |log u - log ratio| is tiny, float32 may decide either way
+    margins = K.accept_margins(case["kind"], t, x0, noise, unif, step_size=case["step_size"],
+                               n_leapfrog=case["n_leapfrog"], M=z[f"{n}/M"] if f"{n}/M" in z else None)
+    for c in range(C):
+        ties = np.nonzero(margins[c] < 1e-4)[0]
+        upto = ties[0] if len(ties) else S
+        np.testing.assert_array_equal(acc[c, :upto], z[f"{n}/acc"][c, :upto], err_msg=f"chain {c}")
+        np.testing.assert_allclose(pos[c, :upto], z[f"{n}/pos"][c, :upto], rtol=1e-5, atol=1e-5, err_msg=f"chain {c}")
+        np.testing.assert_allclose(lp[c, :upto], z[f"{n}/logp"][c, :upto], rtol=1e-5,
+                                   atol=1e-5 * max(1.0, np.abs(z[f"{n}/logp"][c]).max()), err_msg=f"chain {c}")
