@@ -92,13 +92,10 @@ __global__ void k_destandardize(float* __restrict__ x, int64_t n, int d, const f
 
 // one warp per row: ScalarAffine of every coordinate, the conditioning
 // coordinates gathered into cond (fp32 [n, nc]) and/or cond16 (bf16 [n, ldc16],
-// columns nc..ldc16 zeroed: the operand of the first tensor-core GEMM). With
-// ldp, the previous layer's n_part log-determinant partials of the row (fused
-// spline kernel) are added to ld first, in index order.
+// columns nc..ldc16 zeroed: the operand of the first tensor-core GEMM)
 __global__ void k_affine(const float* __restrict__ in, float* __restrict__ out, float* __restrict__ cond,
                          uint16_t* __restrict__ cond16, int ldc16, int64_t n, int d, int nc, int cpar,
-                         const float* __restrict__ th_layer, int inverse, float* __restrict__ ld, int ld_init,
-                         const float* __restrict__ ldp, int n_part) {
+                         const float* __restrict__ th_layer, int inverse, float* __restrict__ ld, int ld_init) {
   const float s = th_layer[0], t = th_layer[1];
   const float es = expf(inverse ? -s : s);
   const int lane = threadIdx.x & 31;
@@ -118,13 +115,7 @@ __global__ void k_affine(const float* __restrict__ in, float* __restrict__ out, 
       for (int c = nc + lane; c < ldc16; c += 32) cond16[r * ldc16 + c] = 0;
     if (ld != nullptr && lane == 0) {
       const float l = (float)d * (inverse ? -s : s);
-      float acc = ld_init ? 0.f : ld[r];
-      if (ldp != nullptr) {
-        float ps = 0.f;
-        for (int j = 0; j < n_part; ++j) ps += ldp[r * n_part + j];
-        acc += ps;
-      }
-      ld[r] = ld_init ? l : acc + l;
+      ld[r] = ld_init ? l : ld[r] + l;
     }
   }
 }
@@ -274,15 +265,13 @@ static int flow_pass(const FmcFlow* f, const FlowGeom& g, const float* x, float*
                      InferWs& w, cudaStream_t st) {
   const int grid = rows_grid(m);
   const bool bf16 = f->precision == FMC_PREC_BF16;
-  int parts = 0;   // log-det partials the previous fused spline layer left in w.ldp
   for (int u = 0; u < g.L; ++u) {
     const int l = inverse ? g.L - 1 - u : u;
     const float* src = (u == 0) ? x : y;
-    // BF16: the conditioning block goes straight to the bf16 GEMM operand, and
-    // the previous layer's log-det partials are folded into ld here
+    // BF16: the conditioning block goes straight to the bf16 GEMM operand
     k_affine<<<grid, 256, 0, st>>>(src, y, bf16 ? nullptr : w.cond, bf16 ? w.cond16 : nullptr, g.w16_cols(l, 0), m,
                                    g.d, g.nc(l), g.cpar(l), f->theta + g.layer_off[l], inverse ? 1 : 0, ld,
-                                   u == 0 ? 1 : 0, parts ? w.ldp : nullptr, parts);
+                                   u == 0 ? 1 : 0);
     FMC_LAUNCH_CHECK();
     int rc;
     if (bf16) {
@@ -290,9 +279,7 @@ static int flow_pass(const FmcFlow* f, const FlowGeom& g, const float* x, float*
       const uint16_t* h_last = nullptr;
       if ((rc = conditioner_bf16_hidden(f, g, l, m, nullptr, w.cond16, w.h16a, w.h16b, &h_last, st))) return rc;
       const int64_t rows = (m + 127) / 128 * 128;
-      if ((rc = tc_linear_spline(st, g, f, l, h_last, m, rows, inverse, y, nullptr, w.ldp))) return rc;
-      parts = spline_ld_parts(g, l);
-      if (u == g.L - 1 && (rc = ld_reduce(st, w.ldp, parts, m, ld))) return rc;
+      if ((rc = tc_linear_spline(st, g, f, l, h_last, m, rows, inverse, y, ld, w.ldp))) return rc;
     } else {
       if ((rc = conditioner(f, g, l, m, w, st))) return rc;
       if ((rc = launch_spline(g.K, inverse, st, w.raw, y, ld, m, g.d, g.nt(l), g.tpar(l), g.cfg))) return rc;

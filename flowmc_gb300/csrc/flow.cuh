@@ -61,8 +61,7 @@ __global__ void k_standardize(const float* __restrict__ x, int64_t n, int d, con
 __global__ void k_destandardize(float* __restrict__ x, int64_t n, int d, const float* __restrict__ aux);
 __global__ void k_affine(const float* __restrict__ in, float* __restrict__ out, float* __restrict__ cond,
                          uint16_t* __restrict__ cond16, int ldc16, int64_t n, int d, int nc, int cpar,
-                         const float* __restrict__ th_layer, int inverse, float* __restrict__ ld, int ld_init,
-                         const float* __restrict__ ldp, int n_part);
+                         const float* __restrict__ th_layer, int inverse, float* __restrict__ ld, int ld_init);
 __global__ void k_base_logprob(const float* __restrict__ y, const float* __restrict__ ld, int64_t n, int d,
                                const float* __restrict__ aux, float* __restrict__ logp);
 __global__ void k_base_sample(const float* __restrict__ z, Rng rng, int64_t n, int d,

@@ -25,7 +25,7 @@ struct TrainWs {
   // fused last-Linear + spline kernels (BF16 path): log-det partials and
   // per-128-row-tile bias-gradient partials; split-K partials of the
   // weight-gradient GEMMs (K = the batch)
-  float *ldp, *bpart, *kpart;
+  float *ldp, *bpart, *kpart, *colpart;
   int64_t kpart_floats;
   // BF16 path (tensor-core GEMMs): activations, gradients and their transposes
   uint16_t *cond16, *condT, *hs16, *hsT, *graw16, *grawT, *gz16[2], *gzT[2];
@@ -70,7 +70,7 @@ static void carve_train(const FlowGeom& g, int64_t n, bool bf16, void* ws, Train
   if (m < 4096) m = 4096;
   w.part_floats = (int64_t)colsum_blocks(n) * m;
   w.part = take(w.part_floats);
-  w.ldp = w.bpart = w.kpart = nullptr;
+  w.ldp = w.bpart = w.kpart = w.colpart = nullptr;
   w.kpart_floats = 0;
   w.cond16 = w.condT = w.hs16 = w.hsT = w.graw16 = w.grawT = nullptr;
   w.gz16[0] = w.gz16[1] = w.gzT[0] = w.gzT[1] = nullptr;
@@ -102,6 +102,8 @@ static void carve_train(const FlowGeom& g, int64_t n, bool bf16, void* ws, Train
         if (f > w.kpart_floats) w.kpart_floats = f;
       }
     w.kpart = w.kpart_floats > 0 ? take(w.kpart_floats) : nullptr;
+    // per-32-row column sums of the tanh-adjoint GEMM outputs (hidden bias gradients)
+    w.colpart = take((w.n128 / 32) * g.h_max());
   }
   if (total) *total = (size_t)used;
 }
@@ -132,6 +134,28 @@ __global__ void k_colsum_final(const float* __restrict__ part, int rb, int m, fl
   float s = 0.f;
   for (int b = 0; b < rb; ++b) s += part[(int64_t)b * m + j];
   out[j] = s;
+}
+
+// out[j] = sum over rows of part[r * m + j] for a tall partial matrix: a
+// block takes 32 columns, its 32 warps rows w, w + 32, ... (coalesced
+// 128-byte loads), then the 32 per-warp sums are added in warp order
+__global__ void __launch_bounds__(1024) k_colsum_rows(const float* __restrict__ part, int rows, int m,
+                                                      float* __restrict__ out) {
+  __shared__ float sh[32][33];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int j = blockIdx.x * 32 + lane;
+  float s = 0.f;
+  if (j < m)
+#pragma unroll 4
+    for (int r = w; r < rows; r += 32) s += part[(int64_t)r * m + j];
+  sh[w][lane] = s;
+  __syncthreads();
+  if (w == 0 && j < m) {
+    float t = 0.f;
+#pragma unroll
+    for (int k = 0; k < 32; ++k) t += sh[k][lane];
+    out[j] = t;
+  }
 }
 
 static int colsum(cudaStream_t st, const float* gm, int64_t n, int m, float* part, float* out) {
@@ -302,6 +326,7 @@ static int backward_mlp_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t
   const uint16_t* gcur = w.graw16;
   const uint16_t* gcurT = w.grawT;
   int nxt = 0;
+  bool have_cp = false;   // w.colpart holds the column sums of gcur
   for (int i = g.nh; i >= 0; --i) {
     const int out = g.lin_out(l, i), in = g.lin_in(l, i);
     const int seg = l * (g.nh + 1) + i;
@@ -315,7 +340,13 @@ static int backward_mlp_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t
                       gl + g.lin_w(l, i), in, in, tc::TC_EPI_F32)))
       return rc;
     if (i < g.nh) {
-      if ((rc = colsum_bf16(st, gcur, n, out, FlowGeom::rup(out, 64), w.part, gl + g.lin_b(l, i)))) return rc;
+      if (have_cp) {
+        // fixed-order reduction of the per-32-row partials the DTANH GEMM left
+        k_colsum_rows<<<(out + 31) / 32, 1024, 0, st>>>(w.colpart, (int)(w.n128 / 32), out, gl + g.lin_b(l, i));
+        FMC_LAUNCH_CHECK();
+      } else if ((rc = colsum_bf16(st, gcur, n, out, FlowGeom::rup(out, 64), w.part, gl + g.lin_b(l, i)))) {
+        return rc;
+      }
     }
     const uint16_t* WT = f->theta_bf16 + g.w16t_off[seg];
     if (i > 0) {
@@ -327,6 +358,11 @@ static int backward_mlp_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t
       e1.ldct = w.n64;
       e1.ct_rows_pad = w.n64;
       const int ldo = (int)FlowGeom::rup(in, 64);
+      have_cp = tc_gemm_stages_output(w.gz16[nxt], ldo, ldo, n);
+      if (have_cp) {
+        e1.colpart = w.colpart;
+        e1.ldpart = in;
+      }
       if ((rc = tc_gemm(st, gcur, n, w.n128, (int)FlowGeom::rup(out, 64), WT, in, g.w16t_rows(l, i), e1, w.gz16[nxt],
                         ldo, ldo, tc::TC_EPI_DTANH_BF16)))
         return rc;
@@ -371,21 +407,17 @@ int flow_loss_grad(const FmcFlow* f, const float* x, int64_t n, float* loss, flo
   // ---- forward, saving layer inputs
   k_standardize<<<eb, 256, 0, st>>>(x, n, d, f->aux, w.xs);
   FMC_LAUNCH_CHECK();
-  int parts = 0;   // log-det partials of the previous fused spline layer, folded in by k_affine
   for (int l = 0; l < g.L; ++l) {
     float* xin = w.xs + (int64_t)l * nd;
     float* xout = w.xs + (int64_t)(l + 1) * nd;
     k_affine<<<rb, 256, 0, st>>>(xin, xout, bf16 ? nullptr : w.cond, bf16 ? w.cond16 : nullptr, g.w16_cols(l, 0),
-                                 n, d, g.nc(l), g.cpar(l), f->theta + g.layer_off[l], 0, w.ld, l == 0 ? 1 : 0,
-                                 parts ? w.ldp : nullptr, parts);
+                                 n, d, g.nc(l), g.cpar(l), f->theta + g.layer_off[l], 0, w.ld, l == 0 ? 1 : 0);
     FMC_LAUNCH_CHECK();
     if (bf16) {
       // the inference path: hidden layers, then the last Linear fused with the spline
       const uint16_t* h_last = nullptr;
       if ((rc = conditioner_bf16_hidden(f, g, l, n, nullptr, w.cond16, w.gz16[0], w.gz16[1], &h_last, st))) return rc;
-      if ((rc = tc_linear_spline(st, g, f, l, h_last, n, w.n128, false, xout, nullptr, w.ldp))) return rc;
-      parts = spline_ld_parts(g, l);
-      if (l == g.L - 1 && (rc = ld_reduce(st, w.ldp, parts, n, w.ld))) return rc;
+      if ((rc = tc_linear_spline(st, g, f, l, h_last, n, w.n128, false, xout, w.ld, w.ldp))) return rc;
     } else {
       if ((rc = recompute_mlp(f, g, l, n, w, st))) return rc;
       if ((rc = launch_spline(g.K, false, st, w.raw, xout, w.ld, n, d, g.nt(l), g.tpar(l), g.cfg))) return rc;
@@ -410,8 +442,7 @@ int flow_loss_grad(const FmcFlow* f, const float* x, int64_t n, float* loss, flo
     const float* th = f->theta + g.layer_off[l];
     float* gl = grad + g.layer_off[l];
     const float* xin = w.xs + (int64_t)l * nd;
-    k_affine<<<rb, 256, 0, st>>>(xin, w.xa, w.cond, nullptr, 0, n, d, g.nc(l), g.cpar(l), th, 0, nullptr, 0, nullptr,
-                                 0);
+    k_affine<<<rb, 256, 0, st>>>(xin, w.xa, w.cond, nullptr, 0, n, d, g.nc(l), g.cpar(l), th, 0, nullptr, 0);
     FMC_LAUNCH_CHECK();
     if (bf16) {
       // hidden activations, then the last Linear recomputed inside the fused
@@ -422,7 +453,7 @@ int flow_loss_grad(const FmcFlow* f, const float* x, int64_t n, float* loss, flo
                                      w.grawT, w.n64, w.bpart)))
         return rc;
       const int ntP = g.lin_out(l, g.nh);
-      k_colsum_final<<<(ntP + 255) / 256, 256, 0, st>>>(w.bpart, (int)(w.n128 / 128), ntP, gl + g.lin_b(l, g.nh));
+      k_colsum_rows<<<(ntP + 31) / 32, 1024, 0, st>>>(w.bpart, (int)(w.n128 / 128), ntP, gl + g.lin_b(l, g.nh));
       FMC_LAUNCH_CHECK();
       if ((rc = backward_mlp_bf16(f, g, l, n, w, gl, st))) return rc;
     } else {

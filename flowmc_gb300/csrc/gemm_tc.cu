@@ -127,6 +127,10 @@ static int launch_tc(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& 
   return FMC_OK;
 }
 
+bool tc_gemm_stages_output(const void* C, int64_t ldc, int n_store, int64_t M) {
+  return ((uintptr_t)C & 15) == 0 && (ldc * 2) % 16 == 0 && n_store >= 64 && M >= 32;
+}
+
 int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K, const uint16_t* B, int N,
             int rows_b, const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store, int epi) {
   FMC_CHECK_ARG(K % tc::BK == 0 && K >= tc::BK, "K=%d must be a positive multiple of 64", K);
@@ -145,7 +149,9 @@ int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K
   // bf16 outputs go out through TMA stores when C can carry a tensor map
   // (16-byte aligned rows, at least one 64 x 32 box)
   const bool bf16_out = epi == tc::TC_EPI_TANH_BF16 || epi == tc::TC_EPI_DTANH_BF16;
-  const bool tstore = bf16_out && ((uintptr_t)C & 15) == 0 && (ldc * 2) % 16 == 0 && n_store >= 64 && M >= 32;
+  const bool tstore = bf16_out && tc_gemm_stages_output(C, ldc, n_store, M);
+  FMC_CHECK_ARG(ep.colpart == nullptr || (epi == tc::TC_EPI_DTANH_BF16 && tstore),
+                "column sums need the tanh-adjoint epilogue with staged TMA stores");
   memset(&mc, 0, sizeof(mc));
   if (tstore && (rc = make_map(&mc, C, n_store, M, ldc, 32))) return rc;
 #define TC_CASE(E)                                                                                            \

@@ -21,6 +21,8 @@ struct EpiArgs {
   int64_t ct_rows_pad;      // rows in [M, ct_rows_pad) get zeros in the copy
   float* kpart;             // mode 3: optional scratch for split-K partial products
   int64_t kpart_floats;     //   (the GEMM splits K when the tile grid leaves SMs idle)
+  float* colpart;           // mode 2 with TMA stores: column sums of the bf16 output per
+  int64_t ldpart;           //   32-row block, row (m / 32) of colpart [ceil(M / 128) * 4, ldpart]
 };
 }  // namespace tc
 
@@ -42,14 +44,9 @@ int conditioner_bf16_hidden(const FmcFlow* f, const FlowGeom& g, int l, int64_t 
 constexpr int kSplineEpiPerQuarter = 3;
 
 // the last Linear of layer l fused with the spline (tc_spline.cu); ldp holds
-// spline_ld_parts(g, l) = kSplineEpiPerQuarter * n_groups floats per row,
-// which are added to ld (ld_reduce) unless ld is NULL (the caller folds them
-// into its next pass over the rows)
+// kSplineEpiPerQuarter * n_groups floats per row, which are then added to ld
 int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l, const uint16_t* A, int64_t M,
                      int64_t rows_a, bool inverse, float* xa, float* ld, float* ldp);
-int spline_ld_parts(const FlowGeom& g, int l);
-// ld[r] += sum of the row's n_part partials (fixed order)
-int ld_reduce(cudaStream_t st, const float* ldp, int n_part, int64_t m, float* ld);
 
 // adjoint of layer l's last Linear + spline (tc_spline.cu), recomputing the
 // Linear from A: dL/dx into gxa (every coordinate), dL/draw in bf16 into graw
@@ -63,6 +60,10 @@ int tc_linear_spline_bwd(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, i
 // theta (fp32, packed) -> zero-padded bf16 weight segments (FlowGeom::w16_off)
 // and their transposes (FlowGeom::w16t_off)
 int pack_bf16_weights(const FlowGeom& g, const float* theta, uint16_t* w16, cudaStream_t st);
+
+// whether tc_gemm writes a bf16 output through TMA stores (and so can leave
+// EpiArgs::colpart column sums): 16-byte aligned rows, one 64 x 32 box
+bool tc_gemm_stages_output(const void* C, int64_t ldc, int n_store, int64_t M);
 
 // C = epi(A . B^T) on tcgen05; A [rows_a, K] bf16 (K a multiple of 64, rows_a
 // a multiple of 128 covering M), B [rows_b, K] bf16 (rows_b a multiple of 256

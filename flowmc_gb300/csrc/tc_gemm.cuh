@@ -481,6 +481,26 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (TSTORE && (i & 1) == 1 && blk_live) {
           fence_proxy_async_smem();
           __syncwarp();
+          if (EPI == TC_EPI_DTANH_BF16 && ep.colpart != nullptr) {
+            // column sums of the staged 32 x 64 block: lane l takes columns
+            // 2l, 2l+1 (one 4-byte word per row: the 32 lanes cover a row's
+            // 128 bytes, no bank conflicts); rows >= M were staged as zeros
+            const uint32_t buf =
+                smem_u32(staging) + (uint32_t)(((warp - 2) * 2 + (blkno & 1)) * kStageBlockBytes);
+            float s0 = 0.f, s1 = 0.f;
+#pragma unroll 8
+            for (int r = 0; r < 32; ++r) {
+              uint32_t v;
+              const uint32_t addr = buf + (uint32_t)(r * 128 + (((lane >> 2) ^ (r & 7)) << 4) + ((lane & 3) << 2));
+              asm volatile("ld.shared.b32 %0, [%1];" : "=r"(v) : "r"(addr));
+              s0 += __uint_as_float(v << 16);
+              s1 += __uint_as_float(v & 0xffff0000u);
+            }
+            const int col = n0 + (c0 & ~63) + 2 * lane;
+            float* dst = ep.colpart + (int64_t)(m0 / 32 + q) * ep.ldpart;
+            if (col < N) dst[col] = s0;
+            if (col + 1 < N) dst[col + 1] = s1;
+          }
           if (lane == 0) {
             tma_store_2d(&tmC, smem_u32(staging) + (uint32_t)(((warp - 2) * 2 + (blkno & 1)) * kStageBlockBytes),
                          n0 + (c0 & ~63), m0 + q * 32);

@@ -492,19 +492,9 @@ int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l
   }
 #undef SPL_CASE
   if (rc) return rc;
-  return ld ? ld_reduce(st, ldp, kSplineEpiPerQuarter * n_groups, M, ld) : FMC_OK;
-}
-
-int spline_ld_parts(const FlowGeom& g, int l) {
-  int dg, bn;
-  return kSplineEpiPerQuarter * spline_groups(g.K, g.nt(l), &dg, &bn);
-}
-
-int ld_reduce(cudaStream_t st, const float* ldp, int n_part, int64_t m, float* ld) {
-  if (m <= 0) return FMC_OK;
-  int64_t blocks = (m + 255) / 256;
+  int64_t blocks = (M + 255) / 256;
   if (blocks > (int64_t)sm_count() * 8) blocks = (int64_t)sm_count() * 8;
-  k_ld_reduce<<<(int)(blocks < 1 ? 1 : blocks), 256, 0, st>>>(ldp, n_part, m, ld);
+  k_ld_reduce<<<(int)(blocks < 1 ? 1 : blocks), 256, 0, st>>>(ldp, kSplineEpiPerQuarter * n_groups, M, ld);
   FMC_LAUNCH_CHECK();
   return FMC_OK;
 }
