@@ -473,8 +473,11 @@ def cpu_baseline(name, w, budget_s: float = 20.0):
 
 def reference_arm(args, w):
     v = cpu_baseline(args.workload, w)
+    per_loop = w["n_chains"] * (w["n_local"] + w["n_global"])
     line = {"impl": "reference", "metric": METRIC, "value": v["value"], "unit": v["unit"], "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * per_loop / v["value"] if v.get("value") else None,
+            "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": args.workload, **{k: w[k] for k in ("d", "n_chains", "n_local", "n_global")}},
             "cpu_baseline": v,
@@ -573,11 +576,15 @@ def main():
     from flowmc_gb300 import diagnostics as D
     from flowmc_gb300 import profiling
 
+    from flowmc_gb300 import replicas
+
     if world > 1:
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
         dist.init_process_group("nccl", rank=rank, world_size=world)
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
+    # independent replicas: every rank samples its own chains
+    w["seed"] = replicas.replica_seed(w["seed"], rank)
     if args.probe == "batched":
         print(json.dumps({"probe": "batched_dense", "mala": batched_probe(dev, "mala"),
                           "hmc": batched_probe(dev, "hmc")}), flush=True)
@@ -639,15 +646,12 @@ def main():
     wall = time.perf_counter() - wall0
     launches = _lib.launch_count() - l0
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
+    ms = replicas.max_over_ranks(e0.elapsed_time(e1), dev)
     if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
         dist.barrier()
     secs = ms / 1e3
     chain_steps = w["n_chains"] * (w["n_local"] + w["n_global"]) * K
-    value = chain_steps * world / secs
+    value = replicas.job_throughput(chain_steps, secs, world)
 
     # ---- diagnostics on the production samples
     pos = sampler.resources["positions_production"].data
