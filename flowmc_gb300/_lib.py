@@ -119,6 +119,7 @@ _SIGNATURES = {
         ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
         ctypes.c_void_p]),
     "fmc_device_error": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int32), ctypes.c_int32]),
+    "fmc_selftest_bounded_wait": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p]),
     "fmc_flow_forward": (ctypes.c_int, [ctypes.POINTER(FmcFlow), ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "fmc_flow_inverse": (ctypes.c_int, [ctypes.POINTER(FmcFlow), ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,

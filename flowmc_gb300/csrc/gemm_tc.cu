@@ -310,6 +310,37 @@ extern "C" int fmc_tc_gemm_bf16(const uint16_t* A, int64_t M, int64_t rows_a, in
   return tc_gemm((cudaStream_t)stream, A, M, rows_a, K, B, N, rows_b, ep, C, ldc, n_store, epilogue);
 }
 
+// Failure-path self-test of the bounded waits: one warp initialises an
+// mbarrier that nothing will complete and waits on it with mbar_wait (the
+// routine every tcgen05 kernel here uses); the wait gives up after about a
+// second and the kernel records that it did. Nothing faults or hangs.
+__global__ void k_selftest_bounded_wait(int* timed_out) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
+  if (threadIdx.x == 0) *timed_out = tc::mbar_wait(&bar, 0) ? 0 : 1;
+}
+
+__device__ int g_selftest_word = -1;
+
+extern "C" int fmc_selftest_bounded_wait(int32_t* timed_out, void* stream) {
+  FMC_CHECK_ARG(timed_out != nullptr, "timed_out is NULL");
+  cudaStream_t st = (cudaStream_t)stream;
+  int* d = nullptr;
+  FMC_CUDA_TRY(cudaGetSymbolAddress((void**)&d, g_selftest_word));
+  FMC_CUDA_TRY(cudaMemsetAsync(d, 0xff, sizeof(int), st));
+  k_selftest_bounded_wait<<<1, 32, 0, st>>>(d);
+  FMC_LAUNCH_CHECK();
+  int h = -1;
+  FMC_CUDA_TRY(cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, st));
+  FMC_CUDA_TRY(cudaStreamSynchronize(st));
+  *timed_out = h;
+  return FMC_OK;
+}
+
 extern "C" int fmc_device_error(int32_t* out, int32_t clear) {
   FMC_CHECK_ARG(out != nullptr, "out is NULL");
   int v = 0;

@@ -61,16 +61,22 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// bounded wait: try_wait itself suspends the thread for a short hardware
-// window, so spin on it first; after 2^16 tries back off with short sleeps.
-// Gives up after roughly one second and returns false.
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// bounded wait: try_wait suspends the thread until the phase completes or an
+// implementation-defined time passes (a few microseconds), so the bound is on
+// wall time (%globaltimer), not on a count of tries: gives up after one second
+// and returns false.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (uint32_t it = 0; it < (1u << 16); ++it)
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  do {
     if (mbar_try_wait(bar, parity)) return true;
-  for (uint32_t it = 0; it < (1u << 23); ++it) {
-    if (mbar_try_wait(bar, parity)) return true;
-    __nanosleep(128);
-  }
+  } while (global_ns() - t0 < 1000000000ull);
   return false;
 }
 

@@ -309,6 +309,12 @@ FMC_API int fmc_select_training_data_noalloc(const float* buf, int32_t n_chains,
 FMC_API int fmc_tc_gemm_bf16(const uint16_t* A, int64_t M, int64_t rows_a, int32_t K, const uint16_t* B,
                              int32_t N, int32_t rows_b, const float* bias, void* C, int64_t ldc, int32_t n_store,
                              int32_t epilogue, void* stream);
+/* Failure-path self-test (no reference counterpart): runs the bounded
+ * mbarrier wait of the tcgen05 kernels on a barrier that nothing completes.
+ * *timed_out = 1 when the wait gave up (after about a second) and the kernel
+ * returned normally; the context stays usable. Synchronises the stream. */
+FMC_API int fmc_selftest_bounded_wait(int32_t* timed_out, void* stream);
+
 /* Device error word of the tensor-core kernels: 1 after a bounded wait
  * expired (synchronous read; clear != 0 resets it). */
 FMC_API int fmc_device_error(int32_t* out, int32_t clear);

@@ -50,3 +50,29 @@ def run(M, K, N, epi, seed=0):
 @pytest.mark.parametrize("epi", [0, 1])
 def test_tc_gemm_matches_torch(cuda, M, K, N, epi):
     run(M, K, N, epi, seed=M + K + N)
+
+
+def test_bounded_wait_expires_and_context_survives(cuda):
+    """Failure path of the tcgen05 kernels' mbarrier waits, without a fault:
+    a wait on a barrier that nothing completes gives up after about a second
+    and reports it; the next GEMM on the same context is still correct."""
+    import ctypes
+    import time
+    from flowmc_gb300 import _lib
+    flag = ctypes.c_int32(-1)
+    t0 = time.perf_counter()
+    _lib.check(_lib.lib().fmc_selftest_bounded_wait(ctypes.byref(flag), _lib.stream_handle()))
+    dt = time.perf_counter() - t0
+    assert flag.value == 1
+    assert 0.5 < dt < 10.0          # one second of wall time, plus launch and copy
+    M, K, N = 256, 128, 256
+    A = torch.randn(M, K, device="cuda").to(torch.bfloat16)
+    B = torch.randn(N, K, device="cuda").to(torch.bfloat16)
+    C = torch.empty(M, N, device="cuda")
+    bias = torch.zeros(N, device="cuda")
+    _lib.check(_lib.lib().fmc_tc_gemm_bf16(A.data_ptr(), M, M, K, B.data_ptr(), N, N, bias.data_ptr(), C.data_ptr(),
+                                           N, N, 1, _lib.stream_handle()))
+    torch.cuda.synchronize()
+    ref = A.float() @ B.float().T
+    torch.testing.assert_close(C, ref, rtol=1e-2, atol=1e-2)
+    assert _lib.device_error() == 0
