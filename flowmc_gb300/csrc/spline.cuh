@@ -250,8 +250,11 @@ __device__ __forceinline__ float rqs_fwd_adjoint(float x, const float* raw, cons
 // softplus. Exponentials, logarithms and divisions use the fast hardware
 // approximations; with bf16 conditioner weights their error is far below the
 // inputs' own rounding. raw: the 3K+1 conditioner outputs with bias added.
+// log(1 + e) with e = exp(-|a|) <= 1 as __logf(1 + e): where 1 + e rounds
+// to 1 the error is at most e < 2^-24 in absolute terms, far below the
+// minimum knot slope (1e-4) the result is added to
 __device__ __forceinline__ float softplus_fast(float a) {
-  return fmaxf(a, 0.f) + log1pf(__expf(-fabsf(a)));
+  return fmaxf(a, 0.f) + __logf(1.f + __expf(-fabsf(a)));
 }
 
 template <int K, bool INV>

@@ -220,15 +220,30 @@ __device__ __forceinline__ bool epi_any(bool v) {
   return r != 0;
 }
 
+// bias rows in shared memory: P floats per transformed coordinate, padded to
+// a multiple of 4 so each row is read as float4
+template <int K>
+struct BiasRows {
+  static constexpr int PP = (3 * K + 1 + 3) / 4 * 4;
+};
+
 template <int KB, bool INV, int STAGES>
 __global__ void __launch_bounds__(kSplThreads, 1)
     k_tc_spline(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int n_groups,
-                int nt, int K, const float* __restrict__ bias, float* __restrict__ xa, int d, int tpar,
-                float* __restrict__ ldp, SplineCfg cfg, int* err) {
+                int nt, int K, const float* __restrict__ bias, int bias_smem, float* __restrict__ xa, int d,
+                int tpar, float* __restrict__ ldp, SplineCfg cfg, int* err) {
   using T = SplineTile<KB>;
-  constexpr int P = T::P, DG = T::DG, BN = T::BN, E = kSplineEpiPerQuarter;
+  constexpr int P = T::P, DG = T::DG, BN = T::BN, E = kSplineEpiPerQuarter, PP = BiasRows<KB>::PP;
+  using S = Smem<BN, STAGES>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  float* sbias = (float*)(base + STAGES * S::STAGE_BYTES + 256);   // after the ring and its barriers
+  if (bias_smem) {
+    for (int i = threadIdx.x; i < nt * PP; i += blockDim.x) {
+      const int t = i / PP, pp = i - t * PP;
+      sbias[i] = pp < P ? __ldg(bias + t * P + pp) : 0.f;
+    }   // visible after pipe_setup's __syncthreads
+  }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nk = (K + BK - 1) / BK;
   const int tiles = (M + BM - 1) / BM * n_groups;
@@ -263,9 +278,21 @@ __global__ void __launch_bounds__(kSplThreads, 1)
         if (gm < M) {
           float* xp = xa + (int64_t)gm * d + 2 * tcoord + tpar;
           const float xv = *xp;
-          const float* bb = bias + (int64_t)tcoord * P;
+          if (bias_smem) {
+            const float4* bb = reinterpret_cast<const float4*>(sbias + tcoord * PP);
 #pragma unroll
-          for (int i = 0; i < P; ++i) raw[i] += __ldg(bb + i);
+            for (int i = 0; i < PP / 4; ++i) {
+              const float4 bv = bb[i];
+              if (4 * i < P) raw[4 * i] += bv.x;
+              if (4 * i + 1 < P) raw[4 * i + 1] += bv.y;
+              if (4 * i + 2 < P) raw[4 * i + 2] += bv.z;
+              if (4 * i + 3 < P) raw[4 * i + 3] += bv.w;
+            }
+          } else {
+            const float* bb = bias + (int64_t)tcoord * P;
+#pragma unroll
+            for (int i = 0; i < P; ++i) raw[i] += __ldg(bb + i);
+          }
           float y, l;
           rqs_apply_fast<KB, INV>(raw, xv, cfg, y, l);
           *xp = y;
@@ -424,18 +451,22 @@ static int launch_spl(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap&
   constexpr int STAGES = 4;
   using S = tc::Smem<tc::SplineTile<KB>::BN, STAGES>;
   auto kern = tc::k_tc_spline<KB, INV, STAGES>;
-  static bool attr = false;
-  if (!attr) {
-    FMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S::TOTAL));
-    attr = true;
+  // the ring, its barriers and (when they fit) the layer's bias rows
+  const size_t with_bias = S::TOTAL + (size_t)nt * tc::BiasRows<KB>::PP * sizeof(float);
+  const int bias_smem = with_bias <= 227 * 1024 ? 1 : 0;
+  const size_t total = bias_smem ? with_bias : (size_t)S::TOTAL;
+  static int attr = 0;
+  if (attr < (int)total) {
+    FMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)total));
+    attr = (int)total;
   }
   int* err = nullptr;
   int rc = tc_error_word(&err);
   if (rc) return rc;
   const int64_t tiles = (M + tc::BM - 1) / tc::BM * n_groups;
   const int64_t grid = tiles < sm_count() ? tiles : sm_count();
-  kern<<<(unsigned)grid, tc::kSplThreads, S::TOTAL, st>>>(ma, mb, (int)M, n_groups, nt, K, bias, xa, d, tpar, ldp,
-                                                           cfg, err);
+  kern<<<(unsigned)grid, tc::kSplThreads, total, st>>>(ma, mb, (int)M, n_groups, nt, K, bias, bias_smem, xa, d,
+                                                       tpar, ldp, cfg, err);
   FMC_LAUNCH_CHECK();
   return FMC_OK;
 }

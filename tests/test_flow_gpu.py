@@ -256,7 +256,10 @@ def gpu_grad_to_full_params(m):
     return F.flatten(tmp)
 
 
-BF16_CONFIGS = [(32, 4, (128, 128), 10), (128, 2, (512, 512), 12), (5, 2, (32, 32), 8), (64, 3, (256, 256), 8)]
+# (700, 2, ...): 350 transformed coordinates, more bias rows than the fused
+# spline kernel stages in shared memory (its global-load path)
+BF16_CONFIGS = [(32, 4, (128, 128), 10), (128, 2, (512, 512), 12), (5, 2, (32, 32), 8), (64, 3, (256, 256), 8),
+                (700, 2, (64, 64), 12)]
 
 
 @pytest.mark.parametrize("d,L,hidden,nb", BF16_CONFIGS, ids=[f"d{c[0]}L{c[1]}K{c[3]}" for c in BF16_CONFIGS])
