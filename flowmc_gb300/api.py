@@ -2,7 +2,7 @@
 from .random import PRNGKey, split  # noqa: F401
 from .resource.buffers import Buffer  # noqa: F401
 from .resource.states import State  # noqa: F401
-from .resource.logPDF import LogPDF, Variable  # noqa: F401
+from .resource.logPDF import LogPDF, TemperedPDF, Variable  # noqa: F401
 from .resource.kernel.MALA import MALA  # noqa: F401
 from .resource.kernel.HMC import HMC  # noqa: F401
 from .resource.kernel.Gaussian_random_walk import GaussianRandomWalk  # noqa: F401
@@ -15,5 +15,7 @@ from .resource.model.nf_model.rqSpline import MaskedCouplingRQSpline  # noqa: F4
 from .resource.optimizer import Optimizer  # noqa: F401
 from .strategy.train_model import TrainModel  # noqa: F401
 from .resource_strategy_bundle.RQSpline_MALA import RQSpline_MALA_Bundle  # noqa: F401
+from .resource_strategy_bundle.RQSpline_MALA_PT import RQSpline_MALA_PT_Bundle  # noqa: F401
+from .strategy.parallel_tempering import ParallelTempering  # noqa: F401
 from .Sampler import Sampler  # noqa: F401
 from . import batched  # noqa: F401

@@ -18,6 +18,24 @@ int check_target(const FmcTarget* t) {
   return FMC_OK;
 }
 
+int dispatch_local(const LocalArgs& a, const FmcLocalParams* params, cudaStream_t st) {
+  Shape sh = default_shape(a.d);
+  if (params->lanes_per_chain > 0) {
+    const int G = params->lanes_per_chain;
+    FMC_CHECK_SUPPORTED(G == 4 || G == 8 || G == 16 || G == 32, "lanes_per_chain=%d not in {4, 8, 16, 32}", G);
+    int V = 1;
+    while (G * V < a.d) V *= 2;
+    FMC_CHECK_SUPPORTED(V <= 8, "lanes_per_chain=%d too small for n_dim=%d", G, a.d);
+    sh = Shape{G, V};
+  }
+  FMC_CHECK_SUPPORTED(sh.G * sh.V >= a.d, "shape too small for n_dim");
+  switch (params->kind) {
+    case FMC_KERNEL_MALA: return launch_local_mala(a, sh, st);
+    case FMC_KERNEL_HMC: return launch_local_hmc(a, sh, st);
+    default: return launch_local_grw(a, sh, st);
+  }
+}
+
 }  // namespace fmc
 
 using namespace fmc;
@@ -67,22 +85,7 @@ extern "C" int fmc_local_steps(const FmcTarget* target, const FmcLocalParams* pa
   a.x_last = x_last;
   a.lp_last = lp_last;
 
-  Shape sh = default_shape(a.d);
-  if (params->lanes_per_chain > 0) {
-    const int G = params->lanes_per_chain;
-    FMC_CHECK_SUPPORTED(G == 4 || G == 8 || G == 16 || G == 32, "lanes_per_chain=%d not in {4, 8, 16, 32}", G);
-    int V = 1;
-    while (G * V < a.d) V *= 2;
-    FMC_CHECK_SUPPORTED(V <= 8, "lanes_per_chain=%d too small for n_dim=%d", G, a.d);
-    sh = Shape{G, V};
-  }
-  FMC_CHECK_SUPPORTED(sh.G * sh.V >= a.d, "shape too small for n_dim");
-  cudaStream_t st = (cudaStream_t)stream;
-  switch (params->kind) {
-    case FMC_KERNEL_MALA: return launch_local_mala(a, sh, st);
-    case FMC_KERNEL_HMC: return launch_local_hmc(a, sh, st);
-    default: return launch_local_grw(a, sh, st);
-  }
+  return dispatch_local(a, params, (cudaStream_t)stream);
 }
 
 template <int TGT, int G, int V>

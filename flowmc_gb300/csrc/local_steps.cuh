@@ -54,7 +54,43 @@ struct LocalArgs {
   float* lp_last;
   int64_t C_pad;
   int32_t tab_smem;   // diag Gaussian / mixture: tables staged in shared memory
+  // parallel tempering (NULL temps: plain target). Row c targets
+  // beta * log L(x) + log prior(x) with beta = 1 / temps[c % n_temps]; the
+  // prior is zero or diagonal Gaussian (prior_iv != NULL).
+  const float* temps;
+  int32_t n_temps;
+  const float* prior_mean;
+  const float* prior_iv;
+  float prior_const;
+  float* acc_count;   // optional: accepted steps per chain
 };
+
+// Tempered log-density (resource/logPDF.py:106-108): (1 / T) * log L(x) +
+// log prior(x), with the gradient scaled the same way.
+template <int G, int V, bool GRAD>
+__device__ __forceinline__ float temper(const LocalArgs& a, float lp, const float (&x)[V], float (&g)[V],
+                                        float beta, int gl) {
+  lp = beta * lp;
+  if constexpr (GRAD) {
+#pragma unroll
+    for (int v = 0; v < V; ++v) g[v] *= beta;
+  }
+  if (a.prior_iv) {
+    float s = 0.f;
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const int j = gl * V + v;
+      if (j < a.d) {
+        const float dx = x[v] - __ldg(a.prior_mean + j);
+        const float iv = __ldg(a.prior_iv + j);
+        s += dx * dx * iv;
+        if constexpr (GRAD) g[v] -= dx * iv;
+      }
+    }
+    lp += -0.5f * group_sum<G>(s) + a.prior_const;
+  }
+  return lp;
+}
 
 template <int V>
 __device__ __forceinline__ void draw_normals(const LocalArgs& a, int64_t c, int s, int gl,
@@ -164,19 +200,24 @@ __global__ void __launch_bounds__(256) k_local_steps(const LocalArgs a) {
       const int j = gl * V + v;
       x[v] = (j < d) ? __ldg(a.x0 + cc * d + j) : 0.f;
     }
+    const bool tempered = a.temps != nullptr;
+    const float beta = tempered ? __fdiv_rn(1.f, __ldg(a.temps + cc % a.n_temps)) : 1.f;
     float lp = target_eval<TGT, G, V, KIND != FMC_KERNEL_GRW>(a.tgt, x, g, gl, stage);
+    if (tempered) lp = temper<G, V, KIND != FMC_KERNEL_GRW>(a, lp, x, g, beta, gl);
     if (KIND != FMC_KERNEL_MALA && a.lp0 != nullptr) lp = __ldg(a.lp0 + cc);
     float xr[V], lpr = lp;
 #pragma unroll
     for (int v = 0; v < V; ++v) xr[v] = x[v];
 
     u32x4 ub{0u, 0u, 0u, 0u};
-    // next stored row (every thin-th step, from row `start`)
+    // next stored row (every thin-th step, from row `start`); no rows are
+    // stored when out_pos is NULL (the tempered chains keep only their end)
+    const bool rec = a.out_pos != nullptr;
     const int64_t row0 = cc * a.buf_len + a.start;
-    float* prow = a.out_pos + row0 * d;
-    float* plp = a.out_logp + row0;
-    float* pacc = a.out_acc + row0;
-    int tcount = 0;
+    float* prow = rec ? a.out_pos + row0 * d : nullptr;
+    float* plp = rec ? a.out_logp + row0 : nullptr;
+    float* pacc = rec ? a.out_acc + row0 : nullptr;
+    int tcount = 0, n_acc = 0;
     for (int s = 0; s < a.S; ++s) {
       float xi[V];
       draw_normals<V>(a, cc, s, gl, xi);
@@ -190,7 +231,8 @@ __global__ void __launch_bounds__(256) k_local_steps(const LocalArgs a) {
           mean0[v] = x[v] + dt2 * g[v] / 2.0f;
           prop[v] = mean0[v] + dt * xi[v];
         }
-        const float lp1 = target_eval<TGT, G, V, true>(a.tgt, prop, g1, gl, stage);
+        float lp1 = target_eval<TGT, G, V, true>(a.tgt, prop, g1, gl, stage);
+        if (tempered) lp1 = temper<G, V, true>(a, lp1, prop, g1, beta, gl);
         float sa = 0.f, sb = 0.f;
 #pragma unroll
         for (int v = 0; v < V; ++v) {
@@ -236,6 +278,7 @@ __global__ void __launch_bounds__(256) k_local_steps(const LocalArgs a) {
 #pragma unroll
           for (int v = 0; v < V; ++v) xq[v] = xq[v] + dt * (p[v] * mc[v]);
           lpq = target_eval<TGT, G, V, true>(a.tgt, xq, gq, gl, stage);
+          if (tempered) lpq = temper<G, V, true>(a, lpq, xq, gq, beta, gl);
 #pragma unroll
           for (int v = 0; v < V; ++v) p[v] = p[v] + ek * gq[v];
         }
@@ -257,7 +300,8 @@ __global__ void __launch_bounds__(256) k_local_steps(const LocalArgs a) {
         float prop[V], gdummy[V];
 #pragma unroll
         for (int v = 0; v < V; ++v) prop[v] = x[v] + xi[v] * dt;
-        const float lpp = target_eval<TGT, G, V, false>(a.tgt, prop, gdummy, gl, stage);
+        float lpp = target_eval<TGT, G, V, false>(a.tgt, prop, gdummy, gl, stage);
+        if (tempered) lpp = temper<G, V, false>(a, lpp, prop, gdummy, beta, gl);
         acc = f_lt_ff(logu, two_sum(lpp, -lp));
         if (acc) {
 #pragma unroll
@@ -265,17 +309,20 @@ __global__ void __launch_bounds__(256) k_local_steps(const LocalArgs a) {
           lp = lpp;
         }
       }
+      n_acc += acc ? 1 : 0;
       if (tcount == 0) {
-        if (active) {
-          store_row<G, V>(prow, x, gl, d);
-          if (gl == 0) {
-            __stcs(plp, lp);
-            __stcs(pacc, acc ? 1.f : 0.f);
+        if (rec) {
+          if (active) {
+            store_row<G, V>(prow, x, gl, d);
+            if (gl == 0) {
+              __stcs(plp, lp);
+              __stcs(pacc, acc ? 1.f : 0.f);
+            }
           }
+          prow += d;
+          ++plp;
+          ++pacc;
         }
-        prow += d;
-        ++plp;
-        ++pacc;
 #pragma unroll
         for (int v = 0; v < V; ++v) xr[v] = x[v];
         lpr = lp;
@@ -288,7 +335,10 @@ __global__ void __launch_bounds__(256) k_local_steps(const LocalArgs a) {
         const int j = gl * V + v;
         if (j < d) a.x_last[cc * d + j] = xr[v];
       }
-      if (gl == 0) a.lp_last[cc] = lpr;
+      if (gl == 0) {
+        a.lp_last[cc] = lpr;
+        if (a.acc_count) a.acc_count[cc] = (float)n_acc;
+      }
     }
   }
 }
@@ -400,6 +450,9 @@ int launch_local_kind(const LocalArgs& a, Shape sh, cudaStream_t st) {
   return FMC_ERR_INVALID_ARG;
 }
 
+// K1 with the (lanes per chain, coordinates per lane) shape params asks for
+// (library default for n_dim when lanes_per_chain is 0)
+int dispatch_local(const LocalArgs& a, const FmcLocalParams* params, cudaStream_t st);
 int launch_local_mala(const LocalArgs& a, Shape sh, cudaStream_t st);
 int launch_local_hmc(const LocalArgs& a, Shape sh, cudaStream_t st);
 int launch_local_grw(const LocalArgs& a, Shape sh, cudaStream_t st);

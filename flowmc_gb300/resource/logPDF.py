@@ -75,3 +75,70 @@ def as_target(logpdf) -> Target:
     if isinstance(logpdf, Target):
         return logpdf
     raise TypeError("expected a LogPDF wrapping a flowmc_gb300 target, or a target")
+
+
+class TemperedPDF(LogPDF):
+    """TemperedPDF (mirrors resource/logPDF.py:84-115 of the reference):
+    ``tempered_log_pdf(T, x) = (1 / T) * log_likelihood(x) + log_prior(x)``,
+    evaluated inside the fused tempered local-step kernel.
+
+    ``log_likelihood`` is a registered device target (or a LogPDF wrapping
+    one). ``log_prior`` is None, the reference bundle's zero prior
+    (``lambda x, _: 0.0`` -- recognised by returning exactly 0.0 on a zero
+    vector without touching a GPU), or a ``targets.DiagGaussian``; other
+    priors cannot run inside the fused kernel and are refused.
+    ``__call__`` is the untempered likelihood, as in the reference (the
+    exchange step compares those values, parallel_tempering.py:386).
+    """
+
+    def __init__(self, log_likelihood, log_prior=None, variables=None, n_dims=None, n_temps=5, max_temp=100):
+        super().__init__(log_likelihood, variables, n_dims)
+        self.log_prior = log_prior
+        self.n_temps = n_temps
+        self.max_temp = max_temp
+        self._prior = _prior_arrays(log_prior, self.n_dims)
+
+    def tempered_log_pdf(self, temperatures, x, data=None):
+        """(1 / T) * log L(x) + log prior(x) for a batch x [n, d] and per-row T."""
+        import torch
+        lp = self.target(x, data)
+        t = torch.as_tensor(temperatures, dtype=torch.float32, device=lp.device)
+        out = (1.0 / t) * lp
+        if self._prior is not None:
+            m, iv, c = self._prior
+            xx = x.reshape(-1, self.n_dims)
+            out = out - 0.5 * (((xx - m.to(xx.device)) ** 2) * iv.to(xx.device)).sum(-1).reshape(out.shape) + c
+        return out
+
+    def prior_arrays(self, device):
+        """(mean, inv_var, const) of the diagonal Gaussian prior on `device`, or None."""
+        if self._prior is None:
+            return None
+        m, iv, c = self._prior
+        return m.to(device), iv.to(device), c
+
+
+def _prior_arrays(prior, n_dims):
+    import numpy as np
+    import torch
+    from ..targets import DiagGaussian
+    if prior is None:
+        return None
+    if isinstance(prior, DiagGaussian):
+        if prior.n_dim != n_dims:
+            raise ValueError(f"prior has {prior.n_dim} coordinates, likelihood has {n_dims}")
+        m = torch.as_tensor(np.asarray(prior.mean, np.float32))
+        iv = torch.as_tensor(np.asarray(prior.inv_var, np.float32))
+        return m, iv, float(prior.const)
+    if callable(prior) and not isinstance(prior, Target):
+        rng = np.random.default_rng(0)
+        probes = [np.zeros(n_dims), rng.normal(size=n_dims), 1e3 * rng.normal(size=n_dims)]
+        try:
+            vals = [prior(p, {}) for p in probes]
+        except Exception:
+            vals = [None]
+        if all(isinstance(v, (int, float)) and float(v) == 0.0 for v in vals):
+            return None
+    raise NotImplementedError(
+        "the fused tempered kernel supports a zero log prior or a targets.DiagGaussian prior; "
+        f"got {type(prior).__name__}")

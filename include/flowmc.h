@@ -111,6 +111,53 @@ FMC_API int fmc_local_steps(const FmcTarget* target, const FmcLocalParams* param
                     int64_t buf_len, int64_t cursor,
                     float* x_last, float* lp_last, void* stream);
 
+/* ---- parallel tempering (strategy/parallel_tempering.py) ------------- */
+/* Tempered local steps: ParallelTempering._ensemble_step
+ * (parallel_tempering.py:250-289) for every chain, i.e. n_steps of the local
+ * kernel for each of the n_chains * n_temps (chain, temperature) rows on
+ * TemperedPDF.tempered_log_pdf (resource/logPDF.py:106-108):
+ *   (1 / temperatures[t]) * log L(x) + log prior(x).
+ * The log-density at x0 is recomputed (parallel_tempering.py:236-238); no
+ * per-step rows are stored (the reference keeps only the last state).
+ *   x0           [n_chains, n_temps, n_dim]  row c * n_temps + t
+ *   temperatures [n_temps] device array (n_temps <= 64)
+ *   prior_mean, prior_inv_var  [n_dim] a diagonal Gaussian log prior
+ *                -0.5 sum (x - m)^2 iv + prior_const, or both NULL = 0
+ *   noise        [n_chains * n_temps, n_steps, n_dim] or NULL (Philox)
+ *   unif         [n_chains * n_temps, n_steps] or NULL (Philox)
+ *   x_last       [n_chains * n_temps, n_dim], lp_last [n_chains * n_temps]
+ *                (tempered log-density)
+ *   acc_count    [n_chains * n_temps] accepted steps, or NULL */
+FMC_API int fmc_pt_local_steps(const FmcTarget* target, const FmcLocalParams* params, const float* x0,
+                               int32_t n_chains, int32_t n_temps, const float* temperatures,
+                               const float* prior_mean, const float* prior_inv_var, float prior_const,
+                               int32_t n_steps, uint64_t seed, uint64_t counter, const float* noise,
+                               const float* unif, float* x_last, float* lp_last, float* acc_count,
+                               void* stream);
+
+/* Exchange sweep: ParallelTempering._exchange (parallel_tempering.py:291-398)
+ * for every chain. log L (untempered, no prior) at each temperature's
+ * position, then for i = 0 .. n_temps-2 in order: swap positions i and i+1
+ * iff log u < (1/T[i+1] - 1/T[i]) * (lp[i] - lp[i+1]).
+ *   x          [n_chains, n_temps, n_dim] positions (not modified)
+ *   unif       [n_chains, n_temps - 1] uniforms, or NULL (Philox)
+ *   out_first  [n_chains, n_dim]  the temperature-1 position after the sweep
+ *   out_rest   [n_chains, n_temps - 1, n_dim] the others, or NULL (not
+ *              written: the reference keeps them only while training,
+ *              parallel_tempering.py:123-132)
+ *   out_logp   [n_chains, n_temps] log L after the sweep, or NULL
+ *   out_acc    [n_chains, n_temps - 1] swap flags, or NULL
+ *   acc_pairs  [n_temps - 1] int32 swaps accepted per pair (zeroed first) */
+FMC_API int fmc_pt_exchange(const FmcTarget* target, const float* x, int32_t n_chains, int32_t n_temps,
+                            const float* temperatures, uint64_t seed, uint64_t counter, const float* unif,
+                            float* out_first, float* out_rest, float* out_logp, float* out_acc,
+                            int32_t* acc_pairs, void* stream);
+
+/* ParallelTempering._adapt_temperature (parallel_tempering.py:400-436) from
+ * the swap counts of fmc_pt_exchange; out may alias temperatures. */
+FMC_API int fmc_pt_adapt_temperatures(const float* temperatures, const int32_t* acc_pairs, int32_t n_chains,
+                                      int32_t n_temps, float* out_temperatures, void* stream);
+
 /* Many dense-Gaussian targets of uneven dimension (1..256) in ONE persistent
  * launch: n_steps of MALA or HMC (identity mass) for every chain of every
  * target, chain tiles pulled by CTAs from an atomic work counter. The local

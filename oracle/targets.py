@@ -23,6 +23,20 @@ def value_grad(t: dict, x: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
     """x [n, d] -> (logp [n], grad [n, d]) in float64."""
     x = np.asarray(x, dtype=np.float64)
     k = t["kind"]
+    if k == "tempered":
+        # TemperedPDF.tempered_log_pdf (resource/logPDF.py:106-108): per-row
+        # beta = 1 / T times the base log-density, plus an optional diagonal
+        # Gaussian log prior
+        lp, g = value_grad(t["base"], x)
+        beta = np.asarray(t["beta"], np.float64)
+        lp, g = beta * lp, beta[:, None] * g
+        pr = t.get("prior")
+        if pr is not None:
+            dx = x - np.asarray(pr["mean"], np.float64)
+            iv = np.asarray(pr["inv_var"], np.float64)
+            lp = lp - 0.5 * np.sum(dx * dx * iv, axis=-1) + pr.get("const", 0.0)
+            g = g - dx * iv
+        return lp, g
     if k == "diag_gaussian":
         m = np.asarray(t["mean"], np.float64)
         iv = np.asarray(t["inv_var"], np.float64)
@@ -79,6 +93,8 @@ def value(t: dict, x: np.ndarray) -> np.ndarray:
 
 
 def n_dim(t: dict) -> int:
+    if t["kind"] == "tempered":
+        return n_dim(t["base"])
     if "n_dim" in t:
         return int(t["n_dim"])
     m = np.asarray(t["mean"])

@@ -27,10 +27,19 @@ def grad(f):
 def vmap(f, in_axes=0):
     def vf(*args):
         axes = in_axes if isinstance(in_axes, (tuple, list)) else (in_axes,) * len(args)
-        n = next(torch.as_tensor(a).shape[ax] for a, ax in zip(args, axes) if ax is not None)
+
+        def size(a, ax):
+            return len(a) if isinstance(a, list) else torch.as_tensor(a).shape[ax]
+
+        def pick(a, ax, i):
+            if ax is None:
+                return a
+            return a[i] if isinstance(a, list) else torch.as_tensor(a).select(ax, i)
+
+        n = next(size(a, ax) for a, ax in zip(args, axes) if ax is not None)
         outs = []
         for i in range(n):
-            outs.append(f(*[torch.as_tensor(a).select(ax, i) if ax is not None else a for a, ax in zip(args, axes)]))
+            outs.append(f(*[pick(a, ax, i) for a, ax in zip(args, axes)]))
         if isinstance(outs[0], tuple):
             return tuple(torch.stack([o[k] for o in outs]) for k in range(len(outs[0])))
         return torch.stack(outs)

@@ -22,3 +22,19 @@ def scan(f, init, xs=None, length=None):
 
 def stop_gradient(x):
     return x.detach() if isinstance(x, torch.Tensor) else x
+
+
+def cond(pred, true_fun, false_fun, *operands):
+    return true_fun(*operands) if bool(pred) else false_fun(*operands)
+
+
+def dynamic_slice_in_dim(x, start, size, axis=0):
+    return x.narrow(axis, int(start), size)
+
+
+def dynamic_update_slice_in_dim(x, update, start, axis=0):
+    out = x.clone()
+    n = update.shape[axis]
+    s = min(max(int(start), 0), x.shape[axis] - n)
+    out.narrow(axis, s, n).copy_(update)
+    return out

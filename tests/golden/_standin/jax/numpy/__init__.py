@@ -96,6 +96,11 @@ def concatenate(xs, axis=0):
     return torch.cat([_t(v) for v in xs], dim=axis)
 
 
+def flip(x, axis=None):
+    x = _t(x)
+    return torch.flip(x, dims=tuple(range(x.dim())) if axis is None else (axis,))
+
+
 def stack(xs, axis=0):
     return torch.stack([_t(v) for v in xs], dim=axis)
 

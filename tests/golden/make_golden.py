@@ -1,10 +1,12 @@
 """Golden vectors from the reference's own source code.
 
 Runs flowMC v0.4.5's MALA, HMC and GaussianRandomWalk kernels
-(resource/kernel/MALA.py:26-89, HMC.py:98-151, Gaussian_random_walk.py:25-61)
-and its RQSpline bijection (knots, forward and inverse:
-resource/model/nf_model/rqSpline.py:20-239, 296-362) on scripted normals and
-uniforms, and saves inputs and outputs to ``reference_vectors.npz`` beside
+(resource/kernel/MALA.py:26-89, HMC.py:98-151, Gaussian_random_walk.py:25-61),
+its RQSpline bijection (knots, forward and inverse:
+resource/model/nf_model/rqSpline.py:20-239, 296-362) and its
+ParallelTempering ensemble step, exchange sweep and temperature adaptation
+(strategy/parallel_tempering.py:205-436, on resource/logPDF.py's TemperedPDF)
+on scripted normals and uniforms, and saves inputs and outputs to ``reference_vectors.npz`` beside
 this file. JAX is not installed here, so the reference modules run against
 the stand-ins under ``_standin/`` (float64 torch tensors, autograd for
 ``jax.value_and_grad``/``jax.grad``, Python loops for ``lax.scan`` and
@@ -33,6 +35,8 @@ from flowMC.resource.kernel.Gaussian_random_walk import GaussianRandomWalk  # no
 from flowMC.resource.kernel.HMC import HMC  # noqa: E402
 from flowMC.resource.kernel.MALA import MALA  # noqa: E402
 from flowMC.resource.model.nf_model.rqSpline import RQSpline  # noqa: E402
+from flowMC.resource.logPDF import TemperedPDF  # noqa: E402
+from flowMC.strategy.parallel_tempering import ParallelTempering  # noqa: E402
 
 
 def jnp_target(t):
@@ -71,6 +75,40 @@ def run_kernel(kernel, logpdf, x0, noise, unif):
         lps.append(float(lp))
         accs.append(float(bool(acc)))
     return np.array(pos), np.array(lps), np.array(accs)
+
+
+def run_parallel_tempering(kernel, f, prior, temps, x0, noise, unif, u_ex):
+    """ParallelTempering's ensemble step and exchange sweep for each chain
+    (strategy/parallel_tempering.py:250-398), then the temperature adaptation
+    on all chains' swap flags (400-436). Key paths: chain c's ensemble key
+    pt<c> splits into one key per temperature, whose step-s subkey is
+    <key>.0^s.1 (split children .0 normals, .1 uniform); the exchange key
+    ex<c> gives step i the uniform at ex<c>.0^i.1."""
+    C, Tn, S, d = noise.shape
+    pt = ParallelTempering(n_steps=S, tempered_logpdf_name="tempered_logpdf", kernel_name="local_sampler",
+                           tempered_buffer_names=["tempered_positions", "temperatures"], state_name="sampler_state")
+    tlp = TemperedPDF(f, prior, n_dims=d, n_temps=Tn)
+    tt = torch.tensor(temps)
+    ens_x, ens_lp, ens_acc, ex_x, ex_lp, ex_acc = [], [], [], [], [], []
+    for c in range(C):
+        for t in range(Tn):
+            for st in range(S):
+                path = f"pt{c}.{t}" + ".0" * st + ".1"
+                jr.DRAWS[path + ".0"] = noise[c, t, st]
+                jr.DRAWS[path + ".1"] = unif[c, t, st]
+        pos, lp, acc = pt._ensemble_step(kernel, jr.Key(f"pt{c}"), torch.tensor(x0[c]), tlp, tt, None)
+        ens_x.append(pos.detach().numpy())
+        ens_lp.append(lp.detach().numpy())
+        ens_acc.append(torch.as_tensor(acc, dtype=torch.float64).numpy())
+        for i in range(Tn - 1):
+            jr.DRAWS[f"ex{c}" + ".0" * i + ".1"] = u_ex[c, i]
+        pos2, lp2, acc2 = pt._exchange(jr.Key(f"ex{c}"), pos.detach(), tlp, tt, None)
+        ex_x.append(pos2.detach().numpy())
+        ex_lp.append(lp2.detach().numpy())
+        ex_acc.append(torch.as_tensor(acc2, dtype=torch.float64).numpy())
+    ex_acc = np.stack(ex_acc)
+    new_t = pt._adapt_temperature(tt, torch.tensor(ex_acc)).numpy()
+    return (np.stack(ens_x), np.stack(ens_lp), np.stack(ens_acc), np.stack(ex_x), np.stack(ex_lp), ex_acc, new_t)
 
 
 class _Conditioner:
@@ -148,9 +186,60 @@ def main():
         out[f"{name}/inv_x"] = xi.numpy()
         out[f"{name}/inv_logdet"] = ldi.numpy()
         cases.append({"name": name, "kind": "rqspline", "n_bins": K})
+    # ParallelTempering: tempered ensemble steps, exchange sweep, adaptation
+    pt_plans = [("mala", "dual_moon5", 0.25, 0, None, 5.0), ("grw", "diag4", 0.8, 0, "gauss", 8.0),
+                ("hmc", "rosenbrock6", 0.02, 4, None, 3.0)]
+    C, Tn, S = 3, 4, 6
+    for kind, tname, step, nlf, prior_kind, tmax in pt_plans:
+        t = targets[tname]
+        d = t["n_dim"]
+        temps = np.linspace(1.0, tmax, Tn)
+        x0 = rng.normal(size=(C, Tn, d))
+        if tname == "dual_moon5":
+            x0 = x0 / np.linalg.norm(x0, axis=-1, keepdims=True) * 2.0
+        if tname == "rosenbrock6":
+            x0 = 0.3 * x0 + 0.5
+        noise = rng.normal(size=(C, Tn, S, d))
+        unif = rng.uniform(1e-6, 1.0, size=(C, Tn, S))
+        u_ex = rng.uniform(1e-6, 1.0, size=(C, Tn - 1))
+        if kind == "mala":
+            kern = MALA(step)
+        elif kind == "grw":
+            kern = GaussianRandomWalk(step)
+        else:
+            kern = HMC(condition_matrix=torch.eye(d, dtype=torch.float64), step_size=step, n_leapfrog=nlf)
+        prior = {"mean": rng.normal(size=d) * 0.5, "inv_var": rng.uniform(0.2, 1.0, size=d), "const": -0.75} \
+            if prior_kind == "gauss" else None
+        if prior is None:
+            prior_f = lambda x, _: 0.0  # noqa: E731  (the bundle's default prior)
+        else:
+            pm, piv, pc = torch.tensor(prior["mean"]), torch.tensor(prior["inv_var"]), prior["const"]
+            prior_f = lambda x, _: -0.5 * jnp.sum((x - pm) ** 2 * piv) + pc  # noqa: E731
+        res = run_parallel_tempering(kern, jnp_target(t), prior_f, temps, x0, noise, unif, u_ex)
+        name = f"pt_{kind}_{tname}"
+        for key, val in zip(("x0", "noise", "unif", "u_exchange", "temps"), (x0, noise, unif, u_ex, temps)):
+            out[f"{name}/{key}"] = val
+        for key, val in zip(("ens_x", "ens_lp", "ens_acc", "ex_x", "ex_lp", "ex_acc", "new_temps"), res):
+            out[f"{name}/{key}"] = val
+        case = {"name": name, "kind": "pt", "local": kind, "target": t, "step_size": step, "n_leapfrog": nlf}
+        if prior is not None:
+            case["prior"] = {k: np.asarray(v).tolist() for k, v in prior.items()}
+        cases.append(case)
+    # temperature adaptation alone on many chains (damping of order one)
+    pt = ParallelTempering(1, "tempered_logpdf", "local_sampler", ["tempered_positions", "temperatures"],
+                           "sampler_state")
+    temps = np.array([1.0, 1.7, 2.9, 4.4, 6.0, 9.0])
+    flags = (rng.uniform(size=(200, 5)) < np.array([0.9, 0.6, 0.75, 0.3, 0.5])).astype(np.float64)
+    out["pt_adapt/temps"] = temps
+    out["pt_adapt/flags"] = flags
+    out["pt_adapt/new_temps"] = pt._adapt_temperature(torch.tensor(temps), torch.tensor(flags)).numpy()
+    cases.append({"name": "pt_adapt", "kind": "pt_adapt"})
     for c in cases:
         if c["kind"] in ("mala", "hmc", "grw"):
             print(f"{c['name']}: acceptance {out[c['name'] + '/acc'].mean():.2f}")
+        if c["kind"] == "pt":
+            print(f"{c['name']}: step acceptance {out[c['name'] + '/ens_acc'].mean():.2f}, "
+                  f"swaps {out[c['name'] + '/ex_acc'].mean():.2f}")
     out["cases"] = np.array(json.dumps(cases))
     path = os.path.join(HERE, "reference_vectors.npz")
     np.savez_compressed(path, **out)
