@@ -99,6 +99,19 @@ class NFModel(Resource):
 
     # ---------------------------------------------------------------- persistence
     def save_model(self, path: str):
+        """The reference's checkpoint (nf_model/base.py:92-93): an equinox
+        tree_serialise_leaves file at path + ".eqx"."""
+        from .eqx_format import save_eqx
+        save_eqx(self, path + ".eqx")
+
+    def load_model(self, path: str):
+        """Load a reference checkpoint (nf_model/base.py:95-96) into this model
+        (same architecture); returns the model."""
+        from .eqx_format import load_eqx
+        return load_eqx(self, path if path.endswith(".eqx") else path + ".eqx")
+
+    def save_npz(self, path: str):
+        """Exact device state (flat parameters and the aux block) as .npz."""
         full = self.to_full()
         arrs = {"aux": self.aux.detach().cpu().numpy()}
         for l, Lr in enumerate(full):
@@ -109,7 +122,7 @@ class NFModel(Resource):
                 arrs[f"l{l}_b{i}"] = b
         np.savez(path + ".npz", **arrs)
 
-    def load_model(self, path: str):
+    def load_npz(self, path: str):
         z = np.load(path if path.endswith(".npz") else path + ".npz")
         layers = []
         for l in range(self.n_layers):
