@@ -116,6 +116,10 @@ _SIGNATURES = {
         ctypes.c_void_p, ctypes.c_void_p]),
     "fmc_pt_adapt_temperatures": (ctypes.c_int, [
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]),
+    "fmc_adam_optimize": (ctypes.c_int, [
+        ctypes.POINTER(FmcTarget), ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_float, ctypes.c_float,
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
+        ctypes.c_void_p, ctypes.c_void_p]),
     "fmc_target_value_grad": (ctypes.c_int, [
         ctypes.POINTER(FmcTarget), ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
         ctypes.c_void_p, ctypes.c_void_p]),

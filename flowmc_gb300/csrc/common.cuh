@@ -108,6 +108,7 @@ enum : uint32_t {
   RNG_TAG_NF_NORMAL = 0x4e4e0000u,
   RNG_TAG_NF_UNIFORM = 0x4e550000u,
   RNG_TAG_PT_EXCHANGE = 0x50580000u,
+  RNG_TAG_ADAM_NOISE = 0x41440000u,
 };
 
 struct Rng {

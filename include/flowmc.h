@@ -158,6 +158,19 @@ FMC_API int fmc_pt_exchange(const FmcTarget* target, const float* x, int32_t n_c
 FMC_API int fmc_pt_adapt_temperatures(const float* temperatures, const int32_t* acc_pairs, int32_t n_chains,
                                       int32_t n_temps, float* out_temperatures, void* stream);
 
+/* ---- pre-sampling optimisation (strategy/optimization.py) ------------ */
+/* AdamOptimization.optimize (optimization.py:85-164) for every chain: n_steps
+ * of optax.adam(learning_rate) (b1 0.9, b2 0.999, eps 1e-8) on -log p(x),
+ * the gradient multiplied by (1 + xi * noise_level) with one standard normal
+ * xi per chain-step, then clipped to [lower, upper] (projection_box).
+ *   x0 [n_chains, n_dim]; lower / upper [n_dim] or NULL (unbounded);
+ *   noise [n_chains, n_steps] normals or NULL (Philox);
+ *   x_out [n_chains, n_dim]; lp_out [n_chains] log p(x_out) or NULL. */
+FMC_API int fmc_adam_optimize(const FmcTarget* target, const float* x0, int32_t n_chains, int32_t n_steps,
+                              float learning_rate, float noise_level, const float* lower, const float* upper,
+                              uint64_t seed, uint64_t counter, const float* noise, float* x_out, float* lp_out,
+                              void* stream);
+
 /* Many dense-Gaussian targets of uneven dimension (1..256) in ONE persistent
  * launch: n_steps of MALA or HMC (identity mass) for every chain of every
  * target, chain tiles pulled by CTAs from an atomic work counter. The local

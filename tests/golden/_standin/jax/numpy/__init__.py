@@ -50,6 +50,14 @@ def exp(x):
     return torch.exp(_t(x))
 
 
+def isinf(x):
+    return torch.isinf(_t(x))
+
+
+def isnan(x):
+    return torch.isnan(_t(x))
+
+
 def sqrt(x):
     return torch.sqrt(_t(x))
 

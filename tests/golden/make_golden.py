@@ -37,6 +37,7 @@ from flowMC.resource.kernel.MALA import MALA  # noqa: E402
 from flowMC.resource.model.nf_model.rqSpline import RQSpline  # noqa: E402
 from flowMC.resource.logPDF import TemperedPDF  # noqa: E402
 from flowMC.strategy.parallel_tempering import ParallelTempering  # noqa: E402
+from flowMC.strategy.optimization import AdamOptimization  # noqa: E402
 
 
 def jnp_target(t):
@@ -234,6 +235,33 @@ def main():
     out["pt_adapt/flags"] = flags
     out["pt_adapt/new_temps"] = pt._adapt_temperature(torch.tensor(temps), torch.tensor(flags)).numpy()
     cases.append({"name": "pt_adapt", "kind": "pt_adapt"})
+    # AdamOptimization.optimize: chain c's key is root.1.c, step s's gradient
+    # noise the scalar normal at root.1.c.0^s.1 (optimization.py:117-157)
+    for tname, n_steps, lr, nl, bounds in (("rosenbrock6", 25, 0.05, 0.5, "per_dim"),
+                                           ("dual_moon5", 30, 0.1, 2.0, "broadcast")):
+        t = targets[tname]
+        d = t["n_dim"]
+        C = 3
+        x0 = rng.normal(size=(C, d))
+        xi = rng.normal(size=(C, n_steps))
+        if bounds == "per_dim":
+            b = np.stack([np.full(d, -0.4), np.full(d, 0.6)], axis=1)
+            b[::2, 0] = -np.inf
+        else:
+            b = np.array([[-1.5, 1.5]])
+        for c in range(C):
+            for st in range(n_steps):
+                jr.DRAWS[f"opt.1.{c}" + ".0" * st + ".1"] = xi[c, st]
+        opt = AdamOptimization(jnp_target(t), n_steps=n_steps, learning_rate=lr, noise_level=nl,
+                               bounds=torch.tensor(b))
+        f = jnp_target(t)
+        _, xo, lpo = opt.optimize(jr.Key("opt"), lambda p, data: -f(p, data), torch.tensor(x0), None)
+        name = f"adam_{tname}"
+        for key, val in (("x0", x0), ("xi", xi), ("bounds", b), ("x", xo.detach().numpy()),
+                         ("logp", lpo.detach().numpy())):
+            out[f"{name}/{key}"] = val
+        cases.append({"name": name, "kind": "adam", "target": t, "n_steps": n_steps, "learning_rate": lr,
+                      "noise_level": nl})
     for c in cases:
         if c["kind"] in ("mala", "hmc", "grw"):
             print(f"{c['name']}: acceptance {out[c['name'] + '/acc'].mean():.2f}")
