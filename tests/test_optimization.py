@@ -98,11 +98,12 @@ def test_cuda_adam_philox_reaches_the_mode(cuda):
     mean = np.linspace(-1, 1, d)
     tgt = TG.DiagGaussian(d, mean=mean, inv_var=np.linspace(0.5, 2, d))
     opt = AdamOptimization(tgt, n_steps=600, learning_rate=0.02, noise_level=0.2)
-    _, _, x = opt(PRNGKey(2), {}, torch.randn(C, d, device="cuda") * 3, {})
+    # Adam moves about one learning rate per step: start within reach
+    _, _, x = opt(PRNGKey(2), {}, torch.randn(C, d, device="cuda"), {})
     # Adam at a fixed rate settles in a band of about the learning rate
     xs = x.cpu().numpy()
     np.testing.assert_allclose(xs, np.broadcast_to(mean, (C, d)), atol=0.08)
     np.testing.assert_allclose(xs.mean(axis=0), mean, atol=0.01)
     # a different key gives different noise, so different (but converged) paths
-    _, _, x2 = opt(PRNGKey(3), {}, torch.randn(C, d, device="cuda") * 3, {})
+    _, _, x2 = opt(PRNGKey(3), {}, torch.randn(C, d, device="cuda"), {})
     assert not torch.equal(x, x2)
