@@ -18,10 +18,16 @@ n_global) * K / timed seconds (summed over ranks, which run independent
 replicas). The working set (chain buffers of several GB, flow weights) is
 far larger than L2, so L2 is not flushed between steps.
 
+By default the K timed loops are captured as one CUDA graph before the timed
+region (``graph_capture_ms``, the one-time capture, is reported separately)
+and the timed region is its replay; ``--eager`` launches them one by one.
+
 ``e2e`` repeats the timed region's loop mix through ``Sampler.sample`` (one
-call per loop) with pinned host buffers: each loop copies its starting
+call per loop, each a replay of that loop's captured schedule unless
+``--eager``) with pinned host buffers: each loop copies its starting
 positions host->device and reads the rows it wrote and its final positions
-back, all inside the wall-clock timed region.
+back, all inside the wall-clock timed region (after one untimed production
+loop that warms the pinned host buffers).
 
 ``--impl reference`` times the CPU restatement of the same loop (the
 reference flowMC itself needs JAX, which this image does not have).
@@ -562,6 +568,8 @@ def main():
     ap.add_argument("--compare", default="",
                     help="T,P: fused bundle and plain FP32 form on the same workload and seed with T training + P "
                          "production loops each; prints their min-ESS/s and moment errors instead of the bench line")
+    ap.add_argument("--eager", action="store_true",
+                    help="launch the timed loops eagerly instead of replaying them as one captured CUDA graph")
     ap.add_argument("--plain-full", action="store_true",
                     help="run the plain FP32 form on the full schedule (min-ESS/s, moment error)")
     args = ap.parse_args()
@@ -637,21 +645,45 @@ def main():
                      f"python bench.py --steps {K} --warmup {W} --workload {args.workload} "
                      f"--precision {args.precision}" + (f" --chains {args.chains}" if args.chains else ""))
         return
+    graph = None
+    capture_ms = None
+    prof = profiling.Profiler()
+    if not args.eager:
+        # the K timed loops as one CUDA graph (untimed one-time setup, reported
+        # as graph_capture_ms); the Profiler's regions become event-record
+        # nodes, so the replay times the same phases
+        epoch = _lib.rng_epoch(dev)
+        l0 = _lib.launch_count()
+        torch.cuda.synchronize()
+        c0 = time.perf_counter()
+        graph = torch.cuda.CUDAGraph()
+        with prof, torch.cuda.graph(graph):
+            _lib.rng_epoch_advance(epoch)
+            x_g, key_g = run(segs[W:], x, key)
+        capture_ms = (time.perf_counter() - c0) * 1e3
+        launches = _lib.launch_count() - l0
     if world > 1:
         dist.barrier()
     clocks = ClockSampler(local_rank)
     clocks.start()
-    l0 = _lib.launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     wall0 = time.perf_counter()
-    with profiling.Profiler() as prof:
+    if graph is not None:
         e0.record()
-        x, key = run(segs[W:], x, key)
+        graph.replay()
         e1.record()
         torch.cuda.synchronize()
+        x, key = x_g, key_g
+    else:
+        l0 = _lib.launch_count()
+        with prof:
+            e0.record()
+            x, key = run(segs[W:], x, key)
+            e1.record()
+            torch.cuda.synchronize()
+        launches = _lib.launch_count() - l0
     wall = time.perf_counter() - wall0
-    launches = _lib.launch_count() - l0
     clk = clocks.stop()
     ms = replicas.max_over_ranks(e0.elapsed_time(e1), dev)
     if world > 1:
@@ -721,7 +753,7 @@ def main():
     # ---- end to end through the public API with host buffers
     e2e = None
     if not args.no_e2e:
-        e2e = end_to_end(sampler, bundle, w, dev, n_train - W, n_prod, x)
+        e2e = end_to_end(sampler, bundle, w, dev, n_train - W, n_prod, x, graph=not args.eager)
 
     line = {
         "metric": METRIC, "value": value, "unit": "chain-steps/s", "n_gpus": world, "steps": K, "warmup": W,
@@ -734,8 +766,10 @@ def main():
                    "n_epochs": w["n_epochs"], "parallelism": f"replicas{world}",
                    "l2": "working set (chain buffers, flow weights) larger than L2; no flush"},
         "roofline": roof, "kernels": kernels, "gpu_launches": launches, "clocks": clk,
-        "wall_s": wall, **extra,
+        "wall_s": wall, "cuda_graph": graph is not None, **extra,
     }
+    if capture_ms is not None:
+        line["graph_capture_ms"] = capture_ms
     if e2e is not None:
         line["e2e"] = e2e
     if rank == 0 and (args.plain_full or args.plain_loops > 0):
@@ -761,12 +795,14 @@ def main():
         dist.destroy_process_group()
 
 
-def end_to_end(sampler, bundle, w, dev, n_train_loops, n_prod_loops, x_dev):
+def end_to_end(sampler, bundle, w, dev, n_train_loops, n_prod_loops, x_dev, graph=True):
     """The timed region's loop mix (n_train_loops training loops, then
     n_prod_loops production loops) driven through Sampler.sample with host
     buffers: every loop copies its starting positions host->device (pinned,
     inside Sampler.sample) and reads back the rows it wrote plus the final
-    positions (device->host, pinned)."""
+    positions (device->host, pinned). With ``graph`` each loop is a replay of
+    its schedule's CUDA graph (Sampler.sample(..., cuda_graph=True)); the two
+    schedules are captured before the timed region."""
     import torch
     train = ["local_stepper", "update_global_step", "model_trainer", "update_model", "global_stepper",
              "update_local_step"]
@@ -781,22 +817,43 @@ def end_to_end(sampler, bundle, w, dev, n_train_loops, n_prod_loops, x_dev):
     state = res["sampler_state"]
     steppers = [sampler.strategies["local_stepper"], sampler.strategies["global_stepper"]]
     plan = [train] * n_train_loops + [prod] * n_prod_loops
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for order in plan:
+    capture_ms = 0.0
+    if graph:
+        for order in (train, prod):
+            if order in plan:
+                sampler.strategy_order = order
+                for s in steppers:
+                    s.set_current_position(0)
+                c0 = time.perf_counter()
+                sampler.capture(x_dev, {})
+                capture_ms += (time.perf_counter() - c0) * 1e3
+
+    def loop(order):
         sampler.strategy_order = order
         for s in steppers:
             s.set_current_position(0)
-        last = sampler.sample(x_host, {})                 # h2d inside Sampler.sample
+        last = sampler.sample(x_host, {}, cuda_graph=graph)   # h2d inside Sampler.sample
         pos_h.copy_(res[state.data["target_positions"]].data[:, :blk], non_blocking=True)
         lp_h.copy_(res[state.data["target_log_prob"]].data[:, :blk], non_blocking=True)
         x_host.copy_(last, non_blocking=True)
         torch.cuda.current_stream().synchronize()
+
+    # one untimed production loop first: the first device->host read into the
+    # fresh pinned buffers costs a one-time ~0.6 s on the Grace host
+    loop(prod)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for order in plan:
+        loop(order)
     secs = time.perf_counter() - t0
     h2d = C * d * 4
     d2h = C * blk * d * 4 + C * blk * 4 + C * d * 4
-    return {"value": C * blk * len(plan) / secs, "unit": "chain-steps/s", "h2d_bytes_per_step": h2d,
-            "d2h_bytes_per_step": d2h, "training_loops": n_train_loops, "production_loops": n_prod_loops}
+    out = {"value": C * blk * len(plan) / secs, "unit": "chain-steps/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "training_loops": n_train_loops, "production_loops": n_prod_loops,
+           "cuda_graph": graph}
+    if graph:
+        out["graph_capture_ms"] = capture_ms
+    return out
 
 
 if __name__ == "__main__":

@@ -40,25 +40,87 @@ class Sampler:
             if key in class_keys and not key.startswith("__"):
                 setattr(self, key, value)
 
-    def sample(self, initial_position, data: dict):
-        """Run every strategy in strategy_order (Sampler.py:84-108)."""
-        dev = self.resources["model"].device if "model" in self.resources else None
+    def _device(self):
+        if "model" in self.resources:
+            return self.resources["model"].device
+        return torch.device("cuda") if torch.cuda.is_available() else None
+
+    def _run(self, rng_key, x, data, order):
+        for strategy in order:
+            if strategy not in self.strategies:
+                raise ValueError(f"Invalid strategy name '{strategy}' provided. "
+                                 f"Available strategies are: {list(self.strategies.keys())}.")
+            rng_key, self.resources, x = self.strategies[strategy](rng_key, self.resources, x, data)
+        return rng_key, x
+
+    def sample(self, initial_position, data: dict, cuda_graph: bool = False):
+        """Run every strategy in strategy_order (Sampler.py:84-108).
+
+        With ``cuda_graph=True`` the schedule runs as a CUDA graph: captured
+        on the first call for this strategy_order (``capture``), then
+        replayed. A replay re-executes exactly the captured launches --
+        including the buffer rows they write -- with fresh random streams
+        (the library's epoch word advances at the start of every replay);
+        host-side strategy state (stepper cursors, sampler state) is not
+        advanced by replays."""
+        dev = self._device()
         x = torch.as_tensor(initial_position, dtype=torch.float32)
         if dev is not None:
             x = x.to(dev, non_blocking=True)
         initial_position = torch.atleast_2d(x)
-        rng_key = self.rng_key
-        last_step = initial_position
         assert isinstance(self.strategy_order, list)
-        for strategy in self.strategy_order:
-            if strategy not in self.strategies:
-                raise ValueError(f"Invalid strategy name '{strategy}' provided. "
-                                 f"Available strategies are: {list(self.strategies.keys())}.")
-            rng_key, self.resources, last_step = self.strategies[strategy](rng_key, self.resources, last_step, data)
+        if cuda_graph:
+            cap = self._captured.get(tuple(self.strategy_order)) if hasattr(self, "_captured") else None
+            if cap is None:
+                cap = self.capture(initial_position, data)
+            return cap.replay(initial_position)
+        _, last_step = self._run(self.rng_key, initial_position, data, self.strategy_order)
         return last_step
+
+    def capture(self, initial_position, data: dict) -> "CapturedSchedule":
+        """Capture strategy_order as one CUDA graph without running it. Work
+        that cannot be captured (the autotuner's probes) runs first; the
+        capture itself advances host-side strategy state once, as one eager
+        run would."""
+        from . import _lib
+        dev = self._device()
+        x0 = torch.atleast_2d(torch.as_tensor(initial_position, dtype=torch.float32).to(dev))
+        for name in self.strategy_order:
+            prep = getattr(self.strategies.get(name), "prepare", None)
+            if prep is not None:
+                prep(self.resources, x0.shape[0])
+        epoch = _lib.rng_epoch(dev)
+        static_x = x0.clone()
+        torch.cuda.synchronize(dev)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            _lib.rng_epoch_advance(epoch)
+            _, out = self._run(self.rng_key, static_x, data, self.strategy_order)
+        cap = CapturedSchedule(g, static_x, out)
+        if not hasattr(self, "_captured"):
+            self._captured = {}
+        self._captured[tuple(self.strategy_order)] = cap
+        return cap
 
     def serialize(self):
         raise NotImplementedError
 
     def deserialize(self):
         raise NotImplementedError
+
+
+class CapturedSchedule:
+    """A strategy schedule captured as one CUDA graph: ``replay(x)`` copies the
+    starting positions into the graph's input and launches the graph; the
+    returned tensor (the schedule's last positions) is the graph's output
+    and is overwritten by the next replay."""
+
+    def __init__(self, graph, static_input, static_output):
+        self.graph = graph
+        self.static_input = static_input
+        self.static_output = static_output
+
+    def replay(self, initial_position):
+        self.static_input.copy_(torch.atleast_2d(initial_position), non_blocking=True)
+        self.graph.replay()
+        return self.static_output

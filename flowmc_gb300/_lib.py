@@ -174,6 +174,8 @@ _SIGNATURES = {
     "fmc_select_training_data_noalloc": (ctypes.c_int, [
         ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int64,
         ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "fmc_rng_epoch_attach": (ctypes.c_int, [ctypes.c_void_p]),
+    "fmc_rng_epoch_advance": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "fmc_last_error": (ctypes.c_char_p, []),
     "fmc_version": (ctypes.c_int, []),
     "fmc_device_sm_count": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int32)]),
@@ -276,3 +278,25 @@ def device_error(clear: bool = True) -> int:
     v = ctypes.c_int32()
     check(lib().fmc_device_error(ctypes.byref(v), 1 if clear else 0))
     return int(v.value)
+
+
+_epoch_words: dict = {}
+
+
+def rng_epoch(device=None) -> torch.Tensor:
+    """The device word (int64 [1]) every random stream of the library folds
+    into its key, created at zero and attached on first use. A CUDA graph
+    that runs ``rng_epoch_advance`` draws fresh numbers on every replay."""
+    dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    if dev.index is None:
+        dev = torch.device("cuda", torch.cuda.current_device())
+    w = _epoch_words.get(dev)
+    if w is None:
+        w = torch.zeros(1, dtype=torch.int64, device=dev)
+        _epoch_words[dev] = w
+    check(lib().fmc_rng_epoch_attach(w.data_ptr()))
+    return w
+
+
+def rng_epoch_advance(word: torch.Tensor) -> None:
+    check(lib().fmc_rng_epoch_advance(word.data_ptr(), stream_handle(word.device)))

@@ -27,6 +27,11 @@ int sm_count() {
   return cached[dev];
 }
 
+static const uint64_t* g_epoch = nullptr;
+const uint64_t* rng_epoch() { return g_epoch; }
+
+__global__ void k_epoch_advance(uint64_t* w) { *w += 1; }
+
 static std::atomic<uint64_t> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
@@ -49,5 +54,17 @@ extern "C" int fmc_device_sm_count(int32_t* out) {
   int n = 0;
   FMC_CUDA_TRY(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
   *out = n;
+  return FMC_OK;
+}
+
+extern "C" int fmc_rng_epoch_attach(uint64_t* word) {
+  fmc::g_epoch = word;
+  return FMC_OK;
+}
+
+extern "C" int fmc_rng_epoch_advance(uint64_t* word, void* stream) {
+  FMC_CHECK_ARG(word != nullptr, "word is NULL");
+  fmc::k_epoch_advance<<<1, 1, 0, (cudaStream_t)stream>>>(word);
+  FMC_LAUNCH_CHECK();
   return FMC_OK;
 }

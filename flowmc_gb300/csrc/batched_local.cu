@@ -153,9 +153,10 @@ __device__ __forceinline__ float chain_sum(int d, F f) {
 }
 
 // normal for (chain c of T, step s, coordinate j): explicit or Philox
-__device__ __forceinline__ float draw_normal(const BatchArgs& a, const BatchTarget& T, int c, int s, int j) {
+__device__ __forceinline__ float draw_normal(const BatchArgs& a, const Rng& rng, const BatchTarget& T, int c, int s,
+                                             int j) {
   if (T.noise) return (c < T.n_chains) ? __ldg(T.noise + ((int64_t)c * a.S + s) * T.d + j) : 0.f;
-  const u32x4 r = a.rng.draw((uint64_t)(T.chain_offset + c), (uint64_t)s, (uint32_t)(j >> 1), RNG_TAG_LOCAL_NORMAL);
+  const u32x4 r = rng.draw((uint64_t)(T.chain_offset + c), (uint64_t)s, (uint32_t)(j >> 1), RNG_TAG_LOCAL_NORMAL);
   float z0, z1;
   box_muller(r.x, r.y, z0, z1);
   return (j & 1) ? z1 : z0;
@@ -163,6 +164,7 @@ __device__ __forceinline__ float draw_normal(const BatchArgs& a, const BatchTarg
 
 __global__ void __launch_bounds__(kBThreads) k_batched_dense(const BatchArgs a) {
   extern __shared__ float sm[];
+  const Rng rng = a.rng.at_epoch();
   float* X = sm;                      // [32][256] current positions
   float* Gx = X + kBT * kBDMax;       // gradient at X
   float* Y = Gx + kBT * kBDMax;       // proposal / leapfrog position
@@ -200,7 +202,7 @@ __global__ void __launch_bounds__(kBThreads) k_batched_dense(const BatchArgs a) 
       if (a.kind == FMC_KERNEL_MALA) {
         const float dt2 = dt * dt;
         for (int j = tid & 7, c = tid >> 3; j < d; j += 8) {
-          const float xi = draw_normal(a, T, c0 + c, s, j);
+          const float xi = draw_normal(a, rng, T, c0 + c, s, j);
           const int i = c * kBDMax + j;
           Y[i] = (X[i] + dt2 * Gx[i] / 2.0f) + dt * xi;
         }
@@ -222,7 +224,7 @@ __global__ void __launch_bounds__(kBThreads) k_batched_dense(const BatchArgs a) 
       } else {
         for (int j = tid & 7, c = tid >> 3; j < d; j += 8) {
           const int i = c * kBDMax + j;
-          Pm[i] = draw_normal(a, T, c0 + c, s, j);
+          Pm[i] = draw_normal(a, rng, T, c0 + c, s, j);
           Y[i] = X[i];
           Gy[i] = Gx[i];
         }
@@ -271,7 +273,7 @@ __global__ void __launch_bounds__(kBThreads) k_batched_dense(const BatchArgs a) 
         const int64_t chain = T.chain_offset + c0 + c;
         float u;
         if (T.unif) u = (c < nc) ? __ldg(T.unif + (int64_t)(c0 + c) * a.S + s) : 1.f;
-        else u = u32_to_unit(a.rng.draw((uint64_t)chain, (uint64_t)s, 0u, RNG_TAG_LOCAL_UNIFORM).x);
+        else u = u32_to_unit(rng.draw((uint64_t)chain, (uint64_t)s, 0u, RNG_TAG_LOCAL_UNIFORM).x);
         const float logu = logf(u);
         ff ratio;
         if (a.kind == FMC_KERNEL_MALA) {
@@ -389,7 +391,7 @@ extern "C" int fmc_batched_dense_local_steps(const FmcTarget* targets, int32_t n
   a.thin = thinning;
   a.buf_len = buf_len;
   a.start = cursor < buf_len - n_rec ? cursor : buf_len - n_rec;
-  a.rng = Rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter};
+  a.rng = Rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter, rng_epoch()};
   a.x0 = x0;
   a.x_last = x_last;
   a.lp_last = lp_last;

@@ -111,9 +111,34 @@ enum : uint32_t {
   RNG_TAG_ADAM_NOISE = 0x41440000u,
 };
 
+// SplitMix64 finaliser (Steele, Lea, Flood 2014) without the additive
+// constant, so that 0 maps to 0.
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// Device word folded into every random stream: a CUDA graph that advances it
+// (fmc_rng_epoch_advance) draws fresh numbers on each replay. The library
+// remembers one attached word (fmc_rng_epoch_attach); NULL or a zero word
+// leaves the streams as they are.
+const uint64_t* rng_epoch();
+
 struct Rng {
   uint32_t k0, k1;     // key = seed
   uint64_t ctr_base;   // call counter, folded into the step word
+  const uint64_t* epoch;
+  // the key this launch uses: the seed mixed with the attached epoch word
+  __device__ __forceinline__ Rng at_epoch() const {
+    Rng r = *this;
+    if (epoch != nullptr) {
+      const uint64_t e = mix64(*epoch);
+      r.k0 ^= (uint32_t)e;
+      r.k1 ^= (uint32_t)(e >> 32);
+    }
+    return r;
+  }
   __device__ __forceinline__ u32x4 draw(uint64_t row, uint64_t step, uint32_t slot, uint32_t tag) const {
     const uint64_t s = step + (ctr_base << 32);
     u32x4 c{(uint32_t)row, (uint32_t)(row >> 32) ^ (uint32_t)(s >> 32), slot, tag ^ (uint32_t)s};

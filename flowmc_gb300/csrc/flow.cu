@@ -140,8 +140,9 @@ __global__ void k_base_logprob(const float* __restrict__ y, const float* __restr
   }
 }
 
-__global__ void k_base_sample(const float* __restrict__ z, Rng rng, int64_t n, int d, const float* __restrict__ aux,
+__global__ void k_base_sample(const float* __restrict__ z, Rng rng0, int64_t n, int d, const float* __restrict__ aux,
                               float* __restrict__ out) {
+  const Rng rng = rng0.at_epoch();
   // jax.random.multivariate_normal(0, c I): mean + z @ cholesky(c I).T = sqrt(c) z
   const float sc = sqrtf(aux[2 * d]);
   const int64_t tot = n * d;
@@ -352,7 +353,7 @@ int flow_sample(const FmcFlow* f, uint64_t seed, uint64_t counter, const float* 
   if ((rc = check_ws(g, n, bf16, ws, ws_bytes, rows))) return rc;
   InferWs w;
   carve_infer(g, rows, bf16, ws, w);
-  const Rng rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter};
+  const Rng rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter, rng_epoch()};
   k_base_sample<<<ew_grid(n * g.d), 256, 0, st>>>(z, rng, n, g.d, f->aux, x);
   FMC_LAUNCH_CHECK();
   for (int64_t r0 = 0; r0 < n; r0 += rows) {

@@ -74,7 +74,7 @@ extern "C" int fmc_local_steps(const FmcTarget* target, const FmcLocalParams* pa
   a.d = target->n_dim;
   a.S = n_steps;
   a.thin = thinning;
-  a.rng = Rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter};
+  a.rng = Rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter, rng_epoch()};
   a.noise = noise;
   a.unif = unif;
   a.out_pos = out_pos;

@@ -93,7 +93,7 @@ __device__ __forceinline__ float temper(const LocalArgs& a, float lp, const floa
 }
 
 template <int V>
-__device__ __forceinline__ void draw_normals(const LocalArgs& a, int64_t c, int s, int gl,
+__device__ __forceinline__ void draw_normals(const LocalArgs& a, const Rng& rng, int64_t c, int s, int gl,
                                              float (&xi)[V]) {
   const int d = a.d;
   if (a.noise) {
@@ -112,13 +112,13 @@ __device__ __forceinline__ void draw_normals(const LocalArgs& a, int64_t c, int 
   if constexpr (V >= 4) {
 #pragma unroll
     for (int q = 0; q < V; q += 4) {
-      const u32x4 r = a.rng.draw(c, s, (uint32_t)(gl * V + q), RNG_TAG_LOCAL_NORMAL);
+      const u32x4 r = rng.draw(c, s, (uint32_t)(gl * V + q), RNG_TAG_LOCAL_NORMAL);
       box_muller(r.x, r.y, xi[q], xi[q + 1]);
       box_muller(r.z, r.w, xi[q + 2], xi[q + 3]);
     }
   } else {
     const int j = gl * V;   // V = 2: j is even
-    const u32x4 r = a.rng.draw(c, s, (uint32_t)(j & ~3), RNG_TAG_LOCAL_NORMAL);
+    const u32x4 r = rng.draw(c, s, (uint32_t)(j & ~3), RNG_TAG_LOCAL_NORMAL);
     const bool hi = (j & 2) != 0;
     float z0, z1;
     box_muller(hi ? r.z : r.x, hi ? r.w : r.y, z0, z1);
@@ -137,9 +137,9 @@ __device__ __forceinline__ void draw_normals(const LocalArgs& a, int64_t c, int 
 // Uniforms come four steps per Philox call: draws are refreshed on steps
 // s = 0 mod 4 (every lane of the group computes the same call, so the group
 // agrees on u) and consumed from `ub`.
-__device__ __forceinline__ float draw_uniform(const LocalArgs& a, int64_t c, int s, u32x4& ub) {
+__device__ __forceinline__ float draw_uniform(const LocalArgs& a, const Rng& rng, int64_t c, int s, u32x4& ub) {
   if (a.unif) return __ldcs(a.unif + (int64_t)c * a.S + s);
-  if ((s & 3) == 0) ub = a.rng.draw(c, (uint64_t)(s >> 2), 0u, RNG_TAG_LOCAL_UNIFORM);
+  if ((s & 3) == 0) ub = rng.draw(c, (uint64_t)(s >> 2), 0u, RNG_TAG_LOCAL_UNIFORM);
   const int r = s & 3;
   return u32_to_unit(r == 0 ? ub.x : r == 1 ? ub.y : r == 2 ? ub.z : ub.w);
 }
@@ -189,6 +189,7 @@ __global__ void __launch_bounds__(256) k_local_steps(const LocalArgs a) {
     }
   }
   const float dt = a.step;
+  const Rng rng = a.rng.at_epoch();
 
   for (int64_t c = blockIdx.x * groups_per_block + gib; c < a.C_pad;
        c += (int64_t)gridDim.x * groups_per_block) {
@@ -220,8 +221,8 @@ __global__ void __launch_bounds__(256) k_local_steps(const LocalArgs a) {
     int tcount = 0, n_acc = 0;
     for (int s = 0; s < a.S; ++s) {
       float xi[V];
-      draw_normals<V>(a, cc, s, gl, xi);
-      const float logu = logf(draw_uniform(a, cc, s, ub));
+      draw_normals<V>(a, rng, cc, s, gl, xi);
+      const float logu = logf(draw_uniform(a, rng, cc, s, ub));
       bool acc;
       if constexpr (KIND == FMC_KERNEL_MALA) {
         const float dt2 = dt * dt;

@@ -42,6 +42,7 @@ __global__ void __launch_bounds__(256) k_nf_accept(const NfArgs a) {
   const int64_t gpb = blockDim.x / G, gib = threadIdx.x / G;
   const int d = a.d;
   float* stage = (TGT == FMC_TARGET_DENSE_GAUSSIAN) ? smem + gib * d : nullptr;
+  const Rng rng = a.rng.at_epoch();
   for (int64_t c = blockIdx.x * gpb + gib; c < a.C_pad; c += (int64_t)gridDim.x * gpb) {
     const bool active = c < a.C;
     const int64_t cc = active ? c : 0;
@@ -66,7 +67,7 @@ __global__ void __launch_bounds__(256) k_nf_accept(const NfArgs a) {
       }
       const float lpp = target_eval<TGT, G, V, false>(a.tgt, p, g, gl, stage);
       const float lnfp = __ldg(a.lnf + row);
-      const float u = a.unif ? __ldg(a.unif + row) : u32_to_unit(a.rng.draw(cc, s, 0u, RNG_TAG_NF_UNIFORM).x);
+      const float u = a.unif ? __ldg(a.unif + row) : u32_to_unit(rng.draw(cc, s, 0u, RNG_TAG_NF_UNIFORM).x);
       // ratio = (lp_p - lp_c) - (lnf_p - lnf_c)   (NF_proposal.py:102-104)
       const ff ratio = ff_add(two_sum(lpp, -lp), ff_neg(two_sum(lnfp, -lnf)));
       const bool acc = f_lt_ff(logf(u), ratio);
@@ -194,7 +195,7 @@ extern "C" int fmc_nf_global_steps(const FmcFlow* flow, const FmcTarget* target,
   a.d = d;
   a.S = n_steps;
   a.thin = thinning;
-  a.rng = Rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter};
+  a.rng = Rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter, rng_epoch()};
   a.unif = unif;
   a.out_pos = out_pos;
   a.out_logp = out_logp;

@@ -164,6 +164,18 @@ struct Perm {
   uint64_t n;
   int half_bits;  // bits per Feistel half (domain = 4^half_bits >= n)
   uint32_t k[4];
+  const uint64_t* epoch;  // folded into the round keys (rng_epoch)
+  __device__ __forceinline__ Perm at_epoch() const {
+    Perm p = *this;
+    if (epoch != nullptr) {
+      const uint64_t e = mix64(*epoch), f = e ? mix64(e ^ 0x9E3779B97F4A7C15ull) : 0ull;
+      p.k[0] ^= (uint32_t)e;
+      p.k[1] ^= (uint32_t)(e >> 32);
+      p.k[2] ^= (uint32_t)f;
+      p.k[3] ^= (uint32_t)(f >> 32);
+    }
+    return p;
+  }
   __device__ __forceinline__ uint64_t round_once(uint64_t v) const {
     const uint32_t mask = (half_bits >= 32) ? 0xffffffffu : ((1u << half_bits) - 1u);
     uint32_t L = (uint32_t)(v >> half_bits) & mask, R = (uint32_t)v & mask;
@@ -186,8 +198,9 @@ struct Perm {
   }
 };
 
-__global__ void k_permute_rows(const float* __restrict__ src, int64_t n, int d, Perm p, int64_t first, int64_t m,
+__global__ void k_permute_rows(const float* __restrict__ src, int64_t n, int d, Perm p0, int64_t first, int64_t m,
                                float* __restrict__ dst) {
+  const Perm p = p0.at_epoch();
   const int64_t tot = m * d;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = e / d;
@@ -272,8 +285,9 @@ __global__ void __launch_bounds__(kScanTile) k_scatter_finite(const int32_t* __r
 
 // out[i] = row of the compacted, per-chain-windowed data picked by index i
 __global__ void k_gather_selected(const float* __restrict__ buf, int d, int C, int history, const int64_t* __restrict__ total,
-                                  const int64_t* __restrict__ comp, Rng rng, const int64_t* __restrict__ idx,
+                                  const int64_t* __restrict__ comp, Rng rng0, const int64_t* __restrict__ idx,
                                   int64_t n_out, float* __restrict__ out, int32_t* __restrict__ err) {
+  const Rng rng = rng0.at_epoch();
   const int64_t T = *total;
   const int64_t per = (C > 0) ? T / C : 0;
   if (T % C != 0 || per == 0) {
@@ -395,6 +409,7 @@ extern "C" int fmc_permute_rows(const float* src, int64_t n, int32_t d, uint64_t
   u32x4 k = philox4x32_10(u32x4{(uint32_t)counter, (uint32_t)(counter >> 32), 0x4b455953u, 0u}, (uint32_t)seed,
                           (uint32_t)(seed >> 32));
   p.k[0] = k.x; p.k[1] = k.y; p.k[2] = k.z; p.k[3] = k.w;
+  p.epoch = rng_epoch();
   if (m == 0) return FMC_OK;
   k_permute_rows<<<grid_ew(m * d), 256, 0, (cudaStream_t)stream>>>(src, n, d, p, first, m, dst);
   FMC_LAUNCH_CHECK();
@@ -437,7 +452,7 @@ extern "C" int fmc_select_training_data(const float* buf, int32_t n_chains, int6
   FMC_LAUNCH_CHECK();
   k_scatter_finite<<<(unsigned)tiles, kScanTile, 0, st>>>(flags, rows, tile, comp);
   FMC_LAUNCH_CHECK();
-  const Rng rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter};
+  const Rng rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter, rng_epoch()};
   k_gather_selected<<<grid_ew(n_out * d), 256, 0, st>>>(buf, d, n_chains, history_window, total, comp, rng, idx,
                                                         n_out, out, err);
   FMC_LAUNCH_CHECK();

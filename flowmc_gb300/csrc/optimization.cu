@@ -35,6 +35,7 @@ __global__ void __launch_bounds__(256) k_adam_optimize(const AdamOptArgs a) {
   const int gpb = blockDim.x / G, gib = threadIdx.x / G;
   const int d = a.d;
   float* stage = (TGT == FMC_TARGET_DENSE_GAUSSIAN) ? smem + gib * d : nullptr;
+  const Rng rng = a.rng.at_epoch();
   float lo[V], hi[V];
 #pragma unroll
   for (int v = 0; v < V; ++v) {
@@ -59,7 +60,7 @@ __global__ void __launch_bounds__(256) k_adam_optimize(const AdamOptArgs a) {
       if (a.noise) {
         xi = __ldg(a.noise + cc * a.S + s);
       } else {
-        const u32x4 r = a.rng.draw((uint64_t)cc, (uint64_t)s, 0u, RNG_TAG_ADAM_NOISE);
+        const u32x4 r = rng.draw((uint64_t)cc, (uint64_t)s, 0u, RNG_TAG_ADAM_NOISE);
         float z1;
         box_muller(r.x, r.y, xi, z1);
       }
@@ -145,7 +146,7 @@ extern "C" int fmc_adam_optimize(const FmcTarget* target, const float* x0, int32
   a.noise_level = noise_level;
   a.lower = lower;
   a.upper = upper;
-  a.rng = Rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter};
+  a.rng = Rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter, rng_epoch()};
   a.noise = noise;
   a.x_out = x_out;
   a.lp_out = lp_out;

@@ -58,6 +58,7 @@ __global__ void __launch_bounds__(256) k_pt_exchange(const ExchangeArgs a) {
   float* Ls = tail + kMaxTemps + gib * T;                    // this group's log-densities
   int* perm = reinterpret_cast<int*>(tail + kMaxTemps + gpb * T) + gib * T;
   for (int i = threadIdx.x; i < kMaxTemps; i += blockDim.x) cnt[i] = 0;
+  const Rng rng = a.rng.at_epoch();
   __syncthreads();
 
   for (int64_t c = blockIdx.x * (int64_t)gpb + gib; c < a.C_pad; c += (int64_t)gridDim.x * gpb) {
@@ -84,7 +85,7 @@ __global__ void __launch_bounds__(256) k_pt_exchange(const ExchangeArgs a) {
         if (a.unif) {
           u = __ldg(a.unif + cc * (T - 1) + i);
         } else {
-          const u32x4 r = a.rng.draw((uint64_t)cc, (uint64_t)i, 0u, RNG_TAG_PT_EXCHANGE);
+          const u32x4 r = rng.draw((uint64_t)cc, (uint64_t)i, 0u, RNG_TAG_PT_EXCHANGE);
           u = u32_to_unit(r.x);
         }
         const bool acc = logf(u) < ratio;
@@ -216,7 +217,7 @@ extern "C" int fmc_pt_local_steps(const FmcTarget* target, const FmcLocalParams*
   a.d = target->n_dim;
   a.S = n_steps;
   a.thin = 1;
-  a.rng = Rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter};
+  a.rng = Rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter, rng_epoch()};
   a.noise = noise;
   a.unif = unif;
   a.buf_len = 1;
@@ -253,7 +254,7 @@ extern "C" int fmc_pt_exchange(const FmcTarget* target, const float* x, int32_t 
   a.T = n_temps;
   a.d = target->n_dim;
   a.temps = temperatures;
-  a.rng = Rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter};
+  a.rng = Rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter, rng_epoch()};
   a.unif = unif;
   a.out_first = out_first;
   a.out_rest = out_rest;

@@ -1,8 +1,10 @@
 """CUDA-event timing of the sampler's phases.
 
 Strategies wrap their fused launches in ``region(name)``; when a Profiler is
-active the region records a start/stop event pair on the launching stream,
-otherwise it costs nothing. ``Profiler.totals_ms()`` synchronises once at
+active the region records a start/stop event pair on the launching stream
+(as event-record nodes when the stream is being captured into a CUDA
+graph, so that a replay times the same regions), otherwise it costs
+nothing. ``Profiler.totals_ms()`` synchronises once at
 the end and sums the device time per region.
 """
 from __future__ import annotations
@@ -43,8 +45,11 @@ def region(name: str, units: float = 0.0):
     if p is None:
         yield
         return
-    a = torch.cuda.Event(enable_timing=True)
-    b = torch.cuda.Event(enable_timing=True)
+    kw = {"enable_timing": True}
+    if torch.cuda.is_current_stream_capturing():
+        kw["external"] = True       # event-record nodes of the captured graph
+    a = torch.cuda.Event(**kw)
+    b = torch.cuda.Event(**kw)
     a.record()
     try:
         yield

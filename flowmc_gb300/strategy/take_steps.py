@@ -101,6 +101,17 @@ class TakeSerialSteps(TakeSteps):
         return x_last
 
 
+    def prepare(self, resources, n_chains: int):
+        """One-time work that must not run inside a CUDA graph capture: the
+        autotuner's timed probes (they synchronise)."""
+        from ..resource.kernel.base import LocalKernel
+        kernel = resources[self.kernel_name]
+        if self.autotune and isinstance(kernel, LocalKernel) and not getattr(kernel, "_tuned", False):
+            from ..autotune import tune_local_kernel
+            tune_local_kernel(kernel, as_target(resources[self.logpdf_name]), n_chains)
+            kernel._tuned = True
+
+
 class TakeGroupSteps(TakeSteps):
     """n_steps proposals drawn at once (take_steps.py:183-206): the NFProposal
     global step."""

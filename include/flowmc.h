@@ -379,6 +379,16 @@ FMC_API int fmc_selftest_bounded_wait(int32_t* timed_out, void* stream);
  * expired (synchronous read; clear != 0 resets it). */
 FMC_API int fmc_device_error(int32_t* out, int32_t clear);
 
+/* ---- random streams under CUDA graph replay ------------------------- */
+/* Attach a caller-owned device word (uint64) that every random stream of
+ * the library folds into its key: launches made (or captured) after the
+ * call read the word when they run, so a captured graph that advances it
+ * draws fresh numbers on each replay. A zero word leaves the streams
+ * unchanged; NULL detaches. Host-side setting, not thread-safe. */
+FMC_API int fmc_rng_epoch_attach(uint64_t* word);
+/* word += 1 on the stream (one tiny kernel; a graph node when captured). */
+FMC_API int fmc_rng_epoch_advance(uint64_t* word, void* stream);
+
 /* ---- library --------------------------------------------------------- */
 FMC_API const char* fmc_last_error(void);
 FMC_API int fmc_version(void);               /* FMC_ABI_VERSION */
