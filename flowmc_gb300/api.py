@@ -12,6 +12,8 @@ from .strategy.update_state import UpdateState  # noqa: F401
 from . import targets  # noqa: F401
 from .resource.kernel.NF_proposal import NFProposal  # noqa: F401
 from .resource.model.nf_model.rqSpline import MaskedCouplingRQSpline  # noqa: F401
+from .resource.model.nf_model.realNVP import RealNVP  # noqa: F401
+from .strategy.optimization import AdamOptimization  # noqa: F401
 from .resource.optimizer import Optimizer  # noqa: F401
 from .strategy.train_model import TrainModel  # noqa: F401
 from .resource_strategy_bundle.RQSpline_MALA import RQSpline_MALA_Bundle  # noqa: F401

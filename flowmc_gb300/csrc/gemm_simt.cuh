@@ -17,6 +17,8 @@ enum GemmEpi : int {
   EPI_BIAS = 1,       // C = AB + bias
   EPI_BIAS_TANH = 2,  // C = tanh(AB + bias)
   EPI_DTANH = 3,      // C = AB * (1 - aux^2)   (aux = tanh output of the forward)
+  EPI_BIAS_RELU = 4,  // C = max(AB + bias, 0)
+  EPI_DRELU = 5,      // C = AB where aux > 0, else 0   (aux = relu output of the forward)
 };
 
 template <bool A_KMAJOR, bool B_KMAJOR, int EPI>
@@ -84,6 +86,10 @@ __global__ void __launch_bounds__(256) k_sgemm(int M, int N, int K, const float*
         v += bias[gj];
       } else if (EPI == EPI_BIAS_TANH) {
         v = tanhf(v + bias[gj]);
+      } else if (EPI == EPI_BIAS_RELU) {
+        v = fmaxf(v + bias[gj], 0.f);
+      } else if (EPI == EPI_DRELU) {
+        v = (aux[gi * ldaux + gj] > 0.f) ? v : 0.f;
       } else {
         const float h = aux[gi * ldaux + gj];
         v = v * (1.f - h * h);

@@ -149,6 +149,41 @@ extern "C" int fmc_nf_workspace_size(const FmcFlow* flow, int32_t n_chains, int3
   return FMC_OK;
 }
 
+// the accept scan over precomputed proposals props [C * S, d] (row c * S + s)
+// and flow log-densities lnf [C * S + C] (the proposals', then the current
+// positions')
+static int launch_accept(const FmcTarget* target, const float* x0, int32_t n_chains, int32_t n_steps,
+                         int32_t thinning, uint64_t seed, uint64_t counter, const float* props, const float* lnf,
+                         const float* unif, float* out_pos, float* out_logp, float* out_acc, int64_t buf_len,
+                         int64_t cursor, float* x_last, float* lp_last, cudaStream_t st) {
+  const int64_t n_rec = ((int64_t)n_steps + thinning - 1) / thinning;
+  NfArgs a{};
+  a.tgt = *target;
+  a.x0 = x0;
+  a.props = props;
+  a.lnf = lnf;
+  a.C = n_chains;
+  a.d = target->n_dim;
+  a.S = n_steps;
+  a.thin = thinning;
+  a.rng = Rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter, rng_epoch()};
+  a.unif = unif;
+  a.out_pos = out_pos;
+  a.out_logp = out_logp;
+  a.out_acc = out_acc;
+  a.buf_len = buf_len;
+  a.start = cursor < buf_len - n_rec ? cursor : buf_len - n_rec;
+  a.x_last = x_last;
+  a.lp_last = lp_last;
+  switch (target->kind) {
+    case FMC_TARGET_DIAG_GAUSSIAN: return launch_nf_tgt<FMC_TARGET_DIAG_GAUSSIAN>(a, st);
+    case FMC_TARGET_DUAL_MOON: return launch_nf_tgt<FMC_TARGET_DUAL_MOON>(a, st);
+    case FMC_TARGET_GAUSS_MIXTURE: return launch_nf_tgt<FMC_TARGET_GAUSS_MIXTURE>(a, st);
+    case FMC_TARGET_ROSENBROCK: return launch_nf_tgt<FMC_TARGET_ROSENBROCK>(a, st);
+    default: return launch_nf_tgt<FMC_TARGET_DENSE_GAUSSIAN>(a, st);
+  }
+}
+
 extern "C" int fmc_nf_global_steps(const FmcFlow* flow, const FmcTarget* target, const float* x0, int32_t n_chains,
                                    int32_t n_steps, int32_t thinning, uint64_t seed, uint64_t counter,
                                    const float* z, const float* unif, float* out_pos, float* out_logp,
@@ -186,29 +221,25 @@ extern "C" int fmc_nf_global_steps(const FmcFlow* flow, const FmcTarget* target,
   FMC_CUDA_TRY(cudaMemcpyAsync(props + rows * d, x0, (size_t)n_chains * d * 4, cudaMemcpyDeviceToDevice, st));
   if ((rc = flow_apply_logprob(flow, props, rows + n_chains, lnf, fws, fws_bytes, st))) return rc;
 
-  NfArgs a{};
-  a.tgt = *target;
-  a.x0 = x0;
-  a.props = props;
-  a.lnf = lnf;
-  a.C = n_chains;
-  a.d = d;
-  a.S = n_steps;
-  a.thin = thinning;
-  a.rng = Rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter, rng_epoch()};
-  a.unif = unif;
-  a.out_pos = out_pos;
-  a.out_logp = out_logp;
-  a.out_acc = out_acc;
-  a.buf_len = buf_len;
-  a.start = cursor < buf_len - n_rec ? cursor : buf_len - n_rec;
-  a.x_last = x_last;
-  a.lp_last = lp_last;
-  switch (target->kind) {
-    case FMC_TARGET_DIAG_GAUSSIAN: return launch_nf_tgt<FMC_TARGET_DIAG_GAUSSIAN>(a, st);
-    case FMC_TARGET_DUAL_MOON: return launch_nf_tgt<FMC_TARGET_DUAL_MOON>(a, st);
-    case FMC_TARGET_GAUSS_MIXTURE: return launch_nf_tgt<FMC_TARGET_GAUSS_MIXTURE>(a, st);
-    case FMC_TARGET_ROSENBROCK: return launch_nf_tgt<FMC_TARGET_ROSENBROCK>(a, st);
-    default: return launch_nf_tgt<FMC_TARGET_DENSE_GAUSSIAN>(a, st);
-  }
+  return launch_accept(target, x0, n_chains, n_steps, thinning, seed, counter, props, lnf, unif, out_pos, out_logp,
+                       out_acc, buf_len, cursor, x_last, lp_last, st);
+}
+
+extern "C" int fmc_nf_accept(const FmcTarget* target, const float* x0, int32_t n_chains, int32_t n_steps,
+                             int32_t thinning, uint64_t seed, uint64_t counter, const float* props, const float* lnf,
+                             const float* unif, float* out_pos, float* out_logp, float* out_acc, int64_t buf_len,
+                             int64_t cursor, float* x_last, float* lp_last, void* stream) {
+  int rc = check_target(target);
+  if (rc) return rc;
+  FMC_CHECK_ARG(n_chains >= 0 && n_steps >= 1 && thinning >= 1, "bad sizes");
+  const int64_t n_rec = ((int64_t)n_steps + thinning - 1) / thinning;
+  FMC_CHECK_ARG(n_rec <= buf_len, "update of %lld rows does not fit a buffer of %lld rows", (long long)n_rec,
+                (long long)buf_len);
+  FMC_CHECK_ARG(cursor >= 0, "cursor < 0");
+  if (n_chains == 0) return FMC_OK;
+  FMC_CHECK_ARG(x0 && props && lnf && out_pos && out_logp && out_acc && x_last, "NULL array argument");
+  if (target->kind == FMC_TARGET_DENSE_GAUSSIAN)
+    FMC_CHECK_SUPPORTED(target->n_dim <= 128, "dense Gaussian group kernel supports n_dim <= 128");
+  return launch_accept(target, x0, n_chains, n_steps, thinning, seed, counter, props, lnf, unif, out_pos, out_logp,
+                       out_acc, buf_len, cursor, x_last, lp_last, (cudaStream_t)stream);
 }

@@ -1,7 +1,9 @@
 """NFProposal (mirrors resource/kernel/NF_proposal.py:15-184 of the reference).
 
 ``group_steps`` runs the whole global step for every chain through
-``fmc_nf_global_steps``: n_steps flow proposals per chain, their flow
+``fmc_nf_global_steps`` (MaskedCouplingRQSpline; other flows such as
+RealNVP make their proposals with their own sample / log_prob launches and
+share the fused accept scan, ``fmc_nf_accept``): n_steps flow proposals per chain, their flow
 log-density (recomputed by the forward pass, NF_proposal.py:165-166) and
 target log-density, and the sequential independent-MH scan
 (NF_proposal.py:91-126), writing straight into the buffers.
@@ -47,6 +49,9 @@ class NFProposal(ProposalBase):
             x_last = torch.empty_like(x0)
         if lp_last is None:
             lp_last = torch.empty(C, device=x0.device)
+        if not hasattr(self.model, "num_bins"):
+            return self._group_steps_generic(seed, x0, target, n_steps, thinning, out_pos, out_logp, out_acc,
+                                             cursor, noise, uniform, x_last, lp_last, counter)
         fs = self.model.c_struct()
         nb = ctypes.c_size_t()
         L = _lib.lib()
@@ -58,6 +63,24 @@ class NFProposal(ProposalBase):
             int(seed) & ((1 << 64) - 1), int(counter), _lib.ptr(noise), _lib.ptr(uniform), out_pos.data_ptr(),
             out_logp.data_ptr(), out_acc.data_ptr(), buf_len, int(cursor), x_last.data_ptr(), lp_last.data_ptr(),
             ptr, size, _lib.stream_handle(x0.device)))
+        return x_last
+
+    def _group_steps_generic(self, seed, x0, target, n_steps, thinning, out_pos, out_logp, out_acc, cursor, noise,
+                             uniform, x_last, lp_last, counter):
+        """Flows without a fused global step (RealNVP): the model's own sample
+        and log_prob launches make the proposals and their densities
+        (NF_proposal.py:130-172), then the fused accept scan."""
+        C, d = x0.shape
+        rows = C * int(n_steps)
+        z = None if noise is None else noise.reshape(rows, d)
+        props = self.model.sample(PRNGKey._raw(int(seed) ^ int(counter)), rows, z=z)
+        lnf = self.model.log_prob(torch.cat([props, x0], 0))
+        tgt = target.c_struct()
+        _lib.check(_lib.lib().fmc_nf_accept(
+            ctypes.byref(tgt), x0.data_ptr(), C, int(n_steps), int(thinning), int(seed) & ((1 << 64) - 1),
+            int(counter), props.data_ptr(), lnf.data_ptr(), _lib.ptr(uniform), out_pos.data_ptr(),
+            out_logp.data_ptr(), out_acc.data_ptr(), out_pos.shape[1], int(cursor), x_last.data_ptr(),
+            lp_last.data_ptr(), _lib.stream_handle(x0.device)))
         return x_last
 
     def kernel(self, rng_key: PRNGKey, position, log_prob, logpdf, data):

@@ -1,6 +1,7 @@
 """Reader and writer for the reference's flow checkpoints (``NFModel.save_model``
 / ``load_model``, resource/model/nf_model/base.py:92-96), which are
-``equinox.tree_serialise_leaves`` files.
+``equinox.tree_serialise_leaves`` files, for MaskedCouplingRQSpline and
+RealNVP.
 
 Format (equinox's published serialisation, restated -- equinox itself is not
 a dependency): the model's pytree leaves in flattening order, each array-like
@@ -80,10 +81,9 @@ def _records(path: str) -> list:
     return recs
 
 
-def load_eqx(model, path: str):
-    """Load a reference checkpoint into `model` (same n_features, n_layers,
-    hidden_size, num_bins); returns the model."""
-    expect = _leaves(model)
+def _read_leaves(path: str, expect: list) -> dict:
+    """The checkpoint's records matched to `expect` ([(name, value)]): array
+    leaves must have the expected shapes, scalar leaves may be absent."""
     recs = _records(path)
     got, r = {}, 0
     for name, v in expect:
@@ -102,6 +102,24 @@ def load_eqx(model, path: str):
         r += 1
     if r != len(recs):
         raise ValueError(f"checkpoint has {len(recs) - r} records beyond the model's leaves")
+    return got
+
+
+def _set_stats(model, got, d):
+    aux = model.aux.detach().cpu().numpy().copy()
+    aux[:d] = got["_data_mean"]
+    aux[d:2 * d] = np.diag(np.atleast_2d(got["_data_cov"]))
+    base_cov = got["base_dist._cov"]
+    if not np.allclose(base_cov, np.eye(d) * base_cov[0, 0]) or got["base_dist._mean"].any():
+        raise ValueError("only a zero-mean isotropic Gaussian base distribution is supported")
+    aux[2 * d] = base_cov[0, 0]
+    return aux
+
+
+def load_eqx(model, path: str):
+    """Load a reference checkpoint into `model` (same n_features, n_layers,
+    hidden_size, num_bins); returns the model."""
+    got = _read_leaves(path, _leaves(model))
     for name, want in (("_n_features", model.n_features), ("layers[1].bijector._num_bins", model.num_bins)):
         if name in got and int(got[name]) != int(want):
             raise ValueError(f"{name} = {got[name]} in the checkpoint, {want} in the model")
@@ -124,12 +142,59 @@ def load_eqx(model, path: str):
                        "scale": float(got["layers[0].bijector.scale"][l]),
                        "shift": float(got["layers[0].bijector.shift"][l])})
     model.load_full(layers)
-    aux = model.aux.detach().cpu().numpy().copy()
-    aux[:d] = got["_data_mean"]
-    aux[d:2 * d] = np.diag(np.atleast_2d(got["_data_cov"]))
-    base_cov = got["base_dist._cov"]
-    if not np.allclose(base_cov, np.eye(d) * base_cov[0, 0]) or got["base_dist._mean"].any():
-        raise ValueError("only a zero-mean isotropic Gaussian base distribution is supported")
-    aux[2 * d] = base_cov[0, 0]
+    aux = _set_stats(model, got, d)
+    model.aux.copy_(model.aux.new_tensor(aux))
+    return model
+
+
+# ---------------------------------------------------------------- RealNVP
+# RealNVP(n_features=d, n_layers=L, n_hidden=H) (realNVP.py:120-176): the
+# NFModel fields, then base_dist, then affine_coupling -- one
+# MaskedCouplingLayer built by eqx.filter_vmap over the layers, so its
+# arrays carry a leading axis L: _mask [L, d] (float), MLPAffine's scale_MLP
+# (Linear weight [L, H, d], bias [L, H], relu skipped, Linear weight
+# [L, d, H], bias [L, d]), shift_MLP (the same) and dt (a Python number).
+# RealNVP re-declares the NFModel fields, which keeps their position.
+
+def _leaves_realnvp(model) -> list:
+    d, L = model.n_features, model.n_layers
+    aux = model.aux.detach().cpu().numpy().astype(np.float32)
+    lay = model.layers_numpy()
+    out = [("_n_features", int(d)),
+           ("_data_mean", aux[:d].copy()),
+           ("_data_cov", np.diag(aux[d:2 * d]).astype(np.float32)),
+           ("base_dist._mean", np.zeros(d, np.float32)),
+           ("base_dist._cov", (np.eye(d) * aux[2 * d]).astype(np.float32)),
+           ("base_dist.learnable", False),
+           ("affine_coupling._mask", aux[2 * d + 2:].reshape(L, d).copy())]
+    for mlp in ("scale", "shift"):
+        for i in range(2):
+            out.append((f"{mlp}_MLP.layers[{2 * i}].weight", np.stack([x[mlp]["W"][i] for x in lay])))
+            out.append((f"{mlp}_MLP.layers[{2 * i}].bias", np.stack([x[mlp]["b"][i] for x in lay])))
+    out.append(("dt", int(model.dt) if float(model.dt).is_integer() else float(model.dt)))
+    return out
+
+
+def save_eqx_realnvp(model, path: str) -> None:
+    with open(path, "wb") as f:
+        for _, v in _leaves_realnvp(model):
+            np.save(f, np.asarray(v), allow_pickle=False)
+
+
+def load_eqx_realnvp(model, path: str):
+    got = _read_leaves(path, _leaves_realnvp(model))
+    d, L = model.n_features, model.n_layers
+    if "_n_features" in got and int(got["_n_features"]) != d:
+        raise ValueError(f"_n_features = {got['_n_features']} in the checkpoint, {d} in the model")
+    if "dt" in got and float(got["dt"]) != float(model.dt):
+        raise ValueError(f"dt = {got['dt']} in the checkpoint, {model.dt} in the model")
+    layers = []
+    for l in range(L):
+        layers.append({mlp: {"W": [got[f"{mlp}_MLP.layers[{2 * i}].weight"][l] for i in range(2)],
+                             "b": [got[f"{mlp}_MLP.layers[{2 * i}].bias"][l] for i in range(2)]}
+                       for mlp in ("scale", "shift")})
+    model.load_layers(layers)
+    aux = _set_stats(model, got, d)
+    aux[2 * d + 2:] = np.asarray(got["affine_coupling._mask"], np.float32).ravel()
     model.aux.copy_(model.aux.new_tensor(aux))
     return model

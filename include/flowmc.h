@@ -158,6 +158,49 @@ FMC_API int fmc_pt_exchange(const FmcTarget* target, const float* x, int32_t n_c
 FMC_API int fmc_pt_adapt_temperatures(const float* temperatures, const int32_t* acc_pairs, int32_t n_chains,
                                       int32_t n_temps, float* out_temperatures, void* stream);
 
+/* ---- RealNVP flow (resource/model/nf_model/realNVP.py) --------------- */
+/* RealNVP(n_features, n_layers, n_hidden): per layer a MaskedCouplingLayer
+ * around MLPAffine(scale_MLP, shift_MLP, dt), each MLP [d, H, d] with relu
+ * (realNVP.py:120-228, common.py:127-208). theta packs, per layer:
+ *   W1 [2H, d] (rows 0..H-1 the scale MLP's first Linear, H..2H-1 the
+ *   shift MLP's), b1 [2H], W2s [d, H], b2s [d], W2t [d, H], b2t [d]
+ * (Equinox Linear layout [out, in]). aux [2d + 2 + n_layers * d]: data_mean,
+ * diag(data_cov), the base Gaussian's covariance scale, 1, then the coupling
+ * masks as floats (optax's weight decay reaches them: they are float leaves
+ * of the reference model). */
+typedef struct FmcRealNVP {
+  int32_t n_dim;
+  int32_t n_layers;
+  int32_t n_hidden;
+  float dt;                          /* MLPAffine dt (1)                     */
+  float* theta;
+  float* aux;
+} FmcRealNVP;
+
+FMC_API int fmc_rnvp_layout(const FmcRealNVP* flow, int64_t* n_params, int64_t* n_aux);
+/* workspace bytes for n rows; mode 0: forward / inverse / log_prob / sample,
+ * 1: loss + gradient */
+FMC_API int fmc_rnvp_workspace_size(const FmcRealNVP* flow, int64_t n, int32_t mode, size_t* bytes);
+/* RealNVP.forward / inverse (realNVP.py:180-207): y and the summed log-det
+ * [n] (inverse: layers in reverse order, negative log-det); no
+ * standardisation. y may alias x. */
+FMC_API int fmc_rnvp_forward(const FmcRealNVP* flow, const float* x, int64_t n, float* y, float* logdet,
+                             void* ws, size_t ws_bytes, void* stream);
+FMC_API int fmc_rnvp_inverse(const FmcRealNVP* flow, const float* y, int64_t n, float* x, float* logdet,
+                             void* ws, size_t ws_bytes, void* stream);
+/* RealNVP.log_prob (realNVP.py:215-222): standardise with data_mean /
+ * diag(data_cov), forward, plus the standard normal log-density. */
+FMC_API int fmc_rnvp_log_prob(const FmcRealNVP* flow, const float* x, int64_t n, float* logp, void* ws,
+                              size_t ws_bytes, void* stream);
+/* RealNVP.sample (realNVP.py:209-213): base normals z [n, d] (or Philox
+ * when NULL) scaled by the base covariance, inverse, de-standardised. */
+FMC_API int fmc_rnvp_sample(const FmcRealNVP* flow, uint64_t seed, uint64_t counter, const float* z, int64_t n,
+                            float* out, void* ws, size_t ws_bytes, void* stream);
+/* loss = -mean(log_prob(x)) and its gradient w.r.t. theta (NFModel.loss_fn,
+ * nf_model/base.py:98-100) with a hand-written backward. */
+FMC_API int fmc_rnvp_loss_grad(const FmcRealNVP* flow, const float* x, int64_t n, float* loss, float* grad,
+                               void* ws, size_t ws_bytes, void* stream);
+
 /* ---- pre-sampling optimisation (strategy/optimization.py) ------------ */
 /* AdamOptimization.optimize (optimization.py:85-164) for every chain: n_steps
  * of optax.adam(learning_rate) (b1 0.9, b2 0.999, eps 1e-8) on -log p(x),
@@ -294,6 +337,16 @@ FMC_API int fmc_nf_global_steps(const FmcFlow* flow, const FmcTarget* target, co
                                 const float* z, const float* unif, float* out_pos, float* out_logp,
                                 float* out_acc, int64_t buf_len, int64_t cursor, float* x_last, float* lp_last,
                                 void* ws, size_t ws_bytes, void* stream);
+
+/* The accept scan of the NF global step (NF_proposal.py:91-126) over
+ * proposals a flow made elsewhere (a RealNVP, say): props [n_chains *
+ * n_steps, n_dim] (row c * n_steps + s), lnf [n_chains * n_steps +
+ * n_chains] their flow log-densities followed by those of x0's rows; the
+ * rest as fmc_nf_global_steps. */
+FMC_API int fmc_nf_accept(const FmcTarget* target, const float* x0, int32_t n_chains, int32_t n_steps,
+                          int32_t thinning, uint64_t seed, uint64_t counter, const float* props, const float* lnf,
+                          const float* unif, float* out_pos, float* out_logp, float* out_acc, int64_t buf_len,
+                          int64_t cursor, float* x_last, float* lp_last, void* stream);
 
 /* ---- training (NFModel.train / TrainModel without host syncs) ---------- */
 /* optax.chain(clip_by_global_norm(max_norm), adamw(lr, b1, b2, eps,

@@ -50,6 +50,10 @@ def exp(x):
     return torch.exp(_t(x))
 
 
+def tanh(x):
+    return torch.tanh(_t(x))
+
+
 def isinf(x):
     return torch.isinf(_t(x))
 

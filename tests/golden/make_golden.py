@@ -38,6 +38,9 @@ from flowMC.resource.model.nf_model.rqSpline import RQSpline  # noqa: E402
 from flowMC.resource.logPDF import TemperedPDF  # noqa: E402
 from flowMC.strategy.parallel_tempering import ParallelTempering  # noqa: E402
 from flowMC.strategy.optimization import AdamOptimization  # noqa: E402
+from flowMC.resource.model.common import MLP, MLPAffine, MaskedCouplingLayer  # noqa: E402
+from flowMC.resource.model.nf_model.realNVP import RealNVP  # noqa: E402
+import jax  # noqa: E402
 
 
 def jnp_target(t):
@@ -110,6 +113,50 @@ def run_parallel_tempering(kernel, f, prior, temps, x0, noise, unif, u_ex):
     ex_acc = np.stack(ex_acc)
     new_t = pt._adapt_temperature(tt, torch.tensor(ex_acc)).numpy()
     return (np.stack(ens_x), np.stack(ens_lp), np.stack(ens_acc), np.stack(ex_x), np.stack(ex_lp), ex_acc, new_t)
+
+
+class _Linear:
+    """eqx.nn.Linear's call: weight @ x + bias."""
+
+    def __init__(self, W, b):
+        self.weight, self.bias = torch.tensor(W), torch.tensor(b)
+
+    def __call__(self, x):
+        return self.weight @ x + self.bias
+
+
+def _mlp(W1, b1, W2, b2):
+    """The reference's MLP object with given weights (common.py:68-112: layers
+    Linear, relu, Linear), built without Equinox's Linear constructor."""
+    m = object.__new__(MLP)
+    m.layers = [_Linear(W1, b1), jax.nn.relu, _Linear(W2, b2)]
+    return m
+
+
+class _RealNVPStandIn:
+    """What RealNVP.forward / inverse / log_prob see (realNVP.py:180-222): the
+    scan over the stacked layers is a loop over the reference's own
+    MaskedCouplingLayer(MLPAffine(...)) objects."""
+
+    def __init__(self, layers, mean, cov, d):
+        self.layers, self.data_mean, self.data_cov, self.n_features = layers, mean, cov, d
+
+    def __call__(self, x):
+        return self.forward(x)
+
+    def forward(self, x):
+        ld = 0.0
+        for lay in self.layers:
+            x, ldi = lay(x, None)
+            ld = ld + ldi
+        return x, ld
+
+    def inverse(self, x):
+        ld = 0.0
+        for lay in reversed(self.layers):
+            x, ldi = lay.inverse(x, None)
+            ld = ld + ldi
+        return x, ld
 
 
 class _Conditioner:
@@ -262,6 +309,41 @@ def main():
             out[f"{name}/{key}"] = val
         cases.append({"name": name, "kind": "adam", "target": t, "n_steps": n_steps, "learning_rate": lr,
                       "noise_level": nl})
+    # RealNVP: the reference's MaskedCouplingLayer / MLPAffine / MLP and
+    # RealNVP.log_prob on fixed weights; masks as float leaves, one case with
+    # weight-decayed masks (0.9999 / 1e-4 instead of 1 / 0 would not arise, but
+    # decay scales the ones: 1 -> 0.9998)
+    for name, d, L, H, decay in (("realnvp_d5", 5, 4, 8, 1.0), ("realnvp_d6_decayed", 6, 3, 16, 0.9998)):
+        masks, Ws = [], []
+        for l in range(L):
+            m = np.ones(d)
+            m[: int(d / 2)] = 0.0
+            m = 1 - m if l % 2 == 0 else m
+            masks.append(m * decay)
+            Ws.append([rng.normal(size=(H, d)) * 0.5, rng.normal(size=H) * 0.3, rng.normal(size=(d, H)) * 0.3,
+                       rng.normal(size=d) * 0.3, rng.normal(size=(H, d)) * 0.5, rng.normal(size=H) * 0.3,
+                       rng.normal(size=(d, H)) * 0.3, rng.normal(size=d) * 0.3])
+        layers = [MaskedCouplingLayer(MLPAffine(_mlp(*w[:4]), _mlp(*w[4:])), torch.tensor(m))
+                  for w, m in zip(Ws, masks)]
+        mean, var = rng.normal(size=d) * 0.5, rng.uniform(0.5, 2.0, size=d)
+        flow = _RealNVPStandIn(layers, torch.tensor(mean), torch.diag(torch.tensor(var)), d)
+        x = rng.normal(size=(7, d)) * 1.5
+        fy, fld, iy, ild, lp = [], [], [], [], []
+        for row in x:
+            y, ld = flow.forward(torch.tensor(row))
+            fy.append(y.numpy()), fld.append(float(ld))
+            xi, ldi = flow.inverse(torch.tensor(row))
+            iy.append(xi.numpy()), ild.append(float(ldi))
+            lp.append(float(RealNVP.log_prob(flow, torch.tensor(row))))
+        out[f"{name}/x"] = x
+        out[f"{name}/masks"] = np.stack(masks)
+        out[f"{name}/mean"], out[f"{name}/var"] = mean, var
+        for i, key in enumerate(("W1s", "b1s", "W2s", "b2s", "W1t", "b1t", "W2t", "b2t")):
+            out[f"{name}/{key}"] = np.stack([w[i] for w in Ws])
+        out[f"{name}/fwd_y"], out[f"{name}/fwd_logdet"] = np.stack(fy), np.array(fld)
+        out[f"{name}/inv_x"], out[f"{name}/inv_logdet"] = np.stack(iy), np.array(ild)
+        out[f"{name}/log_prob"] = np.array(lp)
+        cases.append({"name": name, "kind": "realnvp", "n_dim": d, "n_layers": L, "n_hidden": H})
     for c in cases:
         if c["kind"] in ("mala", "hmc", "grw"):
             print(f"{c['name']}: acceptance {out[c['name'] + '/acc'].mean():.2f}")
