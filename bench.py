@@ -348,6 +348,100 @@ def train_probe(dev, precision="bf16", seed=2):
 
 
 # ---------------------------------------------------------------- plain FP32 form
+def _time(fn, reps=5):
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def pt_probe(dev, chains=16384, temps=8, steps=50):
+    """Parallel tempering on the 64-D 4-mode mixture: one ParallelTempering
+    call = tempered MALA (step 0.05) over chains x temps rows for `steps`
+    steps, the exchange sweep and the adaptation. Reports (chain,
+    temperature)-steps/s of the tempered local kernel and the exchange's
+    achieved HBM bandwidth (reads T x 4d B per chain twice, the second from
+    L2, writes T x 4d B)."""
+    import torch
+    from flowmc_gb300.random import PRNGKey
+    from flowmc_gb300.resource.buffers import Buffer
+    from flowmc_gb300.resource.kernel.MALA import MALA
+    from flowmc_gb300.resource.logPDF import TemperedPDF
+    from flowmc_gb300.resource.states import State
+    from flowmc_gb300.strategy.parallel_tempering import ParallelTempering, pt_exchange, pt_local_steps
+    w = WORKLOADS["mixture64"]
+    tgt, _, _ = make_target("mixture64", w, dev)
+    d = w["d"]
+    tlp = TemperedPDF(tgt, None, n_dims=d)
+    temps_t = torch.linspace(1.0, 10.0, temps, device=dev)
+    x = torch.randn(chains, temps, d, device=dev)
+    kern = MALA(0.05)
+    ms_local = _time(lambda: pt_local_steps(kern, tlp, x, temps_t, steps, 7))
+    xl, _, _ = pt_local_steps(kern, tlp, x, temps_t, steps, 7)
+    first = torch.empty(chains, d, device=dev)
+    rest = torch.empty(chains, temps - 1, d, device=dev)
+    ms_ex = _time(lambda: pt_exchange(tgt, xl, temps_t, 9, out_first=first, out_rest=rest))
+    tp = Buffer("tempered_positions", (chains, temps - 1, d), 2, device=dev)
+    tp.data.normal_()
+    tb = Buffer("temperature", (temps,), 0, device=dev)
+    tb.update_buffer(temps_t)
+    res = {"tempered_logpdf": tlp, "local_sampler": kern, "tempered_positions": tp, "temperatures": tb,
+           "sampler_state": State({"training": True})}
+    strat = ParallelTempering(steps, "tempered_logpdf", "local_sampler", ["tempered_positions", "temperatures"],
+                              "sampler_state")
+    x0 = torch.randn(chains, d, device=dev)
+    ms_call = _time(lambda: strat(PRNGKey(3), res, x0, {}))
+    ex_bytes = chains * temps * d * 4 * 3
+    hbm = measured_peaks()[0]
+    return {"target": "64-D 4-mode mixture", "chains": chains, "temperatures": temps, "steps": steps,
+            "local_ms": ms_local, "row_steps_per_s": chains * temps * steps / (ms_local / 1e3),
+            "exchange_ms": ms_ex, "exchange_gbs": ex_bytes / (ms_ex / 1e3) / 1e9,
+            "exchange_frac_hbm": ex_bytes / (ms_ex / 1e3) / 1e9 / hbm, "strategy_call_ms": ms_call}
+
+
+def realnvp_probe(dev, d=32, layers=8, hidden=256, n=262144, batch=16384):
+    """RealNVP(d, layers, hidden): log_prob over n rows and one loss+gradient
+    on a batch. FP32 FLOPs per row and layer: 2 x (2 H d + 2 d H) forward;
+    the gradient recomputes the forward and runs about twice its FLOPs."""
+    import torch
+    from flowmc_gb300.random import PRNGKey
+    from flowmc_gb300.resource.model.nf_model.realNVP import RealNVP
+    m = RealNVP(d, layers, hidden, PRNGKey(0), device=dev)
+    x = torch.randn(n, d, device=dev)
+    xb = x[:batch].contiguous()
+    ms_lp = _time(lambda: m.log_prob(x))
+    ms_g = _time(lambda: m.loss_and_grad(xb))
+    fl = 2.0 * 4 * hidden * d * layers
+    return {"n_dim": d, "layers": layers, "hidden": hidden, "log_prob_rows": n, "log_prob_ms": ms_lp,
+            "log_prob_rows_per_s": n / (ms_lp / 1e3), "log_prob_fp32_tflops": fl * n / (ms_lp / 1e3) / 1e12,
+            "grad_batch": batch, "grad_ms": ms_g, "grad_rows_per_s": batch / (ms_g / 1e3),
+            "grad_fp32_tflops": 4 * fl * batch / (ms_g / 1e3) / 1e12}
+
+
+def adam_probe(dev, chains=65536, steps=200):
+    """AdamOptimization on the 64-D 4-mode mixture: chains x steps of Adam
+    with gradient noise in one launch."""
+    import torch
+    from flowmc_gb300.random import PRNGKey
+    from flowmc_gb300.strategy.optimization import AdamOptimization
+    w = WORKLOADS["mixture64"]
+    tgt, _, _ = make_target("mixture64", w, dev)
+    opt = AdamOptimization(tgt, n_steps=steps, learning_rate=1e-2, noise_level=1.0)
+    x0 = torch.randn(chains, w["d"], device=dev)
+    import contextlib
+    import io
+    with contextlib.redirect_stdout(io.StringIO()):
+        ms = _time(lambda: opt.optimize(PRNGKey(0), None, x0, {}), reps=3)
+    return {"target": "64-D 4-mode mixture", "chains": chains, "steps": steps, "ms": ms,
+            "chain_steps_per_s": chains * steps / (ms / 1e3)}
+
+
 def plain_arm(name, w, dev, n_train, n_prod, timed_from, mean_ref, var_ref, ess=True):
     """The plain FP32 PyTorch-eager form (flowmc_gb300.plain) on the same
     workload: chain-steps/s over the loops from `timed_from` on, and (when
@@ -558,7 +652,7 @@ def main():
     ap.add_argument("--chains", type=int, default=0, help="override n_chains (small profiling cases)")
     ap.add_argument("--plain-loops", type=int, default=2,
                     help="loops of the plain FP32 form timed for its chain-steps/s (0 = skip)")
-    ap.add_argument("--probe", default="", choices=["", "local", "batched", "train"],
+    ap.add_argument("--probe", default="", choices=["", "local", "batched", "train", "pt", "realnvp", "adam"],
                     help="run only the local-step HBM probe (a small profiling target)")
     ap.add_argument("--kernel-trace", default="",
                     help="write a per-kernel launch list (CUPTI activity timestamps) of the K loops to this "
@@ -607,6 +701,15 @@ def main():
     if args.probe == "train":
         print(json.dumps({"probe": "flow_training_d32", "bf16": train_probe(dev, "bf16"),
                           "fp32": train_probe(dev, "fp32")}), flush=True)
+        return
+    if args.probe == "pt":
+        print(json.dumps({"probe": "parallel_tempering", **pt_probe(dev)}), flush=True)
+        return
+    if args.probe == "realnvp":
+        print(json.dumps({"probe": "realnvp", **realnvp_probe(dev)}), flush=True)
+        return
+    if args.probe == "adam":
+        print(json.dumps({"probe": "adam_optimization", **adam_probe(dev)}), flush=True)
         return
     if args.probe == "local":
         print(json.dumps({"probe": "local_steps", **local_hbm_probe(dev, chains=w["n_chains"] if args.chains else 65536,
