@@ -257,44 +257,63 @@ __device__ __forceinline__ float softplus_fast(float a) {
   return fmaxf(a, 0.f) + __logf(1.f + __expf(-fabsf(a)));
 }
 
+// 2^x on the SFU (ex2.approx.ftz.f32); softmax arguments are <= 0 after the
+// max subtraction, so the approximation's relative error bounds the result
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// The spline of the bin that holds v only, for the fused tensor-core
+// epilogue (same function as rqs_forward/rqs_inverse up to rounding):
+// unnormalised softmax weights e^(raw - max) (one FFMA + ex2 each), the bin
+// found by comparing v with the running knots while carrying only what the
+// bin needs (cumulative sums before it, its own weights, its two slope
+// parameters), and one log for the log-determinant.
 template <int K, bool INV>
 __device__ __forceinline__ void rqs_apply_fast(const float (&raw)[3 * K + 1], float v, const SplineCfg& c, float& out,
                                                float& ld) {
+  constexpr float kLog2e = 1.4426950408889634f;
   float mw = raw[0], mh = raw[K];
 #pragma unroll
   for (int k = 1; k < K; ++k) {
     mw = fmaxf(mw, raw[k]);
     mh = fmaxf(mh, raw[K + k]);
   }
+  const float nmw = -mw * kLog2e, nmh = -mh * kLog2e;
   float ew[K], eh[K], sw = 0.f, sh = 0.f;
 #pragma unroll
   for (int k = 0; k < K; ++k) {
-    ew[k] = __expf(raw[k] - mw);
-    eh[k] = __expf(raw[K + k] - mh);
+    ew[k] = ex2_approx(fmaf(raw[k], kLog2e, nmw));
+    eh[k] = ex2_approx(fmaf(raw[K + k], kLog2e, nmh));
     sw += ew[k];
     sh += eh[k];
   }
   const float scale = (c.rmax - c.rmin) - (float)K * c.min_bin;
   const float fw = __fdividef(scale, sw), fh = __fdividef(scale, sh);
-  // bin 0 by default (also covers v below the range)
-  float cw = 0.f, ch = 0.f;
-  float x0 = c.rmin, y0 = c.rmin, x1 = c.rmax, y1 = c.rmax, r0 = raw[2 * K], r1 = raw[2 * K + 1];
+  // knot k = rmin + (sum of the first k weights) * f + k * min_bin; bin 0 by
+  // default (also covers v below the range)
+  float cw = 0.f, ch = 0.f, bw = 0.f, bh = 0.f, ebw = ew[0], ebh = eh[0], kbf = 0.f;
+  float r0 = raw[2 * K], r1 = raw[2 * K + 1];
 #pragma unroll
-  for (int k = 0; k < K; ++k) {
-    const float xk = c.rmin + cw, yk = c.rmin + ch;
-    cw += ew[k] * fw + c.min_bin;
-    ch += eh[k] * fh + c.min_bin;
-    const float xk1 = (k == K - 1) ? c.rmax : c.rmin + cw;
-    const float yk1 = (k == K - 1) ? c.rmax : c.rmin + ch;
-    if (k == 0 || v >= (INV ? yk : xk)) {
-      x0 = xk; x1 = xk1; y0 = yk; y1 = yk1;
+  for (int k = 1; k < K; ++k) {
+    cw += ew[k - 1];
+    ch += eh[k - 1];
+    const float kn = INV ? fmaf(ch, fh, fmaf((float)k, c.min_bin, c.rmin)) : fmaf(cw, fw, fmaf((float)k, c.min_bin, c.rmin));
+    if (v >= kn) {
+      bw = cw; bh = ch; ebw = ew[k]; ebh = eh[k]; kbf = (float)k;
       r0 = raw[2 * K + k];
       r1 = raw[2 * K + k + 1];
     }
   }
+  const float x0 = fmaf(bw, fw, fmaf(kbf, c.min_bin, c.rmin));
+  const float y0 = fmaf(bh, fh, fmaf(kbf, c.min_bin, c.rmin));
+  const bool last = kbf == (float)(K - 1);   // the last knot is exactly rmax
+  const float w = last ? c.rmax - x0 : fmaf(ebw, fw, c.min_bin);
+  const float h = last ? c.rmax - y0 : fmaf(ebh, fh, c.min_bin);
   const float d0 = softplus_fast(r0 + c.slope_offset) + c.min_slope;
   const float d1 = softplus_fast(r1 + c.slope_offset) + c.min_slope;
-  const float w = x1 - x0, h = y1 - y0;
   const float s = __fdividef(h, w);
   const float st = d1 + d0 - 2.f * s;
   float z;
@@ -314,17 +333,18 @@ __device__ __forceinline__ void rqs_apply_fast(const float (&raw)[3 * K + 1], fl
   const float sq = z * z, q = z - sq, om = 1.f - z;
   const float den = s + st * q;
   const float A = d1 * sq + 2.f * s * q + d0 * om * om;
-  const float lg = 2.f * __logf(s) + __logf(A) - 2.f * __logf(den);
+  // log-det 2 log s + log A - 2 log den as one log; log d0 / log d1 in the tails
+  float arg = __fdividef(s * s * A, den * den);
   if (!INV) {
     out = y0 + __fdividef(h * (s * sq + d0 * q), den);
-    ld = lg;
-    if (v <= c.rmin) { out = (v - c.rmin) * d0 + c.rmin; ld = __logf(d0); }
-    if (v >= c.rmax) { out = (v - c.rmax) * d1 + c.rmax; ld = __logf(d1); }
+    if (v <= c.rmin) { out = (v - c.rmin) * d0 + c.rmin; arg = d0; }
+    if (v >= c.rmax) { out = (v - c.rmax) * d1 + c.rmax; arg = d1; }
+    ld = __logf(arg);
   } else {
     out = w * z + x0;
-    ld = -lg;
-    if (v <= c.rmin) { out = __fdividef(v - c.rmin, d0) + c.rmin; ld = -__logf(d0); }
-    if (v >= c.rmax) { out = __fdividef(v - c.rmax, d1) + c.rmax; ld = -__logf(d1); }
+    if (v <= c.rmin) { out = __fdividef(v - c.rmin, d0) + c.rmin; arg = d0; }
+    if (v >= c.rmax) { out = __fdividef(v - c.rmax, d1) + c.rmax; arg = d1; }
+    ld = -__logf(arg);
   }
 }
 
