@@ -358,17 +358,19 @@ __device__ __forceinline__ void rqs_apply_fast(const float (&raw)[3 * K + 1], fl
 template <int K>
 __device__ __forceinline__ float rqs_fwd_adjoint_fast(const float (&raw)[3 * K + 1], float x, float gy, float gl,
                                                       const SplineCfg& c, uint16_t* __restrict__ out) {
+  constexpr float kLog2e = 1.4426950408889634f;
   float mw = raw[0], mh = raw[K];
 #pragma unroll
   for (int k = 1; k < K; ++k) {
     mw = fmaxf(mw, raw[k]);
     mh = fmaxf(mh, raw[K + k]);
   }
+  const float nmw = -mw * kLog2e, nmh = -mh * kLog2e;
   float pw[K], ph[K], sw = 0.f, sh = 0.f;
 #pragma unroll
   for (int k = 0; k < K; ++k) {
-    pw[k] = __expf(raw[k] - mw);
-    ph[k] = __expf(raw[K + k] - mh);
+    pw[k] = ex2_approx(fmaf(raw[k], kLog2e, nmw));
+    ph[k] = ex2_approx(fmaf(raw[K + k], kLog2e, nmh));
     sw += pw[k];
     sh += ph[k];
   }
@@ -379,23 +381,25 @@ __device__ __forceinline__ float rqs_fwd_adjoint_fast(const float (&raw)[3 * K +
     ph[k] *= ih;
   }
   const float scale = (c.rmax - c.rmin) - (float)K * c.min_bin;
-  float cw = 0.f, ch = 0.f;
-  float x0 = c.rmin, y0 = c.rmin, x1 = c.rmax, y1 = c.rmax, r0 = raw[2 * K], r1 = raw[2 * K + 1];
+  // the bin: cumulative probabilities before it and its own (see rqs_apply_fast)
+  float cpw = 0.f, cph = 0.f, bwn = 0.f, bhn = 0.f, ebw = pw[0], ebh = ph[0];
+  float r0 = raw[2 * K], r1 = raw[2 * K + 1];
   int kb = 0;
 #pragma unroll
-  for (int k = 0; k < K; ++k) {
-    const float xk = c.rmin + cw, yk = c.rmin + ch;
-    cw += pw[k] * scale + c.min_bin;
-    ch += ph[k] * scale + c.min_bin;
-    const float xk1 = (k == K - 1) ? c.rmax : c.rmin + cw;
-    const float yk1 = (k == K - 1) ? c.rmax : c.rmin + ch;
-    if (k == 0 || x >= xk) {
-      x0 = xk; x1 = xk1; y0 = yk; y1 = yk1;
+  for (int k = 1; k < K; ++k) {
+    cpw += pw[k - 1];
+    cph += ph[k - 1];
+    if (x >= fmaf(cpw, scale, fmaf((float)k, c.min_bin, c.rmin))) {
+      bwn = cpw; bhn = cph; ebw = pw[k]; ebh = ph[k]; kb = k;
       r0 = raw[2 * K + k];
       r1 = raw[2 * K + k + 1];
-      kb = k;
     }
   }
+  const bool last = kb == K - 1;   // the last knot is exactly rmax
+  const float x0 = fmaf(bwn, scale, fmaf((float)kb, c.min_bin, c.rmin));
+  const float y0 = fmaf(bhn, scale, fmaf((float)kb, c.min_bin, c.rmin));
+  const float x1 = last ? c.rmax : x0 + fmaf(ebw, scale, c.min_bin);
+  const float y1 = last ? c.rmax : y0 + fmaf(ebh, scale, c.min_bin);
   const float a0 = r0 + c.slope_offset, a1 = r1 + c.slope_offset;
   const float d0 = softplus_fast(a0) + c.min_slope, d1 = softplus_fast(a1) + c.min_slope;
   float gx, g_x0 = 0.f, g_x1 = 0.f, g_y0 = 0.f, g_y1 = 0.f, g_d0 = 0.f, g_d1 = 0.f;
@@ -448,21 +452,18 @@ __device__ __forceinline__ float rqs_fwd_adjoint_fast(const float (&raw)[3 * K +
     g_y0 = gy - g_h;
   }
   // interior knot k (1 <= k <= K-1) is rmin + sum_{i<k} width_i: dL/dwidth_i
-  // collects the gradients of the bin's two knots that lie beyond i
+  // collects the gradients of the bin's two knots that lie beyond i, i.e.
+  // scale (ax0 + ax1) for i < kb, scale ax1 for i = kb, 0 beyond; the softmax
+  // adjoint's sum_j p_j g_j is then closed-form in the bin's sums
   const float ax0 = (kb >= 1) ? g_x0 : 0.f, ax1 = (kb + 1 <= K - 1) ? g_x1 : 0.f;
   const float ay0 = (kb >= 1) ? g_y0 : 0.f, ay1 = (kb + 1 <= K - 1) ? g_y1 : 0.f;
-  float dw = 0.f, dh = 0.f;
+  const float gw_lt = scale * (ax0 + ax1), gw_eq = scale * ax1;
+  const float gh_lt = scale * (ay0 + ay1), gh_eq = scale * ay1;
+  const float dw = gw_lt * bwn + gw_eq * ebw, dh = gh_lt * bhn + gh_eq * ebh;
 #pragma unroll
   for (int i = 0; i < K; ++i) {
-    const float gwi = scale * ((i < kb ? ax0 : 0.f) + (i <= kb ? ax1 : 0.f));
-    const float ghi = scale * ((i < kb ? ay0 : 0.f) + (i <= kb ? ay1 : 0.f));
-    dw += pw[i] * gwi;
-    dh += ph[i] * ghi;
-  }
-#pragma unroll
-  for (int i = 0; i < K; ++i) {
-    const float gwi = scale * ((i < kb ? ax0 : 0.f) + (i <= kb ? ax1 : 0.f));
-    const float ghi = scale * ((i < kb ? ay0 : 0.f) + (i <= kb ? ay1 : 0.f));
+    const float gwi = (i < kb) ? gw_lt : ((i == kb) ? gw_eq : 0.f);
+    const float ghi = (i < kb) ? gh_lt : ((i == kb) ? gh_eq : 0.f);
     out[i] = __bfloat16_as_ushort(__float2bfloat16_rn(pw[i] * (gwi - dw)));
     out[K + i] = __bfloat16_as_ushort(__float2bfloat16_rn(ph[i] * (ghi - dh)));
   }
