@@ -35,10 +35,13 @@ void set_error(const char* fmt, ...);
     }                                            \
   } while (0)
 
+// a failed runtime call also leaves the runtime's last-error state set;
+// it is cleared here so that it is not reported again by the next launch
 #define FMC_CUDA_TRY(expr)                                                   \
   do {                                                                       \
     cudaError_t _e = (expr);                                                 \
     if (_e != cudaSuccess) {                                                 \
+      (void)cudaGetLastError();                                              \
       ::fmc::set_error("%s failed: %s (%s:%d)", #expr, cudaGetErrorString(_e), \
                        __FILE__, __LINE__);                                  \
       return FMC_ERR_CUDA;                                                   \
