@@ -247,3 +247,26 @@ def test_nf_proposal_with_realnvp_matches_oracle(cuda):
     assert agree > 0.98
     rows = (accs == oacc).all(axis=1)
     np.testing.assert_allclose(pos.cpu().numpy()[rows], ox[rows], rtol=1e-4, atol=1e-4)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("d", [1, 2, 3])
+def test_cuda_realnvp_small_dimensions(cuda, d):
+    """d = 1 (every layer either transforms the coordinate with a constant
+    conditioner input or leaves it alone), 2 and 3: passes and gradient agree
+    with the oracle."""
+    m = _random_model(d, 4, 8, 30 + d)
+    o = _oracle_of(m)
+    x = np.random.default_rng(d).normal(size=(257, d))
+    xg = torch.tensor(x, dtype=torch.float32, device="cuda")
+    y, ld = m.forward(xg)
+    yo, ldo = o.forward(x)
+    np.testing.assert_allclose(y.cpu().numpy(), yo, rtol=1e-4, atol=1e-5)
+    np.testing.assert_allclose(ld.cpu().numpy(), ldo, rtol=1e-4, atol=1e-5)
+    xi, _ = m.inverse(y)
+    np.testing.assert_allclose(xi.cpu().numpy(), x, rtol=1e-4, atol=1e-4)
+    loss, grad = m.loss_and_grad(xg)
+    lo, go = R.loss_and_grad(o, x)
+    g = R.pack(go, 4)
+    assert abs(float(loss) - lo) < 1e-4 * max(1.0, abs(lo))
+    assert np.abs(grad.cpu().numpy() - g).max() < 1e-4 * max(1e-3, np.abs(g).max())

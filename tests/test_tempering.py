@@ -349,3 +349,34 @@ def test_pt_strategy_keeps_buffers_outside_training(cuda):
     strat(PRNGKey(1), res, out, {})
     torch.cuda.synchronize()
     assert not torch.equal(tp.data, tp0)
+
+
+@pytest.mark.gpu
+def test_pt_edge_cases(cuda):
+    """One temperature (nothing to exchange, the adaptation is the identity),
+    two temperatures (the adaptation keeps both ends), zero chains, and
+    argument checks that the library reports instead of faulting."""
+    from flowmc_gb300 import _lib
+    from flowmc_gb300.resource.kernel.MALA import MALA
+    from flowmc_gb300.strategy.parallel_tempering import pt_adapt_temperatures, pt_exchange, pt_local_steps
+    d = 3
+    tgt = TG.DiagGaussian(d)
+    tlp = TemperedPDF(tgt, None, n_dims=d)
+    x = torch.randn(16, 1, d, device="cuda")
+    xl, lp, _ = pt_local_steps(MALA(0.3), tlp, x, torch.ones(1, device="cuda"), 5, 1)
+    first = torch.empty(16, d, device="cuda")
+    _, _, _, pairs = pt_exchange(tgt, xl, torch.ones(1, device="cuda"), 2, out_first=first)
+    torch.cuda.synchronize()
+    torch.testing.assert_close(first, xl[:, 0])
+    t2 = torch.tensor([1.0, 4.0], device="cuda")
+    out = pt_adapt_temperatures(t2, torch.tensor([7], dtype=torch.int32, device="cuda"), 16)
+    torch.testing.assert_close(out, t2)
+    # zero chains: a no-op that still zeroes the swap counts
+    z = torch.empty(0, 3, d, device="cuda")
+    _, _, _, pz = pt_exchange(tgt, z, torch.ones(3, device="cuda"), 2, out_first=torch.empty(0, d, device="cuda"),
+                              acc_pairs=torch.full((2,), 5, dtype=torch.int32, device="cuda"))
+    assert pz.tolist() == [0, 0]
+    with pytest.raises(_lib.FlowMCError, match="n_temps"):
+        pt_local_steps(MALA(0.3), tlp, torch.randn(4, 65, d, device="cuda"), torch.ones(65, device="cuda"), 2, 1)
+    with pytest.raises(ValueError):
+        pt_local_steps(MALA(0.3), tlp, torch.randn(4, 2, d + 1, device="cuda"), torch.ones(2, device="cuda"), 2, 1)
