@@ -867,7 +867,9 @@ def main():
                    "flow": f"{w['n_layers']}x{w['hidden']}x{w['n_bins']} bins", "n_training_loops": n_train,
                    "n_production_loops": n_prod, "timed_loops": K, "batch_size": w["batch"],
                    "n_epochs": w["n_epochs"], "parallelism": f"replicas{world}",
-                   "l2": "working set (chain buffers, flow weights) larger than L2; no flush"},
+                   "l2": "working set (chain buffers, flow weights) larger than L2; no flush",
+                   "autotuned": {"lanes_per_chain": getattr(sampler.resources["local_sampler"], "lanes_per_chain", 0),
+                                 "flow_gemm_bn": getattr(sampler.resources["model"], "gemm_bn", 0)}},
         "roofline": roof, "kernels": kernels, "gpu_launches": launches, "clocks": clk,
         "wall_s": wall, "cuda_graph": graph is not None, **extra,
     }

@@ -77,7 +77,7 @@ class FmcFlow(ctypes.Structure):
         ("min_bin_size", ctypes.c_float),
         ("min_knot_slope", ctypes.c_float),
         ("precision", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("gemm_bn", ctypes.c_int32),
         ("theta", ctypes.c_void_p),
         ("theta_bf16", ctypes.c_void_p),
         ("aux", ctypes.c_void_p),

@@ -1,4 +1,5 @@
-"""Autotuner for the chain-block shape of the fused local-step kernel.
+"""Autotuners: the chain-block shape of the fused local-step kernel and the
+tile width of the flow's tensor-core GEMMs.
 
 The local-step kernel assigns each chain to a group of G lanes (4, 8, 16 or
 32) holding V = next_pow2(d / G) coordinates each. Which G is fastest depends
@@ -55,5 +56,37 @@ def tune_local_kernel(kernel, target, n_chains: int, probe_steps: int = 8, reps:
         if ms < best_ms:
             best, best_ms = g, ms
     kernel.lanes_per_chain = best
+    _cache[key] = best
+    return best
+
+
+def tune_flow_gemm(model, n_rows: int = 65536, reps: int = 3) -> int:
+    """Pick the BF16 hidden-layer GEMM tile width (128 or 256 output columns)
+    of a MaskedCouplingRQSpline by timing its log_prob pass over n_rows rows
+    (the NF global step's chunk) with each; the choice changes no result
+    (each output's reduction over K is the same), only the tile count per SM
+    (wave quantisation) and the epilogue's share. Cached per model shape and
+    row count; returns the pick and sets ``model.gemm_bn``."""
+    if getattr(model, "precision", "float32") not in ("bf16", "bfloat16"):
+        return 0
+    key = ("flow_gemm", model.n_features, model.n_layers, tuple(model.hidden_size), model.num_bins, n_rows)
+    if key in _cache:
+        model.gemm_bn = _cache[key]
+        return _cache[key]
+    x = torch.randn(n_rows, model.n_features, device=model.device)
+    best, best_ms = 0, float("inf")
+    for bn in (256, 128):
+        model.gemm_bn = bn
+        model.log_prob(x)   # warm
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            model.log_prob(x)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        if ms < best_ms:
+            best, best_ms = bn, ms
+    model.gemm_bn = best
     _cache[key] = best
     return best

@@ -132,7 +132,7 @@ bool tc_gemm_stages_output(const void* C, int64_t ldc, int n_store, int64_t M) {
 }
 
 int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K, const uint16_t* B, int N,
-            int rows_b, const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store, int epi) {
+            int rows_b, const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store, int epi, int bn) {
   FMC_CHECK_ARG(K % tc::BK == 0 && K >= tc::BK, "K=%d must be a positive multiple of 64", K);
   FMC_CHECK_ARG(rows_a % tc::BM == 0 && rows_a >= M, "A rows %lld must cover M and be a multiple of 128",
                 (long long)rows_a);
@@ -141,7 +141,7 @@ int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K
   if (epi == tc::TC_EPI_TANH_BF16 || epi == tc::TC_EPI_BIAS_F32) FMC_CHECK_ARG(ep.bias != nullptr, "bias is NULL");
   if (epi == tc::TC_EPI_DTANH_BF16) FMC_CHECK_ARG(ep.aux != nullptr, "aux is NULL");
   if (M <= 0) return FMC_OK;
-  const int BN = (N > 128) ? 256 : 128;
+  const int BN = (bn == 128 || bn == 256) ? bn : ((N > 128) ? 256 : 128);
   CUtensorMap ma, mb, mc;
   int rc = make_map(&ma, A, K, rows_a, K, tc::BM);
   if (rc) return rc;
@@ -287,7 +287,7 @@ int conditioner_bf16_hidden(const FmcFlow* f, const FlowGeom& g, int l, int64_t 
     ep.bias = th + g.lin_b(l, i);
     const int ldo = (int)FlowGeom::rup(N, 64);
     int rc = tc_gemm(st, a, m, rows, K, f->theta_bf16 + g.w16_off[seg], N, g.w16_rows(l, i), ep, hbuf[i & 1], ldo, ldo,
-                     tc::TC_EPI_TANH_BF16);
+                     tc::TC_EPI_TANH_BF16, f->gemm_bn);
     if (rc) return rc;
     a = hbuf[i & 1];
   }

@@ -50,6 +50,7 @@ class MaskedCouplingRQSpline(NFModel):
         self.device = torch.device(device) if device is not None else (
             torch.device("cuda") if torch.cuda.is_available() else torch.device("cpu"))
         self.precision = precision
+        self.gemm_bn = 0   # BF16 hidden-layer GEMM tile width; 0 = library choice (autotune.tune_flow_gemm)
         d = self._n_features
         P = 3 * self.num_bins + 1
         self._P = P
@@ -136,6 +137,7 @@ class MaskedCouplingRQSpline(NFModel):
         s.min_bin_size = self.min_bin_size
         s.min_knot_slope = self.min_knot_slope
         s.precision = _lib.PREC_BF16 if self.precision in ("bf16", "bfloat16") else _lib.PREC_FP32
+        s.gemm_bn = int(getattr(self, "gemm_bn", 0))
         s.theta = _lib.ptr(self.theta)
         s.theta_bf16 = _lib.ptr(self.theta_bf16)
         s.aux = _lib.ptr(self.aux)

@@ -8,7 +8,8 @@ reference's behaviour):
   precision          "float32" (default) or "bf16" conditioner GEMMs
   history_window     TrainModel's per-chain window (the reference fixes 100)
   device             where buffers and the flow live
-  autotune           measure the local kernel's chain-block shape on first use
+  autotune           measure the local kernel's chain-block shape and the
+                     flow GEMMs' tile width on first use
 """
 from __future__ import annotations
 
@@ -99,7 +100,7 @@ class RQSpline_MALA_Bundle(ResourceStrategyBundle):
         global_stepper = TakeGroupSteps("logpdf", "global_sampler", "sampler_state",
                                         ["target_positions", "target_log_prob", "target_global_accs"],
                                         n_global_steps, thinning=global_thinning, chain_batch_size=chain_batch_size,
-                                        verbose=verbose)
+                                        verbose=verbose, autotune=autotune)
         model_trainer = TrainModel("model", "positions_training", "optimizer", loss_buffer_name="loss_buffer",
                                    n_epochs=n_epochs, batch_size=batch_size, n_max_examples=n_max_examples,
                                    history_window=history_window, verbose=verbose)

@@ -100,7 +100,6 @@ class TakeSerialSteps(TakeSteps):
                                         pos.data, lp.data, acc.data, cursor, noise=noise, uniform=uniform)
         return x_last
 
-
     def prepare(self, resources, n_chains: int):
         """One-time work that must not run inside a CUDA graph capture: the
         autotuner's timed probes (they synchronise)."""
@@ -114,9 +113,22 @@ class TakeSerialSteps(TakeSteps):
 
 class TakeGroupSteps(TakeSteps):
     """n_steps proposals drawn at once (take_steps.py:183-206): the NFProposal
-    global step."""
+    global step. With ``autotune`` the flow's GEMM tile width is measured on
+    the first call (autotune.tune_flow_gemm)."""
+
+    def _tune(self, kernel, n_chains):
+        model = getattr(kernel, "model", None)
+        if self.autotune and model is not None and not getattr(model, "_gemm_tuned", False):
+            from ..autotune import tune_flow_gemm
+            tune_flow_gemm(model, min(65536, max(128, n_chains * self.n_steps)))
+            model._gemm_tuned = True
+
+    def prepare(self, resources, n_chains: int):
+        """The GEMM tile probe, which synchronises, outside any graph capture."""
+        self._tune(resources[self.kernel_name], n_chains)
 
     def sample(self, kernel, seed, initial_position, target, bufs, cursor, data, noise=None, uniform=None):
+        self._tune(kernel, initial_position.shape[0])
         pos, lp, acc = bufs
         with region("nf_global", units=initial_position.shape[0] * self.n_steps):
             return kernel.group_steps(seed, initial_position, target, self.n_steps, self.thinning,

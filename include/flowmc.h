@@ -274,7 +274,10 @@ typedef struct FmcFlow {
   float range_min, range_max;        /* spline range (-10, 10)            */
   float min_bin_size, min_knot_slope;/* 1e-4, 1e-4 (rqSpline.py:299-300)   */
   int32_t precision;                 /* FMC_PREC_FP32 or FMC_PREC_BF16      */
-  int32_t reserved;
+  int32_t gemm_bn;                   /* BF16 hidden-layer GEMM tile width:
+                                        0 = library choice (256 for outputs
+                                        wider than 128 columns, else 128),
+                                        or 128 / 256 (an autotuner's pick) */
   float* theta;                      /* [n_params] float32 master weights   */
   uint16_t* theta_bf16;              /* [n_params] bf16 shadow (BF16 mode)   */
   float* aux;                        /* [2*n_dim + 2], see above             */

@@ -49,3 +49,25 @@ def test_tuned_shape_matches_default_shape(cuda, kname):
         ok = (acc == outs[0][2]).all(dim=1)
         torch.testing.assert_close(pos[ok], outs[0][0][ok], rtol=1e-3, atol=1e-3)
         torch.testing.assert_close(lp[ok], outs[0][1][ok], rtol=1e-3, atol=1e-3)
+
+
+@pytest.mark.gpu
+def test_flow_gemm_tile_width_is_tuned_and_changes_no_result(cuda):
+    """The BF16 hidden-layer GEMMs give the same log-densities with 128- and
+    256-column tiles (each output's K reduction is the same); the tuner
+    picks one of them and records it on the model."""
+    import torch
+    from flowmc_gb300.autotune import tune_flow_gemm
+    from flowmc_gb300.random import PRNGKey
+    from flowmc_gb300.resource.model.nf_model.rqSpline import MaskedCouplingRQSpline
+    m = MaskedCouplingRQSpline(24, 3, [512, 512], 8, PRNGKey(0), precision="bf16", device="cuda")
+    m.theta.add_(torch.randn_like(m.theta) * 0.02)
+    m.sync_bf16()
+    x = torch.randn(5000, 24, device="cuda")
+    out = {}
+    for bn in (256, 128):
+        m.gemm_bn = bn
+        out[bn] = m.log_prob(x)
+    torch.testing.assert_close(out[128], out[256], rtol=0, atol=0)
+    pick = tune_flow_gemm(m, n_rows=8192, reps=1)
+    assert pick in (128, 256) and m.gemm_bn == pick
