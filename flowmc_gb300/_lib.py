@@ -57,6 +57,7 @@ class FmcLocalParams(ctypes.Structure):
         ("lanes_per_chain", ctypes.c_int32),
         ("momentum_scale", ctypes.c_void_p),
         ("metric_colsum", ctypes.c_void_p),
+        ("momentum_chol", ctypes.c_void_p),
     ]
 
 

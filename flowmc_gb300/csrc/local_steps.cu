@@ -68,6 +68,7 @@ extern "C" int fmc_local_steps(const FmcTarget* target, const FmcLocalParams* pa
   a.step = params->step_size;
   a.mscale = params->momentum_scale;
   a.mcol = params->metric_colsum;
+  a.mchol = params->momentum_chol;
   a.x0 = x0;
   a.lp0 = lp0;
   a.C = n_chains;

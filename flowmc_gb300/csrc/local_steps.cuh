@@ -40,6 +40,8 @@ struct LocalArgs {
   float step;
   const float* mscale;  // HMC momentum scale (diag of cholesky(inv(M)))
   const float* mcol;    // HMC column sums of M
+  const float* mchol;   // HMC with a dense M: cholesky(inv(M)) [d, d] row-major, or NULL
+  int32_t mstage_off;   // floats of dynamic shared memory before the momentum staging
   const float* x0;
   const float* lp0;
   int32_t C, d, S, thin;
@@ -258,11 +260,36 @@ __global__ void __launch_bounds__(256) k_local_steps(const LocalArgs a) {
       } else if constexpr (KIND == FMC_KERNEL_HMC) {
         float p[V], mc[V], xq[V], gq[V];
         float k0 = 0.f;
+        if (a.mchol) {
+          // dense metric: p = xi @ L^T (HMC.py:133-136), the chain's normals
+          // shared through this group's slice of shared memory
+          float* xs = smem + a.mstage_off + gib * d;
+#pragma unroll
+          for (int v = 0; v < V; ++v)
+            if (gl * V + v < d) xs[gl * V + v] = xi[v];
+          __syncwarp();
+#pragma unroll
+          for (int v = 0; v < V; ++v) {
+            const int j = gl * V + v;
+            float acc = 0.f;
+            if (j < d) {
+              const float* Lr = a.mchol + (int64_t)j * d;
+              for (int k = 0; k <= j; ++k) acc = fmaf(__ldg(Lr + k), xs[k], acc);   // L is lower triangular
+            }
+            p[v] = acc;
+          }
+          __syncwarp();   // xs is rewritten at the next step
+        } else {
+#pragma unroll
+          for (int v = 0; v < V; ++v) {
+            const int j = gl * V + v;
+            p[v] = xi[v] * ((j < d) ? ldg_or(a.mscale, j, 1.f) : 0.f);
+          }
+        }
 #pragma unroll
         for (int v = 0; v < V; ++v) {
           const int j = gl * V + v;
           const bool in = j < d;
-          p[v] = xi[v] * (in ? ldg_or(a.mscale, j, 1.f) : 0.f);
           mc[v] = in ? ldg_or(a.mcol, j, 1.f) : 0.f;
           k0 += p[v] * p[v] * mc[v];
           xq[v] = x[v];
@@ -410,6 +437,8 @@ int launch_local_t(const LocalArgs& a0, cudaStream_t st) {
       a.tab_smem = 1;
     }
   }
+  a.mstage_off = (int32_t)(smem / sizeof(float));
+  if (KIND == FMC_KERNEL_HMC && a.mchol != nullptr) smem += (size_t)gpb * a.d * sizeof(float);
   auto kern = k_local_steps<KIND, TGT, G, V>;
   if (smem > 48 * 1024) {
     FMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -211,6 +211,7 @@ extern "C" int fmc_pt_local_steps(const FmcTarget* target, const FmcLocalParams*
   a.step = params->step_size;
   a.mscale = params->momentum_scale;
   a.mcol = params->metric_colsum;
+  a.mchol = params->momentum_chol;
   a.x0 = x0;
   a.lp0 = nullptr;   // the tempered log-density is evaluated at x0 (parallel_tempering.py:236-238)
   a.C = n_chains * n_temps;

@@ -5,8 +5,10 @@ The leapfrog table has rows [0, .5], [1, 1] x n_leapfrog, [1, .5]
 momentum is xi @ cholesky(inv(M)).T and the kinetic energy 0.5 * sum(p^2 * M)
 with numpy broadcasting (for a matrix M: the column sums of M weight p^2),
 H uses the incoming log_prob (HMC.py:118-151). The fused kernel takes the
-momentum scale and the column sums as vectors, so M must be diagonal (the
-reference's own tests use identity metrics, test/unit/test_kernels.py:39-43).
+column sums as a vector and the momentum transform either as the diagonal of
+cholesky(inv(M)) (diagonal M) or as the full lower-triangular factor (dense
+M: one triangular matvec per step, the chain's normals shared through shared
+memory).
 """
 from __future__ import annotations
 
@@ -40,7 +42,9 @@ class HMC(LocalKernel):
         self._cache = {}
 
     def metric_vectors(self, n_dim: int):
-        """(momentum_scale, column_sums) as float64 arrays, or (None, None) for M = I."""
+        """(momentum_scale, column_sums, cholesky factor) as float64 arrays:
+        (None, None, None) for M = I, (diag(L), colsum, None) for a diagonal M,
+        (None, colsum, L) for a dense M, with L = cholesky(inv(M))."""
         M = self.condition_matrix
         if isinstance(M, torch.Tensor):
             M = M.detach().cpu().numpy()
@@ -52,20 +56,21 @@ class HMC(LocalKernel):
         if M.shape != (n_dim, n_dim):
             raise ValueError(f"condition_matrix has shape {M.shape}, expected ({n_dim}, {n_dim})")
         if np.array_equal(M, np.eye(n_dim)):
-            return None, None
-        if np.count_nonzero(M - np.diag(np.diag(M))):
-            raise NotImplementedError("the fused HMC kernel supports diagonal condition matrices")
+            return None, None, None
         L = np.linalg.cholesky(np.linalg.inv(M))
-        return np.diag(L).copy(), M.sum(axis=0)
+        if np.count_nonzero(M - np.diag(np.diag(M))):
+            return None, M.sum(axis=0), L
+        return np.diag(L).copy(), M.sum(axis=0), None
 
     def local_params(self, n_dim, device):
         key = (n_dim, str(device))
         if key not in self._cache:
-            ms, mc = self.metric_vectors(n_dim)
+            ms, mc, L = self.metric_vectors(n_dim)
             tms = None if ms is None else torch.tensor(ms, dtype=torch.float32, device=device)
             tmc = None if mc is None else torch.tensor(mc, dtype=torch.float32, device=device)
-            self._cache[key] = (tms, tmc)
-        tms, tmc = self._cache[key]
+            tl = None if L is None else torch.tensor(L, dtype=torch.float32, device=device).contiguous()
+            self._cache[key] = (tms, tmc, tl)
+        tms, tmc, tl = self._cache[key]
         p = _lib.FmcLocalParams()
         p.kind = self.kernel_kind
         p.n_leapfrog = int(self.n_leapfrog)
@@ -73,7 +78,8 @@ class HMC(LocalKernel):
         p.lanes_per_chain = int(self.lanes_per_chain)
         p.momentum_scale = _lib.ptr(tms) if tms is not None else None
         p.metric_colsum = _lib.ptr(tmc) if tmc is not None else None
-        return p, [tms, tmc]
+        p.momentum_chol = _lib.ptr(tl) if tl is not None else None
+        return p, [tms, tmc, tl]
 
     def print_parameters(self):
         print("HMC parameters:")

@@ -76,6 +76,9 @@ typedef struct FmcLocalParams {
   int32_t lanes_per_chain;    /* 0 = default for n_dim; else 4, 8, 16 or 32 lanes  */
   const float* momentum_scale;/* HMC: [n_dim] = diag(cholesky(inv(M)))   or NULL = 1 */
   const float* metric_colsum; /* HMC: [n_dim] = sum_i M[i, j]            or NULL = 1 */
+  const float* momentum_chol; /* HMC with a dense M: [n_dim, n_dim] row-major
+                                 cholesky(inv(M)) (momentum xi @ L^T), or NULL
+                                 (diagonal: momentum_scale)                     */
 } FmcLocalParams;
 
 /* Run `n_steps` steps of a local kernel for every chain in one persistent

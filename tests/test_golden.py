@@ -87,11 +87,6 @@ def test_cuda_kernels_match_reference_source(cuda, case):
         kern = GaussianRandomWalk(case["step_size"])
     C, S, d = noise.shape
     dev = torch.device("cuda")
-    if case["kind"] == "hmc" and np.count_nonzero(z[f"{n}/M"] - np.diag(np.diag(z[f"{n}/M"]))):
-        # the fused HMC kernel takes diagonal mass matrices only and says so
-        with pytest.raises(NotImplementedError):
-            kern.local_params(d, dev)
-        return
     pos = torch.full((C, S, d), -np.inf, device=dev)
     lp = torch.full((C, S), -np.inf, device=dev)
     acc = torch.full((C, S), -np.inf, device=dev)

@@ -252,3 +252,43 @@ def test_target_value_grad_entry(tgts):
         olp, og = T.value_grad(t, x.astype(np.float64))
         np.testing.assert_allclose(lp.cpu().numpy(), olp, rtol=1e-5, atol=1e-4, err_msg=name)
         np.testing.assert_allclose(g.cpu().numpy(), og, rtol=1e-4, atol=1e-4, err_msg=name)
+
+
+def _spd(d, seed):
+    rng = np.random.default_rng(seed)
+    Q, _ = np.linalg.qr(rng.normal(size=(d, d)))
+    return Q @ np.diag(rng.uniform(0.5, 2.0, size=d)) @ Q.T
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tname,step,nlf,lanes", [("diag20", 0.3, 3, 0), ("mixture", 0.5, 3, 0), ("dense", 0.4, 3, 0),
+                                                  ("diag20", 0.3, 3, 4), ("diag20", 0.3, 3, 32),
+                                                  ("mixture132", 0.3, 3, 0)])
+def test_hmc_dense_mass_matches_oracle(tgts, tname, step, nlf, lanes):
+    """HMC with a dense condition matrix (HMC.py:133-137): momentum
+    xi @ cholesky(inv(M)).T, kinetic energy with M's column sums; the fused
+    kernel against the oracle on the same normals and uniforms."""
+    from flowmc_gb300.resource.kernel.HMC import HMC
+    tgt = tgts[tname]
+    t = tgt.describe()
+    d = tgt.n_dim
+    M = _spd(d, d)
+    C, S = 9, 20
+    rng = np.random.default_rng(7 + d)
+    x0 = rng.normal(size=(C, d)).astype(np.float32)
+    noise = rng.normal(size=(C, S, d)).astype(np.float32)
+    unif = rng.uniform(1e-6, 1, size=(C, S)).astype(np.float32)
+    kern = HMC(condition_matrix=M, step_size=step, n_leapfrog=nlf)
+    pos, lp, acc, xl, ll = _run_gpu(kern, tgt, x0, noise, unif, S, lanes=lanes)
+    opos, olp, oacc, _ = K.take_serial_steps("hmc", t, x0.astype(np.float64), S, noise.astype(np.float64),
+                                             unif.astype(np.float64), step_size=step, n_leapfrog=nlf, M=M)
+    margins = K.accept_margins("hmc", t, x0, noise, unif, step_size=step, n_leapfrog=nlf, M=M)
+    checked = 0
+    for c in range(C):
+        ties = np.nonzero(margins[c] < 1e-4)[0]
+        upto = ties[0] if len(ties) else S
+        np.testing.assert_array_equal(acc[c, :upto], oacc[c, :upto], err_msg=f"chain {c}")
+        np.testing.assert_allclose(pos[c, :upto], opos[c, :upto], rtol=1e-4, atol=1e-4, err_msg=f"chain {c}")
+        checked += upto
+    assert checked >= C * S // 2
+    assert 0 < oacc.mean() < 1   # both outcomes of the accept test occur
