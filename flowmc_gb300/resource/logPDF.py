@@ -133,11 +133,19 @@ def _prior_arrays(prior, n_dims):
     if callable(prior) and not isinstance(prior, Target):
         rng = np.random.default_rng(0)
         probes = [np.zeros(n_dims), rng.normal(size=n_dims), 1e3 * rng.normal(size=n_dims)]
+        def zero(v):
+            # a Python number or a one-element array (the tutorials return jnp.array(0.0))
+            try:
+                a = np.asarray(v.detach().cpu() if hasattr(v, "detach") else v, dtype=np.float64)
+            except Exception:
+                return False
+            return a.size == 1 and float(a.reshape(())) == 0.0
+
         try:
             vals = [prior(p, {}) for p in probes]
         except Exception:
             vals = [None]
-        if all(isinstance(v, (int, float)) and float(v) == 0.0 for v in vals):
+        if all(zero(v) for v in vals):
             return None
     raise NotImplementedError(
         "the fused tempered kernel supports a zero log prior or a targets.DiagGaussian prior; "

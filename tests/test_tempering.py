@@ -86,6 +86,8 @@ def test_tempered_pdf_prior_handling():
     like = TG.DiagGaussian(3, device="cpu")
     assert TemperedPDF(like, None, n_dims=3).prior_arrays("cpu") is None
     assert TemperedPDF(LogPDF(like, n_dims=3), lambda x, _: 0.0, n_dims=3).prior_arrays("cpu") is None
+    assert TemperedPDF(like, lambda x, _: np.array(0.0), n_dims=3).prior_arrays("cpu") is None
+    assert TemperedPDF(like, lambda x, _: torch.zeros(()), n_dims=3).prior_arrays("cpu") is None
     m, iv, c = TemperedPDF(like, TG.DiagGaussian(3, mean=[1, 2, 3], inv_var=[1, 2, 4], const=-0.5, device="cpu"),
                            n_dims=3).prior_arrays("cpu")
     assert m.tolist() == [1, 2, 3] and iv.tolist() == [1, 2, 4] and c == -0.5
