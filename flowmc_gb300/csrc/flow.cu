@@ -100,15 +100,38 @@ __global__ void k_affine(const float* __restrict__ in, float* __restrict__ out, 
   const float es = expf(inverse ? -s : s);
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  // four coordinates per lane when every row is 16-byte aligned and the
+  // conditioning coordinates (every other one) are exactly half of them
+  const bool v4 = (d % 4 == 0) && 2 * nc == d && ((uintptr_t)in & 15) == 0 && ((uintptr_t)out & 15) == 0 &&
+                  (cond == nullptr || ((uintptr_t)cond & 7) == 0) &&
+                  (cond16 == nullptr || (((uintptr_t)cond16 & 3) == 0 && (ldc16 & 1) == 0));
   for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < n; r += warps) {
     const float* ir = in + r * d;
     float* orow = out + r * d;
-    for (int j = lane; j < d; j += 32) {
-      const float v = inverse ? ir[j] * es - t : (ir[j] + t) * es;   // common.py:229, 238
-      orow[j] = v;
-      if ((j & 1) == cpar) {
-        if (cond != nullptr) cond[r * nc + (j >> 1)] = v;
-        if (cond16 != nullptr) cond16[r * ldc16 + (j >> 1)] = f32_to_bf16_rn(v);
+    if (v4) {
+      for (int q = lane; q < d / 4; q += 32) {
+        const float4 a = reinterpret_cast<const float4*>(ir)[q];
+        float4 o;
+        o.x = inverse ? a.x * es - t : (a.x + t) * es;   // common.py:229, 238
+        o.y = inverse ? a.y * es - t : (a.y + t) * es;
+        o.z = inverse ? a.z * es - t : (a.z + t) * es;
+        o.w = inverse ? a.w * es - t : (a.w + t) * es;
+        reinterpret_cast<float4*>(orow)[q] = o;
+        // coordinates 4q + cpar and 4q + 2 + cpar are conditioning ones 2q, 2q + 1
+        const float c0 = cpar ? o.y : o.x, c1 = cpar ? o.w : o.z;
+        if (cond != nullptr) reinterpret_cast<float2*>(cond + r * nc)[q] = make_float2(c0, c1);
+        if (cond16 != nullptr)
+          reinterpret_cast<uint32_t*>(cond16 + r * ldc16)[q] =
+              (uint32_t)f32_to_bf16_rn(c0) | ((uint32_t)f32_to_bf16_rn(c1) << 16);
+      }
+    } else {
+      for (int j = lane; j < d; j += 32) {
+        const float v = inverse ? ir[j] * es - t : (ir[j] + t) * es;   // common.py:229, 238
+        orow[j] = v;
+        if ((j & 1) == cpar) {
+          if (cond != nullptr) cond[r * nc + (j >> 1)] = v;
+          if (cond16 != nullptr) cond16[r * ldc16 + (j >> 1)] = f32_to_bf16_rn(v);
+        }
       }
     }
     if (cond16 != nullptr)
