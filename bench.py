@@ -26,8 +26,9 @@ and the timed region is its replay; ``--eager`` launches them one by one.
 call per loop, each a replay of that loop's captured schedule unless
 ``--eager``) with pinned host buffers: each loop copies its starting
 positions host->device and reads the rows it wrote and its final positions
-back, all inside the wall-clock timed region (after one untimed production
-loop that warms the pinned host buffers).
+back, all inside the wall-clock timed region (after two untimed production
+loops that warm the pinned host buffers). The rows' device->host copy of one
+loop overlaps the next loop on a second stream.
 
 ``--impl reference`` times the CPU restatement of the same loop (the
 reference flowMC itself needs JAX, which this image does not have).
@@ -907,7 +908,12 @@ def end_to_end(sampler, bundle, w, dev, n_train_loops, n_prod_loops, x_dev, grap
     inside Sampler.sample) and reads back the rows it wrote plus the final
     positions (device->host, pinned). With ``graph`` each loop is a replay of
     its schedule's CUDA graph (Sampler.sample(..., cuda_graph=True)); the two
-    schedules are captured before the timed region."""
+    schedules are captured before the timed region. A loop's rows are staged
+    to a device buffer (the next loop rewrites the same rows) and copied to
+    one of two pinned host buffers on a second stream while the next loop
+    runs; the final positions go back to the host on the compute stream, in
+    order before the next loop's host->device copy of them. The clock stops
+    after every copy has landed."""
     import torch
     train = ["local_stepper", "update_global_step", "model_trainer", "update_model", "global_stepper",
              "update_local_step"]
@@ -916,8 +922,12 @@ def end_to_end(sampler, bundle, w, dev, n_train_loops, n_prod_loops, x_dev, grap
     blk = w["n_local"] + w["n_global"]
     x_host = torch.empty(C, d, pin_memory=True)
     x_host.copy_(x_dev)
-    pos_h = torch.empty(C, blk, d, pin_memory=True)
-    lp_h = torch.empty(C, blk, pin_memory=True)
+    pos_h = [torch.empty(C, blk, d, pin_memory=True) for _ in range(2)]
+    lp_h = [torch.empty(C, blk, pin_memory=True) for _ in range(2)]
+    pos_s = [torch.empty(C, blk, d, device=dev) for _ in range(2)]
+    lp_s = [torch.empty(C, blk, device=dev) for _ in range(2)]
+    copy_stream = torch.cuda.Stream(device=dev)
+    done = [None, None]
     res = sampler.resources
     state = res["sampler_state"]
     steppers = [sampler.strategies["local_stepper"], sampler.strategies["global_stepper"]]
@@ -933,23 +943,36 @@ def end_to_end(sampler, bundle, w, dev, n_train_loops, n_prod_loops, x_dev, grap
                 sampler.capture(x_dev, {})
                 capture_ms += (time.perf_counter() - c0) * 1e3
 
-    def loop(order):
+    def loop(i, order):
         sampler.strategy_order = order
         for s in steppers:
             s.set_current_position(0)
         last = sampler.sample(x_host, {}, cuda_graph=graph)   # h2d inside Sampler.sample
-        pos_h.copy_(res[state.data["target_positions"]].data[:, :blk], non_blocking=True)
-        lp_h.copy_(res[state.data["target_log_prob"]].data[:, :blk], non_blocking=True)
-        x_host.copy_(last, non_blocking=True)
-        torch.cuda.current_stream().synchronize()
+        b = i % 2
+        cur = torch.cuda.current_stream()
+        if done[b] is not None:
+            cur.wait_event(done[b])   # the copy of loop i - 2 has left staging buffer b
+        pos_s[b].copy_(res[state.data["target_positions"]].data[:, :blk])
+        lp_s[b].copy_(res[state.data["target_log_prob"]].data[:, :blk])
+        x_host.copy_(last, non_blocking=True)   # ordered before the next loop's h2d on this stream
+        staged = cur.record_event()
+        copy_stream.wait_event(staged)
+        with torch.cuda.stream(copy_stream):
+            pos_h[b].copy_(pos_s[b], non_blocking=True)
+            lp_h[b].copy_(lp_s[b], non_blocking=True)
+            done[b] = copy_stream.record_event()
 
-    # one untimed production loop first: the first device->host read into the
-    # fresh pinned buffers costs a one-time ~0.6 s on the Grace host
-    loop(prod)
+    # one untimed production loop per host buffer first: the first
+    # device->host read into fresh pinned memory costs a one-time ~0.6 s on
+    # the Grace host
+    loop(0, prod)
+    loop(1, prod)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for order in plan:
-        loop(order)
+    for i, order in enumerate(plan):
+        loop(i, order)
+    torch.cuda.synchronize()
+    copy_stream.synchronize()
     secs = time.perf_counter() - t0
     h2d = C * d * 4
     d2h = C * blk * d * 4 + C * blk * 4 + C * d * 4
