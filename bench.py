@@ -853,6 +853,10 @@ def main():
                 "peak_source": src if peak else f"{src} bf16 (this run used FP32 SIMT GEMMs)"}
 
     kernels["local_steps_hbm_probe"] = local_hbm_probe(dev)
+    # the survey's "next" components, each on its own probe workload (seconds in total)
+    kernels["parallel_tempering_probe"] = pt_probe(dev)
+    kernels["realnvp_probe"] = realnvp_probe(dev)
+    kernels["adam_optimization_probe"] = adam_probe(dev)
 
     # ---- end to end through the public API with host buffers
     e2e = None
