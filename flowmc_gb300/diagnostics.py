@@ -130,3 +130,32 @@ def rosenbrock_chain_moments(d: int, a: float = 20.0, b: float = 1.0, c: float =
     if edge > 1e-9:
         raise RuntimeError(f"quadrature grid too narrow (edge mass {edge:.2e})")
     return mean, var
+
+
+def dual_moon_moments(d: int, r0: float = 2.0, sr: float = 0.1, mu: float = 3.0, s0: float = 0.6,
+                      m_r: int = 2000, m_phi: int = 4000):
+    """Exact (quadrature) per-coordinate mean and variance of
+    p(x) ~ exp(-0.5((|x| - r0)/sr)^2) (exp(-0.5((x0 + mu)/s0)^2) + exp(-0.5((x0 - mu)/s0)^2)).
+
+    The density depends on x only through r = |x| and the angle phi between x
+    and the first axis, so in hyperspherical coordinates (volume element
+    r^(d-1) sin(phi)^(d-2) dr dphi) it is a 2-D integral. The mixture in x0 is
+    symmetric, so every mean is 0; var(x0) = E[r^2 cos^2 phi] and the other
+    d - 1 coordinates share E[r^2 sin^2 phi] / (d - 1). Midpoint rule on a
+    uniform (r, phi) grid in float64. Returns (mean [d], var [d])."""
+    if d < 2:
+        raise ValueError("dual_moon_moments needs d >= 2")
+    lo, hi = max(0.0, r0 - 12.0 * sr), r0 + 12.0 * sr
+    r = lo + (np.arange(m_r) + 0.5) * (hi - lo) / m_r
+    phi = (np.arange(m_phi) + 0.5) * np.pi / m_phi
+    R, F = np.meshgrid(r, phi, indexing="ij")
+    x0 = R * np.cos(F)
+    logw = (-0.5 * ((R - r0) / sr) ** 2 + (d - 1) * np.log(R) + (d - 2) * np.log(np.sin(F))
+            + np.logaddexp(-0.5 * ((x0 + mu) / s0) ** 2, -0.5 * ((x0 - mu) / s0) ** 2))
+    w = np.exp(logw - logw.max())
+    w /= w.sum()
+    mean = np.zeros(d)
+    var = np.empty(d)
+    var[0] = (w * x0 ** 2).sum()
+    var[1:] = (w * (R * np.sin(F)) ** 2).sum() / (d - 1)
+    return mean, var

@@ -37,6 +37,18 @@ def rosenbrock_value_grad(x, a=20.0, b=1.0, c=5.0):
     return lp, g
 
 
+def dual_moon_value_grad(x, r0=2.0, sr=0.1, mu=3.0, s0=0.6):
+    r = torch.linalg.vector_norm(x, dim=-1)
+    a = (x[:, 0] + mu) / s0
+    b = (x[:, 0] - mu) / s0
+    ea, eb = -0.5 * a * a, -0.5 * b * b
+    lse = torch.logaddexp(ea, eb)
+    lp = -0.5 * ((r - r0) / sr) ** 2 + lse
+    g = (-(r - r0) / (sr * sr) / r)[:, None] * x
+    g[:, 0] -= (torch.exp(ea - lse) * a + torch.exp(eb - lse) * b) / s0
+    return lp, g
+
+
 def mixture_value_grad(x, means, inv_var, log_w):
     dx = x[:, None, :] - means[None]
     e = log_w[None] - 0.5 * (dx * dx * inv_var[None]).sum(-1)
