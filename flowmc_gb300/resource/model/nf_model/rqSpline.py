@@ -39,6 +39,11 @@ class MaskedCouplingRQSpline(NFModel):
     def __init__(self, n_features: int, n_layers: int, hidden_size: list, num_bins: int, key: PRNGKey,
                  spline_range: tuple = (-10.0, 10.0), precision: str = "float32", device=None, **kwargs):
         self._n_features = int(n_features)
+        if not 2 <= self._n_features <= 4096:
+            # at one feature every other layer has nothing to transform and the
+            # rest condition on nothing: the packed conditioner GEMMs have no
+            # zero-width form
+            raise ValueError(f"MaskedCouplingRQSpline supports 2 to 4096 features, got {self._n_features}")
         self.n_layers = int(n_layers)
         self.hidden_size = [int(h) for h in hidden_size]
         if not 1 <= len(self.hidden_size) <= _lib.FMC_MAX_HIDDEN:

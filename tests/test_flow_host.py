@@ -48,3 +48,9 @@ def test_reference_initialisation_statistics():
     assert np.abs(Wl).max() <= 1 / np.sqrt(256) + 1e-7                     # Equinox U(-1/sqrt(in), ..)
     assert float(m.aux[2 * 64]) == 1.0
     assert torch.equal(m.data_mean, torch.zeros(64))
+
+
+@pytest.mark.parametrize("d", [0, 1, 4097])
+def test_feature_count_outside_the_supported_range(d):
+    with pytest.raises(ValueError, match="2 to 4096 features"):
+        MaskedCouplingRQSpline(d, 2, [8, 8], 4, PRNGKey(0), device="cpu")
