@@ -4,6 +4,8 @@ from __future__ import annotations
 
 import torch
 
+from .profiling import nvtx_range
+
 
 class Sampler:
     n_dim: int
@@ -50,7 +52,8 @@ class Sampler:
             if strategy not in self.strategies:
                 raise ValueError(f"Invalid strategy name '{strategy}' provided. "
                                  f"Available strategies are: {list(self.strategies.keys())}.")
-            rng_key, self.resources, x = self.strategies[strategy](rng_key, self.resources, x, data)
+            with nvtx_range(strategy):
+                rng_key, self.resources, x = self.strategies[strategy](rng_key, self.resources, x, data)
         return rng_key, x
 
     def sample(self, initial_position, data: dict, cuda_graph: bool = False):

@@ -1,4 +1,4 @@
-"""CUDA-event timing of the sampler's phases.
+"""CUDA-event timing of the sampler's phases, and NVTX ranges.
 
 Strategies wrap their fused launches in ``region(name)``; when a Profiler is
 active the region records a start/stop event pair on the launching stream
@@ -6,14 +6,37 @@ active the region records a start/stop event pair on the launching stream
 graph, so that a replay times the same regions), otherwise it costs
 nothing. ``Profiler.totals_ms()`` synchronises once at
 the end and sums the device time per region.
+
+With ``set_nvtx(True)`` (or FLOWMC_NVTX=1 in the environment) every region
+and every strategy call of ``Sampler`` is also an NVTX range, so a timeline
+profiler shows the schedule by name; off by default.
 """
 from __future__ import annotations
 
 import contextlib
+import os
 
 import torch
 
 _active = None
+_nvtx = os.environ.get("FLOWMC_NVTX", "") not in ("", "0")
+
+
+def set_nvtx(enabled: bool) -> None:
+    global _nvtx
+    _nvtx = bool(enabled)
+
+
+@contextlib.contextmanager
+def nvtx_range(name: str):
+    if not _nvtx:
+        yield
+        return
+    torch.cuda.nvtx.range_push(name)
+    try:
+        yield
+    finally:
+        torch.cuda.nvtx.range_pop()
 
 
 class Profiler:
@@ -41,6 +64,16 @@ class Profiler:
 
 @contextlib.contextmanager
 def region(name: str, units: float = 0.0):
+    if _nvtx:
+        with nvtx_range(name), _timed(name, units):
+            yield
+        return
+    with _timed(name, units):
+        yield
+
+
+@contextlib.contextmanager
+def _timed(name: str, units: float):
     p = _active
     if p is None:
         yield

@@ -158,3 +158,21 @@ def test_train_model_strategy(cuda):
     assert isinstance(res["model"], MaskedCouplingRQSpline)
     assert torch.isfinite(res["loss"].data).all() and res["loss"].cursor == 10
     st.check_errors()
+
+
+def test_nvtx_ranges_around_strategies_cpu():
+    """With NVTX on, the sampler still runs its strategies in order (the
+    ranges are no-ops without a timeline profiler attached)."""
+    from flowmc_gb300 import profiling
+    from flowmc_gb300.strategy.lambda_function import Lambda
+    seen = []
+    s = Sampler(3, 2, PRNGKey(0), resources={},
+                strategies={"a": Lambda(lambda *a: seen.append("a")), "b": Lambda(lambda *a: seen.append("b"))},
+                strategy_order=["a", "b", "a"])
+    profiling.set_nvtx(True)
+    try:
+        with profiling.region("outer"):
+            s.sample(torch.zeros(2, 3), {})
+    finally:
+        profiling.set_nvtx(False)
+    assert seen == ["a", "b", "a"]
