@@ -176,3 +176,9 @@ def test_nvtx_ranges_around_strategies_cpu():
     finally:
         profiling.set_nvtx(False)
     assert seen == ["a", "b", "a"]
+
+
+def test_sequential_monte_carlo_is_declared_but_not_constructible():
+    from flowmc_gb300.strategy.sequential_monte_carlo import SequentialMonteCarlo
+    with pytest.raises(TypeError):
+        SequentialMonteCarlo()
