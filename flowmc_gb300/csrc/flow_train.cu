@@ -22,6 +22,9 @@ static int64_t a256(int64_t v) { return (v + 255) / 256 * 256; }
 struct TrainWs {
   float *xs, *xa, *cond, *hs, *raw, *graw, *gh0, *gh1, *gcond, *gy, *gxa, *ld, *logp, *part;
   int64_t part_floats;
+  // FP32 path: split-K partials of the weight-gradient GEMMs (K = the batch)
+  float* spart;
+  int64_t spart_floats;
   // fused last-Linear + spline kernels (BF16 path): log-det partials and
   // per-128-row-tile bias-gradient partials; split-K partials of the
   // weight-gradient GEMMs (K = the batch)
@@ -70,6 +73,21 @@ static void carve_train(const FlowGeom& g, int64_t n, bool bf16, void* ws, Train
   if (m < 4096) m = 4096;
   w.part_floats = (int64_t)colsum_blocks(n) * m;
   w.part = take(w.part_floats);
+  w.spart = nullptr;
+  w.spart_floats = 0;
+  if (!bf16) {
+    int64_t mn = 1;
+    for (int l = 0; l < g.L; ++l)
+      for (int i = 0; i <= g.nh; ++i) {
+        const int64_t f = (int64_t)g.lin_out(l, i) * g.lin_in(l, i);
+        if (f > mn) mn = f;
+      }
+    int64_t s = (int64_t)(16 << 20) / mn;   // about 64 MB of partials at most
+    if (s > kKouterMaxSlices) s = kKouterMaxSlices;
+    if (s < 2) s = 2;
+    w.spart_floats = s * mn;
+    w.spart = take(w.spart_floats);
+  }
   w.ldp = w.bpart = w.kpart = w.colpart = nullptr;
   w.kpart_floats = 0;
   w.cond16 = w.condT = w.hs16 = w.hsT = w.graw16 = w.grawT = nullptr;
@@ -467,9 +485,8 @@ int flow_loss_grad(const FmcFlow* f, const float* x, int64_t n, float* loss, flo
       for (int i = g.nh; i >= 0; --i) {
         const int out = g.lin_out(l, i), in = g.lin_in(l, i);
         const float* a_in = (i == 0) ? w.cond : w.hs + (int64_t)(i - 1) * n * g.h_max();
-        // dW = g^T a_in  [out, in]
-        if ((rc = sgemm<false, false, EPI_NONE>(st, out, in, (int)n, gcur, out, a_in, in, nullptr, nullptr, 0,
-                                                gl + g.lin_w(l, i), in, 0.f)))
+        // dW = g^T a_in  [out, in], split along the batch
+        if ((rc = kouter(st, out, in, n, gcur, out, a_in, in, false, w.spart, w.spart_floats, gl + g.lin_w(l, i))))
           return rc;
         if ((rc = colsum(st, gcur, n, out, w.part, gl + g.lin_b(l, i)))) return rc;
         float* gnext = (i == 0) ? w.gcond : gbufs[i & 1];

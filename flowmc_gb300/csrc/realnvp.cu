@@ -48,7 +48,7 @@ static int rnvp_geom(const FmcRealNVP* f, RnvpGeom& g) {
 }
 
 constexpr int64_t kRnvpChunk = 65536;   // rows per inference chunk
-constexpr int kMaxSlices = 64;         // split-K slices of the weight gradients
+constexpr int kMaxSlices = kKouterMaxSlices;   // split-K slices of the weight gradients
 
 static int grid_for(int64_t tot, int per_sm = 8) {
   int64_t b = (tot + 255) / 256;
@@ -164,90 +164,6 @@ __global__ void k_rnvp_loss(const float* __restrict__ logp, int64_t n, float* __
 __global__ void k_rnvp_scale(const float* __restrict__ y, int64_t tot, float c, float* __restrict__ out) {
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x)
     out[e] = y[e] * c;
-}
-
-// part[z][i][j] = sum over rows k of slice z of A[k*lda + i] * B[k*ldb + j]
-// (ONES: B = 1, N = 1 -- column sums). 64 x 64 tiles, 16 rows per step.
-template <bool ONES>
-__global__ void __launch_bounds__(256) k_sgemm_kouter(int M, int N, int64_t K, int64_t kslice,
-                                                      const float* __restrict__ A, int64_t lda,
-                                                      const float* __restrict__ B, int64_t ldb,
-                                                      float* __restrict__ part) {
-  constexpr int BM = 64, BN = 64, BK = 16;
-  __shared__ __align__(16) float As[BK][BM + 4];
-  __shared__ __align__(16) float Bs[BK][BN + 4];
-  const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
-  const int i0 = blockIdx.y * BM, j0 = blockIdx.x * BN;
-  const int64_t kb = (int64_t)blockIdx.z * kslice;
-  const int64_t ke = (kb + kslice < K) ? kb + kslice : K;
-  float acc[4][4] = {};
-  for (int64_t k0 = kb; k0 < ke; k0 += BK) {
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const int e = tid + r * 256;
-      const int kk = e / BM, ii = e % BM;
-      const int64_t gk = k0 + kk;
-      As[kk][ii] = (gk < ke && i0 + ii < M) ? A[gk * lda + i0 + ii] : 0.f;
-      float b = 0.f;
-      if (gk < ke && j0 + ii < N) b = ONES ? 1.f : B[gk * ldb + j0 + ii];
-      Bs[kk][ii] = b;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < BK; ++kk) {
-      const float4 a = *reinterpret_cast<const float4*>(&As[kk][ty * 4]);
-      const float4 b = *reinterpret_cast<const float4*>(&Bs[kk][tx * 4]);
-      const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int w = 0; w < 4; ++w) acc[u][w] = fmaf(av[u], bv[w], acc[u][w]);
-    }
-    __syncthreads();
-  }
-  float* out = part + (int64_t)blockIdx.z * M * N;
-#pragma unroll
-  for (int u = 0; u < 4; ++u) {
-    const int gi = i0 + ty * 4 + u;
-    if (gi >= M) continue;
-#pragma unroll
-    for (int w = 0; w < 4; ++w) {
-      const int gj = j0 + tx * 4 + w;
-      if (gj < N) out[(int64_t)gi * N + gj] = acc[u][w];
-    }
-  }
-}
-
-__global__ void k_sum_slices(const float* __restrict__ part, int S, int64_t mn, float* __restrict__ out) {
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < mn; e += (int64_t)gridDim.x * blockDim.x) {
-    float s = 0.f;
-    for (int z = 0; z < S; ++z) s += part[(int64_t)z * mn + e];
-    out[e] = s;
-  }
-}
-
-// out [M, N] = A^T B over K rows (A [K, lda], B [K, ldb]); ones: column sums of A
-static int kouter(cudaStream_t st, int M, int N, int64_t K, const float* A, int64_t lda, const float* B, int64_t ldb,
-                  bool ones, float* part, int64_t part_floats, float* out) {
-  const int64_t tiles = (int64_t)((N + 63) / 64) * ((M + 63) / 64);
-  int64_t S = (2 * (int64_t)sm_count() + tiles - 1) / tiles;
-  const int64_t by_rows = (K + 255) / 256;   // at least 256 rows per slice
-  if (S > by_rows) S = by_rows;
-  if (S > kMaxSlices) S = kMaxSlices;
-  if (S * M * N > part_floats) S = part_floats / ((int64_t)M * N);
-  if (S < 1) S = 1;
-  const int64_t kslice = (((K + S - 1) / S) + 15) / 16 * 16;
-  S = (K + kslice - 1) / kslice;
-  if (S < 1) S = 1;
-  dim3 grid((unsigned)((N + 63) / 64), (unsigned)((M + 63) / 64), (unsigned)S);
-  if (ones)
-    k_sgemm_kouter<true><<<grid, 256, 0, st>>>(M, N, K, kslice, A, lda, nullptr, 0, part);
-  else
-    k_sgemm_kouter<false><<<grid, 256, 0, st>>>(M, N, K, kslice, A, lda, B, ldb, part);
-  FMC_LAUNCH_CHECK();
-  k_sum_slices<<<grid_for((int64_t)M * N), 256, 0, st>>>(part, (int)S, (int64_t)M * N, out);
-  FMC_LAUNCH_CHECK();
-  return FMC_OK;
 }
 
 // ------------------------------------------------------------------ layer passes
