@@ -63,6 +63,18 @@ WORKLOADS = {
 }
 
 
+def mixture_means():
+    """The 64-D mixture's four means: +/-4 along the first two columns of a
+    Haar-random orthogonal matrix (QR of a Gaussian matrix with the sign fix,
+    seed 3)."""
+    import numpy as np
+    rng = np.random.default_rng(3)
+    Q, R = np.linalg.qr(rng.normal(size=(64, 64)))
+    Q = Q * np.sign(np.diag(R))
+    u1, u2 = Q[:, 0], Q[:, 1]
+    return np.stack([4 * u1, -4 * u1, 4 * u2, -4 * u2])
+
+
 def make_target(name, w, device):
     import numpy as np
     from flowmc_gb300 import targets as TG
@@ -75,12 +87,7 @@ def make_target(name, w, device):
         t = TG.DualMoon(w["d"], device=device)
         mean, var = dual_moon_moments(w["d"], **t.p)
         return t, mean, var
-    rng = np.random.default_rng(3)
-    Q, R = np.linalg.qr(rng.normal(size=(64, 64)))
-    Q = Q * np.sign(np.diag(R))
-    u1, u2 = Q[:, 0], Q[:, 1]
-    means = np.stack([4 * u1, -4 * u1, 4 * u2, -4 * u2])
-    t = TG.GaussianMixture(means, 0.5, device=device)
+    t = TG.GaussianMixture(mixture_means(), 0.5, device=device)
     mu, cov = t.mean_cov()
     return t, mu, np.diag(cov)
 
@@ -559,9 +566,7 @@ def cpu_baseline(name, w, budget_s: float = 20.0):
     elif name == "dualmoon5":
         t = {"kind": "dual_moon", "n_dim": d, "r0": 2.0, "sr": 0.1, "mu": 3.0, "s0": 0.6}
     else:
-        Q, R = np.linalg.qr(rng.normal(size=(64, 64)))
-        means = np.stack([4 * Q[:, 0], -4 * Q[:, 0], 4 * Q[:, 1], -4 * Q[:, 1]])
-        t = {"kind": "mixture", "mean": means, "inv_var": np.full((4, 64), 2.0),
+        t = {"kind": "mixture", "mean": mixture_means(), "inv_var": np.full((4, 64), 2.0),
              "log_w": np.full(4, np.log(0.25) - 32 * np.log(2 * np.pi * 0.5))}
     P = 3 * w["n_bins"] + 1
     layers = []
