@@ -56,12 +56,14 @@ class TakeSteps(Strategy):
     def _buffers(self, resources):
         state = resources[self.state_name]
         assert isinstance(state, State), "State resource must be a State"
+        # the reference's checks and messages (take_steps.py:74-97)
+        kinds = ("Position", "Log probability", "Acceptance")
         names = [state.data[b] for b in self.buffer_names[:3]]
-        for n in names:
-            assert isinstance(n, str), "Buffer resource name must be a string"
+        for k, n in zip(kinds, names):
+            assert isinstance(n, str), f"{k} buffer resource name must be a string"
         bufs = [resources[n] for n in names]
-        for b in bufs:
-            assert isinstance(b, Buffer), "Buffer resource must be a Buffer"
+        for k, b in zip(kinds, bufs):
+            assert isinstance(b, Buffer), f"{k} buffer resource must be a Buffer"
             assert b.cursor_dim == 1, "chain buffers are written along axis 1"
         return bufs
 

@@ -182,3 +182,23 @@ def test_sequential_monte_carlo_is_declared_but_not_constructible():
     from flowmc_gb300.strategy.sequential_monte_carlo import SequentialMonteCarlo
     with pytest.raises(TypeError):
         SequentialMonteCarlo()
+
+
+def test_take_steps_checks_its_resources_cpu():
+    """take_steps.py:74-97: the State and Buffer checks and their messages."""
+    from flowmc_gb300.resource.buffers import Buffer
+    from flowmc_gb300.resource.kernel.MALA import MALA
+    from flowmc_gb300.resource.states import State
+    from flowmc_gb300.strategy.take_steps import TakeSerialSteps
+    st = TakeSerialSteps("logpdf", "MALA", "state", ["p", "l", "a"], n_steps=2)
+    res = {"MALA": MALA(0.1), "state": {"p": "p"}}
+    with pytest.raises(AssertionError, match="State resource must be a State"):
+        st(PRNGKey(0), res, torch.zeros(2, 3), {})
+    res["state"] = State({"p": "p", "l": 3, "a": "a"}, name="state")
+    with pytest.raises(AssertionError, match="Log probability buffer resource name must be a string"):
+        st(PRNGKey(0), res, torch.zeros(2, 3), {})
+    res["state"] = State({"p": "p", "l": "l", "a": "a"}, name="state")
+    res.update({"p": Buffer("p", (2, 4, 3), 1, device="cpu"), "l": Buffer("l", (2, 4), 1, device="cpu"),
+                "a": "not a buffer"})
+    with pytest.raises(AssertionError, match="Acceptance buffer resource must be a Buffer"):
+        st(PRNGKey(0), res, torch.zeros(2, 3), {})
