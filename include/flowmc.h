@@ -36,7 +36,7 @@ extern "C" {
 enum {
   FMC_OK = 0,
   FMC_ERR_INVALID_ARG = 1,    /* bad pointer / shape / value            */
-  FMC_ERR_UNSUPPORTED = 2,    /* shape or option this build cannot run  */
+  FMC_ERR_UNSUPPORTED = 2,    /* shape or option the library does not run */
   FMC_ERR_CUDA = 3,           /* a CUDA runtime call failed             */
   FMC_ERR_TIMEOUT = 4,        /* a bounded device wait ran out          */
   FMC_ERR_NONFINITE = 5       /* non-finite value where one is forbidden */

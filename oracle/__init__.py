@@ -6,8 +6,8 @@ is an explicit input array, so the CUDA path and the oracle consume the same
 normals and uniforms.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline
-leg may import this package, and only as the checker (or the timed CPU
-baseline); the product path (``flowmc_gb300``) never does.
+leg may import this package, and only to check results against it (or as
+the timed CPU baseline); the product path (``flowmc_gb300``) never does.
 
 Pinning: the reference's own tests hold no numeric golden vectors, only
 known-answer/statistical pins (acceptance -> 1 at tiny steps, N(0, I)
