@@ -18,6 +18,20 @@ def _unavailable(*a, **k):
     raise NotImplementedError("not available in the golden-fixture stand-in")
 
 
+def is_array(x):
+    return hasattr(x, "shape")
+
+
+def partition(tree, pred):
+    """The golden script passes the stacked layers as a plain list of
+    per-layer modules: everything is 'dynamic', nothing is static."""
+    return tree, None
+
+
+def combine(dynamic, static):
+    return dynamic
+
+
 nn = types.SimpleNamespace(Linear=_unavailable, Sequential=_unavailable)
-tree_at = filter_vmap = partition = combine = is_array = apply_updates = _unavailable
+tree_at = filter_vmap = apply_updates = _unavailable
 tree_serialise_leaves = tree_deserialise_leaves = _unavailable

@@ -10,13 +10,15 @@ def _stack(ys):
     return torch.stack([torch.as_tensor(y, dtype=torch.float64) for y in ys])
 
 
-def scan(f, init, xs=None, length=None):
+def scan(f, init, xs=None, length=None, reverse=False):
     carry = init
     ys = []
-    it = xs if xs is not None else range(length)
-    for x in it:
+    it = list(xs) if xs is not None else list(range(length))
+    for x in (reversed(it) if reverse else it):
         carry, y = f(carry, x)
         ys.append(y)
+    if reverse:
+        ys.reverse()
     return carry, _stack(ys) if ys else None
 
 

@@ -143,6 +143,10 @@ def eye(n, dtype=None):
     return torch.eye(n, dtype=dtype or _DT)
 
 
+def atleast_2d(x):
+    return torch.atleast_2d(_t(x))
+
+
 def diag(x):
     return torch.diag(_t(x))
 

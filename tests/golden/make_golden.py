@@ -38,7 +38,8 @@ from flowMC.resource.model.nf_model.rqSpline import RQSpline  # noqa: E402
 from flowMC.resource.logPDF import TemperedPDF  # noqa: E402
 from flowMC.strategy.parallel_tempering import ParallelTempering  # noqa: E402
 from flowMC.strategy.optimization import AdamOptimization  # noqa: E402
-from flowMC.resource.model.common import MLP, MLPAffine, MaskedCouplingLayer  # noqa: E402
+from flowMC.resource.model.common import MLP, MLPAffine, MaskedCouplingLayer, ScalarAffine, Gaussian  # noqa: E402
+from flowMC.resource.model.nf_model.rqSpline import MaskedCouplingRQSpline  # noqa: E402
 from flowMC.resource.model.nf_model.realNVP import RealNVP  # noqa: E402
 import jax  # noqa: E402
 
@@ -120,6 +121,7 @@ class _Linear:
 
     def __init__(self, W, b):
         self.weight, self.bias = torch.tensor(W), torch.tensor(b)
+        self.out_features, self.in_features = self.weight.shape
 
     def __call__(self, x):
         return self.weight @ x + self.bias
@@ -131,6 +133,38 @@ def _mlp(W1, b1, W2, b2):
     m = object.__new__(MLP)
     m.layers = [_Linear(W1, b1), jax.nn.relu, _Linear(W2, b2)]
     return m
+
+
+def _mlp_tanh(Ws, bs):
+    """The reference's MLP object (common.py:68-112) with given weights and
+    tanh between the Linears, as MaskedCouplingRQSpline builds it."""
+    m = object.__new__(MLP)
+    m.layers = []
+    for i, (W, b) in enumerate(zip(Ws, bs)):
+        m.layers.append(_Linear(W, b))
+        if i < len(Ws) - 1:
+            m.layers.append(jax.nn.tanh)
+    return m
+
+
+def _rqspline_flow(layers, n_bins, mean, var, d):
+    """A MaskedCouplingRQSpline whose attributes are set directly
+    (rqSpline.py:392-443 without Equinox's stacking): per layer the pair
+    [MaskedCouplingLayer(ScalarAffine(scale, shift), 0), MaskedCouplingLayer(
+    RQSpline(MLP), mask)] of the reference's own classes, the base
+    Gaussian(0, I), data_mean and diag data_cov. Masks are float 0/1, which
+    the reference's bool masks promote to in (1 - mask) and x * mask."""
+    flow = object.__new__(MaskedCouplingRQSpline)
+    flow.layers = []
+    for L in layers:
+        spline = RQSpline(_mlp_tanh(L["W"], L["b"]), -10.0, 10.0)
+        flow.layers.append([MaskedCouplingLayer(ScalarAffine(L["scale"], L["shift"]), torch.zeros(d, dtype=torch.float64)),
+                            MaskedCouplingLayer(spline, torch.tensor(L["mask"], dtype=torch.float64))])
+    flow.base_dist = Gaussian(torch.zeros(d, dtype=torch.float64), torch.eye(d, dtype=torch.float64), learnable=False)
+    flow._data_mean = torch.tensor(mean)
+    flow._data_cov = torch.diag(torch.tensor(var))
+    flow._n_features = d
+    return flow
 
 
 class _RealNVPStandIn:
@@ -344,6 +378,41 @@ def main():
         out[f"{name}/inv_x"], out[f"{name}/inv_logdet"] = np.stack(iy), np.array(ild)
         out[f"{name}/log_prob"] = np.array(lp)
         cases.append({"name": name, "kind": "realnvp", "n_dim": d, "n_layers": L, "n_hidden": H})
+    # MaskedCouplingRQSpline: the reference's forward, inverse (its layer and
+    # ScalarAffine order) and log_prob (standardisation, base Gaussian) on
+    # fixed weights with non-zero ScalarAffine scale and shift; inputs reach
+    # both spline tails
+    for name, d, L, hidden, K in (("rqsflow_d5", 5, 3, [8, 8], 4), ("rqsflow_d6", 6, 2, [12], 5)):
+        P = 3 * K + 1
+        layers = []
+        for l in range(L):
+            shape = [d] + hidden + [d * P]
+            layers.append({"W": [rng.normal(size=(b, a)) * 0.6 for a, b in zip(shape[:-1], shape[1:])],
+                           "b": [rng.normal(size=b) * 0.3 for b in shape[1:]],
+                           "scale": float(rng.normal() * 0.3), "shift": float(rng.normal() * 0.5),
+                           "mask": ((np.arange(d) + l) % 2).astype(np.float64)})
+        mean, var = rng.normal(size=d) * 0.5, rng.uniform(0.5, 2.0, size=d)
+        flow = _rqspline_flow(layers, K, mean, var, d)
+        x = rng.normal(size=(9, d)) * 4.0
+        x[0, 0], x[1, 1] = 30.0, -30.0          # beyond the spline range after standardising
+        fy, fld, iy, ild, lp = [], [], [], [], []
+        for row in x:
+            y, ld = MaskedCouplingRQSpline.forward(flow, torch.tensor(row))
+            fy.append(y.numpy()), fld.append(float(ld))
+            xi, ldi = MaskedCouplingRQSpline.inverse(flow, torch.tensor(row))
+            iy.append(xi.numpy()), ild.append(float(ldi))
+            lp.append(float(MaskedCouplingRQSpline.log_prob(flow, torch.tensor(row))))
+        out[f"{name}/x"] = x
+        out[f"{name}/mean"], out[f"{name}/var"] = mean, var
+        for l, Ld in enumerate(layers):
+            for i, (W, b) in enumerate(zip(Ld["W"], Ld["b"])):
+                out[f"{name}/W{l}_{i}"], out[f"{name}/b{l}_{i}"] = W, b
+        out[f"{name}/scale"] = np.array([Ld["scale"] for Ld in layers])
+        out[f"{name}/shift"] = np.array([Ld["shift"] for Ld in layers])
+        out[f"{name}/fwd_y"], out[f"{name}/fwd_logdet"] = np.stack(fy), np.array(fld)
+        out[f"{name}/inv_x"], out[f"{name}/inv_logdet"] = np.stack(iy), np.array(ild)
+        out[f"{name}/log_prob"] = np.array(lp)
+        cases.append({"name": name, "kind": "rqsflow", "n_dim": d, "n_layers": L, "hidden": hidden, "n_bins": K})
     for c in cases:
         if c["kind"] in ("mala", "hmc", "grw"):
             print(f"{c['name']}: acceptance {out[c['name'] + '/acc'].mean():.2f}")
