@@ -21,3 +21,11 @@ def cuda():
     from flowmc_gb300 import _lib
     _lib.lib()
     return torch.device("cuda")
+
+
+@pytest.fixture(autouse=True)
+def _seed_torch():
+    """Every test starts from the same torch generator state (CPU and CUDA),
+    so inputs drawn with torch.randn are the same on every run."""
+    import torch
+    torch.manual_seed(0)
