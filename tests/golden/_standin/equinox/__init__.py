@@ -32,6 +32,19 @@ def combine(dynamic, static):
     return dynamic
 
 
+def filter_vmap(f=None, **kw):
+    """Maps f over the leading axis of its first argument (the golden script
+    only vmaps functions of one batch of rows)."""
+    import torch
+
+    def vf(x, *args):
+        outs = [f(row, *args) for row in x]
+        if isinstance(outs[0], tuple):
+            return tuple(torch.stack([torch.as_tensor(o[k]) for o in outs]) for k in range(len(outs[0])))
+        return torch.stack([torch.as_tensor(o) for o in outs])
+    return vf
+
+
 nn = types.SimpleNamespace(Linear=_unavailable, Sequential=_unavailable)
-tree_at = filter_vmap = apply_updates = _unavailable
+tree_at = apply_updates = _unavailable
 tree_serialise_leaves = tree_deserialise_leaves = _unavailable

@@ -13,7 +13,12 @@ def _stack(ys):
 def scan(f, init, xs=None, length=None, reverse=False):
     carry = init
     ys = []
-    it = list(xs) if xs is not None else list(range(length))
+    if xs is None:
+        it = list(range(length))
+    elif isinstance(xs, tuple):
+        it = list(zip(*xs))     # a tuple of arrays scans over their leading axis together
+    else:
+        it = list(xs)           # an array, or the golden script's list of per-layer modules
     for x in (reversed(it) if reverse else it):
         carry, y = f(carry, x)
         ys.append(y)

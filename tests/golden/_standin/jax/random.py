@@ -35,3 +35,12 @@ def normal(key, shape=(), dtype=None):
 
 def uniform(key, shape=(), dtype=None, minval=0.0, maxval=1.0):
     return _draw(key, shape)
+
+
+def multivariate_normal(key, mean, cov, shape=(), dtype=None):
+    """mean + z @ cholesky(cov).T with the scripted standard normals z
+    (jax.random.multivariate_normal's default Cholesky method)."""
+    mean = torch.as_tensor(mean, dtype=torch.float64)
+    cov = torch.as_tensor(cov, dtype=torch.float64)
+    z = _draw(key, tuple(shape) + (mean.shape[-1],))
+    return mean + z @ torch.linalg.cholesky(cov).T

@@ -3,7 +3,11 @@
 Runs flowMC v0.4.5's MALA, HMC and GaussianRandomWalk kernels
 (resource/kernel/MALA.py:26-89, HMC.py:98-151, Gaussian_random_walk.py:25-61),
 its RQSpline bijection (knots, forward and inverse:
-resource/model/nf_model/rqSpline.py:20-239, 296-362) and its
+resource/model/nf_model/rqSpline.py:20-239, 296-362), the whole
+MaskedCouplingRQSpline (rqSpline.py:450-504), NFProposal.kernel with its
+batched and unbatched proposal draws (resource/kernel/NF_proposal.py:27-172),
+RealNVP's layers (nf_model/realNVP.py:180-222), AdamOptimization.optimize
+(strategy/optimization.py:85-164) and its
 ParallelTempering ensemble step, exchange sweep and temperature adaptation
 (strategy/parallel_tempering.py:205-436, on resource/logPDF.py's TemperedPDF)
 on scripted normals and uniforms, and saves inputs and outputs to ``reference_vectors.npz`` beside
@@ -40,6 +44,7 @@ from flowMC.strategy.parallel_tempering import ParallelTempering  # noqa: E402
 from flowMC.strategy.optimization import AdamOptimization  # noqa: E402
 from flowMC.resource.model.common import MLP, MLPAffine, MaskedCouplingLayer, ScalarAffine, Gaussian  # noqa: E402
 from flowMC.resource.model.nf_model.rqSpline import MaskedCouplingRQSpline  # noqa: E402
+from flowMC.resource.kernel.NF_proposal import NFProposal  # noqa: E402
 from flowMC.resource.model.nf_model.realNVP import RealNVP  # noqa: E402
 import jax  # noqa: E402
 
@@ -413,7 +418,66 @@ def main():
         out[f"{name}/inv_x"], out[f"{name}/inv_logdet"] = np.stack(iy), np.array(ild)
         out[f"{name}/log_prob"] = np.array(lp)
         cases.append({"name": name, "kind": "rqsflow", "n_dim": d, "n_layers": L, "hidden": hidden, "n_bins": K})
+    # NFProposal.kernel (NF_proposal.py:27-172) per chain on a 5-D dual moon
+    # with a MaskedCouplingRQSpline proposal: once with the proposals drawn in
+    # one batch, once through sample_flow's batched scan (n_batch_size 3 for
+    # 7 steps: three draws of 3 rows, the last two rows dropped) and the
+    # chunked target evaluation. The normals each chain's proposals start
+    # from are saved as the [S, d] rows the proposals use.
+    t_nf = targets["dual_moon5"]
+    for name, bs in (("nfprop_dual_moon5", 100), ("nfprop_dual_moon5_batched", 3)):
+        d, L, hidden, K, C, S = 5, 2, [8], 6, 3, 7
+        P = 3 * K + 1
+        layers = []
+        for l in range(L):
+            shape = [d] + hidden + [d * P]
+            layers.append({"W": [rng.normal(size=(b, a)) * 0.3 for a, b in zip(shape[:-1], shape[1:])],
+                           "b": [rng.normal(size=b) * 0.2 for b in shape[1:]],
+                           "scale": float(0.35 + 0.05 * rng.normal()), "shift": float(0.1 * rng.normal()),
+                           "mask": ((np.arange(d) + l) % 2).astype(np.float64)})
+        mean, var = rng.normal(size=d) * 0.2, rng.uniform(0.8, 1.5, size=d)
+        flow = _rqspline_flow(layers, K, mean, var, d)
+        prop = object.__new__(NFProposal)
+        prop.model, prop.n_batch_size = flow, bs
+        f = jnp_target(t_nf)
+        # chains start far outside the target's shell, so proposals nearer it
+        # are accepted and the accept/reject mix is not one-sided
+        x0 = rng.normal(size=(C, d)) * 4.0
+        unif = rng.uniform(size=(C, S))
+        z_used = np.empty((C, S, d))
+        pos, lps, accs = [], [], []
+        for c in range(C):
+            if S > bs:
+                n_batch = -(-S // bs)
+                n_sample = -(-S // n_batch)
+                zb = rng.normal(size=(n_batch, n_sample, d))
+                for b in range(n_batch):
+                    jr.DRAWS[f"nf{name}{c}.1" + ".0" * b + ".1"] = zb[b]
+                z_used[c] = zb.reshape(-1, d)[:S]
+            else:
+                z_used[c] = rng.normal(size=(S, d))
+                jr.DRAWS[f"nf{name}{c}.1"] = z_used[c]
+            for s in range(S):
+                jr.DRAWS[f"nf{name}{c}.0" + ".0" * s + ".1"] = unif[c, s]
+            xc = torch.tensor(x0[c])
+            lp0 = f(xc, None)                                         # take_steps.py:200-206
+            px, plp, pacc = prop.kernel(jr.Key(f"nf{name}{c}"), xc, lp0, f, {"n_steps": S})
+            pos.append(torch.as_tensor(px).detach().numpy())
+            lps.append(torch.as_tensor(plp).detach().numpy())
+            accs.append(torch.as_tensor(pacc, dtype=torch.float64).numpy())
+        out[f"{name}/x0"], out[f"{name}/z"], out[f"{name}/unif"] = x0, z_used, unif
+        out[f"{name}/mean"], out[f"{name}/var"] = mean, var
+        for l, Ld in enumerate(layers):
+            for i, (W, b) in enumerate(zip(Ld["W"], Ld["b"])):
+                out[f"{name}/W{l}_{i}"], out[f"{name}/b{l}_{i}"] = W, b
+        out[f"{name}/scale"] = np.array([Ld["scale"] for Ld in layers])
+        out[f"{name}/shift"] = np.array([Ld["shift"] for Ld in layers])
+        out[f"{name}/pos"], out[f"{name}/logp"], out[f"{name}/acc"] = np.stack(pos), np.stack(lps), np.stack(accs)
+        cases.append({"name": name, "kind": "nfproposal", "target": t_nf, "n_dim": d, "n_layers": L,
+                      "hidden": hidden, "n_bins": K, "n_batch_size": bs})
     for c in cases:
+        if c["kind"] == "nfproposal":
+            print(f"{c['name']}: acceptance {out[c['name'] + '/acc'].mean():.2f}")
         if c["kind"] in ("mala", "hmc", "grw"):
             print(f"{c['name']}: acceptance {out[c['name'] + '/acc'].mean():.2f}")
         if c["kind"] == "pt":

@@ -166,3 +166,25 @@ def test_cuda_flow_matches_reference_source(cuda, case):
     close(xi, z[f"{n}/inv_x"])
     close(ldi, z[f"{n}/inv_logdet"])
     close(m.log_prob(xt), z[f"{n}/log_prob"])
+
+
+def _nfprop_cases():
+    _, cases = _load()
+    return [c for c in cases if c["kind"] == "nfproposal"]
+
+
+@pytest.mark.parametrize("case", _nfprop_cases(), ids=lambda c: c["name"])
+def test_oracle_nf_proposal_matches_reference_source(case):
+    """The reference's NFProposal.kernel (NF_proposal.py:27-172) per chain,
+    including sample_flow's batched scan and the chunked target evaluation:
+    fed the same base normals (the rows the proposals use) and uniforms, the
+    oracle's whole-batch global step gives the same accepts, positions and
+    log-densities."""
+    z, _ = _load()
+    n = case["name"]
+    fl = F.Flow(_flow_layers(z, case), case["n_bins"], z[f"{n}/mean"], np.diag(z[f"{n}/var"]))
+    pos, lp, acc = K.nf_proposal_kernel(fl, case["target"], z[f"{n}/x0"], z[f"{n}/z"], z[f"{n}/unif"])
+    np.testing.assert_array_equal(acc, z[f"{n}/acc"])
+    np.testing.assert_allclose(pos, z[f"{n}/pos"], rtol=1e-10, atol=1e-10)
+    np.testing.assert_allclose(lp, z[f"{n}/logp"], rtol=1e-10, atol=1e-10)
+    assert 0 < z[f"{n}/acc"].mean() < 1
