@@ -4,7 +4,9 @@ Runs flowMC v0.4.5's MALA, HMC and GaussianRandomWalk kernels
 (resource/kernel/MALA.py:26-89, HMC.py:98-151, Gaussian_random_walk.py:25-61),
 its RQSpline bijection (knots, forward and inverse:
 resource/model/nf_model/rqSpline.py:20-239, 296-362), the whole
-MaskedCouplingRQSpline (rqSpline.py:450-504), NFProposal.kernel with its
+MaskedCouplingRQSpline (rqSpline.py:450-504), TakeSerialSteps.__call__ with
+thinning into the reference's Buffers over several calls
+(strategy/take_steps.py:60-180, resource/buffers.py:24-41), NFProposal.kernel with its
 batched and unbatched proposal draws (resource/kernel/NF_proposal.py:27-172),
 RealNVP's layers (nf_model/realNVP.py:180-222), AdamOptimization.optimize
 (strategy/optimization.py:85-164) and its
@@ -45,6 +47,9 @@ from flowMC.strategy.optimization import AdamOptimization  # noqa: E402
 from flowMC.resource.model.common import MLP, MLPAffine, MaskedCouplingLayer, ScalarAffine, Gaussian  # noqa: E402
 from flowMC.resource.model.nf_model.rqSpline import MaskedCouplingRQSpline  # noqa: E402
 from flowMC.resource.kernel.NF_proposal import NFProposal  # noqa: E402
+from flowMC.resource.buffers import Buffer  # noqa: E402
+from flowMC.resource.states import State  # noqa: E402
+from flowMC.strategy.take_steps import TakeSerialSteps  # noqa: E402
 from flowMC.resource.model.nf_model.realNVP import RealNVP  # noqa: E402
 import jax  # noqa: E402
 
@@ -475,6 +480,40 @@ def main():
         out[f"{name}/pos"], out[f"{name}/logp"], out[f"{name}/acc"] = np.stack(pos), np.stack(lps), np.stack(accs)
         cases.append({"name": name, "kind": "nfproposal", "target": t_nf, "n_dim": d, "n_layers": L,
                       "hidden": hidden, "n_bins": K, "n_batch_size": bs})
+    # TakeSerialSteps.__call__ (take_steps.py:60-180) with MALA and thinning 3
+    # over 7 steps, called three times into the reference's Buffers of 6 rows:
+    # each call writes ceil(7/3) = 3 rows but advances the cursor by 7 // 3 = 2,
+    # and the third call's start (4) is clamped to 3 by the buffer update
+    name, S, thin, n_calls, R = "takesteps_mala_thin3", 7, 3, 3, 6
+    t = targets["dual_moon5"]
+    C, d = 3, 5
+    f = jnp_target(t)
+    res = {"MALA": MALA(0.2), "logpdf": f,
+           "p": Buffer("p", (C, R, d), 1), "l": Buffer("l", (C, R), 1), "a": Buffer("a", (C, R), 1),
+           "state": State({"p": "p", "l": "l", "a": "a"}, name="state")}
+    strat = TakeSerialSteps("logpdf", "MALA", "state", ["p", "l", "a"], n_steps=S, thinning=thin)
+    x = torch.tensor(rng.normal(size=(C, d)) * 1.5)
+    x0 = x.numpy().copy()
+    noise = rng.normal(size=(n_calls, C, S, d))
+    unif = rng.uniform(size=(n_calls, C, S))
+    lasts, cursors = [], []
+    for k in range(n_calls):
+        for c in range(C):
+            for s in range(S):
+                path = f"ts{k}.1.{c}" + ".0" * s + ".1"
+                jr.DRAWS[path + ".0"] = noise[k, c, s]
+                jr.DRAWS[path + ".1"] = unif[k, c, s]
+        _, res, x = strat(jr.Key(f"ts{k}"), res, x, None)
+        x = torch.as_tensor(x).detach()
+        lasts.append(x.numpy().copy())
+        cursors.append(strat.current_position)
+    out[f"{name}/x0"], out[f"{name}/noise"], out[f"{name}/unif"] = x0, noise, unif
+    out[f"{name}/pos_buf"] = torch.as_tensor(res["p"].data).numpy()
+    out[f"{name}/logp_buf"] = torch.as_tensor(res["l"].data).numpy()
+    out[f"{name}/acc_buf"] = torch.as_tensor(res["a"].data).numpy()
+    out[f"{name}/last"], out[f"{name}/cursor"] = np.stack(lasts), np.array(cursors)
+    cases.append({"name": name, "kind": "takesteps", "local": "mala", "target": t, "step_size": 0.2,
+                  "n_steps": S, "thinning": thin, "n_calls": n_calls, "buf_rows": R})
     for c in cases:
         if c["kind"] == "nfproposal":
             print(f"{c['name']}: acceptance {out[c['name'] + '/acc'].mean():.2f}")

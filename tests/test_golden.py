@@ -188,3 +188,35 @@ def test_oracle_nf_proposal_matches_reference_source(case):
     np.testing.assert_allclose(pos, z[f"{n}/pos"], rtol=1e-10, atol=1e-10)
     np.testing.assert_allclose(lp, z[f"{n}/logp"], rtol=1e-10, atol=1e-10)
     assert 0 < z[f"{n}/acc"].mean() < 1
+
+
+def _takesteps_cases():
+    _, cases = _load()
+    return [c for c in cases if c["kind"] == "takesteps"]
+
+
+@pytest.mark.parametrize("case", _takesteps_cases(), ids=lambda c: c["name"])
+def test_oracle_take_steps_buffers_match_reference_source(case):
+    """The reference's TakeSerialSteps.__call__ and Buffer.update_buffer over
+    several calls with thinning: rows written per call (ceil(S / thinning)),
+    the cursor advanced by S // thinning, the clamped start of the last call,
+    and the returned last positions."""
+    z, _ = _load()
+    n = case["name"]
+    S, thin, R = case["n_steps"], case["thinning"], case["buf_rows"]
+    x = z[f"{n}/x0"]
+    C, d = x.shape
+    pos_buf, lp_buf, acc_buf = np.full((C, R, d), -np.inf), np.full((C, R), -np.inf), np.full((C, R), -np.inf)
+    cursor = 0
+    for k in range(case["n_calls"]):
+        pos, lps, accs, x = K.take_serial_steps(case["local"], case["target"], x, S, z[f"{n}/noise"][k],
+                                                z[f"{n}/unif"][k], step_size=case["step_size"], thinning=thin)
+        pos_buf = K.buffer_update(pos_buf, pos, cursor, 1)
+        lp_buf = K.buffer_update(lp_buf, lps, cursor, 1)
+        acc_buf = K.buffer_update(acc_buf, accs, cursor, 1)
+        cursor += S // thin
+        assert cursor == z[f"{n}/cursor"][k]
+        np.testing.assert_allclose(x, z[f"{n}/last"][k], rtol=1e-10, atol=1e-10)
+    np.testing.assert_array_equal(acc_buf, z[f"{n}/acc_buf"])
+    np.testing.assert_allclose(pos_buf, z[f"{n}/pos_buf"], rtol=1e-10, atol=1e-10)
+    np.testing.assert_allclose(lp_buf, z[f"{n}/logp_buf"], rtol=1e-10, atol=1e-10)
