@@ -54,6 +54,10 @@ def tanh(x):
     return torch.tanh(_t(x))
 
 
+def isfinite(x):
+    return torch.isfinite(_t(x))
+
+
 def isinf(x):
     return torch.isinf(_t(x))
 

@@ -37,6 +37,12 @@ def uniform(key, shape=(), dtype=None, minval=0.0, maxval=1.0):
     return _draw(key, shape)
 
 
+def choice(key, a, shape=(), replace=True, p=None):
+    """The scripted indices into a (with replacement)."""
+    idx = torch.as_tensor(DRAWS[key.path], dtype=torch.long)
+    return torch.as_tensor(a)[idx]
+
+
 def multivariate_normal(key, mean, cov, shape=(), dtype=None):
     """mean + z @ cholesky(cov).T with the scripted standard normals z
     (jax.random.multivariate_normal's default Cholesky method)."""

@@ -6,7 +6,8 @@ its RQSpline bijection (knots, forward and inverse:
 resource/model/nf_model/rqSpline.py:20-239, 296-362), the whole
 MaskedCouplingRQSpline (rqSpline.py:450-504), TakeSerialSteps.__call__ with
 thinning into the reference's Buffers over several calls
-(strategy/take_steps.py:60-180, resource/buffers.py:24-41), NFProposal.kernel with its
+(strategy/take_steps.py:60-180, resource/buffers.py:24-41), TrainModel's
+training-data selection (strategy/train_model.py:66-80), NFProposal.kernel with its
 batched and unbatched proposal draws (resource/kernel/NF_proposal.py:27-172),
 RealNVP's layers (nf_model/realNVP.py:180-222), AdamOptimization.optimize
 (strategy/optimization.py:85-164) and its
@@ -50,6 +51,8 @@ from flowMC.resource.kernel.NF_proposal import NFProposal  # noqa: E402
 from flowMC.resource.buffers import Buffer  # noqa: E402
 from flowMC.resource.states import State  # noqa: E402
 from flowMC.strategy.take_steps import TakeSerialSteps  # noqa: E402
+from flowMC.strategy.train_model import TrainModel  # noqa: E402
+from flowMC.resource.optimizer import Optimizer  # noqa: E402
 from flowMC.resource.model.nf_model.realNVP import RealNVP  # noqa: E402
 import jax  # noqa: E402
 
@@ -514,6 +517,31 @@ def main():
     out[f"{name}/last"], out[f"{name}/cursor"] = np.stack(lasts), np.array(cursors)
     cases.append({"name": name, "kind": "takesteps", "local": "mala", "target": t, "step_size": 0.2,
                   "n_steps": S, "thinning": thin, "n_calls": n_calls, "buf_rows": R})
+    # TrainModel.__call__'s data selection (train_model.py:66-80): a buffer
+    # with unfilled (-inf) rows, the history window, and scripted
+    # jax.random.choice indices; the model's train() is replaced by a recorder
+    # of the rows it was given
+    name, C, Sb, d, window, n_max = "train_select", 4, 9, 3, 5, 23
+    buf = rng.normal(size=(C, Sb, d))
+    buf[:, 7:] = -np.inf                                   # two rows per chain not yet written
+    choice = rng.integers(0, C * window, size=n_max)
+    jr.DRAWS["tm.1"] = choice
+    seen = {}
+
+    def _record(rng, data, optim, state, num_epochs, batch_size, verbose):
+        seen["data"] = torch.as_tensor(data).numpy().copy()
+        return rng, model, state, torch.zeros(num_epochs, dtype=torch.float64)
+    model = object.__new__(MaskedCouplingRQSpline)
+    model.train = _record
+    opt = object.__new__(Optimizer)
+    opt.optim, opt.optim_state = None, None
+    data_buf = Buffer("data", (C, Sb, d), 1)
+    data_buf.data = torch.tensor(buf)
+    tm = TrainModel("model", "data", "opt", n_epochs=2, batch_size=8, n_max_examples=n_max,
+                    history_window=window)
+    tm(jr.Key("tm"), {"model": model, "data": data_buf, "opt": opt}, torch.zeros(C, d), None)
+    out[f"{name}/buf"], out[f"{name}/choice"], out[f"{name}/selected"] = buf, choice, seen["data"]
+    cases.append({"name": name, "kind": "train_select", "history_window": window, "n_max_examples": n_max})
     for c in cases:
         if c["kind"] == "nfproposal":
             print(f"{c['name']}: acceptance {out[c['name'] + '/acc'].mean():.2f}")

@@ -220,3 +220,15 @@ def test_oracle_take_steps_buffers_match_reference_source(case):
     np.testing.assert_array_equal(acc_buf, z[f"{n}/acc_buf"])
     np.testing.assert_allclose(pos_buf, z[f"{n}/pos_buf"], rtol=1e-10, atol=1e-10)
     np.testing.assert_allclose(lp_buf, z[f"{n}/logp_buf"], rtol=1e-10, atol=1e-10)
+
+
+def test_oracle_training_selection_matches_reference_source():
+    """TrainModel.__call__'s selection (train_model.py:66-80) run by the
+    reference on a buffer with unfilled rows: finite rows per chain, the last
+    history_window of them, then the scripted choice indices."""
+    from oracle import flow as OF
+    z, cases = _load()
+    case = next(c for c in cases if c["kind"] == "train_select")
+    n = case["name"]
+    got = OF.select_training_data(z[f"{n}/buf"], case["history_window"], z[f"{n}/choice"])
+    np.testing.assert_array_equal(got, z[f"{n}/selected"])
