@@ -78,7 +78,18 @@ class Sampler:
                 cap = self.capture(initial_position, data)
             return cap.replay(initial_position)
         _, last_step = self._run(self.rng_key, initial_position, data, self.strategy_order)
+        self.poll_errors()
         return last_step
+
+    def _pollers(self):
+        return [s for s in self.strategies.values() if hasattr(s, "poll_errors")]
+
+    def poll_errors(self):
+        """Raise the first error a strategy's device-side check recorded (a
+        training-data selection whose finite rows do not split evenly over
+        the chains). Waits only for the events recorded after those checks."""
+        for s in self._pollers():
+            s.poll_errors()
 
     def capture(self, initial_position, data: dict) -> "CapturedSchedule":
         """Capture strategy_order as one CUDA graph without running it. Work
@@ -99,7 +110,7 @@ class Sampler:
         with torch.cuda.graph(g):
             _lib.rng_epoch_advance(epoch)
             _, out = self._run(self.rng_key, static_x, data, self.strategy_order)
-        cap = CapturedSchedule(g, static_x, out)
+        cap = CapturedSchedule(g, static_x, out, self._pollers())
         if not hasattr(self, "_captured"):
             self._captured = {}
         self._captured[tuple(self.strategy_order)] = cap
@@ -118,12 +129,27 @@ class CapturedSchedule:
     returned tensor (the schedule's last positions) is the graph's output
     and is overwritten by the next replay."""
 
-    def __init__(self, graph, static_input, static_output):
+    def __init__(self, graph, static_input, static_output, pollers=()):
         self.graph = graph
         self.static_input = static_input
         self.static_output = static_output
+        self.pollers = list(pollers)
 
     def replay(self, initial_position):
+        """Launch the graph. Errors that the previous replay's device-side
+        checks recorded are raised first (that replay has finished by then,
+        or this call waits for it)."""
+        self.poll_errors()
         self.static_input.copy_(torch.atleast_2d(initial_position), non_blocking=True)
         self.graph.replay()
+        if self.pollers:
+            ev = torch.cuda.Event()
+            ev.record()
+            for p in self.pollers:
+                p.mark_error_copy(ev)
         return self.static_output
+
+    def poll_errors(self):
+        """Raise the error recorded by the last replay's checks (waits for that replay)."""
+        for p in self.pollers:
+            p.poll_errors()

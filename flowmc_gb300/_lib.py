@@ -166,8 +166,10 @@ _SIGNATURES = {
     "fmc_flag_less": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "fmc_copy_if": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                    ctypes.c_void_p]),
+    "fmc_column_stats_workspace_size": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int32,
+                                                       ctypes.POINTER(ctypes.c_size_t)]),
     "fmc_column_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p,
-                                        ctypes.c_void_p, ctypes.c_void_p]),
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "fmc_permute_rows": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_uint64,
                                         ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
                                         ctypes.c_void_p]),
@@ -269,6 +271,16 @@ class Workspace:
         base = self._buf.data_ptr()
         off = (-base) % 256
         return base + off, self._buf.numel() - off
+
+
+def column_stats(x: torch.Tensor, mean: torch.Tensor, var: torch.Tensor, ws: "Workspace") -> None:
+    """fmc_column_stats of x [n, d] into mean [d] and var [d], partials in ws."""
+    n, d = x.shape
+    nb = ctypes.c_size_t()
+    check(lib().fmc_column_stats_workspace_size(n, d, ctypes.byref(nb)))
+    ptr, size = ws.get(nb.value, x.device)
+    check(lib().fmc_column_stats(x.data_ptr(), n, d, mean.data_ptr(), var.data_ptr(), ptr, size,
+                                 stream_handle(x.device)))
 
 
 def launch_count() -> int:

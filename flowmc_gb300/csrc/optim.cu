@@ -14,6 +14,8 @@
 //    "Ciphers with arbitrary finite domains", CT-RSA 2002).
 //  * fmc_select_training_data: TrainModel's finite-row filter, per-chain
 //    history window and with-replacement resampling (train_model.py:66-80).
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <mutex>
 #include "common.cuh"
 #include "gemm_tc.cuh"
@@ -114,11 +116,10 @@ __global__ void k_copy_if(const int32_t* __restrict__ flag, const uint4* __restr
 // column); the final kernel merges the blocks in index order with the
 // pairwise update of Chan, Golub and LeVeque (1979):
 //   n = na + nb, delta = mb - ma, m = ma + delta nb / n, M2 = M2a + M2b + delta^2 na nb / n.
-// Partials live in a static device buffer (one column tile at a time), so
-// concurrent calls on different streams of one device must not overlap.
+// Partials live in the caller's workspace (one column tile at a time):
+// 2 * kColStatBlocks * min(d, kColStatCols) floats.
 constexpr int kColStatBlocks = 512;
 constexpr int kColStatCols = 512;
-__device__ float g_colstat_scratch[2 * kColStatBlocks * kColStatCols];
 
 // x points at the tile's first column; row stride d, tile width dc
 __global__ void k_colstat_partial(const float* __restrict__ x, int64_t n, int d, int dc, int64_t rows_per,
@@ -291,7 +292,13 @@ __global__ void k_gather_selected(const float* __restrict__ buf, int d, int C, i
   const int64_t T = *total;
   const int64_t per = (C > 0) ? T / C : 0;
   if (T % C != 0 || per == 0) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) *err = 1;  // the reference's reshape would fail
+    // the reference's reshape would fail: raise the error word and fill the
+    // output with NaN, so that a caller that trains on it sees NaN losses
+    // instead of stale memory
+    if (blockIdx.x == 0 && threadIdx.x == 0) *err = 1;
+    const int64_t tot = n_out * d;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x)
+      out[e] = __int_as_float(0x7fc00000);
     return;
   }
   const int64_t hw = per < history ? per : history;
@@ -302,7 +309,12 @@ __global__ void k_gather_selected(const float* __restrict__ buf, int d, int C, i
     const int j = (int)(e - i * d);
     uint64_t k;
     if (idx) {
-      k = (uint64_t)idx[i];
+      // NumPy/JAX indexing: a negative index counts from the end; what is
+      // still out of range is clamped (JAX's gather clamps)
+      int64_t ki = idx[i];
+      if (ki < 0) ki += (int64_t)N;
+      if (ki < 0) ki = 0;
+      k = (uint64_t)ki;
       if (k >= N) k = N - 1;
     } else {
       const uint32_t u = rng.draw((uint64_t)i, 0, 0u, 0x53454c00u).x;
@@ -371,12 +383,24 @@ extern "C" int fmc_copy_if(const int32_t* flag, const void* src, void* dst, size
   return FMC_OK;
 }
 
-extern "C" int fmc_column_stats(const float* x, int64_t n, int32_t d, float* mean, float* var, void* stream) {
+extern "C" int fmc_column_stats_workspace_size(int64_t n, int32_t d, size_t* bytes) {
+  FMC_CHECK_ARG(bytes != nullptr && n >= 2 && d >= 1, "bad arguments");
+  const int dc = d < kColStatCols ? d : kColStatCols;
+  *bytes = (size_t)2 * kColStatBlocks * dc * sizeof(float);
+  return FMC_OK;
+}
+
+extern "C" int fmc_column_stats(const float* x, int64_t n, int32_t d, float* mean, float* var, void* ws,
+                                size_t ws_bytes, void* stream) {
   FMC_CHECK_ARG(x && mean && var, "NULL pointer");
   FMC_CHECK_ARG(n >= 2 && d >= 1, "need n >= 2 rows and d >= 1");
+  size_t need = 0;
+  int rc = fmc_column_stats_workspace_size(n, d, &need);
+  if (rc) return rc;
+  FMC_CHECK_ARG(ws && ws_bytes >= need, "workspace of %zu bytes < %zu needed", ws_bytes, need);
+  FMC_CHECK_ARG(((uintptr_t)ws & 15) == 0, "workspace must be 16-byte aligned");
   cudaStream_t st = (cudaStream_t)stream;
-  float* part = nullptr;
-  FMC_CUDA_TRY(cudaGetSymbolAddress((void**)&part, g_colstat_scratch));
+  float* part = (float*)ws;
   // column tiles of at most kColStatCols; per tile enough row blocks to cover
   // the SMs a few times over (at most kColStatBlocks, at least 64 rows each)
   for (int c0 = 0; c0 < d; c0 += kColStatCols) {
@@ -418,6 +442,8 @@ extern "C" int fmc_permute_rows(const float* src, int64_t n, int32_t d, uint64_t
 
 extern "C" int fmc_select_workspace_size(int32_t n_chains, int64_t n_steps, size_t* bytes) {
   FMC_CHECK_ARG(bytes != nullptr && n_chains >= 1 && n_steps >= 1, "bad arguments");
+  // rows * 8 bytes of compacted row ids must not overflow
+  FMC_CHECK_ARG(n_steps <= (INT64_MAX / 16) / n_chains, "n_chains * n_steps too large");
   const int64_t rows = (int64_t)n_chains * n_steps;
   const int64_t tiles = (rows + kScanTile - 1) / kScanTile;
   *bytes = (size_t)(rows * 4 + 256 + tiles * 4 + 256 + rows * 8 + 256 + 64);
@@ -431,7 +457,8 @@ extern "C" int fmc_select_training_data(const float* buf, int32_t n_chains, int6
   FMC_CHECK_ARG(buf && out && err, "NULL pointer");
   FMC_CHECK_ARG(n_chains >= 1 && n_steps >= 1 && d >= 1 && history_window >= 1 && n_out >= 1, "bad sizes");
   size_t need = 0;
-  fmc_select_workspace_size(n_chains, n_steps, &need);
+  int rc = fmc_select_workspace_size(n_chains, n_steps, &need);
+  if (rc) return rc;
   FMC_CHECK_ARG(ws && ws_bytes >= need, "workspace of %zu bytes < %zu needed", ws_bytes, need);
   cudaStream_t st = (cudaStream_t)stream;
   const int64_t rows = (int64_t)n_chains * n_steps;
@@ -479,21 +506,57 @@ constexpr size_t kNoAllocSelectBytes =
              kNoAllocSelectMaxRows * 8 + 256 + 64);
 static __device__ __align__(256) uint8_t g_noalloc_select_scratch[kNoAllocSelectBytes];
 
+// the unique id of the calling thread's current context (cuCtxGetId, reached
+// through the runtime's driver entry points so the library needs no -lcuda);
+// 0 when no context is current yet
+static int current_context_id(unsigned long long* id) {
+  static PFN_cuCtxGetCurrent_v4000 get_cur = nullptr;
+  static PFN_cuCtxGetId_v12000 get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_cur = (PFN_cuCtxGetCurrent_v4000)p;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (PFN_cuCtxGetId_v12000)p;
+  });
+  FMC_CHECK_SUPPORTED(get_cur != nullptr && get_id != nullptr, "cuCtxGetCurrent / cuCtxGetId are unavailable");
+  CUcontext ctx = nullptr;
+  *id = 0;
+  if (get_cur(&ctx) != CUDA_SUCCESS || ctx == nullptr) return FMC_OK;
+  FMC_CHECK_SUPPORTED(get_id(ctx, id) == CUDA_SUCCESS, "cuCtxGetId failed");
+  return FMC_OK;
+}
+
 static int noalloc_select_scratch(void** out) {
-  // the array's name is only a host-side handle; its device address comes from
-  // cudaGetSymbolAddress, looked up once per device with that device current
+  // The array's name is only a host-side handle; its device address comes
+  // from cudaGetSymbolAddress with the device current. The look-up is done
+  // on a device's first call and cached per device, keyed by the context's
+  // unique id: a context destroyed and re-created (cudaDeviceReset) reloads
+  // the module, so the next call looks the address up again.
+  struct Entry {
+    unsigned long long ctx;
+    void* addr;
+  };
   static std::mutex mu;
-  static void* addr[256] = {nullptr};
+  static Entry cache[256] = {};
   int dev = 0;
   FMC_CUDA_TRY(cudaGetDevice(&dev));
   FMC_CHECK_SUPPORTED(dev >= 0 && dev < 256, "device ordinal %d out of range", dev);
   std::lock_guard<std::mutex> lock(mu);
-  if (addr[dev] == nullptr) {
+  unsigned long long ctx = 0;
+  int rc = current_context_id(&ctx);
+  if (rc) return rc;
+  if (ctx == 0 || cache[dev].addr == nullptr || cache[dev].ctx != ctx) {
     void* p = nullptr;
-    FMC_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_select_scratch));
-    addr[dev] = p;
+    FMC_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_select_scratch));   // makes the primary context current
+    if ((rc = current_context_id(&ctx))) return rc;
+    cache[dev] = Entry{ctx, p};
   }
-  *out = addr[dev];
+  *out = cache[dev].addr;
   return FMC_OK;
 }
 
@@ -504,6 +567,11 @@ extern "C" int fmc_select_training_data_noalloc(const float* buf, int32_t n_chai
                                                 uint64_t counter, const int64_t* idx, float* out, int32_t* err,
                                                 void* stream) {
   FMC_CHECK_ARG(n_chains >= 1 && n_steps >= 1, "bad sizes");
+  // compare before multiplying, so that no product can overflow
+  FMC_CHECK_ARG(n_steps <= fmc::kNoAllocSelectMaxRows / n_chains,
+                "n_chains * n_steps exceeds the %lld rows the static scratch of "
+                "fmc_select_training_data_noalloc holds; use fmc_select_training_data with a workspace",
+                (long long)fmc::kNoAllocSelectMaxRows);
   const int64_t rows = (int64_t)n_chains * n_steps;
   FMC_CHECK_ARG(rows <= fmc::kNoAllocSelectMaxRows,
                 "n_chains * n_steps = %lld rows exceeds the %lld rows the static scratch of "

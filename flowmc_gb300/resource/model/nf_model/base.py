@@ -69,7 +69,9 @@ class NFModel(Resource):
                [(t, t.clone()) for t in state.tensors()]
         # nf_model/base.py:187-188: data_mean / data_cov from the training data
         if N >= 2:
-            _lib.check(L.fmc_column_stats(data.data_ptr(), N, d, self.aux.data_ptr(), self.aux[d:].data_ptr(), stream))
+            if getattr(self, "_colstat_ws", None) is None:
+                self._colstat_ws = _lib.Workspace()
+            _lib.column_stats(data, self.aux[:d], self.aux[d:2 * d], self._colstat_ws)
         steps = N // batch_size
         batch = torch.empty(batch_size if steps > 0 else N, d, device=dev)
         grad = torch.empty(self.n_params, device=dev)

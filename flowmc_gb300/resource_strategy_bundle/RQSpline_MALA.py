@@ -116,7 +116,7 @@ class RQSpline_MALA_Bundle(ResourceStrategyBundle):
             return rng_key, resources, initial_position
 
         def update_model(rng_key, resources, initial_position, data):
-            # RQSpline_MALA.py:333-350: point the global sampler at the trained model
+            # RQSpline_MALA.py:215-232: point the global sampler at the trained model
             resources["global_sampler"].model = resources["model"]
             return rng_key, resources, initial_position
 

@@ -38,6 +38,8 @@ class TrainModel(Strategy):
         self.history_window = history_window
         self._ws = _lib.Workspace()
         self._err = None
+        self._err_host = None     # pinned copy of the device error word
+        self._err_event = None    # recorded after the copy (eager runs and graph replays)
 
     def select(self, seed: int, buf: torch.Tensor, idx: torch.Tensor | None = None) -> torch.Tensor:
         C, S, d = buf.shape
@@ -52,14 +54,49 @@ class TrainModel(Strategy):
         _lib.check(L.fmc_select_training_data(buf.data_ptr(), C, S, d, self.history_window, self.n_max_examples,
                                               int(seed) & ((1 << 64) - 1), 0, _lib.ptr(idx), out.data_ptr(),
                                               self._err.data_ptr(), ptr, size, _lib.stream_handle(dev)))
+        # the error word goes to pinned host memory behind the selection (a
+        # copy node when captured), so that a later poll needs no stream sync
+        if self._err_host is None:
+            self._err_host = torch.zeros((), dtype=torch.int32, pin_memory=True)
+        self._err_host.copy_(self._err, non_blocking=True)
+        if not torch.cuda.is_current_stream_capturing():
+            self.mark_error_copy()
         return out
+
+    _MSG = "finite training rows do not split evenly over the chains"
+
+    def mark_error_copy(self, event=None):
+        """Record (or take) the event after which the pinned error word is valid."""
+        if event is None:
+            event = torch.cuda.Event()
+            event.record()
+        self._err_event = event
+
+    def poll_errors(self):
+        """Raise ValueError if a finished selection found finite rows that do
+        not split evenly over the chains (the reference's reshape would raise
+        there; the selection then fills the training data with NaN). Waits
+        only for the event recorded after that selection's copy, not for the
+        stream."""
+        ev = self._err_event
+        if ev is None or self._err_host is None:
+            return
+        ev.synchronize()
+        self._err_event = None
+        if int(self._err_host.item()) != 0:
+            self._err_host.zero_()
+            self._err.zero_()
+            raise ValueError(self._MSG)
 
     def check_errors(self):
         """Raise if a selection found finite rows that do not split evenly over
         the chains (the reference's reshape would raise). Synchronises."""
         if self._err is not None and int(self._err.item()) != 0:
             self._err.zero_()
-            raise ValueError("finite training rows do not split evenly over the chains")
+            if self._err_host is not None:
+                self._err_host.zero_()
+            self._err_event = None
+            raise ValueError(self._MSG)
 
     def __call__(self, rng_key, resources, initial_position, data):
         model = resources[self.model_resource]
@@ -68,6 +105,8 @@ class TrainModel(Strategy):
         assert isinstance(data_resource, Buffer), "Data resource must be a buffer"
         optimizer = resources[self.optimizer_resource]
         assert isinstance(optimizer, Optimizer), "Optimizer resource must be an optimizer"
+        if not torch.cuda.is_current_stream_capturing():
+            self.poll_errors()      # the previous call's selection, long finished
         rng_key, subkey = split(rng_key)                              # train_model.py:72
         training_data = self.select(subkey.value, data_resource.data)
         rng_key, subkey = split(rng_key)                              # train_model.py:81
@@ -76,7 +115,7 @@ class TrainModel(Strategy):
             print(f"Training data shape: {tuple(training_data.shape)}")
             print(f"n_epochs: {self.n_epochs}")
             print(f"batch_size: {self.batch_size}")
-        # the key returned by NFModel.train replaces rng_key (train_model.py:369-377)
+        # the key returned by NFModel.train replaces rng_key (train_model.py:81-97)
         with region("train", units=self.n_epochs * max(1, self.n_max_examples // self.batch_size)):
             rng_key, model, state, loss_values = model.train(subkey, training_data, optimizer,
                                                              optimizer.optim_state, self.n_epochs, self.batch_size,

@@ -44,7 +44,7 @@ enum {
 
 /* ---- target log-densities (replace the user's JAX callable) --------- */
 /* A registered device target: value and analytic gradient in the kernels.
- * Replaces `LogPDF.__call__` (resource/logPDF.py:225-226) plus
+ * Replaces `LogPDF.__call__` (resource/logPDF.py:60-61) plus
  * `jax.value_and_grad(logpdf)` (resource/kernel/MALA.py:59, HMC.py:73-78). */
 enum {
   FMC_TARGET_DIAG_GAUSSIAN = 0, /* -0.5 sum_j (x_j-mean_j)^2 * inv_var_j + scalars[0]   */
@@ -238,7 +238,7 @@ FMC_API int fmc_batched_dense_local_steps(const FmcTarget* targets, int32_t n_ta
                                           void* ws, size_t ws_bytes, void* stream);
 
 /* Evaluate a registered target (value and gradient) on a batch.
- * Replaces jax.vmap(jax.value_and_grad(LogPDF)) (resource/logPDF.py:225-226).
+ * Replaces jax.vmap(jax.value_and_grad(LogPDF)) (resource/logPDF.py:60-61).
  *   x [n, n_dim] -> logp [n], grad [n, n_dim] (grad may be NULL). */
 FMC_API int fmc_target_value_grad(const FmcTarget* target, const float* x, int64_t n,
                           float* logp, float* grad, void* stream);
@@ -381,9 +381,11 @@ FMC_API int fmc_copy_if(const int32_t* flag, const void* src, void* dst, size_t 
 
 /* data_mean and diag(data_cov) of x [n, d] (nf_model/base.py:187-188):
  * mean [d], unbiased variance [d]. Deterministic two-stage reduction whose
- * partials live in a static device buffer: calls on different streams of
- * one device must not run concurrently. */
-FMC_API int fmc_column_stats(const float* x, int64_t n, int32_t d, float* mean, float* var, void* stream);
+ * partials live in the caller's workspace (16-byte aligned, at least
+ * fmc_column_stats_workspace_size bytes, at most 2 MiB). */
+FMC_API int fmc_column_stats_workspace_size(int64_t n, int32_t d, size_t* bytes);
+FMC_API int fmc_column_stats(const float* x, int64_t n, int32_t d, float* mean, float* var, void* ws,
+                             size_t ws_bytes, void* stream);
 
 /* dst[r] = src[perm(first + r)] for r < m, perm a pseudo-random permutation of
  * [0, n) keyed by (seed, counter): the epoch shuffle of NFModel.train_epoch

@@ -170,14 +170,15 @@ def buffer_update(buf: np.ndarray, upd: np.ndarray, start: int, axis: int) -> np
     return out
 
 
-def nf_proposal_kernel(flow, t, x, z, u):
+def nf_proposal_kernel(flow, t, x, z, u, return_ratio=False):
     """NFProposal.kernel for every chain (NF_proposal.py:27-128).
 
     flow: an ``oracle.flow.Flow``; x [C, d] current positions; z [C, S, d]
     the base-distribution normals of the proposals; u [C, S] the MH
     uniforms. log_prob of the proposals is recomputed by the forward pass
     (NF_proposal.py:165-167), and the incoming log_prob is logpdf(x)
-    (take_steps.py:200-206).
+    (take_steps.py:200-206). With return_ratio the log acceptance ratio of
+    every step [C, S] is returned as well (for tie margins in tests).
     """
     C, S, d = z.shape
     lp = T.value(t, x)
@@ -189,11 +190,13 @@ def nf_proposal_kernel(flow, t, x, z, u):
     out_x = np.empty((C, S, d))
     out_lp = np.empty((C, S))
     out_acc = np.empty((C, S))
+    out_ratio = np.empty((C, S))
     for s in range(S):                                    # NF_proposal.py:91-126
         ratio = (lp_p[:, s] - lp) - (lnf_p[:, s] - lnf)
+        out_ratio[:, s] = ratio
         acc = np.log(u[:, s]) < ratio
         x = np.where(acc[:, None], props[:, s], x)
         lp = np.where(acc, lp_p[:, s], lp)
         lnf = np.where(acc, lnf_p[:, s], lnf)
         out_x[:, s], out_lp[:, s], out_acc[:, s] = x, lp, acc
-    return out_x, out_lp, out_acc
+    return (out_x, out_lp, out_acc, out_ratio) if return_ratio else (out_x, out_lp, out_acc)

@@ -21,15 +21,17 @@ the stand-ins under ``_standin/`` (float64 torch tensors, autograd for
 oracle's targets written with ``jax.numpy`` calls, so the reference kernels
 differentiate them themselves.
 
-Run in a checkout that has the reference source (REFERENCE_SRC, default
-/root/reference/src):  python tests/golden/make_golden.py
+Run with REFERENCE_SRC set to the src/ directory of a flowMC v0.4.5
+checkout:  REFERENCE_SRC=<checkout>/src python tests/golden/make_golden.py
 """
 import json
 import os
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("REFERENCE_SRC", "/root/reference/src")
+REF = os.environ.get("REFERENCE_SRC")
+if not REF or not os.path.isdir(os.path.join(REF, "flowMC")):
+    sys.exit("set REFERENCE_SRC to the src/ directory of a flowMC v0.4.5 checkout")
 sys.path.insert(0, os.path.join(HERE, "_standin"))
 sys.path.insert(0, REF)
 
@@ -542,6 +544,46 @@ def main():
     tm(jr.Key("tm"), {"model": model, "data": data_buf, "opt": opt}, torch.zeros(C, d), None)
     out[f"{name}/buf"], out[f"{name}/choice"], out[f"{name}/selected"] = buf, choice, seen["data"]
     cases.append({"name": name, "kind": "train_select", "history_window": window, "n_max_examples": n_max})
+    # NFModel.loss_fn (nf_model/base.py:98-100), -mean(vmap(log_prob)(x)), run
+    # by the reference's own code on a flow of the reference's classes; its
+    # gradient with respect to every trainable leaf (per layer ScalarAffine
+    # scale and shift, each conditioner Linear's weight and bias) comes from
+    # autograd, the stand-in for eqx.filter_value_and_grad. Inputs reach both
+    # spline tails.
+    name, d, L, hidden, K = "nfloss_d5", 5, 3, [8, 8], 4
+    P = 3 * K + 1
+    layers = []
+    for l in range(L):
+        shape = [d] + hidden + [d * P]
+        layers.append({"W": [rng.normal(size=(b, a)) * 0.6 for a, b in zip(shape[:-1], shape[1:])],
+                       "b": [rng.normal(size=b) * 0.3 for b in shape[1:]],
+                       "scale": float(rng.normal() * 0.3), "shift": float(rng.normal() * 0.5),
+                       "mask": ((np.arange(d) + l) % 2).astype(np.float64)})
+    mean, var = rng.normal(size=d) * 0.5, rng.uniform(0.5, 2.0, size=d)
+    flow = _rqspline_flow(layers, K, mean, var, d)
+    x = rng.normal(size=(13, d)) * 3.0
+    x[0, 0], x[1, 1] = 30.0, -30.0
+    leaves = []
+    for aff, spl in flow.layers:
+        for t in (aff.bijector.scale, aff.bijector.shift):
+            t.requires_grad_(True)
+        lins = [m for m in spl.bijector.conditioner.layers if isinstance(m, _Linear)]
+        for lin in lins:
+            lin.weight.requires_grad_(True)
+            lin.bias.requires_grad_(True)
+        leaves.append((aff.bijector.scale, aff.bijector.shift, lins))
+    loss = flow.loss_fn(torch.tensor(x))
+    flat = [t for sc, sh, lins in leaves for t in [sc, sh] + [u for lin in lins for u in (lin.weight, lin.bias)]]
+    grads = torch.autograd.grad(loss, flat)
+    out[f"{name}/x"], out[f"{name}/mean"], out[f"{name}/var"] = x, mean, var
+    for l, Ld in enumerate(layers):
+        for i, (W, b) in enumerate(zip(Ld["W"], Ld["b"])):
+            out[f"{name}/W{l}_{i}"], out[f"{name}/b{l}_{i}"] = W, b
+    out[f"{name}/scale"] = np.array([Ld["scale"] for Ld in layers])
+    out[f"{name}/shift"] = np.array([Ld["shift"] for Ld in layers])
+    out[f"{name}/loss"] = np.array(float(loss.detach()))
+    out[f"{name}/grad"] = np.concatenate([g.detach().numpy().ravel() for g in grads])
+    cases.append({"name": name, "kind": "nfloss", "n_dim": d, "n_layers": L, "hidden": hidden, "n_bins": K})
     for c in cases:
         if c["kind"] == "nfproposal":
             print(f"{c['name']}: acceptance {out[c['name'] + '/acc'].mean():.2f}")

@@ -160,6 +160,49 @@ def test_train_model_strategy(cuda):
     st.check_errors()
 
 
+@pytest.mark.gpu
+def test_train_model_uneven_rows_raise(cuda):
+    """A chain that produced a NaN row leaves finite rows that do not split
+    evenly over the chains: the reference's reshape raises there
+    (train_model.py:66-70). Here the selection fills the training data with
+    NaN (the epoch losses are NaN, never stale memory) and the strategy's
+    next call, or Sampler.poll_errors, raises ValueError without a stream
+    sync; a CUDA-graph replay raises on the next replay."""
+    from flowmc_gb300.resource.buffers import Buffer
+    from flowmc_gb300.resource.model.nf_model.rqSpline import MaskedCouplingRQSpline
+    from flowmc_gb300.resource.optimizer import Optimizer
+    from flowmc_gb300.strategy.lambda_function import Lambda
+    from flowmc_gb300.strategy.train_model import TrainModel
+    C, S, d = 4, 20, 2
+    model = MaskedCouplingRQSpline(d, 2, [8, 8], 4, PRNGKey(10), device="cuda")
+    data = Buffer("test_data", (C, S, d), 1, device="cuda")
+    rows = torch.randn(C, S, d, device="cuda")
+    rows[2, 7, 1] = float("nan")
+    data.update_buffer(rows)
+    loss = Buffer("loss", (6,), 0, device="cuda")
+    res = {"test_data": data, "optimizer": Optimizer(model), "model": model, "loss": loss}
+    st = TrainModel("model", "test_data", "optimizer", loss_buffer_name="loss", n_epochs=3, batch_size=32,
+                    n_max_examples=64, history_window=5, verbose=False)
+    _, res, _ = st(PRNGKey(1), res, torch.zeros(C, d, device="cuda"), {})
+    assert torch.isnan(res["loss"].data[:3]).all()
+    with pytest.raises(ValueError, match="do not split evenly"):
+        st(PRNGKey(2), res, torch.zeros(C, d, device="cuda"), {})
+    # through the Sampler: eager run, then a captured schedule
+    s = Sampler(d, C, PRNGKey(0), resources=res, strategies={"train": st, "noop": Lambda(lambda *a: None)},
+                strategy_order=["train"])
+    with pytest.raises(ValueError, match="do not split evenly"):
+        s.sample(torch.zeros(C, d), {})
+    cap = s.capture(torch.zeros(C, d, device="cuda"), {})
+    cap.replay(torch.zeros(C, d, device="cuda"))
+    with pytest.raises(ValueError, match="do not split evenly"):
+        cap.replay(torch.zeros(C, d, device="cuda"))
+    # finite rows that split evenly: no error
+    data.update_buffer(torch.randn(C, S, d, device="cuda"))
+    _, res, _ = st(PRNGKey(3), res, torch.zeros(C, d, device="cuda"), {})
+    s.poll_errors()
+    st.check_errors()
+
+
 def test_nvtx_ranges_around_strategies_cpu():
     """With NVTX on, the sampler still runs its strategies in order (the
     ranges are no-ops without a timeline profiler attached)."""

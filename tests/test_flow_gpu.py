@@ -335,8 +335,7 @@ def test_column_stats_matches_numpy(cuda, n, d):
     xt = torch.tensor(x, device="cuda")
     mean = torch.empty(d, device="cuda")
     var = torch.empty(d, device="cuda")
-    _lib.check(_lib.lib().fmc_column_stats(xt.data_ptr(), n, d, mean.data_ptr(), var.data_ptr(),
-                                           _lib.stream_handle()))
+    _lib.column_stats(xt, mean, var, _lib.Workspace())
     x64 = x.astype(np.float64)
     np.testing.assert_allclose(mean.cpu().numpy(), x64.mean(0), rtol=1e-5, atol=1e-5)
     np.testing.assert_allclose(var.cpu().numpy(), x64.var(0, ddof=1), rtol=2e-4, atol=1e-6)

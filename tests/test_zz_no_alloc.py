@@ -6,8 +6,11 @@ no-allocation policy -- and keeps its scratch in a static device array
 instead of a caller workspace. Here it is called through the C ABI and must
 reproduce the workspace entry point (fmc_select_training_data) exactly, on
 two calls in a row (the second call reuses the static scratch the first left
-behind). Selection is index work, so the tolerance is bit-exact. Sizes past
-its stated maximum (n_chains * n_steps > 2**20 rows) are refused on the host.
+behind), and, on a third call with scripted choice indices, the rows the
+reference's own TrainModel selected (the golden train_select case, made by
+tests/golden/make_golden.py from the reference's source). Selection is index
+work, so the tolerance is bit-exact. Sizes past its stated maximum
+(n_chains * n_steps > 2**20 rows) are refused on the host.
 """
 import ctypes
 
@@ -18,7 +21,7 @@ import torch
 pytestmark = pytest.mark.gpu
 
 
-def _select(lib, fn_name, buf, hw, n_out, seed, ws=None):
+def _select(lib, fn_name, buf, hw, n_out, seed, idx=None):
     from flowmc_gb300 import _lib
     C, S, d = buf.shape
     out = torch.full((n_out, d), float("nan"), device=buf.device)
@@ -29,10 +32,10 @@ def _select(lib, fn_name, buf, hw, n_out, seed, ws=None):
         _lib.check(lib.fmc_select_workspace_size(C, S, ctypes.byref(nb)))
         ws = torch.empty(nb.value + 256, dtype=torch.uint8, device=buf.device)
         base = ws.data_ptr() + (-ws.data_ptr()) % 256
-        _lib.check(lib.fmc_select_training_data(buf.data_ptr(), C, S, d, hw, n_out, seed, 0, None, out.data_ptr(),
-                                                err.data_ptr(), base, nb.value, stream))
+        _lib.check(lib.fmc_select_training_data(buf.data_ptr(), C, S, d, hw, n_out, seed, 0, _lib.ptr(idx),
+                                                out.data_ptr(), err.data_ptr(), base, nb.value, stream))
     else:
-        _lib.check(lib.fmc_select_training_data_noalloc(buf.data_ptr(), C, S, d, hw, n_out, seed, 0, None,
+        _lib.check(lib.fmc_select_training_data_noalloc(buf.data_ptr(), C, S, d, hw, n_out, seed, 0, _lib.ptr(idx),
                                                         out.data_ptr(), err.data_ptr(), stream))
     torch.cuda.synchronize()
     assert int(err.item()) == 0
@@ -54,6 +57,16 @@ def test_noalloc_selection_matches_workspace_entry_point(cuda):
         got = _select(lib, "fmc_select_training_data_noalloc", tb, hw, n_out, seed)
         assert np.isfinite(got).all()
         np.testing.assert_array_equal(got, ref)
+    # third call: the reference's own selection (golden vectors)
+    from test_golden import _load
+    z, gcases = _load()
+    case = next(c for c in gcases if c["kind"] == "train_select")
+    n = case["name"]
+    gbuf = torch.tensor(z[f"{n}/buf"].astype(np.float32), device="cuda")
+    choice = torch.tensor(z[f"{n}/choice"].astype(np.int64), device="cuda")
+    got = _select(lib, "fmc_select_training_data_noalloc", gbuf, case["history_window"], choice.numel(), 0,
+                  idx=choice)
+    np.testing.assert_array_equal(got, z[f"{n}/selected"].astype(np.float32))
 
 
 def test_noalloc_selection_rejects_oversized_buffers(cuda):
