@@ -295,17 +295,46 @@ def batched_probe(dev, kind="mala", steps=2000, thin=20, seed=1):
     sms = ctypes_sm_count()
     fp32_peak = sms * 128 * 2 * measured_peaks_raw().get("sm_max_mhz", 2070.0) * 1e6 / 1e12
     worst_mean = worst_cov = 0.0
+    worst_pred = 0.0
+    pred_long = {}
+    kept = np.arange(steps // thin)[(steps // thin) // 2:] * thin + 1     # step index of each kept row
     for t, cov in enumerate(covs):
         pos = outs[t][0][:, outs[t][0].shape[1] // 2:].reshape(-1, int(dims[t])).double()
         mu = pos.mean(0).cpu().numpy()
         emp = torch.cov(pos.T).cpu().numpy()
         worst_mean = max(worst_mean, float(np.max(np.abs(mu) / np.sqrt(np.diag(cov)))))
         worst_cov = max(worst_cov, float(np.linalg.norm(emp - cov) / np.linalg.norm(cov)))
-    return {"kind": kind, "targets": 48, "chains": C, "dims": [int(dims.min()), int(dims.max())],
-            "mean_d": float(dims.mean()), "steps": steps, "thinning": thin, "ms": ms,
-            "chain_steps_per_s": C * steps / (ms / 1e3), "fp32_tflops": flops / (ms / 1e3) / 1e12,
-            "fp32_peak_nominal_tflops": fp32_peak, "frac_fp32": flops / (ms / 1e3) / 1e12 / fp32_peak,
-            "worst_mean_error_sd": worst_mean, "worst_cov_rel_frobenius": worst_cov}
+        if kind == "mala":
+            lam = np.linalg.eigvalsh(cov)
+            worst_pred = max(worst_pred, langevin_cov_error(lam, step[t], kept))
+            for n in (2000, 20000, 200000):
+                kn = np.arange(n // thin)[(n // thin) // 2:] * thin + 1
+                pred_long[n] = max(pred_long.get(n, 0.0), langevin_cov_error(lam, step[t], kn))
+    out = {"kind": kind, "targets": 48, "chains": C, "dims": [int(dims.min()), int(dims.max())],
+           "mean_d": float(dims.mean()), "steps": steps, "thinning": thin, "ms": ms,
+           "chain_steps_per_s": C * steps / (ms / 1e3), "fp32_tflops": flops / (ms / 1e3) / 1e12,
+           "fp32_peak_nominal_tflops": fp32_peak, "frac_fp32": flops / (ms / 1e3) / 1e12 / fp32_peak,
+           "worst_mean_error_sd": worst_mean, "worst_cov_rel_frobenius": worst_cov}
+    if kind == "mala":
+        out["predicted_worst_cov_rel_frobenius"] = worst_pred
+        out["predicted_worst_cov_rel_frobenius_vs_steps"] = {str(k): v for k, v in sorted(pred_long.items())}
+    return out
+
+
+def langevin_cov_error(lam, h, kept_steps):
+    """Covariance error that slow mixing alone explains for MALA on N(0, Sigma)
+    from x0 ~ N(0, I): with every proposal accepted the chain is the
+    unadjusted Langevin recursion x' = x - (h^2 / 2) Sigma^-1 x + h xi, so
+    along an eigenvector (eigenvalue lam) the variance after n steps is
+    v* + a^(2n) (1 - v*), a = 1 - h^2 / (2 lam), v* = h^2 / (1 - a^2). The
+    sample covariance over the kept steps then has eigenvalues mean_n v_n;
+    returns its relative Frobenius distance to Sigma (sampling noise not
+    included)."""
+    import numpy as np
+    a = 1.0 - h * h / (2.0 * lam)
+    vstar = h * h / (1.0 - a * a)
+    vbar = np.array([np.mean(vs + a2 ** kept_steps * (1.0 - vs)) for vs, a2 in zip(vstar, a * a)])
+    return float(np.linalg.norm(vbar - lam) / np.linalg.norm(lam))
 
 
 def ctypes_sm_count():
@@ -490,31 +519,39 @@ def plain_arm(name, w, dev, n_train, n_prod, timed_from, mean_ref, var_ref, ess=
     return out
 
 
-def compare_arms(name, w, dev, T, P, precision, plain=True, graph=False):
-    """Equal-work comparison: the fused bundle and the plain FP32 form each run
-    T training + P production loops from the same seed. Wall clock covers the
-    whole schedule (training included, as ESS/s is defined); the fused arm is
-    timed on a second sampler after a warm-up run of the first (one-time
-    set-up, autotuning and workspace growth excluded), the plain arm from its
-    first loop, after an untimed warm-up run of one training and one
-    production loop. min-ESS: rank-normalised bulk ESS over the production
-    samples; moment error against the workload's reference moments. With `graph` the
-    fused arm's schedule is captured as one CUDA graph on the fresh sampler
-    (untimed, like the other one-time costs) and the timed run is its one
-    replay."""
+def compare_arms(name, w, dev, T, P, precision, seeds, plain=True, graph=True):
+    """Equal-work comparison at each seed: the fused bundle and the plain FP32
+    form each run T training + P production loops from the same seed. Wall
+    clock covers the whole schedule (training included, as ESS/s is
+    defined). One-time costs are excluded in both arms: the fused arm warms
+    up once (autotuning, workspace growth) on a sampler that is then
+    dropped, and with `graph` each seed's schedule is captured as a CUDA
+    graph before its timed replay (capture reported separately); the plain
+    arm runs one untimed training + production loop first. min-ESS:
+    rank-normalised bulk ESS over the production samples; moment error
+    against the workload's reference moments. Returns the per-seed results
+    and their means, with the ratios of the means (fused / plain)."""
+    import numpy as np
     import torch
     from flowmc_gb300 import diagnostics as D
     prec = "bf16" if precision == "bf16" else "float32"
-    out = {"workload": name, "seed": w["seed"], "training_loops": T, "production_loops": P}
-    cap_ms = None
-    for rep in range(2):
-        sampler, bundle, target, mean_ref, var_ref, x0 = build_sampler(name, w, T, P, prec, dev)
+    out = {"workload": name, "training_loops": T, "production_loops": P, "seeds": list(seeds),
+           "cuda_graph": graph, "precision": precision, "fused": [], "plain_fp32": []}
+    # fused warm-up (untimed): one full schedule at the first seed
+    sampler, _, _, _, _, x0 = build_sampler(name, dict(w, seed=seeds[0]), T, P, prec, dev)
+    sampler.sample(x0, {})
+    torch.cuda.synchronize()
+    del sampler
+    for sd in seeds:
+        ws = dict(w, seed=sd)
+        sampler, bundle, target, mean_ref, var_ref, x0 = build_sampler(name, ws, T, P, prec, dev)
+        cap_ms = None
         if graph:
             torch.cuda.synchronize()
-            t0 = time.perf_counter()
+            c0 = time.perf_counter()
             cap = sampler.capture(x0, {})
             torch.cuda.synchronize()
-            cap_ms = 1e3 * (time.perf_counter() - t0)
+            cap_ms = 1e3 * (time.perf_counter() - c0)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         if graph:
@@ -523,102 +560,223 @@ def compare_arms(name, w, dev, T, P, precision, plain=True, graph=False):
             sampler.sample(x0, {})
         torch.cuda.synchronize()
         secs = time.perf_counter() - t0
-    pos = sampler.resources["positions_production"].data
-    ess = D.ess_bulk(pos)
-    out["fused"] = {"seconds": secs, "min_ess": float(ess.min()), "min_ess_per_s": float(ess.min()) / secs,
-                    "moment_error": D.moment_error(pos, mean_ref, var_ref),
-                    "chain_steps_per_s": w["n_chains"] * (w["n_local"] + w["n_global"]) * (T + P) / secs,
-                    "cuda_graph": graph}
-    if graph:
-        out["fused"]["graph_capture_ms"] = cap_ms
-    if not plain:
-        return out
-    # one untimed training + production loop first: module loading and the
-    # allocator's first growth are one-time costs in the plain arm too
-    plain_arm(name, w, dev, 1, 1, 0, mean_ref, var_ref, ess=False)
-    pl = plain_arm(name, w, dev, T, P, 0, mean_ref, var_ref)
-    out["plain_fp32"] = {"seconds": pl["seconds"], "min_ess": pl.get("min_ess"),
-                         "min_ess_per_s": pl.get("min_ess_per_s"), "moment_error": pl.get("moment_error"),
-                         "chain_steps_per_s": pl["value"]}
-    f, q = out["fused"], out["plain_fp32"]
-    if q.get("min_ess_per_s"):
-        out["ratio_min_ess_per_s"] = f["min_ess_per_s"] / q["min_ess_per_s"]
-        out["ratio_moment_error"] = f["moment_error"] / q["moment_error"]
+        pos = sampler.resources["positions_production"].data
+        ess = D.ess_bulk(pos)
+        f = {"seed": sd, "seconds": secs, "min_ess": float(ess.min()), "min_ess_per_s": float(ess.min()) / secs,
+             "moment_error": D.moment_error(pos, mean_ref, var_ref),
+             "chain_steps_per_s": w["n_chains"] * (w["n_local"] + w["n_global"]) * (T + P) / secs}
+        if cap_ms is not None:
+            f["graph_capture_ms"] = cap_ms
+        out["fused"].append(f)
+        del sampler, bundle, pos
+        if graph:
+            del cap
+        if plain:
+            if len(out["plain_fp32"]) == 0:
+                # one untimed training + production loop: module loading and the
+                # allocator's first growth are one-time costs in the plain arm too
+                plain_arm(name, ws, dev, 1, 1, 0, mean_ref, var_ref, ess=False)
+            pl = plain_arm(name, ws, dev, T, P, 0, mean_ref, var_ref)
+            out["plain_fp32"].append({"seed": sd, "seconds": pl["seconds"], "min_ess": pl.get("min_ess"),
+                                      "min_ess_per_s": pl.get("min_ess_per_s"),
+                                      "moment_error": pl.get("moment_error"), "chain_steps_per_s": pl["value"]})
+        torch.cuda.empty_cache()
+
+    def stat(rows, k, f):
+        v = [r[k] for r in rows if r.get(k) is not None]
+        return f(v) if len(v) > (1 if f is _sd else 0) else None
+
+    summ = {}
+    for arm in ("fused", "plain_fp32"):
+        if out[arm]:
+            summ[arm] = {k: stat(out[arm], k, _mean) for k in ("min_ess_per_s", "moment_error",
+                                                                "chain_steps_per_s", "seconds")}
+            summ[arm]["moment_error_sd"] = stat(out[arm], "moment_error", _sd)
+    out["mean"] = summ
+    if "plain_fp32" in summ and summ["plain_fp32"]["min_ess_per_s"]:
+        fm, pm = summ["fused"], summ["plain_fp32"]
+        out["ratio_min_ess_per_s"] = fm["min_ess_per_s"] / pm["min_ess_per_s"]
+        out["ratio_moment_error"] = fm["moment_error"] / pm["moment_error"]
+        out["ratio_chain_steps_per_s"] = fm["chain_steps_per_s"] / pm["chain_steps_per_s"]
     return out
 
 
+def _mean(v):
+    return float(sum(v) / len(v))
+
+
+def _sd(v):
+    m = _mean(v)
+    return float((sum((x - m) ** 2 for x in v) / (len(v) - 1)) ** 0.5)
+
+
+def moment_trajectory(name, w, dev, n_loops, precision):
+    """The fused bundle for n_loops training + n_loops production loops; the
+    moment error and min-ESS of the production rows written so far, after
+    every production loop (does the workload converge on this schedule?)."""
+    import torch
+    from flowmc_gb300 import diagnostics as D
+    prec = "bf16" if precision == "bf16" else "float32"
+    sampler, bundle, target, mean_ref, var_ref, x0 = build_sampler(name, w, n_loops, n_loops, prec, dev)
+    segs = loop_segments(bundle.strategy_order, n_loops)
+    x, key = x0.to(dev), sampler.rng_key
+    blk = w["n_local"] + w["n_global"]
+    rows = []
+    for i, seg in enumerate(segs):
+        for s in seg:
+            key, sampler.resources, x = sampler.strategies[s](key, sampler.resources, x, {})
+        if i >= n_loops:
+            k = i - n_loops + 1
+            pos = sampler.resources["positions_production"].data[:, :k * blk]
+            ess = D.ess_bulk(pos) if k >= 2 else None
+            rows.append({"production_loops": k, "moment_error": D.moment_error(pos, mean_ref, var_ref),
+                         "min_ess": float(ess.min()) if ess is not None else None})
+    torch.cuda.synchronize()
+    return {"workload": name, "training_loops": n_loops, "production_loops": n_loops, "rows": rows}
+
+
 # ---------------------------------------------------------------- CPU baseline
-def cpu_baseline(name, w, budget_s: float = 20.0):
-    """The oracle restatement (float64 NumPy, all host cores through BLAS)
-    timed on a bounded sample of the same loop, scaled to chain-steps/s of
-    the whole workload: one production loop (local + global phase) for a
-    few chains, and one training step on a small batch, extrapolated by
-    rows."""
+def oracle_target(name, w):
+    """The workload's target as an oracle target dict."""
     import numpy as np
-    from oracle import flow as OF
-    from oracle import flow_torch as OFT
-    from oracle import kernels as OK
-    from flowmc_gb300.diagnostics import rosenbrock_chain_moments  # noqa: F401  (same package data)
-    rng = np.random.default_rng(0)
     d = w["d"]
     if name == "rosenbrock128":
-        t = {"kind": "rosenbrock", "n_dim": d, "a": 20.0, "b": 1.0, "c": 5.0}
-    elif name == "dualmoon5":
-        t = {"kind": "dual_moon", "n_dim": d, "r0": 2.0, "sr": 0.1, "mu": 3.0, "s0": 0.6}
-    else:
-        t = {"kind": "mixture", "mean": mixture_means(), "inv_var": np.full((4, 64), 2.0),
-             "log_w": np.full(4, np.log(0.25) - 32 * np.log(2 * np.pi * 0.5))}
-    P = 3 * w["n_bins"] + 1
-    layers = []
-    for i in range(w["n_layers"]):
-        shape = [d] + w["hidden"] + [d * P]
-        layers.append({"W": [rng.normal(size=(b, a)) * 0.05 / np.sqrt(a) for a, b in zip(shape[:-1], shape[1:])],
-                       "b": [np.zeros(b) for b in shape[1:]], "scale": 0.0, "shift": 0.0,
-                       "mask": ((np.arange(d) + i) % 2).astype(bool)})
-    flow = OF.Flow(layers, w["n_bins"], np.zeros(d), np.eye(d))
-    C = 8
-    x = rng.normal(size=(C, d)) * 0.3 + 0.5
-    S1, S2 = w["n_local"], w["n_global"]
+        return {"kind": "rosenbrock", "n_dim": d, "a": 20.0, "b": 1.0, "c": 5.0}
+    if name == "dualmoon5":
+        return {"kind": "dual_moon", "n_dim": d, "r0": 2.0, "sr": 0.1, "mu": 3.0, "s0": 0.6}
+    return {"kind": "mixture", "mean": mixture_means(), "inv_var": np.full((4, 64), 2.0),
+            "log_w": np.full(4, np.log(0.25) - 32 * np.log(2 * np.pi * 0.5))}
+
+
+class OracleBundle:
+    """The bundle's loop restated by the oracle (float64 NumPy on the host
+    cores, BLAS threads on every core), on a bounded sample of the workload:
+    `n_chains` chains of the same target, local kernel, step counts and flow
+    shape. A training loop (between its local and global phase, as the
+    bundle's schedule has it, RQSpline_MALA.py:251-273) selects `n_max` rows
+    from the last 100 rows of every chain (train_model.py:66-80) and takes
+    n_epochs AdamW steps on them, one full batch per epoch (the reference's
+    rule when batch_size > n_max_examples, nf_model/base.py:148-149)."""
+
+    def __init__(self, name, w, n_chains, n_max, seed=0):
+        import numpy as np
+        from oracle import flow as OF
+        self.np = np
+        self.w, self.C, self.n_max = w, n_chains, n_max
+        self.rng = np.random.default_rng(seed)
+        self.t = oracle_target(name, w)
+        d = w["d"]
+        P = 3 * w["n_bins"] + 1
+        layers = []
+        for i in range(w["n_layers"]):
+            shape = [d] + w["hidden"] + [d * P]
+            layers.append({"W": [self.rng.normal(size=(b, a)) * 0.05 / np.sqrt(a)
+                                 for a, b in zip(shape[:-1], shape[1:])],
+                           "b": [np.zeros(b) for b in shape[1:]], "scale": 0.0, "shift": 0.0,
+                           "mask": ((np.arange(d) + i) % 2).astype(bool)})
+        self.flow = OF.Flow(layers, w["n_bins"], np.zeros(d), np.eye(d))
+        n_par = OF.flatten(self.flow).size
+        self.st = OF.AdamWState(np.zeros(n_par), np.zeros(n_par))
+        self.x = self.rng.normal(size=(n_chains, d))
+        self.hist = np.zeros((n_chains, 0, d))
+
+    def loop(self, train: bool):
+        from oracle import flow as OF
+        from oracle import flow_torch as OFT
+        from oracle import kernels as OK
+        np, w, C, d = self.np, self.w, self.C, self.w["d"]
+        S1, S2 = w["n_local"], w["n_global"]
+        pos, _, _, self.x = OK.take_serial_steps(w["local"], self.t, self.x, S1, self.rng.normal(size=(C, S1, d)),
+                                                 self.rng.uniform(size=(C, S1)), step_size=w["step"],
+                                                 n_leapfrog=w["n_leapfrog"], M=np.eye(d))
+        self.hist = np.concatenate([self.hist, pos], 1)[:, -100:]
+        if train:
+            idx = self.rng.integers(0, self.hist.shape[0] * self.hist.shape[1], size=self.n_max)
+            data = OF.select_training_data(self.hist, 100, idx)
+            self.flow.data_mean = data.mean(0)
+            self.flow.data_cov = np.diag(data.var(0, ddof=1))
+            for _ in range(w["n_epochs"]):
+                _, g = OFT.loss_and_grad(self.flow, data)
+                p, _ = OF.adamw_update(OF.flatten(self.flow), g, self.st, w["lr"])
+                OF.unflatten(self.flow, p)
+        gx, _, _ = OK.nf_proposal_kernel(self.flow, self.t, self.x, self.rng.normal(size=(C, S2, d)),
+                                         self.rng.uniform(1e-12, 1.0, size=(C, S2)))
+        self.x = gx[:, -1]
+        self.hist = np.concatenate([self.hist, gx], 1)[:, -100:]
+
+
+REF_CHAINS, REF_MAX = 8, 64
+
+
+def ref_sample_text(w, C, n_max):
+    return (f"oracle float64 NumPy restatement of the bundle loop on {C} of the {w['n_chains']} chains "
+            f"(same target, {w['local']} kernel, {w['n_local']} local + {w['n_global']} global steps, "
+            f"{w['n_layers']}x{w['hidden']}x{w['n_bins']} flow); training loops select {n_max} of the "
+            f"{w['n_max']} examples and take {w['n_epochs']} full-batch AdamW steps")
+
+
+def cpu_baseline(name, w, budget_s: float = 20.0):
+    """The oracle restatement timed on the host cores on a bounded sample of
+    the workload (OracleBundle on REF_CHAINS chains): one training loop and
+    then production loops until about `budget_s` seconds have passed. The
+    value is the measured chain-steps/s of that sample, not a projection."""
+    ob = OracleBundle(name, w, REF_CHAINS, REF_MAX, seed=w["seed"])
     t0 = time.perf_counter()
-    OK.take_serial_steps(w["local"], t, x, S1, rng.normal(size=(C, S1, d)), rng.uniform(size=(C, S1)),
-                         step_size=w["step"], n_leapfrog=w["n_leapfrog"], M=np.eye(d))
-    t_local = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    OK.nf_proposal_kernel(flow, t, x, rng.normal(size=(C, S2, d)), rng.uniform(size=(C, S2)))
-    t_global = time.perf_counter() - t0
-    rows = 256
-    t0 = time.perf_counter()
-    OFT.loss_and_grad(flow, rng.normal(size=(rows, d)))
-    t_train_rows = time.perf_counter() - t0
-    n_loops = 40
-    n_train = 20
-    per_chain_loop = (t_local + t_global) / C
-    train_loop = t_train_rows / rows * w["n_epochs"] * w["n_max"]
-    total = n_loops * per_chain_loop * w["n_chains"] + n_train * train_loop
-    value = w["n_chains"] * (S1 + S2) * n_loops / total
-    try:
-        import threadpoolctl
-        cores = max(int(i.get("num_threads", 1)) for i in threadpoolctl.threadpool_info()) or os.cpu_count()
-    except Exception:
-        cores = os.cpu_count()
-    return {"value": value, "unit": "chain-steps/s", "cores": cores, "kind": "port",
-            "sample": (f"oracle float64 NumPy: one loop ({S1} local + {S2} global steps) for {C} chains "
-                       f"({t_local + t_global:.1f}s) and one flow loss+gradient on {rows} rows "
-                       f"({t_train_rows:.1f}s), scaled to {w['n_chains']} chains x 40 loops with 20 training "
-                       f"loops of {w['n_epochs']} x {w['n_max']} rows")}
+    ob.loop(True)
+    loops = 1
+    while time.perf_counter() - t0 < budget_s and loops < 40:
+        ob.loop(False)
+        loops += 1
+    secs = time.perf_counter() - t0
+    return {"value": REF_CHAINS * (w["n_local"] + w["n_global"]) * loops / secs, "unit": "chain-steps/s",
+            "cores": os.cpu_count(), "kind": "port",
+            "sample": ref_sample_text(w, REF_CHAINS, REF_MAX) + f"; measured over 1 training + {loops - 1} "
+                      f"production loops in {secs:.1f} s"}
+
+
+def schedule(W, K):
+    """(training loops, production loops) of a W + K loop run: the first half
+    (at least W) trains."""
+    n_total = W + K
+    n_train = max(W, n_total // 2)
+    return n_train, n_total - n_train
+
+
+def workload_config(name, w, W, K, world):
+    n_train, n_prod = schedule(W, K)
+    return {"workload": name, "n_dim": w["d"], "n_chains": w["n_chains"], "local_kernel": w["local"],
+            "step_size": w["step"], "n_leapfrog": w["n_leapfrog"],
+            "n_local_steps": w["n_local"], "n_global_steps": w["n_global"],
+            "flow": f"{w['n_layers']}x{w['hidden']}x{w['n_bins']} bins", "learning_rate": w["lr"],
+            "n_training_loops": n_train, "n_production_loops": n_prod, "timed_loops": K, "batch_size": w["batch"],
+            "n_epochs": w["n_epochs"], "n_max_examples": w["n_max"], "parallelism": f"replicas{world}",
+            "l2": "working set (chain buffers, flow weights) larger than L2; no flush"}
 
 
 def reference_arm(args, w):
-    v = cpu_baseline(args.workload, w)
-    per_loop = w["n_chains"] * (w["n_local"] + w["n_global"])
-    line = {"impl": "reference", "metric": METRIC, "value": v["value"], "unit": v["unit"], "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * per_loop / v["value"] if v.get("value") else None,
-            "higher_is_better": True, "scaling": "weak",
+    """The reference's CPU path (the oracle restatement; JAX is not in the
+    image) on the same workload and schedule: W untimed warm-up loops, then
+    the K timed loops, each one loop of OracleBundle on REF_CHAINS chains
+    (training loops first, as in the fused arm). value = the sample's
+    chain-steps over the timed loops / their measured wall time."""
+    W, K = max(1, args.warmup), max(1, args.steps)
+    n_train, _ = schedule(W, K)
+    ob = OracleBundle(args.workload, w, REF_CHAINS, REF_MAX, seed=w["seed"])
+    for i in range(W):
+        ob.loop(i < n_train)
+    t0 = time.perf_counter()
+    for i in range(W, W + K):
+        ob.loop(i < n_train)
+    secs = time.perf_counter() - t0
+    value = REF_CHAINS * (w["n_local"] + w["n_global"]) * K / secs
+    sample = ref_sample_text(w, REF_CHAINS, REF_MAX) + f"; {K} timed loops in {secs:.1f} s"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "chain-steps/s", "n_gpus": args.gpus,
+            "steps": K, "warmup": W, "ms_per_step": 1e3 * secs / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, **{k: w[k] for k in ("d", "n_chains", "n_local", "n_global")}},
-            "cpu_baseline": v,
-            "e2e": {"value": v["value"], "unit": v["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "config": workload_config(args.workload, w, W, K, args.gpus),
+            "cpu_baseline": {"value": value, "unit": "chain-steps/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "chain-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
@@ -695,12 +853,19 @@ def main():
                     help="write a per-kernel launch list (CUPTI activity timestamps) of the K loops to this "
                          "file instead of the bench line; its times are not bench values")
     ap.add_argument("--seeds", default="",
-                    help="with --compare: comma-separated workload seeds; the fused arm runs each, the plain arm the first")
+                    help="with --compare: comma-separated workload seeds; both arms run each")
     ap.add_argument("--compare", default="",
-                    help="T,P: fused bundle and plain FP32 form on the same workload and seed with T training + P "
+                    help="T,P: fused bundle and plain FP32 form on the same workload and seeds with T training + P "
                          "production loops each; prints their min-ESS/s and moment errors instead of the bench line")
-    ap.add_argument("--compare-graph", action="store_true",
-                    help="with --compare: time the fused arm as one replay of its schedule captured as a CUDA graph")
+    ap.add_argument("--no-plain", action="store_true", help="with --compare: the fused arm only")
+    ap.add_argument("--cmp-workload", default="mixture64", choices=list(WORKLOADS),
+                    help="workload of the equal-work comparison carried by the bench line")
+    ap.add_argument("--cmp-loops", default="2,20", help="T,P of that comparison (empty: skip it)")
+    ap.add_argument("--cmp-seeds", default="3,4,5,6", help="seeds of that comparison")
+    ap.add_argument("--trajectory", type=int, default=0,
+                    help="run T training + T production loops of the fused bundle and print the moment error of "
+                         "the production rows after every production loop")
+    ap.add_argument("--batched-steps", type=int, default=2000, help="steps of --probe batched")
     ap.add_argument("--eager", action="store_true",
                     help="launch the timed loops eagerly instead of replaying them as one captured CUDA graph")
     ap.add_argument("--plain-full", action="store_true",
@@ -734,8 +899,8 @@ def main():
     # independent replicas: every rank samples its own chains
     w["seed"] = replicas.replica_seed(w["seed"], rank)
     if args.probe == "batched":
-        print(json.dumps({"probe": "batched_dense", "mala": batched_probe(dev, "mala"),
-                          "hmc": batched_probe(dev, "hmc")}), flush=True)
+        print(json.dumps({"probe": "batched_dense", "mala": batched_probe(dev, "mala", steps=args.batched_steps),
+                          "hmc": batched_probe(dev, "hmc", steps=args.batched_steps)}), flush=True)
         return
     if args.probe == "train":
         print(json.dumps({"probe": "flow_training_d32", "bf16": train_probe(dev, "bf16"),
@@ -757,17 +922,17 @@ def main():
     if args.compare:
         T, P = (int(v) for v in args.compare.split(","))
         seeds = [int(v) for v in args.seeds.split(",")] if args.seeds else [w["seed"]]
-        res = []
-        for i, sd in enumerate(seeds):
-            ws = dict(w, seed=sd)
-            res.append(compare_arms(args.workload, ws, dev, T, P, args.precision, plain=(i == 0),
-                                    graph=args.compare_graph))
-        print(json.dumps({"compare": res[0] if len(res) == 1 else res}), flush=True)
+        res = compare_arms(args.workload, w, dev, T, P, args.precision, seeds, plain=not args.no_plain,
+                           graph=not args.eager)
+        print(json.dumps({"compare": res}), flush=True)
+        return
+    if args.trajectory:
+        print(json.dumps({"trajectory": moment_trajectory(args.workload, w, dev, args.trajectory,
+                                                          args.precision)}), flush=True)
         return
     W, K = max(1, args.warmup), max(1, args.steps)
     n_total = W + K
-    n_train = max(W, n_total // 2)
-    n_prod = n_total - n_train
+    n_train, n_prod = schedule(W, K)
     precision = "bf16" if args.precision == "bf16" else "float32"
     sampler, bundle, target, mean_ref, var_ref, x0 = build_sampler(args.workload, w, n_train, n_prod, precision, dev)
     segs = loop_segments(bundle.strategy_order, n_train)
@@ -851,7 +1016,7 @@ def main():
     ga = acc_g.reshape(w["n_chains"], -1, blk)[:, :, w["n_local"]:].mean().item()
     extra["acceptance"] = {"local": la, "global": ga}
 
-    # ---- roofline per phase (device time from CUDA events inside the timed region)
+    # ---- per phase (device time from CUDA events inside the timed region)
     hbm, bf16, bf16_s, src = measured_peaks()
     tot = prof.totals_ms()
     cnt = prof.counts()
@@ -872,26 +1037,24 @@ def main():
         flops = (2 * props + props / w["n_global"]) * ff
         t_s = tot["nf_global"] / 1e3
         kernels["nf_global"] = {"ms": tot["nf_global"], "launches": cnt["nf_global"],
-                                "achieved_tflops": flops / t_s / 1e12, "frac_bf16": flops / t_s / 1e12 / bf16,
+                                "achieved_tflops": flops / t_s / 1e12, "frac_bf16_sustained": flops / t_s / 1e12 / bf16_s,
                                 "useful_flops_per_sample_pass": ff}
     if "train" in tot:
         steps = prof.units["train"]
         flops = steps * w["batch"] * 3 * ff
         t_s = tot["train"] / 1e3
         kernels["train"] = {"ms": tot["train"], "launches": cnt["train"], "achieved_tflops": flops / t_s / 1e12,
-                            "frac_bf16": flops / t_s / 1e12 / bf16}
-    dom = max(kernels, key=lambda k: kernels[k]["ms"])
-    dk = kernels[dom]
-    if dom == "local_steps":
-        roof = {"bound": "hbm", "kernel": "k_local_steps", "achieved": dk["achieved_gbs"], "peak": hbm,
-                "unit": "GB/s", "frac": dk["frac_hbm"], "traffic": None, "peak_source": src}
-    else:
-        peak = bf16 if args.precision == "bf16" else None
-        roof = {"bound": "tensor", "kernel": dom, "achieved": dk["achieved_tflops"], "peak": peak or bf16,
-                "unit": "TFLOP/s", "frac": dk["achieved_tflops"] / (peak or bf16), "traffic": None,
-                "peak_source": src if peak else f"{src} bf16 (this run used FP32 SIMT GEMMs)"}
+                            "frac_bf16_sustained": flops / t_s / 1e12 / bf16_s}
 
-    kernels["local_steps_hbm_probe"] = local_hbm_probe(dev)
+    # ---- per kernel: CUDA events around every launch (library timers, on the
+    # launch stream) over one eager training loop and one eager production
+    # loop run after the timed region, weighted by the timed mix
+    n_tr_timed = max(0, n_train - W)
+    per_k = kernel_timing_pass(sampler, bundle, segs, x, key, n_train, n_tr_timed, K - n_tr_timed, w, hbm, bf16_s)
+    kernels["per_kernel"] = per_k
+    roof = roofline_line(per_k, hbm, bf16, bf16_s, src, w)
+
+    kernels["local_steps_hbm_probe"] = local_hbm_probe(dev, lanes=(0, 8, 16, 32))
     # the survey's "next" components, each on its own probe workload (seconds in total)
     kernels["parallel_tempering_probe"] = pt_probe(dev)
     kernels["realnvp_probe"] = realnvp_probe(dev)
@@ -906,14 +1069,9 @@ def main():
         "metric": METRIC, "value": value, "unit": "chain-steps/s", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "bf16" if args.precision == "bf16" else "f32", "data": "synthetic",
-        "config": {"workload": args.workload, "n_dim": w["d"], "n_chains": w["n_chains"],
-                   "local_kernel": w["local"], "n_local_steps": w["n_local"], "n_global_steps": w["n_global"],
-                   "flow": f"{w['n_layers']}x{w['hidden']}x{w['n_bins']} bins", "n_training_loops": n_train,
-                   "n_production_loops": n_prod, "timed_loops": K, "batch_size": w["batch"],
-                   "n_epochs": w["n_epochs"], "parallelism": f"replicas{world}",
-                   "l2": "working set (chain buffers, flow weights) larger than L2; no flush",
-                   "autotuned": {"lanes_per_chain": getattr(sampler.resources["local_sampler"], "lanes_per_chain", 0),
-                                 "flow_gemm_bn": getattr(sampler.resources["model"], "gemm_bn", 0)}},
+        "config": workload_config(args.workload, w, W, K, world),
+        "autotuned": {"lanes_per_chain": getattr(sampler.resources["local_sampler"], "lanes_per_chain", 0),
+                      "flow_gemm_bn": getattr(sampler.resources["model"], "gemm_bn", 0)},
         "roofline": roof, "kernels": kernels, "gpu_launches": launches, "clocks": clk,
         "wall_s": wall, "cuda_graph": graph is not None, **extra,
     }
@@ -921,6 +1079,10 @@ def main():
         line["graph_capture_ms"] = capture_ms
     if e2e is not None:
         line["e2e"] = e2e
+    del sampler, bundle, pos
+    graph = None
+    torch.cuda.empty_cache()
+    ratio = {}
     if rank == 0 and (args.plain_full or args.plain_loops > 0):
         if args.plain_full:
             pl = plain_arm(args.workload, w, dev, n_train, n_prod, W, mean_ref, var_ref)
@@ -928,10 +1090,28 @@ def main():
             nt = max(1, args.plain_loops // 2)
             pl = plain_arm(args.workload, w, dev, nt, args.plain_loops - nt, 0, mean_ref, var_ref, ess=False)
         line["plain_fp32"] = pl
-        ratio = {"chain_steps_per_s": value / pl["value"]}
+        ratio = {"workload": args.workload, "chain_steps_per_s": value / pl["value"]}
         if "min_ess_per_s" in pl and "min_ess_per_s" in line:
             ratio["min_ess_per_s"] = line["min_ess_per_s"] / pl["min_ess_per_s"]
             ratio["moment_error_ratio"] = line["moment_error"] / pl["moment_error"]
+    if rank == 0 and args.cmp_loops:
+        # the equal-work, converged comparison of the two forms (both arms
+        # trained, several seeds), on its own workload
+        T, P = (int(v) for v in args.cmp_loops.split(","))
+        seeds = [int(v) for v in args.cmp_seeds.split(",")]
+        wc = dict(WORKLOADS[args.cmp_workload])
+        cmp_ = compare_arms(args.cmp_workload, wc, dev, T, P, args.precision, seeds, plain=True, graph=True)
+        line["comparison"] = cmp_
+        if "ratio_min_ess_per_s" in cmp_:
+            ratio["comparison"] = {"workload": args.cmp_workload, "seeds": seeds,
+                                   "min_ess_per_s": cmp_["ratio_min_ess_per_s"],
+                                   "moment_error_ratio": cmp_["ratio_moment_error"],
+                                   "chain_steps_per_s": cmp_["ratio_chain_steps_per_s"],
+                                   "fused_moment_error": cmp_["mean"]["fused"]["moment_error"],
+                                   "plain_moment_error": cmp_["mean"]["plain_fp32"]["moment_error"]}
+            ratio["min_ess_per_s"] = cmp_["ratio_min_ess_per_s"]
+            ratio["moment_error_ratio"] = cmp_["ratio_moment_error"]
+    if ratio:
         line["fused_over_plain"] = ratio
     if rank == 0 and not args.no_cpu:
         try:
@@ -942,6 +1122,97 @@ def main():
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def kernel_timing_pass(sampler, bundle, segs, x, key, n_train, n_tr_timed, n_pr_timed, w, hbm, bf16_s):
+    """Per-kernel CUDA-event times (the library's launch timers) over one
+    eager training loop and one eager production loop of the same sampler;
+    totals are weighted to the timed mix (n_tr_timed training + n_pr_timed
+    production loops). For the tensor-core kernels: algorithmic FLOPs per
+    launch over the average launch time against the sustained BF16 peak
+    (they run inside a long step); the others against HBM bandwidth."""
+    import torch
+    from flowmc_gb300 import _lib
+    res = {}
+    runs = (("train", segs[0], n_tr_timed), ("production", segs[-1], n_pr_timed))
+    for tag, seg, weight in runs:
+        torch.cuda.synchronize()
+        _lib.kernel_timing(True)
+        for s in seg:
+            key, sampler.resources, x = sampler.strategies[s](key, sampler.resources, x, {})
+        torch.cuda.synchronize()
+        got = _lib.kernel_timing_read()
+        _lib.kernel_timing(False)
+        for k, v in got.items():
+            r = res.setdefault(k, {"launches_per_loop": {}, "ms": 0.0, "launches": 0.0, "flops": 0.0,
+                                   "bytes": 0.0})
+            r["launches_per_loop"][tag] = v["launches"]
+            r["ms"] += weight * v["ms"]
+            r["launches"] += weight * v["launches"]
+            r["flops"] += weight * v["flops"]
+            r["bytes"] += weight * v["bytes"]
+    out = {}
+    total = sum(r["ms"] for r in res.values()) or 1.0
+    for k, r in sorted(res.items(), key=lambda kv: -kv[1]["ms"]):
+        n = max(r["launches"], 1.0)
+        o = {"launches_per_loop": r["launches_per_loop"], "avg_us": 1e3 * r["ms"] / n,
+             "timed_mix_ms": r["ms"], "share_of_timed_kernels": r["ms"] / total}
+        if r["flops"] > 0:
+            o["flops_per_launch"] = r["flops"] / n
+            o["achieved_tflops"] = r["flops"] / (r["ms"] / 1e3) / 1e12
+            o["frac_bf16_sustained"] = o["achieved_tflops"] / bf16_s
+        if r["bytes"] > 0:
+            o["bytes_per_launch"] = r["bytes"] / n
+            o["achieved_gbs"] = r["bytes"] / (r["ms"] / 1e3) / 1e9
+            o["frac_hbm"] = o["achieved_gbs"] / hbm
+        out[k] = o
+    out["_how"] = ("CUDA events recorded by the library on each launch's stream around every launch of one eager "
+                   "training loop and one eager production loop, weighted to the timed loop mix")
+    return out
+
+
+def spline_operand_traffic(w, rows):
+    """Operand traffic of one k_tc_spline launch over `rows` rows of the
+    workload's flow (analytic): every (128-row, group) tile loads its A tile
+    and the group's weights from L2 into shared memory, plus the epilogue's
+    reads and writes of x and its log-det partials. Most of it is L2 -> SMEM
+    (A and the weights are L2-resident); ncu is not run on the tcgen05
+    kernels here, so this model stands in for dram__bytes."""
+    P = 3 * w["n_bins"] + 1
+    dg = 256 // P
+    bn = ((dg * P + 15) // 16) * 16
+    nt = w["d"] // 2
+    groups = -(-nt // dg)
+    H = w["hidden"][-1]
+    tiles = -(-rows // 128) * groups
+    return tiles * (128 * H * 2 + bn * H * 2) + rows * nt * 8 + rows * 3 * groups * 4
+
+
+def roofline_line(per_k, hbm, bf16, bf16_s, src, w):
+    """The dominant kernel of the timed mix (largest share of per-kernel event
+    time) with its achieved rate against the sustained peak. For the fused
+    spline kernels `traffic` is the analytic per-launch operand traffic
+    (spline_operand_traffic); ncu is not run on the tcgen05 kernels here."""
+    ks = [k for k in per_k if not k.startswith("_")]
+    dom = max(ks, key=lambda k: per_k[k]["timed_mix_ms"])
+    d = per_k[dom]
+    if "achieved_tflops" in d and dom.startswith("k_tc"):
+        r = {"bound": "tensor", "kernel": dom, "achieved": d["achieved_tflops"], "peak": bf16_s,
+             "unit": "TFLOP/s", "frac": d["achieved_tflops"] / bf16_s, "traffic": None,
+             "peak_source": f"{src} bf16_tflops_sustained (kernel timed inside a long step)",
+             "avg_launch_us": d["avg_us"], "flops_per_launch": d["flops_per_launch"]}
+        if dom in ("k_tc_spline_fwd", "k_tc_spline_inv"):
+            P = 3 * w["n_bins"] + 1
+            rows = d["flops_per_launch"] / (2.0 * (w["d"] // 2) * P * w["hidden"][-1])
+            r["traffic"] = spline_operand_traffic(w, int(round(rows)))
+            r["traffic_source"] = ("analytic: A and weight tiles loaded L2 -> shared memory per (128-row, group) "
+                                   "tile plus the epilogue's x and partials, per launch; ncu is not run on the "
+                                   "tcgen05 kernels on this pool")
+            r["rows_per_launch"] = rows
+        return r
+    return {"bound": "hbm", "kernel": dom, "achieved": d.get("achieved_gbs"), "peak": hbm, "unit": "GB/s",
+            "frac": (d.get("achieved_gbs") or 0.0) / hbm, "traffic": None, "peak_source": src,
+            "avg_launch_us": d["avg_us"]}
 
 
 def end_to_end(sampler, bundle, w, dev, n_train_loops, n_prod_loops, x_dev, graph=True):

@@ -135,6 +135,12 @@ _SIGNATURES = {
         ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
         ctypes.c_void_p]),
     "fmc_device_error": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int32), ctypes.c_int32]),
+    "fmc_device_error_set": (ctypes.c_int, [ctypes.c_int32]),
+    "fmc_kernel_timing_enable": (ctypes.c_int, [ctypes.c_int32]),
+    "fmc_kernel_timing_reset": (ctypes.c_int, []),
+    "fmc_kernel_timing_read": (ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(ctypes.c_int64),
+                                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                              ctypes.POINTER(ctypes.c_double)]),
     "fmc_selftest_bounded_wait": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p]),
     "fmc_flow_forward": (ctypes.c_int, [ctypes.POINTER(FmcFlow), ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
@@ -281,6 +287,29 @@ def column_stats(x: torch.Tensor, mean: torch.Tensor, var: torch.Tensor, ws: "Wo
     ptr, size = ws.get(nb.value, x.device)
     check(lib().fmc_column_stats(x.data_ptr(), n, d, mean.data_ptr(), var.data_ptr(), ptr, size,
                                  stream_handle(x.device)))
+
+
+KERNEL_IDS = {"k_tc_spline_fwd": 0, "k_tc_spline_inv": 1, "k_tc_spline_bwd": 2, "k_tc_gemm_tanh": 3,
+              "k_tc_gemm_dtanh": 4, "k_tc_gemm_f32": 5, "k_local_steps": 6, "k_nf_accept": 7}
+
+
+def kernel_timing(on: bool) -> None:
+    """Start (and reset) or stop the library's per-kernel event timing."""
+    check(lib().fmc_kernel_timing_enable(1 if on else 0))
+    if on:
+        check(lib().fmc_kernel_timing_reset())
+
+
+def kernel_timing_read() -> dict:
+    """{kernel: {launches, ms, flops, bytes}} since the last reset (synchronises)."""
+    out = {}
+    for name, kid in KERNEL_IDS.items():
+        n, ms, fl, by = ctypes.c_int64(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        check(lib().fmc_kernel_timing_read(kid, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(fl),
+                                           ctypes.byref(by)))
+        if n.value:
+            out[name] = {"launches": int(n.value), "ms": ms.value, "flops": fl.value, "bytes": by.value}
+    return out
 
 
 def launch_count() -> int:

@@ -62,6 +62,21 @@ void set_error(const char* fmt, ...);
 int sm_count();  // cached per device
 void count_launch();  // process-wide tally of kernel launches (fmc_launch_count)
 
+// ---------------------------------------------------------------- kernel timing
+// Optional per-kernel timing (fmc_kernel_timing_*): while enabled, a
+// KernelTimer scope records a CUDA event pair on the launch stream around
+// the launch it encloses, together with the launch's algorithmic FLOPs and
+// bytes as the caller states them. Launches on a capturing stream are not
+// timed. The ids below are the FMC_KT_* values of flowmc.h.
+struct KernelTimer {
+  int slot = -1;
+  cudaStream_t st = nullptr;
+  KernelTimer(int kid, cudaStream_t stream, double flops, double bytes);
+  ~KernelTimer();
+  KernelTimer(const KernelTimer&) = delete;
+  KernelTimer& operator=(const KernelTimer&) = delete;
+};
+
 // ---------------------------------------------------------------- Philox
 // Philox-4x32 with 10 rounds, constants from the SC'11 paper (Table 2 and
 // the Weyl key schedule). counter = 4 x u32, key = 2 x u32.

@@ -115,9 +115,19 @@ static int launch_tc(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& 
   const int64_t items = tiles * splits;
   const int64_t grid = items < sm_count() ? items : sm_count();   // persistent: one CTA per SM
   void* out = splits > 1 ? (void*)ep.kpart : C;
-  kern<<<(unsigned)grid, tc::kThreads, TOTAL, st>>>(ma, mb, mc, (int)M, N, K, ep, out, ldc, n_store, splits, M * ldc,
-                                                   err);
-  FMC_LAUNCH_CHECK();
+  {
+    const bool bf16_out = EPI == tc::TC_EPI_TANH_BF16 || EPI == tc::TC_EPI_DTANH_BF16;
+    const int kid = EPI == tc::TC_EPI_TANH_BF16 ? FMC_KT_TC_GEMM_TANH
+                    : EPI == tc::TC_EPI_DTANH_BF16 ? FMC_KT_TC_GEMM_DTANH
+                                                   : FMC_KT_TC_GEMM_F32;
+    // A and B once, C written (bf16 or fp32), the tanh input read back in mode 2
+    const double bytes = (double)M * K * 2 + (double)N * K * 2 + (double)M * N * (bf16_out ? 2 : 4) +
+                         (EPI == tc::TC_EPI_DTANH_BF16 ? (double)M * N * 2 : 0.0);
+    KernelTimer kt(kid, st, 2.0 * (double)M * N * K, bytes);
+    kern<<<(unsigned)grid, tc::kThreads, TOTAL, st>>>(ma, mb, mc, (int)M, N, K, ep, out, ldc, n_store, splits,
+                                                     M * ldc, err);
+    FMC_LAUNCH_CHECK();
+  }
   if (splits > 1) {
     int64_t blocks = (M * n_store + 255) / 256;
     if (blocks > (int64_t)sm_count() * 8) blocks = (int64_t)sm_count() * 8;
@@ -338,6 +348,11 @@ extern "C" int fmc_selftest_bounded_wait(int32_t* timed_out, void* stream) {
   FMC_CUDA_TRY(cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, st));
   FMC_CUDA_TRY(cudaStreamSynchronize(st));
   *timed_out = h;
+  return FMC_OK;
+}
+
+extern "C" int fmc_device_error_set(int32_t value) {
+  FMC_CUDA_TRY(cudaMemcpyToSymbol(g_tc_error, &value, sizeof(int)));
   return FMC_OK;
 }
 

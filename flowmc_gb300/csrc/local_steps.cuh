@@ -449,6 +449,10 @@ int launch_local_t(const LocalArgs& a0, cudaStream_t st) {
   const int64_t need = (a.C_pad + gpb - 1) / gpb;
   const int64_t cap = (int64_t)sm_count() * per_sm;
   const int blocks = (int)(need < cap ? need : cap);
+  // algorithmic bytes: the stored rows (float32 position + log-density +
+  // acceptance per thinned step), plus the starting state read once
+  const double rows = a.out_pos ? (double)a.C * ((a.S + a.thin - 1) / a.thin) : 0.0;
+  KernelTimer kt(FMC_KT_LOCAL_STEPS, st, 0.0, rows * (4.0 * a.d + 8.0) + (double)a.C * (4.0 * a.d + 4.0));
   kern<<<blocks, threads, smem, st>>>(a);
   FMC_LAUNCH_CHECK();
   return FMC_OK;

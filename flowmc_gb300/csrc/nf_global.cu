@@ -115,6 +115,10 @@ static int launch_nf_t(const NfArgs& a0, cudaStream_t st) {
   int64_t blocks = (a.C_pad + gpb - 1) / gpb;
   const int64_t cap = (int64_t)sm_count() * 8;
   if (blocks > cap) blocks = cap;
+  // proposals and their flow densities read, thinned rows written
+  const double n_rec = (double)((a.S + a.thin - 1) / a.thin);
+  KernelTimer kt(FMC_KT_NF_ACCEPT, st, 0.0,
+                 (double)a.C * a.S * (4.0 * a.d + 4.0) + (double)a.C * n_rec * (4.0 * a.d + 8.0));
   k_nf_accept<TGT, G, V><<<(int)blocks, threads, smem, st>>>(a);
   FMC_LAUNCH_CHECK();
   return FMC_OK;

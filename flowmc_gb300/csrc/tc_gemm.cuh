@@ -193,6 +193,19 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+// Fail fast after a broken pipeline: when the device error word is already
+// raised (a bounded wait of an earlier tensor-core launch expired and nobody
+// cleared the word), the CTA does no work at all -- no TMEM allocation, no
+// waits -- so that a run whose tensor-core pipeline broke ends within one
+// wait bound instead of one bound per later launch. The decision is made by
+// one thread and shared, so every thread of the CTA takes the same branch.
+__device__ __forceinline__ bool tc_skip(const int* err) {
+  __shared__ int s_skip;
+  if (threadIdx.x == 0) s_skip = *(const volatile int*)err;
+  __syncthreads();
+  return s_skip != 0;
+}
+
 // Persistent GEMM: each CTA walks work items t = blockIdx.x, +gridDim.x, ...
 // Item t is K-slice s = t % splits of tile t / splits (tile u covers rows
 // (u / n_tiles) * 128 and columns (u % n_tiles) * BN); with splits > 1 the
@@ -209,6 +222,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               const __grid_constant__ CUtensorMap tmC, int M, int N, int K, const EpiArgs ep, void* __restrict__ C,
               int64_t ldc, int n_store, int splits, int64_t split_stride, int* err) {
   static_assert(!TSTORE || EPI == TC_EPI_TANH_BF16 || EPI == TC_EPI_DTANH_BF16, "TMA store: bf16 epilogues only");
+  if (tc_skip(err)) return;
   extern __shared__ uint8_t smem_raw[];
   using S = Smem<BN, STAGES>;
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);

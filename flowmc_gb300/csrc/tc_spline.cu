@@ -235,6 +235,7 @@ __global__ void __launch_bounds__(kSplThreads, 1)
   using T = SplineTile<KB>;
   constexpr int P = T::P, DG = T::DG, BN = T::BN, E = kSplineEpiPerQuarter, PP = BiasRows<KB>::PP;
   using S = Smem<BN, STAGES>;
+  if (tc_skip(err)) return;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   float* sbias = (float*)(base + STAGES * S::STAGE_BYTES + 256);   // after the ring and its barriers
@@ -328,6 +329,7 @@ __global__ void __launch_bounds__(kSplThreads, 1)
   using T = SplineTile<KB>;
   constexpr int P = T::P, DG = T::DG, DGP = T::DGP, BN = T::BN, SP = T::SP, E = kSplineEpiPerQuarter;
   using S = Smem<BN, STAGES>;
+  if (tc_skip(err)) return;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   // staging tile after the ring and its barriers
@@ -512,16 +514,25 @@ int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l
   int rc = make_tma_map_bf16(&ma, A, Kd, rows_a, Kd, tc::BM);
   if (rc) return rc;
   if ((rc = make_tma_map_bf16(&mb, Bg, Kd, (int64_t)n_groups * bn, Kd, bn))) return rc;
+  {
+    // useful work: the last Linear's nt * P outputs over its H_last inputs,
+    // the A rows and the group weights once, x read and written, partials
+    const int hl = g.H[g.nh - 1];
+    const double flops = 2.0 * (double)M * nt * g.P * hl;
+    const double bytes = (double)M * hl * 2 + (double)nt * g.P * hl * 2 + (double)M * nt * 8 +
+                         (double)M * kSplineEpiPerQuarter * n_groups * 4;
+    KernelTimer kt(inverse ? FMC_KT_TC_SPLINE_INV : FMC_KT_TC_SPLINE_FWD, st, flops, bytes);
 #define SPL_CASE(k)                                                                                              \
   if (g.K == k) {                                                                                                \
     rc = inverse ? launch_spl<k, true>(st, ma, mb, M, n_groups, nt, Kd, bias, xa, g.d, g.tpar(l), ldp, g.cfg)    \
                  : launch_spl<k, false>(st, ma, mb, M, n_groups, nt, Kd, bias, xa, g.d, g.tpar(l), ldp, g.cfg);  \
   } else
-  FMC_SPLINE_BINS(SPL_CASE) {
-    set_error("n_bins=%d is not instantiated for the fused spline", g.K);
-    return FMC_ERR_UNSUPPORTED;
-  }
+    FMC_SPLINE_BINS(SPL_CASE) {
+      set_error("n_bins=%d is not instantiated for the fused spline", g.K);
+      return FMC_ERR_UNSUPPORTED;
+    }
 #undef SPL_CASE
+  }
   if (rc) return rc;
   int64_t blocks = (M + 255) / 256;
   if (blocks > (int64_t)sm_count() * 8) blocks = (int64_t)sm_count() * 8;
@@ -559,6 +570,12 @@ int tc_linear_spline_bwd(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, i
   a.nt = nt;
   a.tpar = g.tpar(l);
   a.cpar = g.cpar(l);
+  const int hl = g.H[g.nh - 1];
+  const double flops = 2.0 * (double)M * nt * g.P * hl;
+  // A and the weights once, x / dL/dy read, dL/dx written, dL/draw in two bf16 layouts
+  const double bytes = (double)M * hl * 2 + (double)nt * g.P * hl * 2 + (double)M * nt * 12 +
+                       (double)M * nt * g.P * 4;
+  KernelTimer kt(FMC_KT_TC_SPLINE_BWD, st, flops, bytes);
 #define SPL_CASE(k)                                                  \
   if (g.K == k) {                                                    \
     rc = launch_spl_bwd<k>(st, ma, mb, M, n_groups, Kd, a, g.cfg);   \

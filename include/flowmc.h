@@ -437,8 +437,14 @@ FMC_API int fmc_tc_gemm_bf16(const uint16_t* A, int64_t M, int64_t rows_a, int32
 FMC_API int fmc_selftest_bounded_wait(int32_t* timed_out, void* stream);
 
 /* Device error word of the tensor-core kernels: 1 after a bounded wait
- * expired (synchronous read; clear != 0 resets it). */
+ * expired (synchronous read; clear != 0 resets it). While the word is
+ * raised, every later tensor-core launch returns at once without work (no
+ * TMEM allocation, no waits), so a broken pipeline costs one wait bound in
+ * total, not one per launch; the outputs of those launches are not written.
+ * fmc_device_error_set writes the word (synchronous): clearing it after a
+ * failure, or raising it to test the early return. */
 FMC_API int fmc_device_error(int32_t* out, int32_t clear);
+FMC_API int fmc_device_error_set(int32_t value);
 
 /* ---- random streams under CUDA graph replay ------------------------- */
 /* Attach a caller-owned device word (uint64) that every random stream of
@@ -457,6 +463,31 @@ FMC_API int fmc_version(void);               /* FMC_ABI_VERSION */
 FMC_API int fmc_device_sm_count(int32_t* out);
 /* Number of kernels this library has launched in the process (host counter). */
 FMC_API int fmc_launch_count(uint64_t* out);
+
+/* ---- per-kernel timing (profiling aid; no counterpart in the reference,
+ * whose JAX path has no kernels of its own) ---------------------------
+ * While enabled, every launch of the kernels listed below on a stream that
+ * is not capturing is bracketed by a CUDA event pair recorded on its launch
+ * stream, and the launch's algorithmic FLOPs and bytes (useful work, not
+ * padding) are noted. fmc_kernel_timing_read synchronises on the recorded
+ * events and returns the totals per kernel since the last reset; at most
+ * 16384 launches are recorded between reads. Enabling creates the event
+ * pool on the current device once. Off by default; costs two event
+ * records per timed launch. */
+enum {
+  FMC_KT_TC_SPLINE_FWD = 0,   /* k_tc_spline, forward (fused last Linear + spline)  */
+  FMC_KT_TC_SPLINE_INV = 1,   /* k_tc_spline, inverse                               */
+  FMC_KT_TC_SPLINE_BWD = 2,   /* k_tc_spline_bwd (training adjoint)                 */
+  FMC_KT_TC_GEMM_TANH = 3,    /* k_tc_gemm, bias + tanh -> bf16 (hidden layers)     */
+  FMC_KT_TC_GEMM_DTANH = 4,   /* k_tc_gemm, tanh adjoint -> bf16 (backward)         */
+  FMC_KT_TC_GEMM_F32 = 5,     /* k_tc_gemm, fp32 outputs (weight gradients)         */
+  FMC_KT_LOCAL_STEPS = 6,     /* k_local_steps (MALA / HMC / GRW local phase)       */
+  FMC_KT_NF_ACCEPT = 7,       /* k_nf_accept (target + independent-MH scan)         */
+  FMC_KT_COUNT = 8
+};
+FMC_API int fmc_kernel_timing_enable(int32_t on);
+FMC_API int fmc_kernel_timing_reset(void);
+FMC_API int fmc_kernel_timing_read(int32_t kid, int64_t* launches, double* ms, double* flops, double* bytes);
 
 #ifdef __cplusplus
 }

@@ -137,14 +137,29 @@ def rqs_inverse(y, xp, yp, sl):
     return x, ld
 
 
-def mlp(Ws, bs, x):
-    """MLP.__call__ (common.py:109-112): tanh after every layer but the last."""
-    h = x
+def mlp(Ws, bs, x, bf16=False):
+    """MLP.__call__ (common.py:109-112): tanh after every layer but the last.
+
+    bf16=True models the BF16-conditioner arithmetic (not the reference's):
+    the input, every weight matrix and every hidden activation are rounded to
+    bfloat16, the products and biases stay in float64. It measures the error
+    that BF16 operands alone cause, the scale a BF16 kernel is held to."""
+    h = round_bf16(x) if bf16 else x
     for i, (W, b) in enumerate(zip(Ws, bs)):
-        h = h @ W.T + b
+        h = h @ (round_bf16(W) if bf16 else W).T + b
         if i < len(Ws) - 1:
             h = np.tanh(h)
+            if bf16:
+                h = round_bf16(h)
     return h
+
+
+def round_bf16(a):
+    """Round to the nearest bfloat16 (ties to even), returned as float64: the
+    float32 value's top 16 bits after adding 0x7fff plus the kept lsb."""
+    u = np.ascontiguousarray(np.asarray(a, np.float32)).view(np.uint32)
+    u = (u + (((u >> 16) & 1) + 0x7FFF)).astype(np.uint32) & np.uint32(0xFFFF0000)
+    return u.view(np.float32).astype(np.float64)
 
 
 @dataclasses.dataclass
@@ -156,6 +171,7 @@ class Flow:
     data_mean: np.ndarray
     data_cov: np.ndarray          # [d, d] (only the diagonal is read)
     base_cov_scale: float = 1.0   # base Gaussian covariance = scale * I
+    bf16: bool = False            # conditioners with bfloat16 operands (see mlp)
 
     @property
     def d(self):
@@ -164,7 +180,7 @@ class Flow:
     def coupling(self, layer, x, inverse: bool):
         """MaskedCouplingLayer(RQSpline) (common.py:150-168, rqSpline.py:347-361)."""
         m = layer["mask"].astype(np.float64)
-        raw = mlp(layer["W"], layer["b"], x * m)
+        raw = mlp(layer["W"], layer["b"], x * m, self.bf16)
         n, d = x.shape
         P = 3 * self.n_bins + 1
         xp, yp, sl = spline_params(raw.reshape(n, d, P), self.n_bins)

@@ -9,14 +9,19 @@ Two flow shapes:
 
 Tolerances (BF16 GEMM inputs, FP32 accumulation, FP32 spline):
   * flow log-probs within 2e-2 relative to max(1, |log q|), per row;
-  * forward / inverse / sample outputs within 2e-2 of max(1, max |x|);
+  * forward / inverse / sample outputs and log-determinants: per value, the error against
+    the float64 oracle stays within 3x the error that BF16 operands alone
+    cause (the oracle run with its conditioner inputs, weights and hidden
+    activations rounded to bfloat16), in the maximum and in the median.
+    At 12 random layers that error exceeds 2e-2 of the output scale in the
+    worst coordinates, so the per-coordinate bar is BF16's own, not 2e-2;
   * NFProposal global step (fmc_nf_global_steps, scripted normals and
     uniforms): accept decisions identical to the oracle's at every step of a
     chain up to its first near-tie, where a near-tie is a step whose oracle
     margin |log u - ratio| is below twice the measured error of the ratio's
     ingredients (flow log-densities and target log-densities of the BF16
     proposals against the oracle's); accepted positions and log-densities
-    on those steps within the flow tolerance.
+    on those steps within the output and log-prob tolerances above.
 
 Reference: resource/kernel/NF_proposal.py:27-128 (the global step),
 resource/model/nf_model/rqSpline.py:450-504 (forward, inverse, sample,
@@ -26,6 +31,7 @@ import numpy as np
 import pytest
 import torch
 
+from oracle import flow as F
 from oracle import kernels as K
 from oracle import targets as OT
 from test_flow_gpu import gpu_model, rand_flow, to_f32
@@ -51,12 +57,26 @@ def rel_err(a, ref):
     return np.abs(a - ref) / np.maximum(1.0, np.abs(ref))
 
 
+def bf16_flow(fl):
+    """The same flow with BF16 conditioner operands (oracle.flow.mlp)."""
+    return F.Flow(fl.layers, fl.n_bins, fl.data_mean, fl.data_cov, fl.base_cov_scale, bf16=True)
+
+
+def assert_within_bf16(got, ref, emul, what):
+    """|got - ref| within 3x |emul - ref| (BF16 operands alone) in the maximum
+    and the median over coordinates."""
+    e, b = np.abs(got - ref), np.abs(emul - ref)
+    assert e.max() <= 3.0 * b.max() + 1e-4, (what, "max", e.max(), b.max())
+    assert np.median(e) <= 3.0 * np.median(b) + 1e-5, (what, "median", np.median(e), np.median(b))
+
+
 @pytest.mark.parametrize("d,L,hidden,nb", DEEP, ids=[f"d{c[0]}L{c[1]}H{c[2][0]}K{c[3]}" for c in DEEP])
 def test_flow_bf16_full_depth_passes(cuda, d, L, hidden, nb):
     """log_prob, forward, inverse and sample of the full-depth BF16 flow."""
     from flowmc_gb300 import _lib
     from flowmc_gb300.random import PRNGKey
     fl = deep_flow(d, L, hidden, nb)
+    fb = bf16_flow(fl)
     m = gpu_model(fl, hidden, precision="bf16")
     rng = np.random.default_rng(7)
     x = (rng.normal(size=(400, d)) * 1.5).astype(np.float32)
@@ -70,18 +90,20 @@ def test_flow_bf16_full_depth_passes(cuda, d, L, hidden, nb):
 
     y, ld = m.forward(xt)
     oy, old = fl.forward(x64)
-    assert np.abs(y.cpu().numpy() - oy).max() <= BF16_TOL * max(1.0, np.abs(oy).max())
-    assert rel_err(ld.cpu().numpy(), old).max() <= BF16_TOL
+    by, bld = fb.forward(x64)
+    assert_within_bf16(y.cpu().numpy(), oy, by, "forward")
+    assert_within_bf16(ld.cpu().numpy(), old, bld, "forward log-det")
 
     xi, ldi = m.inverse(xt)
     oxi, oldi = fl.inverse(x64)
-    assert np.abs(xi.cpu().numpy() - oxi).max() <= BF16_TOL * max(1.0, np.abs(oxi).max())
-    assert rel_err(ldi.cpu().numpy(), oldi).max() <= BF16_TOL
+    bxi, bldi = fb.inverse(x64)
+    assert_within_bf16(xi.cpu().numpy(), oxi, bxi, "inverse")
+    assert_within_bf16(ldi.cpu().numpy(), oldi, bldi, "inverse log-det")
 
     z = rng.normal(size=(400, d)).astype(np.float32)
     s = m.sample(PRNGKey(1), 400, z=torch.tensor(z, device="cuda")).cpu().numpy()
-    os_ = fl.sample(z.astype(np.float64))
-    assert np.abs(s - os_).max() <= BF16_TOL * max(1.0, np.abs(os_).max())
+    z64 = z.astype(np.float64)
+    assert_within_bf16(s, fl.sample(z64), fb.sample(z64), "sample")
 
 
 def _target(kind, d, fl, fit):
@@ -143,7 +165,8 @@ def test_nf_global_step_bf16_full_depth(cuda, d, L, hidden, nb, kind):
     olq, olq0 = fl.log_prob(os_), fl.log_prob(x064)
     lpt_g, lpt_o = OT.value_grad(t, gs64)[0], OT.value_grad(t, os_)[0]
     assert rel_err(glq, olq).max() <= BF16_TOL
-    assert np.abs(gs64 - os_).max() <= BF16_TOL * max(1.0, np.abs(os_).max())
+    bs_ = bf16_flow(fl).sample(z64.reshape(C * S, d))
+    assert_within_bf16(gs64, os_, bs_, "proposals")
     eps = (np.abs(glq - olq).max() + np.abs(glq0 - olq0).max() + np.abs(lpt_g - lpt_o).max()
            + 1e-5 * np.abs(lpt_o).max())
     margin = np.abs(np.log(u64) - oratio)
@@ -153,7 +176,9 @@ def test_nf_global_step_bf16_full_depth(cuda, d, L, hidden, nb, kind):
     g_acc = acc.cpu().numpy()
     np.testing.assert_array_equal(g_acc[cmp_mask], oacc[cmp_mask])
     gx, glp = pos.cpu().numpy(), lp.cpu().numpy()
-    assert np.abs(gx[cmp_mask] - ox[cmp_mask]).max() <= BF16_TOL * max(1.0, np.abs(ox).max())
+    # accepted rows are proposals (or the starting rows): within the BF16
+    # error of the proposals themselves
+    assert np.abs(gx[cmp_mask] - ox[cmp_mask]).max() <= 3.0 * np.abs(bs_ - os_).max() + 1e-4
     assert rel_err(glp[cmp_mask], olp[cmp_mask]).max() <= BF16_TOL
     # the comparison is not vacuous: most steps are away from ties, and (for
     # the fitted target, where the flow is a fair proposal) both decisions occur

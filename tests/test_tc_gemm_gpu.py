@@ -76,3 +76,30 @@ def test_bounded_wait_expires_and_context_survives(cuda):
     ref = A.float() @ B.float().T
     torch.testing.assert_close(C, ref, rtol=1e-2, atol=1e-2)
     assert _lib.device_error() == 0
+
+
+def test_raised_error_word_skips_tensor_core_work(cuda):
+    """While the device error word is raised (a bounded wait expired earlier
+    and nobody cleared it), a tensor-core launch returns at once without
+    touching its output; once the word is cleared the same GEMM is correct."""
+    import time
+    from flowmc_gb300 import _lib
+    M, K, N = 512, 256, 256
+    A = torch.randn(M, K, device="cuda").to(torch.bfloat16)
+    B = torch.randn(N, K, device="cuda").to(torch.bfloat16)
+    bias = torch.zeros(N, device="cuda")
+    C = torch.full((M, N), float("nan"), device="cuda")
+    _lib.check(_lib.lib().fmc_device_error_set(1))
+    t0 = time.perf_counter()
+    for _ in range(20):
+        _lib.check(_lib.lib().fmc_tc_gemm_bf16(A.data_ptr(), M, M, K, B.data_ptr(), N, N, bias.data_ptr(),
+                                               C.data_ptr(), N, N, 1, _lib.stream_handle()))
+    torch.cuda.synchronize()
+    assert time.perf_counter() - t0 < 0.5          # no wait ran out: nothing waited at all
+    assert torch.isnan(C).all()
+    assert _lib.device_error() == 1                 # read and cleared
+    _lib.check(_lib.lib().fmc_tc_gemm_bf16(A.data_ptr(), M, M, K, B.data_ptr(), N, N, bias.data_ptr(),
+                                           C.data_ptr(), N, N, 1, _lib.stream_handle()))
+    torch.cuda.synchronize()
+    torch.testing.assert_close(C, A.float() @ B.float().T, rtol=1e-2, atol=1e-2)
+    assert _lib.device_error() == 0
