@@ -58,6 +58,7 @@ class FmcLocalParams(ctypes.Structure):
         ("momentum_scale", ctypes.c_void_p),
         ("metric_colsum", ctypes.c_void_p),
         ("momentum_chol", ctypes.c_void_p),
+        ("philox_rounds", ctypes.c_int32),
     ]
 
 
@@ -79,6 +80,7 @@ class FmcFlow(ctypes.Structure):
         ("min_knot_slope", ctypes.c_float),
         ("precision", ctypes.c_int32),
         ("gemm_bn", ctypes.c_int32),
+        ("spline_tile", ctypes.c_int32),
         ("theta", ctypes.c_void_p),
         ("theta_bf16", ctypes.c_void_p),
         ("aux", ctypes.c_void_p),

@@ -78,15 +78,18 @@ struct KernelTimer {
 };
 
 // ---------------------------------------------------------------- Philox
-// Philox-4x32 with 10 rounds, constants from the SC'11 paper (Table 2 and
-// the Weyl key schedule). counter = 4 x u32, key = 2 x u32.
+// Philox-4x32 with R rounds, constants from the SC'11 paper (Table 2 and
+// the Weyl key schedule). counter = 4 x u32, key = 2 x u32. R = 10 is the
+// paper's recommended count; R = 7 is the smallest it reports as
+// Crush-resistant (an option of the local-step kernel, off by default).
 struct u32x4 { uint32_t x, y, z, w; };
 
-__host__ __device__ __forceinline__ u32x4 philox4x32_10(u32x4 c, uint32_t k0, uint32_t k1) {
+template <int R>
+__host__ __device__ __forceinline__ u32x4 philox4x32(u32x4 c, uint32_t k0, uint32_t k1) {
   const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
   const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
 #pragma unroll
-  for (int r = 0; r < 10; ++r) {
+  for (int r = 0; r < R; ++r) {
     // one 32x32 -> 64-bit multiply gives both halves of each product
     const uint64_t p0 = (uint64_t)M0 * c.x, p1 = (uint64_t)M1 * c.z;
     const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
@@ -96,6 +99,10 @@ __host__ __device__ __forceinline__ u32x4 philox4x32_10(u32x4 c, uint32_t k0, ui
     k1 += W1;
   }
   return c;
+}
+
+__host__ __device__ __forceinline__ u32x4 philox4x32_10(u32x4 c, uint32_t k0, uint32_t k1) {
+  return philox4x32<10>(c, k0, k1);
 }
 
 // u32 -> uniform in (0, 1]: 24 significant bits, never 0 (log finite).
@@ -147,6 +154,7 @@ struct Rng {
   uint32_t k0, k1;     // key = seed
   uint64_t ctr_base;   // call counter, folded into the step word
   const uint64_t* epoch;
+  int32_t rounds = 10; // Philox rounds: 10, or 7 where a caller opts in
   // the key this launch uses: the seed mixed with the attached epoch word
   __device__ __forceinline__ Rng at_epoch() const {
     Rng r = *this;
@@ -160,7 +168,7 @@ struct Rng {
   __device__ __forceinline__ u32x4 draw(uint64_t row, uint64_t step, uint32_t slot, uint32_t tag) const {
     const uint64_t s = step + (ctr_base << 32);
     u32x4 c{(uint32_t)row, (uint32_t)(row >> 32) ^ (uint32_t)(s >> 32), slot, tag ^ (uint32_t)s};
-    return philox4x32_10(c, k0, k1);
+    return rounds == 7 ? philox4x32<7>(c, k0, k1) : philox4x32<10>(c, k0, k1);
   }
 };
 

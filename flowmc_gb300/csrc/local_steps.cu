@@ -75,7 +75,9 @@ extern "C" int fmc_local_steps(const FmcTarget* target, const FmcLocalParams* pa
   a.d = target->n_dim;
   a.S = n_steps;
   a.thin = thinning;
-  a.rng = Rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter, rng_epoch()};
+  FMC_CHECK_ARG(params->philox_rounds == 0 || params->philox_rounds == 7 || params->philox_rounds == 10,
+                "philox_rounds must be 0, 7 or 10");
+  a.rng = Rng{(uint32_t)seed, (uint32_t)(seed >> 32), counter, rng_epoch(), params->philox_rounds == 7 ? 7 : 10};
   a.noise = noise;
   a.unif = unif;
   a.out_pos = out_pos;

@@ -136,14 +136,20 @@ __device__ __forceinline__ void draw_normals(const LocalArgs& a, const Rng& rng,
     if (gl * V + v >= d) xi[v] = 0.f;
 }
 
-// Uniforms come four steps per Philox call: draws are refreshed on steps
-// s = 0 mod 4 (every lane of the group computes the same call, so the group
-// agrees on u) and consumed from `ub`.
-__device__ __forceinline__ float draw_uniform(const LocalArgs& a, const Rng& rng, int64_t c, int s, u32x4& ub) {
+// Uniforms: step s takes component s & 3 of the Philox block keyed by s >> 2.
+// The G lanes of a group share the work: on steps s = 0 mod 4G, lane gl
+// computes block (s >> 2) + gl into `ub`, and each step the owner lane
+// ((s >> 2) mod G) hands its component to the whole group with a shuffle,
+// so the group agrees on u. One Philox call per 4G steps per lane instead of
+// one per 4 steps; the stream is the same as one lane drawing every block.
+template <int G>
+__device__ __forceinline__ float draw_uniform(const LocalArgs& a, const Rng& rng, int64_t c, int s, int gl,
+                                              u32x4& ub) {
   if (a.unif) return __ldcs(a.unif + (int64_t)c * a.S + s);
-  if ((s & 3) == 0) ub = rng.draw(c, (uint64_t)(s >> 2), 0u, RNG_TAG_LOCAL_UNIFORM);
+  if (s % (4 * G) == 0) ub = rng.draw(c, (uint64_t)((s >> 2) + gl), 0u, RNG_TAG_LOCAL_UNIFORM);
   const int r = s & 3;
-  return u32_to_unit(r == 0 ? ub.x : r == 1 ? ub.y : r == 2 ? ub.z : ub.w);
+  const uint32_t mine = r == 0 ? ub.x : r == 1 ? ub.y : r == 2 ? ub.z : ub.w;
+  return u32_to_unit(__shfl_sync(0xffffffffu, mine, (s >> 2) % G, G));
 }
 
 template <int G, int V>
@@ -224,7 +230,7 @@ __global__ void __launch_bounds__(256) k_local_steps(const LocalArgs a) {
     for (int s = 0; s < a.S; ++s) {
       float xi[V];
       draw_normals<V>(a, rng, cc, s, gl, xi);
-      const float logu = logf(draw_uniform(a, rng, cc, s, ub));
+      const float logu = logf(draw_uniform<G>(a, rng, cc, s, gl, ub));
       bool acc;
       if constexpr (KIND == FMC_KERNEL_MALA) {
         const float dt2 = dt * dt;
@@ -248,10 +254,19 @@ __global__ void __launch_bounds__(256) k_local_steps(const LocalArgs a) {
         sb = group_sum<G>(sb);
         // ratio = (lp1 - lp0) - log q(prop | x) + log q(x | prop)
         //       = (lp1 - lp0) + (|prop - mean0|^2 - |x - mean1|^2) / (2 dt^2)
-        // (the Gaussian normalisers cancel)
-        const ff q = two_sum(sa, -sb);
-        const ff ratio = ff_add(two_sum(lp1, -lp), ff_mul_f(q, 0.5f / dt2));
-        acc = f_lt_ff(logu, ratio);
+        // (the Gaussian normalisers cancel). Decided in float32 when log u
+        // is farther from the float32 ratio than that ratio's rounding error
+        // can reach; otherwise in float-float (accepts identical either way).
+        const float c2 = 0.5f / dt2;
+        const float rf = (lp1 - lp) + (sa - sb) * c2;
+        const float bound = 4.8e-7f * (fabsf(lp1) + fabsf(lp) + (sa + sb) * c2) + 1e-30f;
+        if (fabsf(logu - rf) > bound) {
+          acc = logu < rf;
+        } else {
+          const ff q = two_sum(sa, -sb);
+          const ff ratio = ff_add(two_sum(lp1, -lp), ff_mul_f(q, c2));
+          acc = f_lt_ff(logu, ratio);
+        }
         if (acc) {
 #pragma unroll
           for (int v = 0; v < V; ++v) { x[v] = prop[v]; g[v] = g1[v]; }
@@ -314,11 +329,18 @@ __global__ void __launch_bounds__(256) k_local_steps(const LocalArgs a) {
 #pragma unroll
         for (int v = 0; v < V; ++v) k1 += p[v] * p[v] * mc[v];
         k1 = 0.5f * group_sum<G>(k1);
-        // log_acc = (-lp + K0) - (-lpq + K1)
-        const ff h0 = two_sum(-lp, k0);
-        const ff h1 = two_sum(-lpq, k1);
-        const ff log_acc = ff_add(h0, ff_neg(h1));
-        acc = f_lt_ff(logu, log_acc);
+        // log_acc = (-lp + K0) - (-lpq + K1), decided in float32 away from
+        // the float32 rounding band, else in float-float (as for MALA)
+        const float rf = (lpq - lp) + (k0 - k1);
+        const float bound = 4.8e-7f * (fabsf(lp) + fabsf(lpq) + k0 + k1) + 1e-30f;
+        if (fabsf(logu - rf) > bound) {
+          acc = logu < rf;
+        } else {
+          const ff h0 = two_sum(-lp, k0);
+          const ff h1 = two_sum(-lpq, k1);
+          const ff log_acc = ff_add(h0, ff_neg(h1));
+          acc = f_lt_ff(logu, log_acc);
+        }
         if (acc) {
 #pragma unroll
           for (int v = 0; v < V; ++v) { x[v] = xq[v]; g[v] = gq[v]; }

@@ -193,6 +193,90 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+// ---- CTA pairs (tcgen05 cta_group::2). Two CTAs of a cluster share one
+// 256-row MMA: each holds its 128 rows of A and half of the B rows in its own
+// shared memory (at the same offsets), the even CTA issues
+// tcgen05.mma.cta_group::2 for both, and each CTA's TMEM receives its own
+// 128 accumulator rows over all N columns. B is read once per pair instead of
+// once per CTA.
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+// shared::cluster address of the variable at shared::cta address `a` in CTA `rank`
+__device__ __forceinline__ uint32_t mapa_shared(uint32_t a, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+
+// every thread of both CTAs: arrive (release) and wait (acquire) on the
+// cluster barrier (the non-aligned forms: warps need not be converged)
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+
+// bounded wait on a barrier of this CTA that threads of the peer CTA (or the
+// pair's MMAs and copies) also complete: acquire at cluster scope
+__device__ __forceinline__ bool mbar_try_wait_cl(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_cl(uint64_t* bar, uint32_t parity) {
+  if (mbar_try_wait_cl(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  do {
+    if (mbar_try_wait_cl(bar, parity)) return true;
+  } while (global_ns() - t0 < 1000000000ull);
+  return false;
+}
+
+// arrive on an mbarrier given by its shared::cluster address (either CTA)
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t cl_addr) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cl_addr) : "memory");
+}
+
+// TMA load into this CTA's shared memory whose completion is counted on an
+// mbarrier of either CTA of the pair (shared::cluster address)
+__device__ __forceinline__ void tma_load_2d_pair(void* dst, const CUtensorMap* map, uint32_t bar_cl, int c0, int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], "
+      "[%2];" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(bar_cl), "r"(c0), "r"(c1)
+      : "memory");
+}
+
+// M = 256 instruction descriptor of a CTA pair (each CTA: 128 rows)
+__host__ __device__ constexpr uint32_t idesc_bf16_f32_pair(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16_pair(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+// arrive on the mbarrier at this shared offset in both CTAs once every MMA
+// the pair issued so far has completed
+__device__ __forceinline__ void mma_commit_pair(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+          smem_u32(bar)),
+      "h"((uint16_t)3)
+      : "memory");
+}
+
 // Fail fast after a broken pipeline: when the device error word is already
 // raised (a bounded wait of an earlier tensor-core launch expired and nobody
 // cleared the word), the CTA does no work at all -- no TMEM allocation, no

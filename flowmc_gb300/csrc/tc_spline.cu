@@ -425,6 +425,259 @@ __global__ void __launch_bounds__(kSplThreads, 1)
   pipe_teardown(p, warp, lane, err);
 }
 
+// ---------------------------------------------------------------- CTA pairs
+// k_tc_spline2: the same fused last Linear + spline, with (256-row, group)
+// tiles computed by a CTA pair (cluster of 2, tcgen05 cta_group::2). Each
+// CTA loads its 128 rows of A and half (BN / 2 rows) of the group's weights;
+// the even CTA issues the M = 256 MMAs for both; each CTA runs the epilogue
+// of its own 128 rows from its own TMEM. Per CTA and tile the operand traffic
+// from L2 is 128 x K (A) + BN / 2 x K (B) instead of 128 x K + BN x K.
+//
+// Barriers: the ring's `full` barriers of the even CTA count both CTAs'
+// copies (its producer arms them with both halves' bytes; the odd CTA's
+// copies signal them across the pair); `empty`, `acc_full` and `mma_done`
+// exist in both CTAs and are completed by the pair's commits (multicast);
+// `acc_empty` of the even CTA counts the epilogue warps of both CTAs.
+// Every wait is bounded; the pair agrees on the fail-fast decision first.
+
+// the error-word check of tc_skip, made by the even CTA for the pair
+__device__ __forceinline__ bool tc_skip_pair(const int* err) {
+  __shared__ int s_skip;
+  if (threadIdx.x == 0) s_skip = (cluster_ctarank() == 0) ? *(const volatile int*)err : 0;
+  cluster_sync_all();
+  int v;
+  asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(mapa_shared(smem_u32(&s_skip), 0)) : "memory");
+  cluster_sync_all();   // the even CTA's word stays readable until both have read it
+  return v != 0;
+}
+
+template <int BH, int STAGES>
+struct PairSmem {
+  static constexpr int A_BYTES = BM * BK * 2;
+  static constexpr int B_BYTES = BH * BK * 2;
+  static constexpr int STAGE_BYTES = ((A_BYTES + B_BYTES + 1023) / 1024) * 1024;
+  static constexpr int RING = STAGES * STAGE_BYTES;
+};
+
+template <int BH, int STAGES>
+__device__ __forceinline__ Pipe pipe_setup_pair(uint8_t* base, int warp, uint32_t rank) {
+  using S = PairSmem<BH, STAGES>;
+  Pipe p;
+  p.base = base;
+  p.full = (uint64_t*)(base + S::RING);
+  p.empty = p.full + STAGES;
+  p.acc_full = p.empty + STAGES;
+  p.acc_empty = p.acc_full + 2;
+  p.mma_done = p.acc_empty + 2;
+  p.tmem_slot = (uint32_t*)(p.mma_done + 1);
+  p.abort_flag = (volatile int*)(p.tmem_slot + 1);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&p.full[s], 1);
+      mbar_init(&p.empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&p.acc_full[b], 1);
+      mbar_init(&p.acc_empty[b], 2 * kSplEpiWarps);
+    }
+    mbar_init(p.mma_done, 1);
+    *p.abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(p.tmem_slot)),
+                 "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  // both CTAs' barriers are initialised before either side signals the other's
+  cluster_sync_all();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  p.tmem = *p.tmem_slot;
+  (void)rank;
+  return p;
+}
+
+// warp 0, one lane, in both CTAs: this CTA's A rows and B half of every tile
+template <int BH, int STAGES>
+__device__ __forceinline__ void producer_pair(const Pipe& p, const CUtensorMap* tmA, const CUtensorMap* tmB,
+                                              int tiles, int n_groups, int nk, uint32_t rank) {
+  using S = PairSmem<BH, STAGES>;
+  const int n_pairs = gridDim.x / 2, pair = blockIdx.x / 2;
+  uint32_t it = 0;
+  for (int t = pair; t < tiles && !*p.abort_flag; t += n_pairs) {
+    const int m0 = (t / n_groups) * (2 * BM) + (int)rank * BM;
+    const int n0 = (t % n_groups) * (2 * BH) + (int)rank * BH;
+    for (int k = 0; k < nk; ++k, ++it) {
+      const int s = it % STAGES;
+      const uint32_t ph = (it / STAGES) & 1u;
+      if (it >= (uint32_t)STAGES && !mbar_wait_cl(&p.empty[s], ph ^ 1u)) {
+        *p.abort_flag = 1;
+        break;
+      }
+      if (*p.abort_flag) break;
+      uint8_t* sa = p.base + s * S::STAGE_BYTES;
+      uint8_t* sb = sa + S::A_BYTES;
+      const uint32_t full_cl = mapa_shared(smem_u32(&p.full[s]), 0);
+      if (rank == 0) mbar_expect_tx(&p.full[s], 2 * (S::A_BYTES + S::B_BYTES));
+      tma_load_2d_pair(sa, tmA, full_cl, k * BK, m0);
+      tma_load_2d_pair(sb, tmB, full_cl, k * BK, n0);
+    }
+  }
+  if (*p.abort_flag) {
+    // this CTA's copies still in flight must land before it exits; their
+    // completion is counted on the even CTA's barriers, so wait on the
+    // stages' release by the MMA side instead (bounded)
+    for (uint32_t j = it > (uint32_t)STAGES ? it - STAGES : 0; j < it; ++j)
+      mbar_wait_cl(&p.empty[j % STAGES], (j / STAGES) & 1u);
+  }
+}
+
+// warp 1, one lane, even CTA only: the pair's MMAs of every tile
+template <int BN, int BH, int STAGES>
+__device__ __forceinline__ void mma_issuer_pair(const Pipe& p, int tiles, int nk) {
+  using S = PairSmem<BH, STAGES>;
+  const uint32_t idesc = idesc_bf16_f32_pair(BN);
+  const int n_pairs = gridDim.x / 2, pair = blockIdx.x / 2;
+  uint32_t it = 0;
+  int local = 0;
+  for (int t = pair; t < tiles && !*p.abort_flag; t += n_pairs, ++local) {
+    const int b = local & 1, use = local >> 1;
+    if (use > 0 && !mbar_wait_cl(&p.acc_empty[b], (uint32_t)(use - 1) & 1u)) {
+      *p.abort_flag = 1;
+      break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t dcol = p.tmem + (uint32_t)(b * 256);
+    bool stop = false;
+    for (int k = 0; k < nk; ++k, ++it) {
+      const int s = it % STAGES;
+      const uint32_t ph = (it / STAGES) & 1u;
+      if (!mbar_wait_cl(&p.full[s], ph) || *p.abort_flag) {
+        *p.abort_flag = 1;
+        stop = true;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint8_t* sa = p.base + s * S::STAGE_BYTES;
+      const uint8_t* sb = sa + S::A_BYTES;
+      const uint64_t da = smem_desc_sw128(sa), db = smem_desc_sw128(sb);
+#pragma unroll
+      for (int kk = 0; kk < BK / 16; ++kk)
+        mma_bf16_pair(dcol, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, (k > 0 || kk > 0) ? 1u : 0u);
+      mma_commit_pair(&p.empty[s]);
+    }
+    if (stop) break;
+    mma_commit_pair(&p.acc_full[b]);
+  }
+  // fires in both CTAs once every MMA issued so far has finished
+  mma_commit_pair(p.mma_done);
+}
+
+__device__ __forceinline__ void pipe_teardown_pair(const Pipe& p, int warp, int lane, uint32_t rank, int* err) {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    // the even CTA's MMAs read both CTAs' shared memory and write both TMEMs
+    if (lane == 0) mbar_wait_cl(p.mma_done, 0);
+    __syncwarp();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(p.tmem), "r"(512));
+  }
+  if (threadIdx.x == 0 && *p.abort_flag) atomicExch(err, 1);
+  // neither CTA leaves while the other may still signal its barriers
+  cluster_sync_all();
+  (void)rank;
+}
+
+template <int KB, bool INV, int STAGES>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kSplThreads, 1)
+    k_tc_spline2(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M,
+                 int n_groups, int nt, int K, const float* __restrict__ bias, int bias_smem, float* __restrict__ xa,
+                 int d, int tpar, float* __restrict__ ldp, SplineCfg cfg, int* err) {
+  using T = SplineTile<KB>;
+  constexpr int P = T::P, DG = T::DG, BN = T::BN, BH = BN / 2, E = kSplineEpiPerQuarter, PP = BiasRows<KB>::PP;
+  static_assert(BN % 32 == 0, "a CTA pair splits the group's weight rows in two multiples of 16");
+  using S = PairSmem<BH, STAGES>;
+  if (tc_skip_pair(err)) return;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  float* sbias = (float*)(base + S::RING + 256 + S::B_BYTES);   // after the ring, its barriers and the slack
+  if (bias_smem) {
+    for (int i = threadIdx.x; i < nt * PP; i += blockDim.x) {
+      const int t = i / PP, pp = i - t * PP;
+      sbias[i] = pp < P ? __ldg(bias + t * P + pp) : 0.f;
+    }   // visible after the set-up's barriers
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t rank = cluster_ctarank();
+  const int nk = (K + BK - 1) / BK;
+  const int tiles = (M + 2 * BM - 1) / (2 * BM) * n_groups;
+  const Pipe p = pipe_setup_pair<BH, STAGES>(base, warp, rank);
+  const uint32_t acc_empty_cl0 = mapa_shared(smem_u32(&p.acc_empty[0]), 0);
+  const uint32_t acc_empty_cl1 = mapa_shared(smem_u32(&p.acc_empty[1]), 0);
+
+  if (warp == 0) {
+    if (lane == 0) producer_pair<BH, STAGES>(p, &tmA, &tmB, tiles, n_groups, nk, rank);
+  } else if (warp == 1) {
+    if (lane == 0 && rank == 0) mma_issuer_pair<BN, BH, STAGES>(p, tiles, nk);
+  } else {
+    const int q = warp & 3;          // TMEM lane quarter
+    const int h = (warp - 2) >> 2;   // coordinates h, h + E, ... of the group
+    const int row = q * 32 + lane;
+    const int n_pairs = gridDim.x / 2, pair = blockIdx.x / 2;
+    int local = 0;
+    for (int t = pair; t < tiles; t += n_pairs, ++local) {
+      const int b = local & 1, use = local >> 1;
+      const int m0 = (t / n_groups) * (2 * BM) + (int)rank * BM, g = t % n_groups;
+      const int gm = m0 + row;
+      if (*p.abort_flag || !mbar_wait_cl(&p.acc_full[b], (uint32_t)use & 1u)) {
+        *p.abort_flag = 1;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t tb = p.tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * 256);
+      float ldsum = 0.f;
+#pragma unroll 1
+      for (int u = h; u < DG; u += E) {
+        const int tcoord = g * DG + u;
+        if (tcoord >= nt) break;
+        float raw[P];
+        tmem_ld_cols<P>(tb + (uint32_t)(u * P), raw);   // warp-collective: every lane loads
+        if (gm < M) {
+          float* xp = xa + (int64_t)gm * d + 2 * tcoord + tpar;
+          const float xv = *xp;
+          if (bias_smem) {
+            const float4* bb = reinterpret_cast<const float4*>(sbias + tcoord * PP);
+#pragma unroll
+            for (int i = 0; i < PP / 4; ++i) {
+              const float4 bv = bb[i];
+              if (4 * i < P) raw[4 * i] += bv.x;
+              if (4 * i + 1 < P) raw[4 * i + 1] += bv.y;
+              if (4 * i + 2 < P) raw[4 * i + 2] += bv.z;
+              if (4 * i + 3 < P) raw[4 * i + 3] += bv.w;
+            }
+          } else {
+            const float* bb = bias + (int64_t)tcoord * P;
+#pragma unroll
+            for (int i = 0; i < P; ++i) raw[i] += __ldg(bb + i);
+          }
+          float y, l;
+          rqs_apply_fast<KB, INV>(raw, xv, cfg, y, l);
+          *xp = y;
+          ldsum += l;
+        }
+      }
+      if (gm < M) ldp[(int64_t)gm * (E * n_groups) + E * g + h] = ldsum;
+      // this warp's TMEM lanes of accumulator b are read: tell the even CTA's MMA warp
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive_cluster(b ? acc_empty_cl1 : acc_empty_cl0);
+    }
+  }
+  pipe_teardown_pair(p, warp, lane, rank, err);
+}
+
 }  // namespace tc
 
 // ld[r] += sum of the row's kSplineEpiPerQuarter * n_groups partials (fixed order)
@@ -473,6 +726,47 @@ static int launch_spl(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap&
   return FMC_OK;
 }
 
+// the CTA-pair variant: a persistent grid of as many pairs as can be resident
+template <int KB, bool INV>
+static int launch_spl2(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& mb, int64_t M, int n_groups, int nt,
+                       int K, const float* bias, float* xa, int d, int tpar, float* ldp, SplineCfg cfg) {
+  constexpr int STAGES = 6;
+  using T = tc::SplineTile<KB>;
+  using S = tc::PairSmem<T::BN / 2, STAGES>;
+  auto kern = tc::k_tc_spline2<KB, INV, STAGES>;
+  // ring, alignment slack, barriers; one B half of slack after the ring keeps
+  // every operand read of the last stage inside the allocation
+  const size_t ring = (size_t)S::RING + 1024 /*align slack*/ + 256 /*barriers*/;
+  const size_t ring_slack = ring + (size_t)S::B_BYTES;
+  const size_t with_bias = ring_slack + (size_t)nt * tc::BiasRows<KB>::PP * sizeof(float);
+  const int bias_smem = with_bias <= 227 * 1024 ? 1 : 0;
+  const size_t total = bias_smem ? with_bias : ring_slack;
+  static int attr = 0;
+  if (attr < (int)total) {
+    FMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)total));
+    attr = (int)total;
+  }
+  static int max_pairs = 0;
+  if (max_pairs == 0) {
+    cudaLaunchConfig_t cfg_l = {};
+    cfg_l.gridDim = dim3(2 * (unsigned)(sm_count() / 2), 1, 1);
+    cfg_l.blockDim = dim3(tc::kSplThreads, 1, 1);
+    cfg_l.dynamicSmemBytes = total;
+    int n = 0;
+    FMC_CUDA_TRY(cudaOccupancyMaxActiveClusters(&n, (void*)kern, &cfg_l));
+    max_pairs = n > 0 ? n : 1;
+  }
+  int* err = nullptr;
+  int rc = tc_error_word(&err);
+  if (rc) return rc;
+  const int64_t tiles = (M + 2 * tc::BM - 1) / (2 * tc::BM) * n_groups;
+  const int64_t pairs = tiles < max_pairs ? tiles : max_pairs;
+  kern<<<(unsigned)(2 * pairs), tc::kSplThreads, total, st>>>(ma, mb, (int)M, n_groups, nt, K, bias, bias_smem, xa, d,
+                                                             tpar, ldp, cfg, err);
+  FMC_LAUNCH_CHECK();
+  return FMC_OK;
+}
+
 template <int KB>
 static int launch_spl_bwd(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& mb, int64_t M, int n_groups,
                           int K, const tc::SplineBwdArgs& a, SplineCfg cfg) {
@@ -510,10 +804,13 @@ int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l
   const int Kd = g.w16_cols(l, g.nh);
   const uint16_t* Bg = f->theta_bf16 + g.w16g_off[l];
   const float* bias = f->theta + g.layer_off[l] + g.lin_b(l, g.nh);
+  // CTA pairs (256-row tiles, half the weight rows per CTA) unless one-CTA
+  // tiles are asked for, or the group width does not split in two multiples of 16
+  const bool pair = f->spline_tile != 128 && bn % 32 == 0;
   CUtensorMap ma, mb;
   int rc = make_tma_map_bf16(&ma, A, Kd, rows_a, Kd, tc::BM);
   if (rc) return rc;
-  if ((rc = make_tma_map_bf16(&mb, Bg, Kd, (int64_t)n_groups * bn, Kd, bn))) return rc;
+  if ((rc = make_tma_map_bf16(&mb, Bg, Kd, (int64_t)n_groups * bn, Kd, pair ? bn / 2 : bn))) return rc;
   {
     // useful work: the last Linear's nt * P outputs over its H_last inputs,
     // the A rows and the group weights once, x read and written, partials
@@ -524,8 +821,12 @@ int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l
     KernelTimer kt(inverse ? FMC_KT_TC_SPLINE_INV : FMC_KT_TC_SPLINE_FWD, st, flops, bytes);
 #define SPL_CASE(k)                                                                                              \
   if (g.K == k) {                                                                                                \
-    rc = inverse ? launch_spl<k, true>(st, ma, mb, M, n_groups, nt, Kd, bias, xa, g.d, g.tpar(l), ldp, g.cfg)    \
-                 : launch_spl<k, false>(st, ma, mb, M, n_groups, nt, Kd, bias, xa, g.d, g.tpar(l), ldp, g.cfg);  \
+    if (pair)                                                                                                    \
+      rc = inverse ? launch_spl2<k, true>(st, ma, mb, M, n_groups, nt, Kd, bias, xa, g.d, g.tpar(l), ldp, g.cfg) \
+                   : launch_spl2<k, false>(st, ma, mb, M, n_groups, nt, Kd, bias, xa, g.d, g.tpar(l), ldp, g.cfg); \
+    else                                                                                                         \
+      rc = inverse ? launch_spl<k, true>(st, ma, mb, M, n_groups, nt, Kd, bias, xa, g.d, g.tpar(l), ldp, g.cfg)  \
+                   : launch_spl<k, false>(st, ma, mb, M, n_groups, nt, Kd, bias, xa, g.d, g.tpar(l), ldp, g.cfg); \
   } else
     FMC_SPLINE_BINS(SPL_CASE) {
       set_error("n_bins=%d is not instantiated for the fused spline", g.K);

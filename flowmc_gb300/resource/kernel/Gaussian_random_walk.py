@@ -26,6 +26,7 @@ class GaussianRandomWalk(LocalKernel):
         p.kind = self.kernel_kind
         p.step_size = float(self.step_size)
         p.lanes_per_chain = int(self.lanes_per_chain)
+        p.philox_rounds = int(self.philox_rounds)
         return p, []
 
     def print_parameters(self):

@@ -76,6 +76,7 @@ class HMC(LocalKernel):
         p.n_leapfrog = int(self.n_leapfrog)
         p.step_size = float(self.step_size)
         p.lanes_per_chain = int(self.lanes_per_chain)
+        p.philox_rounds = int(self.philox_rounds)
         p.momentum_scale = _lib.ptr(tms) if tms is not None else None
         p.metric_colsum = _lib.ptr(tmc) if tmc is not None else None
         p.momentum_chol = _lib.ptr(tl) if tl is not None else None

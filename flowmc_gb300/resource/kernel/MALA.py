@@ -28,6 +28,7 @@ class MALA(LocalKernel):
         p.n_leapfrog = 0
         p.step_size = float(self.step_size)
         p.lanes_per_chain = int(self.lanes_per_chain)
+        p.philox_rounds = int(self.philox_rounds)
         return p, []
 
     def print_parameters(self):

@@ -35,6 +35,7 @@ class LocalKernel(ProposalBase):
 
     kernel_kind: int
     lanes_per_chain: int = 0   # 0 = library default; set by the autotuner
+    philox_rounds: int = 10    # in-kernel noise generator: Philox-4x32-10, or 7 (opt-in, another stream)
 
     def local_params(self, n_dim: int, device) -> tuple[_lib.FmcLocalParams, list]:
         raise NotImplementedError

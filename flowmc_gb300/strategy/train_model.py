@@ -48,22 +48,31 @@ class TrainModel(Strategy):
         L = _lib.lib()
         _lib.check(L.fmc_select_workspace_size(C, S, ctypes.byref(nb)))
         ptr, size = self._ws.get(nb.value, dev)
-        if self._err is None or self._err.device != dev:
-            self._err = torch.zeros((), dtype=torch.int32, device=dev)
+        self._error_words(dev)
         out = torch.empty(self.n_max_examples, d, device=dev)
         _lib.check(L.fmc_select_training_data(buf.data_ptr(), C, S, d, self.history_window, self.n_max_examples,
                                               int(seed) & ((1 << 64) - 1), 0, _lib.ptr(idx), out.data_ptr(),
                                               self._err.data_ptr(), ptr, size, _lib.stream_handle(dev)))
         # the error word goes to pinned host memory behind the selection (a
         # copy node when captured), so that a later poll needs no stream sync
-        if self._err_host is None:
-            self._err_host = torch.zeros((), dtype=torch.int32, pin_memory=True)
         self._err_host.copy_(self._err, non_blocking=True)
         if not torch.cuda.is_current_stream_capturing():
             self.mark_error_copy()
         return out
 
     _MSG = "finite training rows do not split evenly over the chains"
+
+    def _error_words(self, dev):
+        """The device error word and its pinned host copy (allocated outside
+        any CUDA-graph capture: Sampler.capture calls prepare first)."""
+        if self._err is None or self._err.device != dev:
+            self._err = torch.zeros((), dtype=torch.int32, device=dev)
+        if self._err_host is None:
+            self._err_host = torch.zeros((), dtype=torch.int32, pin_memory=True)
+
+    def prepare(self, resources, n_chains):
+        """Before a CUDA-graph capture: allocate what select() needs."""
+        self._error_words(resources[self.data_resource].data.device)
 
     def mark_error_copy(self, event=None):
         """Record (or take) the event after which the pinned error word is valid."""

@@ -24,7 +24,7 @@
 extern "C" {
 #endif
 
-#define FMC_ABI_VERSION 1
+#define FMC_ABI_VERSION 2
 
 #if defined(__GNUC__)
 #define FMC_API __attribute__((visibility("default")))
@@ -79,6 +79,9 @@ typedef struct FmcLocalParams {
   const float* momentum_chol; /* HMC with a dense M: [n_dim, n_dim] row-major
                                  cholesky(inv(M)) (momentum xi @ L^T), or NULL
                                  (diagonal: momentum_scale)                     */
+  int32_t philox_rounds;      /* in-kernel noise: 0 or 10 = Philox-4x32-10; 7 =
+                                 Philox-4x32-7 (fewer instructions, another
+                                 stream; Salmon et al. report it Crush-resistant) */
 } FmcLocalParams;
 
 /* Run `n_steps` steps of a local kernel for every chain in one persistent
@@ -281,6 +284,10 @@ typedef struct FmcFlow {
                                         0 = library choice (256 for outputs
                                         wider than 128 columns, else 128),
                                         or 128 / 256 (an autotuner's pick) */
+  int32_t spline_tile;               /* BF16 fused last Linear + spline rows
+                                        per tile: 0 = library choice (256),
+                                        128 = one CTA per tile, 256 = a CTA
+                                        pair (cta_group::2) per tile */
   float* theta;                      /* [n_params] float32 master weights   */
   uint16_t* theta_bf16;              /* [n_params] bf16 shadow (BF16 mode)   */
   float* aux;                        /* [2*n_dim + 2], see above             */

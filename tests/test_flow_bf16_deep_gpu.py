@@ -20,8 +20,10 @@ Tolerances (BF16 GEMM inputs, FP32 accumulation, FP32 spline):
     chain up to its first near-tie, where a near-tie is a step whose oracle
     margin |log u - ratio| is below twice the measured error of the ratio's
     ingredients (flow log-densities and target log-densities of the BF16
-    proposals against the oracle's); accepted positions and log-densities
-    on those steps within the output and log-prob tolerances above.
+    proposals against the oracle's); the proposals and their flow
+    log-densities within the BF16-operand bar above; accepted positions and
+    target log-densities on the compared steps within the proposals' own
+    measured error.
 
 Reference: resource/kernel/NF_proposal.py:27-128 (the global step),
 resource/model/nf_model/rqSpline.py:450-504 (forward, inverse, sample,
@@ -164,9 +166,12 @@ def test_nf_global_step_bf16_full_depth(cuda, d, L, hidden, nb, kind):
     os_ = fl.sample(z64.reshape(C * S, d))
     olq, olq0 = fl.log_prob(os_), fl.log_prob(x064)
     lpt_g, lpt_o = OT.value_grad(t, gs64)[0], OT.value_grad(t, os_)[0]
-    assert rel_err(glq, olq).max() <= BF16_TOL
-    bs_ = bf16_flow(fl).sample(z64.reshape(C * S, d))
+    # the proposals and their flow log-densities (each at its own proposal)
+    # within the error of the same quantities with BF16 operands
+    fb = bf16_flow(fl)
+    bs_ = fb.sample(z64.reshape(C * S, d))
     assert_within_bf16(gs64, os_, bs_, "proposals")
+    assert_within_bf16(glq, olq, fb.log_prob(bs_), "proposal flow log-densities")
     eps = (np.abs(glq - olq).max() + np.abs(glq0 - olq0).max() + np.abs(lpt_g - lpt_o).max()
            + 1e-5 * np.abs(lpt_o).max())
     margin = np.abs(np.log(u64) - oratio)
@@ -177,9 +182,11 @@ def test_nf_global_step_bf16_full_depth(cuda, d, L, hidden, nb, kind):
     np.testing.assert_array_equal(g_acc[cmp_mask], oacc[cmp_mask])
     gx, glp = pos.cpu().numpy(), lp.cpu().numpy()
     # accepted rows are proposals (or the starting rows): within the BF16
-    # error of the proposals themselves
+    # error of the proposals themselves, and their target log-densities
+    # within the target's measured spread over those proposals
     assert np.abs(gx[cmp_mask] - ox[cmp_mask]).max() <= 3.0 * np.abs(bs_ - os_).max() + 1e-4
-    assert rel_err(glp[cmp_mask], olp[cmp_mask]).max() <= BF16_TOL
+    lp_tol = 1.5 * np.abs(lpt_g - lpt_o).max() + 1e-5 * np.abs(lpt_o).max() + 1e-4
+    assert np.abs(glp[cmp_mask] - olp[cmp_mask]).max() <= lp_tol
     # the comparison is not vacuous: most steps are away from ties, and (for
     # the fitted target, where the flow is a fair proposal) both decisions occur
     assert cmp_mask.mean() >= 0.5, (cmp_mask.mean(), eps)

@@ -339,3 +339,29 @@ def test_column_stats_matches_numpy(cuda, n, d):
     x64 = x.astype(np.float64)
     np.testing.assert_allclose(mean.cpu().numpy(), x64.mean(0), rtol=1e-5, atol=1e-5)
     np.testing.assert_allclose(var.cpu().numpy(), x64.var(0, ddof=1), rtol=2e-4, atol=1e-6)
+
+
+@pytest.mark.parametrize("d,L,hidden,nb", [(128, 2, (512, 512), 12), (64, 2, (256, 256), 8), (6, 2, (64, 64), 3)],
+                         ids=["d128K12", "d64K8", "d6K3"])
+def test_spline_cta_pair_tiles_match_single_cta(cuda, d, L, hidden, nb):
+    """The fused last Linear + spline on CTA pairs (tcgen05 cta_group::2,
+    256-row tiles, half the group's weights per CTA) against one-CTA 128-row
+    tiles: the same products in the same K order, so log_prob, forward and
+    inverse agree to float32 rounding (1e-6 relative), at row counts that
+    leave the last pair's second CTA partly or wholly past the end."""
+    fl = to_f32(rand_flow(d, L, hidden, nb, seed=d + 3 * L, wscale=0.3))
+    m = gpu_model(fl, hidden, precision="bf16")
+    rng = np.random.default_rng(5)
+    for n in (50, 128, 300, 1000, 70000):
+        x = torch.tensor((rng.normal(size=(n, d)) * 1.5).astype(np.float32), device="cuda")
+        outs = {}
+        for tile in (128, 256):
+            m.spline_tile = tile
+            y, ld = m.forward(x)
+            xi, ldi = m.inverse(x)
+            outs[tile] = [m.log_prob(x), y, ld, xi, ldi]
+        from flowmc_gb300 import _lib
+        assert _lib.device_error() == 0
+        for a, b in zip(outs[128], outs[256]):
+            torch.testing.assert_close(b, a, rtol=1e-6, atol=1e-6)
+    m.spline_tile = 0

@@ -213,8 +213,11 @@ def test_acceptance_goes_to_one(tgts, kind, step):
     assert bool(acc.all())
 
 
+@pytest.mark.parametrize("rounds", [10, 7])
 @pytest.mark.parametrize("kind,step,nlf", [("mala", 1.0, 0), ("hmc", 0.1, 5), ("grw", 1.0, 0)])
-def test_moments_standard_normal_philox(tgts, kind, step, nlf):
+def test_moments_standard_normal_philox(tgts, kind, step, nlf, rounds):
+    """test_kernels.py:135-184 (N(0, I) moments within 3e-2), with the
+    default Philox-4x32-10 noise and the opt-in Philox-4x32-7 noise."""
     from flowmc_gb300.resource.kernel.base import run_local_steps
     dev = torch.device("cuda")
     C, S = 2048, 1000
@@ -222,10 +225,48 @@ def test_moments_standard_normal_philox(tgts, kind, step, nlf):
     pos = torch.empty(C, S, 2, device=dev)
     lp = torch.empty(C, S, device=dev)
     acc = torch.empty(C, S, device=dev)
-    run_local_steps(_kernel(kind, step, nlf), tgts["std2"], x0, S, 1, 3, 0, pos, lp, acc, 0)
+    k = _kernel(kind, step, nlf)
+    k.philox_rounds = rounds
+    run_local_steps(k, tgts["std2"], x0, S, 1, 3, 0, pos, lp, acc, 0)
     p = pos.double()
     assert abs(p.mean().item()) < 3e-2
     assert abs(p.var().item() - 1) < 3e-2
+
+
+def test_philox7_moments_64d_mixture_directions(tgts):
+    """Philox-4x32-7 noise at a width where every lane draws several blocks
+    (64-D standard normal, GRW, 16 lanes x 4 coordinates): per-coordinate
+    means and variances within 4 standard errors of their targets, the
+    cross-coordinate correlation near 0, and a stream different from the
+    10-round one."""
+    from flowmc_gb300 import targets as TG
+    from flowmc_gb300.resource.kernel.base import run_local_steps
+    dev = torch.device("cuda")
+    tgt = TG.DiagGaussian(64, device=dev)
+    C, S = 4096, 400
+    x0 = torch.randn(C, 64, device=dev)
+    res = {}
+    for rounds in (10, 7):
+        pos = torch.empty(C, S, 64, device=dev)
+        lp = torch.empty(C, S, device=dev)
+        acc = torch.empty(C, S, device=dev)
+        k = _kernel("grw", 0.3, 0)
+        k.philox_rounds = rounds
+        run_local_steps(k, tgt, x0, S, 1, 11, 0, pos, lp, acc, 0)
+        res[rounds] = pos[:, 200:].reshape(-1, 64).double()
+    p = res[7]
+    assert not torch.equal(res[7], res[10])
+    # effective sample size is well below C * 200 (autocorrelated chains):
+    # compare with a generous bound from the 10-round run's spread
+    m, v = p.mean(0), p.var(0)
+    m10, v10 = res[10].mean(0), res[10].var(0)
+    tol_m = 6 * float(m10.abs().mean()) + 1e-2
+    tol_v = 6 * float((v10 - 1).abs().mean()) + 1e-2
+    assert float(m.abs().max()) < tol_m, (float(m.abs().max()), tol_m)
+    assert float((v - 1).abs().max()) < tol_v, (float((v - 1).abs().max()), tol_v)
+    c = torch.corrcoef(p[::7, :8].T)
+    off = c - torch.eye(8, dtype=c.dtype, device=c.device)
+    assert float(off.abs().max()) < 0.05
 
 
 def test_errors_are_reported_not_raised_on_device(tgts):
