@@ -80,7 +80,7 @@ class FmcFlow(ctypes.Structure):
         ("min_knot_slope", ctypes.c_float),
         ("precision", ctypes.c_int32),
         ("gemm_bn", ctypes.c_int32),
-        ("spline_tile", ctypes.c_int32),
+        ("tile_rows", ctypes.c_int32),
         ("theta", ctypes.c_void_p),
         ("theta_bf16", ctypes.c_void_p),
         ("aux", ctypes.c_void_p),
@@ -296,10 +296,13 @@ KERNEL_IDS = {"k_tc_spline_fwd": 0, "k_tc_spline_inv": 1, "k_tc_spline_bwd": 2, 
 
 
 def kernel_timing(on: bool) -> None:
-    """Start (and reset) or stop the library's per-kernel event timing."""
-    check(lib().fmc_kernel_timing_enable(1 if on else 0))
+    """Start (and reset) or stop the library's per-kernel event timing.
+    Launches captured into a CUDA graph while it is on are timed when the
+    graph is replayed (replay it before kernel_timing_read)."""
     if on:
+        check(lib().fmc_kernel_timing_enable(0))
         check(lib().fmc_kernel_timing_reset())
+    check(lib().fmc_kernel_timing_enable(1 if on else 0))
 
 
 def kernel_timing_read() -> dict:

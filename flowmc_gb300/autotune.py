@@ -61,32 +61,44 @@ def tune_local_kernel(kernel, target, n_chains: int, probe_steps: int = 8, reps:
 
 
 def tune_flow_gemm(model, n_rows: int = 65536, reps: int = 3) -> int:
-    """Pick the BF16 hidden-layer GEMM tile width (128 or 256 output columns)
-    of a MaskedCouplingRQSpline by timing its log_prob pass over n_rows rows
-    (the NF global step's chunk) with each; the choice changes no result
-    (each output's reduction over K is the same), only the tile count per SM
-    (wave quantisation) and the epilogue's share. Cached per model shape and
-    row count; returns the pick and sets ``model.gemm_bn``."""
+    """Pick the BF16 flow's tensor-core tile shapes by measurement: the
+    hidden-layer GEMM tile width (128 or 256 output columns, ``gemm_bn``)
+    and the rows per tile of the fused spline and hidden GEMMs (128 rows on
+    one CTA, or 256 rows on a CTA pair with tcgen05 cta_group::2 and half
+    the weights per CTA, ``tile_rows``). Each candidate is timed on the
+    forward (log_prob) and inverse (sample) passes over n_rows rows (the NF
+    global step's chunk); no choice changes a result (every output's
+    reduction over K is the same), only wave quantisation, operand traffic
+    and the epilogue's share. Cached per model shape and row count; sets
+    ``model.gemm_bn`` and ``model.tile_rows`` and returns the GEMM width."""
     if getattr(model, "precision", "float32") not in ("bf16", "bfloat16"):
         return 0
-    key = ("flow_gemm", model.n_features, model.n_layers, tuple(model.hidden_size), model.num_bins, n_rows)
+    key = ("flow_tiles", model.n_features, model.n_layers, tuple(model.hidden_size), model.num_bins, n_rows)
     if key in _cache:
-        model.gemm_bn = _cache[key]
-        return _cache[key]
+        model.gemm_bn, model.tile_rows = _cache[key]
+        return model.gemm_bn
+    from .random import PRNGKey
     x = torch.randn(n_rows, model.n_features, device=model.device)
-    best, best_ms = 0, float("inf")
-    for bn in (256, 128):
-        model.gemm_bn = bn
-        model.log_prob(x)   # warm
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(reps):
-            model.log_prob(x)
-        e1.record()
-        e1.synchronize()
-        ms = e0.elapsed_time(e1)
-        if ms < best_ms:
-            best, best_ms = bn, ms
-    model.gemm_bn = best
+    z = torch.randn(n_rows, model.n_features, device=model.device)
+    best, best_ms = (0, 0), float("inf")
+    timings = {}
+    for tile_rows in (256, 128):
+        for bn in (256, 128):
+            model.gemm_bn, model.tile_rows = bn, tile_rows
+            model.log_prob(x)   # warm
+            model.sample(PRNGKey(0), n_rows, z=z)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                model.log_prob(x)
+                model.sample(PRNGKey(0), n_rows, z=z)
+            e1.record()
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            timings[f"tile_rows={tile_rows},gemm_bn={bn}"] = ms
+            if ms < best_ms:
+                best, best_ms = (bn, tile_rows), ms
+    model.gemm_bn, model.tile_rows = best
+    model.tile_timings_ms = timings
     _cache[key] = best
-    return best
+    return best[0]

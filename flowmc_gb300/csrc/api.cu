@@ -54,10 +54,19 @@ struct KernelTotals {
 KernelTotals g_totals[FMC_KT_COUNT];
 }  // namespace
 
+// On a capturing stream the events become event-record nodes of the graph
+// (cudaEventRecordExternal): a replay of the graph then records them with the
+// kernels running back to back, which is how launches should be timed (an
+// eager launch sequence can leave the GPU waiting for the host between an
+// event and its kernel).
+static cudaError_t record_event(cudaEvent_t e, cudaStream_t stream, bool capturing) {
+  return capturing ? cudaEventRecordWithFlags(e, stream, cudaEventRecordExternal) : cudaEventRecord(e, stream);
+}
+
 KernelTimer::KernelTimer(int kid, cudaStream_t stream, double flops, double bytes) {
   if (!g_timing_on.load(std::memory_order_relaxed) || kid < 0 || kid >= FMC_KT_COUNT) return;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-  if (cudaStreamIsCapturing(stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+  if (cudaStreamIsCapturing(stream, &cs) != cudaSuccess) {
     (void)cudaGetLastError();
     return;
   }
@@ -67,8 +76,10 @@ KernelTimer::KernelTimer(int kid, cudaStream_t stream, double flops, double byte
   t.kid = kid;
   t.flops = flops;
   t.bytes = bytes;
-  if (cudaEventRecord(t.e0, stream) != cudaSuccess) {
+  capturing = cs == cudaStreamCaptureStatusActive;
+  if (record_event(t.e0, stream, capturing) != cudaSuccess) {
     (void)cudaGetLastError();
+    t.kid = -1;
     return;
   }
   slot = i;
@@ -77,7 +88,7 @@ KernelTimer::KernelTimer(int kid, cudaStream_t stream, double flops, double byte
 
 KernelTimer::~KernelTimer() {
   if (slot < 0) return;
-  if (cudaEventRecord(g_slots[slot].e1, st) != cudaSuccess) {
+  if (record_event(g_slots[slot].e1, st, capturing) != cudaSuccess) {
     (void)cudaGetLastError();
     g_slots[slot].kid = -1;
   }

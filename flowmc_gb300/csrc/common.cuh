@@ -66,10 +66,12 @@ void count_launch();  // process-wide tally of kernel launches (fmc_launch_count
 // Optional per-kernel timing (fmc_kernel_timing_*): while enabled, a
 // KernelTimer scope records a CUDA event pair on the launch stream around
 // the launch it encloses, together with the launch's algorithmic FLOPs and
-// bytes as the caller states them. Launches on a capturing stream are not
-// timed. The ids below are the FMC_KT_* values of flowmc.h.
+// bytes as the caller states them. On a capturing stream the pair becomes
+// two event-record nodes of the graph, timed when the graph is replayed.
+// The ids are the FMC_KT_* values of flowmc.h.
 struct KernelTimer {
   int slot = -1;
+  bool capturing = false;
   cudaStream_t st = nullptr;
   KernelTimer(int kid, cudaStream_t stream, double flops, double bytes);
   ~KernelTimer();

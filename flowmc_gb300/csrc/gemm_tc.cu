@@ -137,12 +137,61 @@ static int launch_tc(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& 
   return FMC_OK;
 }
 
+// the CTA-pair form (bf16 outputs through TMA stores): 256-row tiles, a
+// persistent grid of as many clusters of 2 as can be resident
+template <int BN, int STAGES, int EPI>
+static int launch_tc_pair(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap& mc,
+                          int64_t M, int N, int K, const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store) {
+  using S = tc::Smem<BN / 2, STAGES>;
+  constexpr int TOTAL = S::TOTAL + 768 + tc::kStagingBytes;
+  static_assert(TOTAL <= 227 * 1024, "tcgen05 GEMM: shared memory over the per-CTA limit");
+  auto kern = tc::k_tc_gemm<BN, STAGES, EPI, true, true>;
+  static bool attr_set = false;
+  if (!attr_set) {
+    FMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, TOTAL));
+    attr_set = true;
+  }
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.blockDim = dim3(tc::kThreads, 1, 1);
+  cfg.dynamicSmemBytes = TOTAL;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  static int max_pairs = 0;
+  if (max_pairs == 0) {
+    cfg.gridDim = dim3(2 * (unsigned)(sm_count() / 2), 1, 1);
+    int n = 0;
+    FMC_CUDA_TRY(cudaOccupancyMaxActiveClusters(&n, (void*)kern, &cfg));
+    max_pairs = n > 0 ? n : 1;
+  }
+  int* err = nullptr;
+  FMC_CUDA_TRY(cudaGetSymbolAddress((void**)&err, g_tc_error));
+  const int64_t tiles = (M + 2 * tc::BM - 1) / (2 * tc::BM) * ((n_store + BN - 1) / BN);
+  FMC_CHECK_SUPPORTED(tiles < (1ll << 26) && M < (1ll << 31), "GEMM too large (%lld tiles)", (long long)tiles);
+  const int64_t pairs = tiles < max_pairs ? tiles : max_pairs;
+  cfg.gridDim = dim3(2 * (unsigned)pairs, 1, 1);
+  const int kid = EPI == tc::TC_EPI_TANH_BF16 ? FMC_KT_TC_GEMM_TANH : FMC_KT_TC_GEMM_DTANH;
+  const double bytes = (double)M * K * 2 + (double)N * K * 2 + (double)M * N * 2 +
+                       (EPI == tc::TC_EPI_DTANH_BF16 ? (double)M * N * 2 : 0.0);
+  KernelTimer kt(kid, st, 2.0 * (double)M * N * K, bytes);
+  int Mi = (int)M, one = 1;
+  int64_t stride = M * ldc;
+  FMC_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, ma, mb, mc, Mi, N, K, ep, C, ldc, n_store, one, stride, err));
+  FMC_LAUNCH_CHECK();
+  return FMC_OK;
+}
+
 bool tc_gemm_stages_output(const void* C, int64_t ldc, int n_store, int64_t M) {
   return ((uintptr_t)C & 15) == 0 && (ldc * 2) % 16 == 0 && n_store >= 64 && M >= 32;
 }
 
 int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K, const uint16_t* B, int N,
-            int rows_b, const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store, int epi, int bn) {
+            int rows_b, const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store, int epi, int bn, bool pair) {
   FMC_CHECK_ARG(K % tc::BK == 0 && K >= tc::BK, "K=%d must be a positive multiple of 64", K);
   FMC_CHECK_ARG(rows_a % tc::BM == 0 && rows_a >= M, "A rows %lld must cover M and be a multiple of 128",
                 (long long)rows_a);
@@ -164,6 +213,14 @@ int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K
                 "column sums need the tanh-adjoint epilogue with staged TMA stores");
   memset(&mc, 0, sizeof(mc));
   if (tstore && (rc = make_map(&mc, C, n_store, M, ldc, 32))) return rc;
+  if (pair && tstore && BN == 256) {
+    // B in boxes of half the tile's rows: each CTA of a pair loads one half
+    if ((rc = make_map(&mb, B, K, rows_b, K, BN / 2))) return rc;
+    if (epi == tc::TC_EPI_TANH_BF16)
+      return launch_tc_pair<256, 4, tc::TC_EPI_TANH_BF16>(st, ma, mb, mc, M, N, K, ep, C, ldc, n_store);
+    if (epi == tc::TC_EPI_DTANH_BF16)
+      return launch_tc_pair<256, 4, tc::TC_EPI_DTANH_BF16>(st, ma, mb, mc, M, N, K, ep, C, ldc, n_store);
+  }
 #define TC_CASE(E)                                                                                            \
   if (epi == E) {                                                                                             \
     if (BN == 256) return launch_tc<256, 4, E, false>(st, ma, mb, mc, M, N, K, ep, C, ldc, n_store);          \
@@ -297,7 +354,7 @@ int conditioner_bf16_hidden(const FmcFlow* f, const FlowGeom& g, int l, int64_t 
     ep.bias = th + g.lin_b(l, i);
     const int ldo = (int)FlowGeom::rup(N, 64);
     int rc = tc_gemm(st, a, m, rows, K, f->theta_bf16 + g.w16_off[seg], N, g.w16_rows(l, i), ep, hbuf[i & 1], ldo, ldo,
-                     tc::TC_EPI_TANH_BF16, f->gemm_bn);
+                     tc::TC_EPI_TANH_BF16, f->gemm_bn, f->tile_rows != 128);
     if (rc) return rc;
     a = hbuf[i & 1];
   }

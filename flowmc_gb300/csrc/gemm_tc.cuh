@@ -69,9 +69,12 @@ bool tc_gemm_stages_output(const void* C, int64_t ldc, int n_store, int64_t M);
 // a multiple of 128 covering M), B [rows_b, K] bf16 (rows_b a multiple of 256
 // covering N). bf16 epilogues store n_store columns (zeros beyond N), fp32
 // epilogues n_store (= N) columns.
-// bn: the output tile width, 128 or 256 (0: 256 when N > 128, else 128)
+// bn: the output tile width, 128 or 256 (0: 256 when N > 128, else 128);
+// pair: 256-row tiles on CTA pairs (cta_group::2) where the epilogue writes
+// bf16 through TMA stores and the tile is 256 columns wide
 int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K, const uint16_t* B, int N,
-            int rows_b, const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store, int epi, int bn = 0);
+            int rows_b, const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store, int epi, int bn = 0,
+            bool pair = false);
 
 // scratch (floats) that tc_gemm's fp32 mode uses for split-K partials of an
 // M x N x K product when EpiArgs::kpart is given (0: it would not split)

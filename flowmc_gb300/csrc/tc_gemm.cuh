@@ -290,6 +290,17 @@ __device__ __forceinline__ bool tc_skip(const int* err) {
   return s_skip != 0;
 }
 
+// the error-word check of tc_skip, made by the even CTA for the pair
+__device__ __forceinline__ bool tc_skip_pair(const int* err) {
+  __shared__ int s_skip;
+  if (threadIdx.x == 0) s_skip = (cluster_ctarank() == 0) ? *(const volatile int*)err : 0;
+  cluster_sync_all();
+  int v;
+  asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(mapa_shared(smem_u32(&s_skip), 0)) : "memory");
+  cluster_sync_all();   // the even CTA's word stays readable until both have read it
+  return v != 0;
+}
+
 // Persistent GEMM: each CTA walks work items t = blockIdx.x, +gridDim.x, ...
 // Item t is K-slice s = t % splits of tile t / splits (tile u covers rows
 // (u / n_tiles) * 128 and columns (u % n_tiles) * BN); with splits > 1 the
@@ -300,15 +311,21 @@ __device__ __forceinline__ bool tc_skip(const int* err) {
 // shared-memory staging and TMA stores on tmC ([M, n_store] bf16, box 64 x 32);
 // the shared memory then holds the ring, its barriers, 768 bytes of padding
 // and the staging buffers (kStagingBytes, 1024-byte aligned).
-template <int BN, int STAGES, int EPI, bool TSTORE>
+// PAIR (launched as clusters of 2, no split-K): a tile is 256 rows x BN
+// columns computed by a CTA pair with tcgen05 cta_group::2 -- each CTA loads
+// its 128 rows of A and BN / 2 rows of B (tmB's box is BN / 2 rows), the
+// even CTA issues the MMAs, each CTA runs the epilogue of its own rows.
+template <int BN, int STAGES, int EPI, bool TSTORE, bool PAIR = false>
 __global__ void __launch_bounds__(kThreads, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
               const __grid_constant__ CUtensorMap tmC, int M, int N, int K, const EpiArgs ep, void* __restrict__ C,
               int64_t ldc, int n_store, int splits, int64_t split_stride, int* err) {
   static_assert(!TSTORE || EPI == TC_EPI_TANH_BF16 || EPI == TC_EPI_DTANH_BF16, "TMA store: bf16 epilogues only");
-  if (tc_skip(err)) return;
+  static_assert(!PAIR || BN % 32 == 0, "a CTA pair splits B into two multiples of 16 rows");
+  if (PAIR ? tc_skip_pair(err) : tc_skip(err)) return;
   extern __shared__ uint8_t smem_raw[];
-  using S = Smem<BN, STAGES>;
+  constexpr int BNL = PAIR ? BN / 2 : BN;   // B rows this CTA loads per stage
+  using S = Smem<BNL, STAGES>;
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* staging = base + STAGES * S::STAGE_BYTES + 1024;
   uint64_t* full = (uint64_t*)(base + STAGES * S::STAGE_BYTES);
@@ -323,8 +340,14 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int nk = (K + BK - 1) / BK;
   const int nks = (nk + splits - 1) / splits;   // K chunks per slice
   const int n_tiles = (n_store + BN - 1) / BN;
-  const int m_tiles = (M + BM - 1) / BM;
+  constexpr int TM = PAIR ? 2 * BM : BM;        // rows per tile
+  const int m_tiles = (M + TM - 1) / TM;
   const int tiles = n_tiles * m_tiles * splits;
+  const uint32_t rank = PAIR ? cluster_ctarank() : 0u;
+  const int t_first = PAIR ? (int)(blockIdx.x / 2) : (int)blockIdx.x;   // work items of this CTA (pair)
+  const int t_step = PAIR ? (int)(gridDim.x / 2) : (int)gridDim.x;
+  // waits: barriers that the other CTA of a pair also completes acquire at cluster scope
+  auto wait = [](uint64_t* bar, uint32_t ph) { return PAIR ? mbar_wait_cl(bar, ph) : mbar_wait(bar, ph); };
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -333,58 +356,79 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_empty[b], kEpiWarps);
+      mbar_init(&acc_empty[b], (PAIR ? 2 : 1) * kEpiWarps);
     }
     mbar_init(mma_done, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(2 * BN));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    if constexpr (PAIR) {
+      asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                   "r"(2 * BN));
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+    } else {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                   "r"(2 * BN));
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
+  if constexpr (PAIR) cluster_sync_all();   // both CTAs' barriers exist before either signals the other's
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
   if (warp == 0) {
     if (lane == 0) {
       uint32_t it = 0;
-      for (int t = blockIdx.x; t < tiles && !*abort_flag; t += gridDim.x) {
+      for (int t = t_first; t < tiles && !*abort_flag; t += t_step) {
         const int u = t / splits, sl = t - u * splits;
-        const int m0 = (u / n_tiles) * BM, n0 = (u % n_tiles) * BN;
+        const int m0 = (u / n_tiles) * TM + (int)rank * BM, n0 = (u % n_tiles) * BN + (int)rank * BNL;
         const int kb = sl * nks, ke = (kb + nks < nk) ? kb + nks : nk;
         for (int k = kb; k < ke; ++k, ++it) {
           const int s = it % STAGES;
           const uint32_t ph = (it / STAGES) & 1u;
-          if (it >= (uint32_t)STAGES && !mbar_wait(&empty[s], ph ^ 1u)) {
+          if (it >= (uint32_t)STAGES && !wait(&empty[s], ph ^ 1u)) {
             *abort_flag = 1;
             break;
           }
           if (*abort_flag) break;
           uint8_t* sa = base + s * S::STAGE_BYTES;
           uint8_t* sb = sa + S::A_BYTES;
-          mbar_expect_tx(&full[s], S::STAGE_BYTES);
-          tma_load_2d(sa, &tmA, &full[s], k * BK, m0);
-          tma_load_2d(sb, &tmB, &full[s], k * BK, n0);
+          if constexpr (PAIR) {
+            // both CTAs' copies count on the even CTA's barrier
+            const uint32_t full_cl = mapa_shared(smem_u32(&full[s]), 0);
+            if (rank == 0) mbar_expect_tx(&full[s], 2 * (S::A_BYTES + S::B_BYTES));
+            tma_load_2d_pair(sa, &tmA, full_cl, k * BK, m0);
+            tma_load_2d_pair(sb, &tmB, full_cl, k * BK, n0);
+          } else {
+            mbar_expect_tx(&full[s], S::STAGE_BYTES);
+            tma_load_2d(sa, &tmA, &full[s], k * BK, m0);
+            tma_load_2d(sb, &tmB, &full[s], k * BK, n0);
+          }
         }
       }
       if (*abort_flag) {
-        // let the copies still in flight land before the CTA exits (bounded)
-        for (uint32_t j = it > (uint32_t)STAGES ? it - STAGES : 0; j < it; ++j)
-          mbar_wait(&full[j % STAGES], (j / STAGES) & 1u);
+        // let the copies still in flight land before the CTA exits (bounded;
+        // a pair's copies count on the even CTA, so the odd one waits on the
+        // stages' release instead)
+        for (uint32_t j = it > (uint32_t)STAGES ? it - STAGES : 0; j < it; ++j) {
+          if (PAIR && rank != 0)
+            wait(&empty[j % STAGES], (j / STAGES) & 1u);
+          else
+            wait(&full[j % STAGES], (j / STAGES) & 1u);
+        }
       }
     }
   } else if (warp == 1) {
-    if (lane == 0) {
-      const uint32_t idesc = idesc_bf16_f32(BN);
+    if (lane == 0 && rank == 0) {
+      const uint32_t idesc = PAIR ? idesc_bf16_f32_pair(BN) : idesc_bf16_f32(BN);
       uint32_t it = 0;
       int local = 0;
-      for (int t = blockIdx.x; t < tiles && !*abort_flag; t += gridDim.x, ++local) {
+      for (int t = t_first; t < tiles && !*abort_flag; t += t_step, ++local) {
         const int b = local & 1, use = local >> 1;
-        if (use > 0 && !mbar_wait(&acc_empty[b], (uint32_t)(use - 1) & 1u)) {
+        if (use > 0 && !wait(&acc_empty[b], (uint32_t)(use - 1) & 1u)) {
           *abort_flag = 1;
           break;
         }
@@ -396,7 +440,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int k = kb; k < ke; ++k, ++it) {
           const int s = it % STAGES;
           const uint32_t ph = (it / STAGES) & 1u;
-          if (!mbar_wait(&full[s], ph) || *abort_flag) {
+          if (!wait(&full[s], ph) || *abort_flag) {
             *abort_flag = 1;
             stop = true;
             break;
@@ -408,16 +452,19 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
           for (int kk = 0; kk < BK / 16; ++kk) {
             // advance along K inside the swizzle atom: 16 bf16 = 32 bytes
-            mma_bf16(d, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, (k > kb || kk > 0) ? 1u : 0u);
+            if constexpr (PAIR)
+              mma_bf16_pair(d, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, (k > kb || kk > 0) ? 1u : 0u);
+            else
+              mma_bf16(d, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, (k > kb || kk > 0) ? 1u : 0u);
           }
-          mma_commit(&empty[s]);
+          if constexpr (PAIR) mma_commit_pair(&empty[s]); else mma_commit(&empty[s]);
         }
         if (stop) break;
-        mma_commit(&acc_full[b]);
+        if constexpr (PAIR) mma_commit_pair(&acc_full[b]); else mma_commit(&acc_full[b]);
       }
       // fires once every MMA issued so far has finished (also after an abort),
-      // so the TMEM can be released safely
-      mma_commit(mma_done);
+      // so the TMEM can be released safely (in both CTAs of a pair)
+      if constexpr (PAIR) mma_commit_pair(mma_done); else mma_commit(mma_done);
     }
   } else {
     // epilogue warps: TMEM lane quarter = warp % 4, one accumulator row per
@@ -431,12 +478,14 @@ __global__ void __launch_bounds__(kThreads, 1)
     const bool aux_vec = (((uintptr_t)ep.aux & 15) == 0) && ((ep.ldaux * 2) % 16 == 0);
     int blkno = 0;   // staged blocks so far (selects the staging buffer)
     int local = 0;
-    for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++local) {
+    const uint32_t acc_empty_cl0 = PAIR ? mapa_shared(smem_u32(&acc_empty[0]), 0) : 0u;
+    const uint32_t acc_empty_cl1 = PAIR ? mapa_shared(smem_u32(&acc_empty[1]), 0) : 0u;
+    for (int t = t_first; t < tiles; t += t_step, ++local) {
       const int b = local & 1, use = local >> 1;
       const int u = t / splits, sl = t - u * splits;
-      const int m0 = (u / n_tiles) * BM, n0 = (u % n_tiles) * BN;
+      const int m0 = (u / n_tiles) * TM + (int)rank * BM, n0 = (u % n_tiles) * BN;
       const int gm = m0 + row;
-      if (*abort_flag || !mbar_wait(&acc_full[b], (uint32_t)use & 1u)) {
+      if (*abort_flag || !wait(&acc_full[b], (uint32_t)use & 1u)) {
         *abort_flag = 1;
         break;
       }
@@ -570,12 +619,20 @@ __global__ void __launch_bounds__(kThreads, 1)
           tmem_ld32_issue(tbase + (uint32_t)col_of(i + 1), nxt);
           prefetch(col_of(i + 1), bl_nxt, av_nxt);
         } else {
-          // this warp's TMEM lanes of buffer b are read: release them to the MMA warp
+          // this warp's TMEM lanes of buffer b are read: release them to the
+          // MMA warp (the even CTA's, for a pair)
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
           __syncwarp();
-          if (lane == 0) mbar_arrive(&acc_empty[b]);
+          if (lane == 0) {
+            if constexpr (PAIR)
+              mbar_arrive_cluster(b ? acc_empty_cl1 : acc_empty_cl0);
+            else
+              mbar_arrive(&acc_empty[b]);
+          }
         }
-        const bool blk_live = n0 + (c0 & ~63) < n_store;   // uniform
+        // uniform: a 64-column block inside the output, of a CTA with rows
+        // inside it (the odd CTA of the last pair can lie wholly past row M)
+        const bool blk_live = n0 + (c0 & ~63) < n_store && m0 < M;
         if (TSTORE && (i & 1) == 0 && blk_live) {
           // the staging buffer about to be filled was last used two blocks ago
           if (lane == 0) bulk_wait_read_1();
@@ -620,12 +677,17 @@ __global__ void __launch_bounds__(kThreads, 1)
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 1) {
-    if (lane == 0) mbar_wait(mma_done, 0);
+    if (lane == 0) wait(mma_done, 0);
     __syncwarp();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN));
+    if constexpr (PAIR)
+      asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN));
+    else
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN));
   }
   if (threadIdx.x == 0 && *abort_flag) atomicExch(err, 1);
+  // neither CTA of a pair leaves while the other may still signal its barriers
+  if constexpr (PAIR) cluster_sync_all();
 }
 
 }  // namespace tc

@@ -440,17 +440,6 @@ __global__ void __launch_bounds__(kSplThreads, 1)
 // `acc_empty` of the even CTA counts the epilogue warps of both CTAs.
 // Every wait is bounded; the pair agrees on the fail-fast decision first.
 
-// the error-word check of tc_skip, made by the even CTA for the pair
-__device__ __forceinline__ bool tc_skip_pair(const int* err) {
-  __shared__ int s_skip;
-  if (threadIdx.x == 0) s_skip = (cluster_ctarank() == 0) ? *(const volatile int*)err : 0;
-  cluster_sync_all();
-  int v;
-  asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(mapa_shared(smem_u32(&s_skip), 0)) : "memory");
-  cluster_sync_all();   // the even CTA's word stays readable until both have read it
-  return v != 0;
-}
-
 template <int BH, int STAGES>
 struct PairSmem {
   static constexpr int A_BYTES = BM * BK * 2;
@@ -806,7 +795,7 @@ int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l
   const float* bias = f->theta + g.layer_off[l] + g.lin_b(l, g.nh);
   // CTA pairs (256-row tiles, half the weight rows per CTA) unless one-CTA
   // tiles are asked for, or the group width does not split in two multiples of 16
-  const bool pair = f->spline_tile != 128 && bn % 32 == 0;
+  const bool pair = f->tile_rows != 128 && bn % 32 == 0;
   CUtensorMap ma, mb;
   int rc = make_tma_map_bf16(&ma, A, Kd, rows_a, Kd, tc::BM);
   if (rc) return rc;

@@ -56,7 +56,7 @@ class MaskedCouplingRQSpline(NFModel):
             torch.device("cuda") if torch.cuda.is_available() else torch.device("cpu"))
         self.precision = precision
         self.gemm_bn = 0   # BF16 hidden-layer GEMM tile width; 0 = library choice (autotune.tune_flow_gemm)
-        self.spline_tile = 0   # BF16 fused spline rows per tile (128 one CTA, 256 a CTA pair); 0 = library choice
+        self.tile_rows = 0   # BF16 tensor-core tile rows (128 one CTA, 256 a CTA pair); 0 = library choice
         d = self._n_features
         P = 3 * self.num_bins + 1
         self._P = P
@@ -144,7 +144,7 @@ class MaskedCouplingRQSpline(NFModel):
         s.min_knot_slope = self.min_knot_slope
         s.precision = _lib.PREC_BF16 if self.precision in ("bf16", "bfloat16") else _lib.PREC_FP32
         s.gemm_bn = int(getattr(self, "gemm_bn", 0))
-        s.spline_tile = int(getattr(self, "spline_tile", 0))
+        s.tile_rows = int(getattr(self, "tile_rows", 0))
         s.theta = _lib.ptr(self.theta)
         s.theta_bf16 = _lib.ptr(self.theta_bf16)
         s.aux = _lib.ptr(self.aux)

@@ -284,10 +284,12 @@ typedef struct FmcFlow {
                                         0 = library choice (256 for outputs
                                         wider than 128 columns, else 128),
                                         or 128 / 256 (an autotuner's pick) */
-  int32_t spline_tile;               /* BF16 fused last Linear + spline rows
-                                        per tile: 0 = library choice (256),
-                                        128 = one CTA per tile, 256 = a CTA
-                                        pair (cta_group::2) per tile */
+  int32_t tile_rows;                 /* rows per tensor-core tile of the BF16
+                                        flow kernels (fused last Linear +
+                                        spline, hidden-layer GEMMs): 0 =
+                                        library choice (256), 128 = one CTA
+                                        per tile, 256 = a CTA pair
+                                        (tcgen05 cta_group::2) per tile */
   float* theta;                      /* [n_params] float32 master weights   */
   uint16_t* theta_bf16;              /* [n_params] bf16 shadow (BF16 mode)   */
   float* aux;                        /* [2*n_dim + 2], see above             */
@@ -473,14 +475,17 @@ FMC_API int fmc_launch_count(uint64_t* out);
 
 /* ---- per-kernel timing (profiling aid; no counterpart in the reference,
  * whose JAX path has no kernels of its own) ---------------------------
- * While enabled, every launch of the kernels listed below on a stream that
- * is not capturing is bracketed by a CUDA event pair recorded on its launch
- * stream, and the launch's algorithmic FLOPs and bytes (useful work, not
- * padding) are noted. fmc_kernel_timing_read synchronises on the recorded
- * events and returns the totals per kernel since the last reset; at most
- * 16384 launches are recorded between reads. Enabling creates the event
- * pool on the current device once. Off by default; costs two event
- * records per timed launch. */
+ * While enabled, every launch of the kernels listed below is bracketed by a
+ * CUDA event pair recorded on its launch stream, and the launch's
+ * algorithmic FLOPs and bytes (useful work, not padding) are noted. On a
+ * stream that is capturing a CUDA graph the pair is recorded as external
+ * event nodes of the graph: replay the graph before reading, and the times
+ * are those of that replay, with the kernels back to back as the graph runs
+ * them. fmc_kernel_timing_read synchronises on the recorded events and
+ * returns the totals per kernel since the last reset; at most 16384 launches
+ * are recorded between reads. Enabling creates the event pool on the
+ * current device once. Off by default; costs two event records per timed
+ * launch. */
 enum {
   FMC_KT_TC_SPLINE_FWD = 0,   /* k_tc_spline, forward (fused last Linear + spline)  */
   FMC_KT_TC_SPLINE_INV = 1,   /* k_tc_spline, inverse                               */

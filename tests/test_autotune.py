@@ -71,3 +71,4 @@ def test_flow_gemm_tile_width_is_tuned_and_changes_no_result(cuda):
     torch.testing.assert_close(out[128], out[256], rtol=0, atol=0)
     pick = tune_flow_gemm(m, n_rows=8192, reps=1)
     assert pick in (128, 256) and m.gemm_bn == pick
+    assert m.tile_rows in (128, 256) and len(m.tile_timings_ms) == 4

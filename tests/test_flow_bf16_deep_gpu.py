@@ -18,9 +18,9 @@ Tolerances (BF16 GEMM inputs, FP32 accumulation, FP32 spline):
   * NFProposal global step (fmc_nf_global_steps, scripted normals and
     uniforms): accept decisions identical to the oracle's at every step of a
     chain up to its first near-tie, where a near-tie is a step whose oracle
-    margin |log u - ratio| is below twice the measured error of the ratio's
-    ingredients (flow log-densities and target log-densities of the BF16
-    proposals against the oracle's); the proposals and their flow
+    margin |log u - ratio| is below twice the measured error of that step's
+    ratio ingredients (flow and target log-densities of its BF16 proposal and
+    of the chain's current state against the oracle's); the proposals and their flow
     log-densities within the BF16-operand bar above; accepted positions and
     target log-densities on the compared steps within the proposals' own
     measured error.
@@ -172,8 +172,17 @@ def test_nf_global_step_bf16_full_depth(cuda, d, L, hidden, nb, kind):
     bs_ = fb.sample(z64.reshape(C * S, d))
     assert_within_bf16(gs64, os_, bs_, "proposals")
     assert_within_bf16(glq, olq, fb.log_prob(bs_), "proposal flow log-densities")
-    eps = (np.abs(glq - olq).max() + np.abs(glq0 - olq0).max() + np.abs(lpt_g - lpt_o).max()
-           + 1e-5 * np.abs(lpt_o).max())
+    # per step, the error of the ratio's ingredients: the proposal's flow and
+    # target log-densities (each at its own BF16 / float64 point) plus those
+    # of the current state -- the start, then the last proposal the oracle
+    # accepted -- with float32 rounding of the target on top
+    err_p = (np.abs(glq - olq) + np.abs(lpt_g - lpt_o) + 1e-5 * np.abs(lpt_o)).reshape(C, S)
+    lpt0 = OT.value_grad(t, x064)[0]
+    cur = np.abs(glq0 - olq0) + 1e-5 * np.abs(lpt0)
+    eps = np.empty((C, S))
+    for s_ in range(S):
+        eps[:, s_] = err_p[:, s_] + cur
+        cur = np.where(oacc[:, s_] > 0.5, err_p[:, s_], cur)
     margin = np.abs(np.log(u64) - oratio)
     near = margin <= 2.0 * eps
     first_tie = np.where(near.any(1), near.argmax(1), S)    # per chain: steps compared = [0, first_tie)
@@ -189,6 +198,6 @@ def test_nf_global_step_bf16_full_depth(cuda, d, L, hidden, nb, kind):
     assert np.abs(glp[cmp_mask] - olp[cmp_mask]).max() <= lp_tol
     # the comparison is not vacuous: most steps are away from ties, and (for
     # the fitted target, where the flow is a fair proposal) both decisions occur
-    assert cmp_mask.mean() >= 0.5, (cmp_mask.mean(), eps)
+    assert cmp_mask.mean() >= 0.5, (cmp_mask.mean(), float(np.median(eps)))
     if kind == "diag":
         assert 0.05 <= oacc[cmp_mask].mean() <= 0.95, oacc[cmp_mask].mean()

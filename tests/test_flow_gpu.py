@@ -356,7 +356,7 @@ def test_spline_cta_pair_tiles_match_single_cta(cuda, d, L, hidden, nb):
         x = torch.tensor((rng.normal(size=(n, d)) * 1.5).astype(np.float32), device="cuda")
         outs = {}
         for tile in (128, 256):
-            m.spline_tile = tile
+            m.tile_rows = tile
             y, ld = m.forward(x)
             xi, ldi = m.inverse(x)
             outs[tile] = [m.log_prob(x), y, ld, xi, ldi]
@@ -364,4 +364,4 @@ def test_spline_cta_pair_tiles_match_single_cta(cuda, d, L, hidden, nb):
         assert _lib.device_error() == 0
         for a, b in zip(outs[128], outs[256]):
             torch.testing.assert_close(b, a, rtol=1e-6, atol=1e-6)
-    m.spline_tile = 0
+    m.tile_rows = 0

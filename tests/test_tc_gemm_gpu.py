@@ -103,3 +103,40 @@ def test_raised_error_word_skips_tensor_core_work(cuda):
     torch.cuda.synchronize()
     torch.testing.assert_close(C, A.float() @ B.float().T, rtol=1e-2, atol=1e-2)
     assert _lib.device_error() == 0
+
+
+def test_kernel_timing_eager_and_captured(cuda):
+    """fmc_kernel_timing_*: an eager launch and a launch captured into a CUDA
+    graph (timed on replay) are each counted once, with positive time and
+    the GEMM's 2 M N K FLOPs."""
+    from flowmc_gb300 import _lib
+    M, K, N = 4096, 512, 512
+    A = torch.randn(M, K, device="cuda").to(torch.bfloat16)
+    B = torch.randn(N, K, device="cuda").to(torch.bfloat16)
+    bias = torch.zeros(N, device="cuda")
+    C = torch.empty(M, N, device="cuda")
+
+    def gemm():
+        _lib.check(_lib.lib().fmc_tc_gemm_bf16(A.data_ptr(), M, M, K, B.data_ptr(), N, N, bias.data_ptr(),
+                                               C.data_ptr(), N, N, 1, _lib.stream_handle()))
+
+    gemm()
+    torch.cuda.synchronize()
+    _lib.kernel_timing(True)
+    gemm()
+    got = _lib.kernel_timing_read()
+    assert got["k_tc_gemm_f32"]["launches"] == 1 and got["k_tc_gemm_f32"]["ms"] > 0
+    assert got["k_tc_gemm_f32"]["flops"] == 2.0 * M * N * K
+    _lib.kernel_timing(True)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        gemm()
+    _lib.kernel_timing(False)
+    g.replay()
+    torch.cuda.synchronize()
+    got = _lib.kernel_timing_read()
+    assert got["k_tc_gemm_f32"]["launches"] == 1 and got["k_tc_gemm_f32"]["ms"] > 0
+    torch.testing.assert_close(C, A.float() @ B.float().T, rtol=1e-2, atol=1e-2)
+    _lib.kernel_timing(False)
