@@ -139,6 +139,7 @@ _SIGNATURES = {
     "fmc_device_error": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int32), ctypes.c_int32]),
     "fmc_device_error_set": (ctypes.c_int, [ctypes.c_int32]),
     "fmc_kernel_timing_enable": (ctypes.c_int, [ctypes.c_int32]),
+    "fmc_kernel_grid": (ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
     "fmc_kernel_timing_reset": (ctypes.c_int, []),
     "fmc_kernel_timing_read": (ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(ctypes.c_int64),
                                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
@@ -315,6 +316,13 @@ def kernel_timing_read() -> dict:
         if n.value:
             out[name] = {"launches": int(n.value), "ms": ms.value, "flops": fl.value, "bytes": by.value}
     return out
+
+
+def kernel_grid(name: str) -> tuple[int, int]:
+    """(CTAs, CTAs per cluster) of the last launch of a timed kernel."""
+    a, b = ctypes.c_int32(), ctypes.c_int32()
+    check(lib().fmc_kernel_grid(KERNEL_IDS[name], ctypes.byref(a), ctypes.byref(b)))
+    return int(a.value), int(b.value)
 
 
 def launch_count() -> int:

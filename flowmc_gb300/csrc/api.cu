@@ -52,7 +52,14 @@ struct KernelTotals {
   double ms, flops, bytes;
 };
 KernelTotals g_totals[FMC_KT_COUNT];
+std::atomic<int> g_grid[FMC_KT_COUNT][2];
 }  // namespace
+
+void note_grid(int kid, int ctas, int cluster) {
+  if (kid < 0 || kid >= FMC_KT_COUNT) return;
+  g_grid[kid][0].store(ctas, std::memory_order_relaxed);
+  g_grid[kid][1].store(cluster, std::memory_order_relaxed);
+}
 
 // On a capturing stream the events become event-record nodes of the graph
 // (cudaEventRecordExternal): a replay of the graph then records them with the
@@ -146,6 +153,15 @@ extern "C" int fmc_kernel_timing_read(int32_t kid, int64_t* launches, double* ms
   *ms = g_totals[kid].ms;
   *flops = g_totals[kid].flops;
   *bytes = g_totals[kid].bytes;
+  return FMC_OK;
+}
+
+extern "C" int fmc_kernel_grid(int32_t kid, int32_t* ctas, int32_t* cluster) {
+  using namespace fmc;
+  FMC_CHECK_ARG(kid >= 0 && kid < FMC_KT_COUNT, "kernel id %d out of range", kid);
+  FMC_CHECK_ARG(ctas && cluster, "NULL pointer");
+  *ctas = g_grid[kid][0].load(std::memory_order_relaxed);
+  *cluster = g_grid[kid][1].load(std::memory_order_relaxed);
   return FMC_OK;
 }
 

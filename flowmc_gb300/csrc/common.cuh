@@ -69,6 +69,9 @@ void count_launch();  // process-wide tally of kernel launches (fmc_launch_count
 // bytes as the caller states them. On a capturing stream the pair becomes
 // two event-record nodes of the graph, timed when the graph is replayed.
 // The ids are the FMC_KT_* values of flowmc.h.
+// launch geometry of the last launch of kernel `kid` (fmc_kernel_grid)
+void note_grid(int kid, int ctas, int cluster);
+
 struct KernelTimer {
   int slot = -1;
   bool capturing = false;

@@ -21,7 +21,10 @@ struct FlowGeom {
   // kernel, tc_spline.cu): group g = DG transformed coordinates x P rows,
   // padded to BN rows; [n_groups(l) * BN, round_up(H_last, 64)]
   int64_t w16g_off[FMC_MAX_LAYERS + 1];
-  int spl_dg, spl_bn;
+  // spline groups: a coordinate's P raw parameters sit at a column pitch of
+  // spl_pp = round_up(P, 8) (so the epilogue reads them with 8-column TMEM
+  // loads at 8-aligned columns), spl_dg coordinates per group, spl_bn rows
+  int spl_pp, spl_dg, spl_bn;
   int64_t n_w16;
 
   // conditioning coordinates of layer l: j = 2k + cpar(l); transformed: j = 2k + tpar(l)

@@ -328,7 +328,7 @@ static int recompute_hidden_bf16(const FmcFlow* f, const FlowGeom& g, int l, int
     ep.ct_rows_pad = w.n64;
     const int ldo = (int)FlowGeom::rup(N, 64);
     if ((rc = tc_gemm(st, a, n, w.n128, K, f->theta_bf16 + g.w16_off[seg], N, g.w16_rows(l, i), ep, h, ldo, ldo,
-                      tc::TC_EPI_TANH_BF16, f->gemm_bn, f->tile_rows != 128)))
+                      tc::TC_EPI_TANH_BF16, f->gemm_bn, f->tile_rows == 256)))
       return rc;
     a = h;
   }

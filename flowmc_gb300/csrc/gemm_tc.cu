@@ -124,6 +124,7 @@ static int launch_tc(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& 
     const double bytes = (double)M * K * 2 + (double)N * K * 2 + (double)M * N * (bf16_out ? 2 : 4) +
                          (EPI == tc::TC_EPI_DTANH_BF16 ? (double)M * N * 2 : 0.0);
     KernelTimer kt(kid, st, 2.0 * (double)M * N * K, bytes);
+    note_grid(kid, (int)grid, 1);
     kern<<<(unsigned)grid, tc::kThreads, TOTAL, st>>>(ma, mb, mc, (int)M, N, K, ep, out, ldc, n_store, splits,
                                                      M * ldc, err);
     FMC_LAUNCH_CHECK();
@@ -179,6 +180,7 @@ static int launch_tc_pair(cudaStream_t st, const CUtensorMap& ma, const CUtensor
   const double bytes = (double)M * K * 2 + (double)N * K * 2 + (double)M * N * 2 +
                        (EPI == tc::TC_EPI_DTANH_BF16 ? (double)M * N * 2 : 0.0);
   KernelTimer kt(kid, st, 2.0 * (double)M * N * K, bytes);
+  note_grid(kid, (int)(2 * pairs), 2);
   int Mi = (int)M, one = 1;
   int64_t stride = M * ldc;
   FMC_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, ma, mb, mc, Mi, N, K, ep, C, ldc, n_store, one, stride, err));
@@ -250,7 +252,7 @@ __global__ void k_pack_bf16(FlowGeom g, const float* __restrict__ theta, uint16_
     // grouped copy of layer l's last Linear for the fused spline kernel
     const int l = blockIdx.y - 2 * nseg;
     const int i = g.nh, in = g.lin_in(l, i), nt = g.nt(l);
-    const int cols = g.w16_cols(l, i), DG = g.spl_dg, BN = g.spl_bn;
+    const int cols = g.w16_cols(l, i), DG = g.spl_dg, BN = g.spl_bn, PP = g.spl_pp;
     const int rows = g.spl_groups(l) * BN;
     const float* W = theta + g.layer_off[l] + g.lin_w(l, i);
     uint16_t* dst = w16 + g.w16g_off[l];
@@ -258,10 +260,10 @@ __global__ void k_pack_bf16(FlowGeom g, const float* __restrict__ theta, uint16_
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
       const int r = (int)(e / cols), c = (int)(e - (int64_t)r * cols);
       const int grp = r / BN, rr = r - grp * BN;
-      const int u = rr / g.P, p = rr - u * g.P;
+      const int u = rr / PP, p = rr - u * PP;
       const int t = grp * DG + u;
       float v = 0.f;
-      if (u < DG && t < nt && c < in) v = W[((int64_t)t * g.P + p) * in + c];
+      if (u < DG && p < g.P && t < nt && c < in) v = W[((int64_t)t * g.P + p) * in + c];
       dst[e] = f32_to_bf16_rn(v);
     }
     return;
@@ -354,7 +356,7 @@ int conditioner_bf16_hidden(const FmcFlow* f, const FlowGeom& g, int l, int64_t 
     ep.bias = th + g.lin_b(l, i);
     const int ldo = (int)FlowGeom::rup(N, 64);
     int rc = tc_gemm(st, a, m, rows, K, f->theta_bf16 + g.w16_off[seg], N, g.w16_rows(l, i), ep, hbuf[i & 1], ldo, ldo,
-                     tc::TC_EPI_TANH_BF16, f->gemm_bn, f->tile_rows != 128);
+                     tc::TC_EPI_TANH_BF16, f->gemm_bn, f->tile_rows == 256);
     if (rc) return rc;
     a = hbuf[i & 1];
   }

@@ -346,8 +346,12 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t rank = PAIR ? cluster_ctarank() : 0u;
   const int t_first = PAIR ? (int)(blockIdx.x / 2) : (int)blockIdx.x;   // work items of this CTA (pair)
   const int t_step = PAIR ? (int)(gridDim.x / 2) : (int)gridDim.x;
-  // waits: barriers that the other CTA of a pair also completes acquire at cluster scope
-  auto wait = [](uint64_t* bar, uint32_t ph) { return PAIR ? mbar_wait_cl(bar, ph) : mbar_wait(bar, ph); };
+  // waits: the ring and accumulator-full barriers are completed by copies
+  // and MMA commits (asynchronous proxy), which a CTA-scope acquire covers;
+  // the accumulator-empty barrier of a pair counts the odd CTA's threads too
+  // and is waited on at cluster scope (wait_cl)
+  auto wait = [](uint64_t* bar, uint32_t ph) { return mbar_wait(bar, ph); };
+  auto wait_cl = [](uint64_t* bar, uint32_t ph) { return PAIR ? mbar_wait_cl(bar, ph) : mbar_wait(bar, ph); };
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -428,7 +432,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       int local = 0;
       for (int t = t_first; t < tiles && !*abort_flag; t += t_step, ++local) {
         const int b = local & 1, use = local >> 1;
-        if (use > 0 && !wait(&acc_empty[b], (uint32_t)(use - 1) & 1u)) {
+        if (use > 0 && !wait_cl(&acc_empty[b], (uint32_t)(use - 1) & 1u)) {
           *abort_flag = 1;
           break;
         }
@@ -677,7 +681,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 1) {
-    if (lane == 0) wait(mma_done, 0);
+    if (lane == 0) wait_cl(mma_done, 0);
     __syncwarp();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if constexpr (PAIR)

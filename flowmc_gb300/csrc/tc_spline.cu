@@ -43,17 +43,38 @@ constexpr int kSplThreads = 64 + kSplEpiThreads;
 template <int K>
 struct SplineTile {
   static constexpr int P = 3 * K + 1;
-  static constexpr int DG = 256 / P;
-  static constexpr int DGP = DG * P;
-  static constexpr int BN = ((DGP + 15) / 16) * 16;
+  static constexpr int PPC = (P + 7) / 8 * 8;      // accumulator columns per coordinate
+  static constexpr int DG = 256 / PPC;
+  static constexpr int DGP = DG * P;               // staged (unpadded) columns of the adjoint
+  static constexpr int BN = ((DG * PPC + 15) / 16) * 16;
   // bf16 row pitch of the adjoint staging tile: an even count whose half is
   // odd, so the 32 rows a warp touches in one column fall in 32 banks
   static constexpr int SP = ((DGP + 1) / 2 % 2 == 1) ? ((DGP + 1) / 2) * 2 : ((DGP + 1) / 2 + 1) * 2;
   static constexpr int STG_BYTES = BM * SP * 2;
 };
 
-// N consecutive accumulator columns of this thread's lane; every register is
-// pinned after the wait so no use can be scheduled before the data arrive
+// The first N of the PPC accumulator columns at taddr (a multiple of 8
+// columns), read with 8-column loads (tcgen05.ld .32x32b.x8, each at an
+// 8-aligned column); every register is pinned after the wait so no use can be
+// scheduled before the data arrive.
+template <int N, int PPC>
+__device__ __forceinline__ void tmem_ld_coord(uint32_t taddr, float (&v)[N]) {
+  static_assert(PPC % 8 == 0 && N <= PPC, "column pitch");
+  uint32_t r[PPC];
+#pragma unroll
+  for (int i = 0; i < PPC; i += 8)
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(r[i]), "=r"(r[i + 1]), "=r"(r[i + 2]), "=r"(r[i + 3]), "=r"(r[i + 4]), "=r"(r[i + 5]),
+                   "=r"(r[i + 6]), "=r"(r[i + 7])
+                 : "r"(taddr + (uint32_t)i));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < PPC; ++i) asm volatile("" : "+r"(r[i]));
+#pragma unroll
+  for (int i = 0; i < N; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// N consecutive accumulator columns of this thread's lane, one column per load
 template <int N>
 __device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, float (&v)[N]) {
   uint32_t r[N];
@@ -275,7 +296,7 @@ __global__ void __launch_bounds__(kSplThreads, 1)
         const int tcoord = g * DG + u;
         if (tcoord >= nt) break;
         float raw[P];
-        tmem_ld_cols<P>(tb + (uint32_t)(u * P), raw);   // warp-collective: every lane loads
+        tmem_ld_coord<P, T::PPC>(tb + (uint32_t)(u * T::PPC), raw);   // warp-collective: every lane loads
         if (gm < M) {
           float* xp = xa + (int64_t)gm * d + 2 * tcoord + tpar;
           const float xv = *xp;
@@ -371,7 +392,7 @@ __global__ void __launch_bounds__(kSplThreads, 1)
       for (int u = h; u < nu; u += E) {
         const int tcoord = g * DG + u;
         float raw[P];
-        tmem_ld_cols<P>(tb + (uint32_t)(u * P), raw);
+        tmem_ld_coord<P, T::PPC>(tb + (uint32_t)(u * T::PPC), raw);
         uint16_t* srow = stg + row * SP + u * P;
         if (row_ok) {
           const float* bb = a.bias + (int64_t)tcoord * P;
@@ -500,7 +521,7 @@ __device__ __forceinline__ void producer_pair(const Pipe& p, const CUtensorMap* 
     for (int k = 0; k < nk; ++k, ++it) {
       const int s = it % STAGES;
       const uint32_t ph = (it / STAGES) & 1u;
-      if (it >= (uint32_t)STAGES && !mbar_wait_cl(&p.empty[s], ph ^ 1u)) {
+      if (it >= (uint32_t)STAGES && !mbar_wait(&p.empty[s], ph ^ 1u)) {
         *p.abort_flag = 1;
         break;
       }
@@ -518,7 +539,7 @@ __device__ __forceinline__ void producer_pair(const Pipe& p, const CUtensorMap* 
     // completion is counted on the even CTA's barriers, so wait on the
     // stages' release by the MMA side instead (bounded)
     for (uint32_t j = it > (uint32_t)STAGES ? it - STAGES : 0; j < it; ++j)
-      mbar_wait_cl(&p.empty[j % STAGES], (j / STAGES) & 1u);
+      mbar_wait(&p.empty[j % STAGES], (j / STAGES) & 1u);
   }
 }
 
@@ -542,7 +563,7 @@ __device__ __forceinline__ void mma_issuer_pair(const Pipe& p, int tiles, int nk
     for (int k = 0; k < nk; ++k, ++it) {
       const int s = it % STAGES;
       const uint32_t ph = (it / STAGES) & 1u;
-      if (!mbar_wait_cl(&p.full[s], ph) || *p.abort_flag) {
+      if (!mbar_wait(&p.full[s], ph) || *p.abort_flag) {
         *p.abort_flag = 1;
         stop = true;
         break;
@@ -620,7 +641,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kSplThreads, 1)
       const int b = local & 1, use = local >> 1;
       const int m0 = (t / n_groups) * (2 * BM) + (int)rank * BM, g = t % n_groups;
       const int gm = m0 + row;
-      if (*p.abort_flag || !mbar_wait_cl(&p.acc_full[b], (uint32_t)use & 1u)) {
+      if (*p.abort_flag || !mbar_wait(&p.acc_full[b], (uint32_t)use & 1u)) {
         *p.abort_flag = 1;
         break;
       }
@@ -632,7 +653,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kSplThreads, 1)
         const int tcoord = g * DG + u;
         if (tcoord >= nt) break;
         float raw[P];
-        tmem_ld_cols<P>(tb + (uint32_t)(u * P), raw);   // warp-collective: every lane loads
+        tmem_ld_coord<P, T::PPC>(tb + (uint32_t)(u * T::PPC), raw);   // warp-collective: every lane loads
         if (gm < M) {
           float* xp = xa + (int64_t)gm * d + 2 * tcoord + tpar;
           const float xv = *xp;
@@ -682,10 +703,10 @@ int tc_error_word(int** out);
 int make_tma_map_bf16(CUtensorMap* m, const void* base, int64_t inner, int64_t outer, int64_t ld, int box_outer);
 
 int spline_groups(int K_bins, int nt, int* dg, int* bn) {
-  const int P = 3 * K_bins + 1;
-  const int DG = 256 / P;
+  const int P = 3 * K_bins + 1, PP = (P + 7) / 8 * 8;
+  const int DG = 256 / PP;
   *dg = DG;
-  *bn = ((DG * P + 15) / 16) * 16;
+  *bn = ((DG * PP + 15) / 16) * 16;
   return (nt + DG - 1) / DG;
 }
 
@@ -709,6 +730,7 @@ static int launch_spl(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap&
   if (rc) return rc;
   const int64_t tiles = (M + tc::BM - 1) / tc::BM * n_groups;
   const int64_t grid = tiles < sm_count() ? tiles : sm_count();
+  note_grid(INV ? FMC_KT_TC_SPLINE_INV : FMC_KT_TC_SPLINE_FWD, (int)grid, 1);
   kern<<<(unsigned)grid, tc::kSplThreads, total, st>>>(ma, mb, (int)M, n_groups, nt, K, bias, bias_smem, xa, d,
                                                        tpar, ldp, cfg, err);
   FMC_LAUNCH_CHECK();
@@ -750,10 +772,23 @@ static int launch_spl2(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap
   if (rc) return rc;
   const int64_t tiles = (M + 2 * tc::BM - 1) / (2 * tc::BM) * n_groups;
   const int64_t pairs = tiles < max_pairs ? tiles : max_pairs;
+  note_grid(INV ? FMC_KT_TC_SPLINE_INV : FMC_KT_TC_SPLINE_FWD, (int)(2 * pairs), 2);
   kern<<<(unsigned)(2 * pairs), tc::kSplThreads, total, st>>>(ma, mb, (int)M, n_groups, nt, K, bias, bias_smem, xa, d,
                                                              tpar, ldp, cfg, err);
   FMC_LAUNCH_CHECK();
   return FMC_OK;
+}
+
+// one-CTA tiles, or CTA pairs where the group's weight rows split into two
+// multiples of 16 (the pair kernel exists only for those widths)
+template <int KB, bool INV>
+static int launch_spl_tiles(bool pair, cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& mb, int64_t M,
+                            int n_groups, int nt, int K, const float* bias, float* xa, int d, int tpar, float* ldp,
+                            SplineCfg cfg) {
+  if constexpr (tc::SplineTile<KB>::BN % 32 == 0) {
+    if (pair) return launch_spl2<KB, INV>(st, ma, mb, M, n_groups, nt, K, bias, xa, d, tpar, ldp, cfg);
+  }
+  return launch_spl<KB, INV>(st, ma, mb, M, n_groups, nt, K, bias, xa, d, tpar, ldp, cfg);
 }
 
 template <int KB>
@@ -775,6 +810,7 @@ static int launch_spl_bwd(cudaStream_t st, const CUtensorMap& ma, const CUtensor
   if (rc) return rc;
   const int64_t tiles = (M + tc::BM - 1) / tc::BM * n_groups;
   const int64_t grid = tiles < sm_count() ? tiles : sm_count();
+  note_grid(FMC_KT_TC_SPLINE_BWD, (int)grid, 1);
   kern<<<(unsigned)grid, tc::kSplThreads, TOTAL, st>>>(ma, mb, (int)M, n_groups, K, a, cfg, err);
   FMC_LAUNCH_CHECK();
   return FMC_OK;
@@ -793,9 +829,10 @@ int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l
   const int Kd = g.w16_cols(l, g.nh);
   const uint16_t* Bg = f->theta_bf16 + g.w16g_off[l];
   const float* bias = f->theta + g.layer_off[l] + g.lin_b(l, g.nh);
-  // CTA pairs (256-row tiles, half the weight rows per CTA) unless one-CTA
-  // tiles are asked for, or the group width does not split in two multiples of 16
-  const bool pair = f->tile_rows != 128 && bn % 32 == 0;
+  // CTA pairs (256-row tiles, half the weight rows per CTA) when asked for
+  // and the group width splits in two multiples of 16; one-CTA tiles by
+  // default (measured faster on GB300 at the sampler's shapes)
+  const bool pair = f->tile_rows == 256 && bn % 32 == 0;
   CUtensorMap ma, mb;
   int rc = make_tma_map_bf16(&ma, A, Kd, rows_a, Kd, tc::BM);
   if (rc) return rc;
@@ -808,14 +845,13 @@ int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l
     const double bytes = (double)M * hl * 2 + (double)nt * g.P * hl * 2 + (double)M * nt * 8 +
                          (double)M * kSplineEpiPerQuarter * n_groups * 4;
     KernelTimer kt(inverse ? FMC_KT_TC_SPLINE_INV : FMC_KT_TC_SPLINE_FWD, st, flops, bytes);
-#define SPL_CASE(k)                                                                                              \
-  if (g.K == k) {                                                                                                \
-    if (pair)                                                                                                    \
-      rc = inverse ? launch_spl2<k, true>(st, ma, mb, M, n_groups, nt, Kd, bias, xa, g.d, g.tpar(l), ldp, g.cfg) \
-                   : launch_spl2<k, false>(st, ma, mb, M, n_groups, nt, Kd, bias, xa, g.d, g.tpar(l), ldp, g.cfg); \
-    else                                                                                                         \
-      rc = inverse ? launch_spl<k, true>(st, ma, mb, M, n_groups, nt, Kd, bias, xa, g.d, g.tpar(l), ldp, g.cfg)  \
-                   : launch_spl<k, false>(st, ma, mb, M, n_groups, nt, Kd, bias, xa, g.d, g.tpar(l), ldp, g.cfg); \
+#define SPL_CASE(k)                                                                                          \
+  if (g.K == k) {                                                                                            \
+    rc = inverse                                                                                             \
+             ? launch_spl_tiles<k, true>(pair, st, ma, mb, M, n_groups, nt, Kd, bias, xa, g.d, g.tpar(l), ldp,  \
+                                         g.cfg)                                                              \
+             : launch_spl_tiles<k, false>(pair, st, ma, mb, M, n_groups, nt, Kd, bias, xa, g.d, g.tpar(l), ldp, \
+                                          g.cfg);                                                            \
   } else
     FMC_SPLINE_BINS(SPL_CASE) {
       set_error("n_bins=%d is not instantiated for the fused spline", g.K);

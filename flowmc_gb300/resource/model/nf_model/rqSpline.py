@@ -56,7 +56,7 @@ class MaskedCouplingRQSpline(NFModel):
             torch.device("cuda") if torch.cuda.is_available() else torch.device("cpu"))
         self.precision = precision
         self.gemm_bn = 0   # BF16 hidden-layer GEMM tile width; 0 = library choice (autotune.tune_flow_gemm)
-        self.tile_rows = 0   # BF16 tensor-core tile rows (128 one CTA, 256 a CTA pair); 0 = library choice
+        self.tile_rows = 0   # BF16 tensor-core tile rows (128 one CTA, 256 a CTA pair); 0 = library choice (128)
         d = self._n_features
         P = 3 * self.num_bins + 1
         self._P = P

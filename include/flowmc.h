@@ -286,10 +286,12 @@ typedef struct FmcFlow {
                                         or 128 / 256 (an autotuner's pick) */
   int32_t tile_rows;                 /* rows per tensor-core tile of the BF16
                                         flow kernels (fused last Linear +
-                                        spline, hidden-layer GEMMs): 0 =
-                                        library choice (256), 128 = one CTA
-                                        per tile, 256 = a CTA pair
-                                        (tcgen05 cta_group::2) per tile */
+                                        spline, hidden-layer GEMMs): 0 or
+                                        128 = one CTA per tile (the library
+                                        choice), 256 = a CTA pair (tcgen05
+                                        cta_group::2) per tile where the
+                                        tile width allows (an autotuner's
+                                        pick) */
   float* theta;                      /* [n_params] float32 master weights   */
   uint16_t* theta_bf16;              /* [n_params] bf16 shadow (BF16 mode)   */
   float* aux;                        /* [2*n_dim + 2], see above             */
@@ -500,6 +502,10 @@ enum {
 FMC_API int fmc_kernel_timing_enable(int32_t on);
 FMC_API int fmc_kernel_timing_reset(void);
 FMC_API int fmc_kernel_timing_read(int32_t kid, int64_t* launches, double* ms, double* flops, double* bytes);
+/* Launch geometry of the last launch of kernel `kid` (whether or not timing
+ * is on): CTAs in the grid and CTAs per cluster (2 for CTA pairs); 0, 0
+ * before its first launch. */
+FMC_API int fmc_kernel_grid(int32_t kid, int32_t* ctas, int32_t* cluster);
 
 #ifdef __cplusplus
 }
