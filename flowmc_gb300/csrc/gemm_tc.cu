@@ -57,6 +57,30 @@ int make_tma_map_bf16(CUtensorMap* m, const void* base, int64_t inner, int64_t o
   return FMC_OK;
 }
 
+// 2-D fp32 tensor [outer, inner] (row stride = inner elements), box
+// {box_inner, box_outer}, no swizzle, out-of-range elements read as zero
+int make_tma_map_f32(CUtensorMap* m, const void* base, int64_t inner, int64_t outer, int box_inner, int box_outer) {
+  auto fn = encode_fn();
+  FMC_CHECK_SUPPORTED(fn != nullptr, "cuTensorMapEncodeTiled is unavailable");
+  FMC_CHECK_ARG(((uintptr_t)base & 15) == 0, "TMA base address must be 16-byte aligned");
+  FMC_CHECK_ARG((inner * 4) % 16 == 0, "TMA row stride must be a multiple of 16 bytes");
+  FMC_CHECK_ARG((box_inner * 4) % 16 == 0 && box_inner <= 256 && box_outer <= 256, "bad TMA box");
+  FMC_CHECK_ARG(inner >= box_inner && outer >= 1, "tensor narrower than one TMA box");
+  cuuint64_t dims[2] = {(cuuint64_t)inner, (cuuint64_t)outer};
+  cuuint64_t strides[1] = {(cuuint64_t)(inner * 4)};
+  cuuint32_t box[2] = {(cuuint32_t)box_inner, (cuuint32_t)box_outer};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled (fp32) failed (%d): inner=%lld outer=%lld box=%dx%d", (int)r,
+              (long long)inner, (long long)outer, box_inner, box_outer);
+    return FMC_ERR_CUDA;
+  }
+  return FMC_OK;
+}
+
 // C[m, n] = sum over the split-K slices of part[s * stride + m * ldc + n] (fixed order)
 __global__ void k_splitk_reduce(const float* __restrict__ part, int splits, int64_t stride, int64_t M, int n_store,
                                 int64_t ldc, float* __restrict__ C) {

@@ -248,23 +248,41 @@ struct BiasRows {
   static constexpr int PP = (3 * K + 1 + 3) / 4 * 4;
 };
 
+// x tiles staged through shared memory (x_tma): the group's column span of
+// a 128-row tile -- 2 DG floats per row, the transformed coordinates and the
+// conditioning ones between them -- is one TMA box of the fp32 tensor map
+// tmX over x [M, d]. The first epilogue warp's lane 0 loads the next tile's
+// box while the current tile is computed (two buffers) and, after the
+// epilogue warps have written y into the buffer, stores the box back. Every
+// tile owns its rows' column span alone, so the write-back (which also
+// rewrites the untouched conditioning columns with their own values) races
+// with nothing. Without x_tma (row stride not a multiple of 16 bytes) each
+// thread reads and writes its coordinates of x directly.
 template <int KB, bool INV, int STAGES>
 __global__ void __launch_bounds__(kSplThreads, 1)
-    k_tc_spline(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int n_groups,
-                int nt, int K, const float* __restrict__ bias, int bias_smem, float* __restrict__ xa, int d,
-                int tpar, float* __restrict__ ldp, SplineCfg cfg, int* err) {
+    k_tc_spline(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                const __grid_constant__ CUtensorMap tmX, int x_tma, int M, int n_groups, int nt, int K,
+                const float* __restrict__ bias, int bias_smem, float* __restrict__ xa, int d, int tpar,
+                float* __restrict__ ldp, SplineCfg cfg, int* err) {
   using T = SplineTile<KB>;
   constexpr int P = T::P, DG = T::DG, BN = T::BN, E = kSplineEpiPerQuarter, PP = BiasRows<KB>::PP;
+  constexpr int XS = 2 * DG;   // floats per row of an x box
   using S = Smem<BN, STAGES>;
   if (tc_skip(err)) return;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   float* sbias = (float*)(base + STAGES * S::STAGE_BYTES + 256);   // after the ring and its barriers
+  uint64_t* xfull = (uint64_t*)(base + STAGES * S::STAGE_BYTES + 192);   // [2], in the barrier block
+  float* xbuf = (float*)((((uintptr_t)(sbias + (bias_smem ? nt * PP : 0))) + 127) & ~(uintptr_t)127);
   if (bias_smem) {
     for (int i = threadIdx.x; i < nt * PP; i += blockDim.x) {
       const int t = i / PP, pp = i - t * PP;
       sbias[i] = pp < P ? __ldg(bias + t * P + pp) : 0.f;
     }   // visible after pipe_setup's __syncthreads
+  }
+  if (threadIdx.x == 0) {
+    mbar_init(&xfull[0], 1);
+    mbar_init(&xfull[1], 1);   // pipe_setup's fence and barrier publish these
   }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nk = (K + BK - 1) / BK;
@@ -279,12 +297,38 @@ __global__ void __launch_bounds__(kSplThreads, 1)
     const int q = warp & 3;          // TMEM lane quarter
     const int h = (warp - 2) >> 2;   // coordinates h, h + E, ... of the group
     const int row = q * 32 + lane;
+    const bool xt = x_tma != 0;
+    const bool elect = warp == 2 && lane == 0;   // issues the x boxes' copies
+    constexpr uint32_t kXBytes = BM * XS * 4;
+    int issued = 0;   // x boxes loaded so far (by the elected lane)
+    if (xt && elect && (int)blockIdx.x < tiles) {
+      const int t0 = blockIdx.x;
+      mbar_expect_tx(&xfull[0], kXBytes);
+      tma_load_2d(xbuf, &tmX, &xfull[0], 2 * (t0 % n_groups) * DG, (t0 / n_groups) * BM);
+      issued = 1;
+    }
     int local = 0;
     for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++local) {
       const int b = local & 1, use = local >> 1;
       const int m0 = (t / n_groups) * BM, g = t % n_groups;
       const int gm = m0 + row;
-      if (*p.abort_flag || !mbar_wait(&p.acc_full[b], (uint32_t)use & 1u)) {
+      float* xb = xbuf + b * (BM * XS);
+      if (xt && elect) {
+        // the next tile's box goes into the other buffer once the previous
+        // tile's store has finished reading it
+        bulk_wait_read_0();
+        const int tn = t + (int)gridDim.x;
+        if (tn < tiles) {
+          mbar_expect_tx(&xfull[b ^ 1], kXBytes);
+          tma_load_2d(xbuf + (b ^ 1) * (BM * XS), &tmX, &xfull[b ^ 1], 2 * (tn % n_groups) * DG,
+                      (tn / n_groups) * BM);
+          ++issued;
+        }
+      }
+      // every epilogue warp leaves the loop at the same tile (named barriers follow)
+      bool bad = *p.abort_flag || !mbar_wait(&p.acc_full[b], (uint32_t)use & 1u);
+      if (xt && !bad) bad = !mbar_wait(&xfull[b], (uint32_t)use & 1u);
+      if (epi_any(bad)) {
         *p.abort_flag = 1;
         break;
       }
@@ -298,7 +342,7 @@ __global__ void __launch_bounds__(kSplThreads, 1)
         float raw[P];
         tmem_ld_coord<P, T::PPC>(tb + (uint32_t)(u * T::PPC), raw);   // warp-collective: every lane loads
         if (gm < M) {
-          float* xp = xa + (int64_t)gm * d + 2 * tcoord + tpar;
+          float* xp = xt ? xb + row * XS + 2 * u + tpar : xa + (int64_t)gm * d + 2 * tcoord + tpar;
           const float xv = *xp;
           if (bias_smem) {
             const float4* bb = reinterpret_cast<const float4*>(sbias + tcoord * PP);
@@ -323,6 +367,21 @@ __global__ void __launch_bounds__(kSplThreads, 1)
       }
       if (gm < M) ldp[(int64_t)gm * (E * n_groups) + E * g + h] = ldsum;
       release_acc(p, b, lane);
+      if (xt) {
+        // y is in the buffer: make the writes visible to the copy engine, then
+        // one lane stores the box (rows past M are clipped by the store)
+        fence_proxy_async_smem();
+        epi_sync(1);
+        if (elect) {
+          tma_store_2d_f32(&tmX, smem_u32(xb), 2 * g * DG, m0);
+          bulk_commit();
+        }
+      }
+    }
+    if (xt && elect) {
+      bulk_wait_all();   // the stores have completed before the CTA exits
+      // boxes loaded for tiles the loop did not finish (after an abort) land first (bounded)
+      for (int k = local; k < issued; ++k) mbar_wait(&xfull[k & 1], (uint32_t)(k >> 1) & 1u);
     }
   }
   pipe_teardown(p, warp, lane, err);
@@ -701,6 +760,7 @@ __global__ void k_ld_reduce(const float* __restrict__ ldp, int n_part, int64_t m
 
 int tc_error_word(int** out);
 int make_tma_map_bf16(CUtensorMap* m, const void* base, int64_t inner, int64_t outer, int64_t ld, int box_outer);
+int make_tma_map_f32(CUtensorMap* m, const void* base, int64_t inner, int64_t outer, int box_inner, int box_outer);
 
 int spline_groups(int K_bins, int nt, int* dg, int* bn) {
   const int P = 3 * K_bins + 1, PP = (P + 7) / 8 * 8;
@@ -714,12 +774,21 @@ template <int KB, bool INV>
 static int launch_spl(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& mb, int64_t M, int n_groups, int nt,
                       int K, const float* bias, float* xa, int d, int tpar, float* ldp, SplineCfg cfg) {
   constexpr int STAGES = 4;
-  using S = tc::Smem<tc::SplineTile<KB>::BN, STAGES>;
+  using T = tc::SplineTile<KB>;
+  using S = tc::Smem<T::BN, STAGES>;
   auto kern = tc::k_tc_spline<KB, INV, STAGES>;
-  // the ring, its barriers and (when they fit) the layer's bias rows
-  const size_t with_bias = S::TOTAL + (size_t)nt * tc::BiasRows<KB>::PP * sizeof(float);
-  const int bias_smem = with_bias <= 227 * 1024 ? 1 : 0;
-  const size_t total = bias_smem ? with_bias : (size_t)S::TOTAL;
+  // the ring, its barriers, (when they fit) the layer's bias rows and the two
+  // x boxes (when x's row stride allows a tensor map)
+  const size_t bias_bytes = (size_t)nt * tc::BiasRows<KB>::PP * sizeof(float);
+  const size_t x_bytes = 128 + 2 * (size_t)tc::BM * 2 * T::DG * sizeof(float);
+  CUtensorMap mx;
+  memset(&mx, 0, sizeof(mx));
+  int x_tma = make_tma_map_f32(&mx, xa, d, M, 2 * T::DG, tc::BM) == FMC_OK ? 1 : 0;
+  if (!x_tma) (void)cudaGetLastError();
+  if (x_tma && S::TOTAL + x_bytes > 227 * 1024) x_tma = 0;
+  const size_t base_bytes = (size_t)S::TOTAL + (x_tma ? x_bytes : 0);
+  const int bias_smem = base_bytes + bias_bytes <= 227 * 1024 ? 1 : 0;
+  const size_t total = base_bytes + (bias_smem ? bias_bytes : 0);
   static int attr = 0;
   if (attr < (int)total) {
     FMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)total));
@@ -731,8 +800,8 @@ static int launch_spl(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap&
   const int64_t tiles = (M + tc::BM - 1) / tc::BM * n_groups;
   const int64_t grid = tiles < sm_count() ? tiles : sm_count();
   note_grid(INV ? FMC_KT_TC_SPLINE_INV : FMC_KT_TC_SPLINE_FWD, (int)grid, 1);
-  kern<<<(unsigned)grid, tc::kSplThreads, total, st>>>(ma, mb, (int)M, n_groups, nt, K, bias, bias_smem, xa, d,
-                                                       tpar, ldp, cfg, err);
+  kern<<<(unsigned)grid, tc::kSplThreads, total, st>>>(ma, mb, mx, x_tma, (int)M, n_groups, nt, K, bias, bias_smem,
+                                                       xa, d, tpar, ldp, cfg, err);
   FMC_LAUNCH_CHECK();
   return FMC_OK;
 }
