@@ -59,8 +59,21 @@ struct SplineTile {
 // scheduled before the data arrive.
 template <int N, int PPC>
 __device__ __forceinline__ void tmem_ld_coord(uint32_t taddr, float (&v)[N]) {
-  static_assert(PPC % 8 == 0 && N <= PPC, "column pitch");
+  static_assert(N <= PPC, "column pitch");
   uint32_t r[PPC];
+  if constexpr (PPC % 8 != 0) {
+    // any other pitch: one column per load
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];" : "=r"(r[i]) : "r"(taddr + (uint32_t)i));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      asm volatile("" : "+r"(r[i]));
+      v[i] = __uint_as_float(r[i]);
+    }
+    return;
+  }
 #pragma unroll
   for (int i = 0; i < PPC; i += 8)
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
