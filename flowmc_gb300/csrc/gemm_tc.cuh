@@ -44,7 +44,8 @@ int conditioner_bf16_hidden(const FmcFlow* f, const FlowGeom& g, int l, int64_t 
 constexpr int kSplineEpiPerQuarter = 3;
 
 // the last Linear of layer l fused with the spline (tc_spline.cu); ldp holds
-// kSplineEpiPerQuarter * n_groups floats per row, which are then added to ld
+// kSplineEpiPerQuarter * n_groups partials per row (partial-major, [parts, M]),
+// which are then added to ld
 int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l, const uint16_t* A, int64_t M,
                      int64_t rows_a, bool inverse, float* xa, float* ld, float* ldp);
 

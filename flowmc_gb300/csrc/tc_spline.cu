@@ -13,7 +13,7 @@
 //   k_tc_spline      epilogue: bias, knots of the selected bin only, the
 //                    spline (rqSpline.py:42-239) on x = xa[row, 2t + tpar]
 //                    written back into xa; per-row log-determinant partials
-//                    into ldp[row, E*g + h]
+//                    into ldp[(E*g + h) * M + row]
 //   k_tc_spline_bwd  epilogue: bias, knots, the spline adjoint of the
 //                    selected bin (rqs_fwd_adjoint_fast) given dL/dy = gy[row, 2t + tpar] and
 //                    dL/dlogdet = gld; dL/dx into gxa, dL/draw as bf16 staged
@@ -378,7 +378,7 @@ __global__ void __launch_bounds__(kSplThreads, 1)
           ldsum += l;
         }
       }
-      if (gm < M) ldp[(int64_t)gm * (E * n_groups) + E * g + h] = ldsum;
+      if (gm < M) ldp[(int64_t)(E * g + h) * M + gm] = ldsum;   // partial-major: a warp writes 128 contiguous bytes
       release_acc(p, b, lane);
       if (xt) {
         // y is in the buffer: make the writes visible to the copy engine, then
@@ -415,18 +415,32 @@ struct SplineBwdArgs {
   int d, nt, tpar, cpar;
 };
 
+// With x_tma the group's column span of x and of dL/dy for a 128-row tile
+// arrive as two TMA boxes (loaded one tile ahead, two buffers each), the
+// adjoint is written into the dL/dy box in place -- its conditioning columns
+// keep dL/dy, which is their dL/dx -- and the box is stored to gxa. Each tile
+// owns its rows' column span, as in the forward kernel.
 template <int KB, int STAGES>
 __global__ void __launch_bounds__(kSplThreads, 1)
-    k_tc_spline_bwd(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M,
-                    int n_groups, int K, const SplineBwdArgs a, SplineCfg cfg, int* err) {
+    k_tc_spline_bwd(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                    const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmGy,
+                    const __grid_constant__ CUtensorMap tmGx, int x_tma, int M, int n_groups, int K,
+                    const SplineBwdArgs a, SplineCfg cfg, int* err) {
   using T = SplineTile<KB>;
   constexpr int P = T::P, DG = T::DG, DGP = T::DGP, BN = T::BN, SP = T::SP, E = kSplineEpiPerQuarter;
+  constexpr int XS = 2 * DG;   // floats per row of a box
   using S = Smem<BN, STAGES>;
   if (tc_skip(err)) return;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  // staging tile after the ring and its barriers
+  // staging tile after the ring and its barriers, then the boxes
   uint16_t* stg = (uint16_t*)(base + STAGES * S::STAGE_BYTES + 256);
+  uint64_t* xfull = (uint64_t*)(base + STAGES * S::STAGE_BYTES + 192);   // [2], in the barrier block
+  float* boxes = (float*)((((uintptr_t)(stg + BM * SP)) + 127) & ~(uintptr_t)127);   // [2][x | dL/dy]
+  if (threadIdx.x == 0) {
+    mbar_init(&xfull[0], 1);
+    mbar_init(&xfull[1], 1);   // pipe_setup's fence and barrier publish these
+  }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nk = (K + BK - 1) / BK;
   const int tiles = (M + BM - 1) / BM * n_groups;
@@ -443,6 +457,20 @@ __global__ void __launch_bounds__(kSplThreads, 1)
     const int row = q * 32 + lane;
     const int et = threadIdx.x - 64;   // 0 .. kSplEpiThreads-1
     const int ew = et >> 5;
+    const bool xt = x_tma != 0;
+    const bool elect = warp == 2 && lane == 0;   // issues the boxes' copies
+    constexpr uint32_t kBox = BM * XS;           // floats per box
+    auto load_boxes = [&](int tt, int buf) {
+      float* xb = boxes + (2 * buf) * kBox;
+      mbar_expect_tx(&xfull[buf], 2 * kBox * 4);
+      tma_load_2d(xb, &tmX, &xfull[buf], 2 * (tt % n_groups) * DG, (tt / n_groups) * BM);
+      tma_load_2d(xb + kBox, &tmGy, &xfull[buf], 2 * (tt % n_groups) * DG, (tt / n_groups) * BM);
+    };
+    int issued = 0;
+    if (xt && elect && (int)blockIdx.x < tiles) {
+      load_boxes(blockIdx.x, 0);
+      issued = 1;
+    }
     int local = 0;
     for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++local) {
       const int b = local & 1, use = local >> 1;
@@ -450,8 +478,21 @@ __global__ void __launch_bounds__(kSplThreads, 1)
       const int m0 = mt * BM;
       const int gm = m0 + row;
       const bool row_ok = gm < M;
+      float* xb = boxes + (2 * b) * kBox;
+      float* gb = xb + kBox;
+      if (xt && elect) {
+        // the next tile's boxes go into the other buffers once the previous
+        // tile's store has finished reading them
+        bulk_wait_read_0();
+        const int tn = t + (int)gridDim.x;
+        if (tn < tiles) {
+          load_boxes(tn, b ^ 1);
+          ++issued;
+        }
+      }
       // the tile loop has named barriers: all epilogue warps leave it together
-      const bool bad = *p.abort_flag || !mbar_wait(&p.acc_full[b], (uint32_t)use & 1u);
+      bool bad = *p.abort_flag || !mbar_wait(&p.acc_full[b], (uint32_t)use & 1u);
+      if (xt && !bad) bad = !mbar_wait(&xfull[b], (uint32_t)use & 1u);
       if (epi_any(bad)) {
         *p.abort_flag = 1;
         break;
@@ -470,22 +511,32 @@ __global__ void __launch_bounds__(kSplThreads, 1)
           const float* bb = a.bias + (int64_t)tcoord * P;
 #pragma unroll
           for (int i = 0; i < P; ++i) raw[i] += __ldg(bb + i);
-          const int64_t j = (int64_t)gm * a.d + 2 * tcoord + a.tpar;
-          a.gxa[j] = rqs_fwd_adjoint_fast<KB>(raw, a.xa[j], a.gy[j], a.gld, cfg, srow);
+          if (xt) {
+            const int jb = row * XS + 2 * u + a.tpar;
+            gb[jb] = rqs_fwd_adjoint_fast<KB>(raw, xb[jb], gb[jb], a.gld, cfg, srow);
+          } else {
+            const int64_t j = (int64_t)gm * a.d + 2 * tcoord + a.tpar;
+            a.gxa[j] = rqs_fwd_adjoint_fast<KB>(raw, a.xa[j], a.gy[j], a.gld, cfg, srow);
+          }
         } else {
 #pragma unroll
           for (int i = 0; i < P; ++i) srow[i] = 0;
         }
       }
       release_acc(p, b, lane);
-      if (g == 0 && row_ok) {
+      if (!xt && g == 0 && row_ok) {
         const int ncond = a.d - a.nt;
         for (int k = h; k < ncond; k += E) {
           const int64_t j = (int64_t)gm * a.d + 2 * k + a.cpar;
           a.gxa[j] = a.gy[j];
         }
       }
+      if (xt) fence_proxy_async_smem();   // the box's generic writes, before the store reads it
       epi_sync(1);
+      if (xt && elect) {
+        tma_store_2d_f32(&tmGx, smem_u32(gb), 2 * g * DG, m0);
+        bulk_commit();
+      }
       // row-major copy: the group's columns are contiguous in [t*P + p] order;
       // the last group also zeroes the padding columns up to ldg
       {
@@ -513,6 +564,11 @@ __global__ void __launch_bounds__(kSplThreads, 1)
         if (lane == 0) a.bpart[(int64_t)mt * ntP + col] = s;
       }
       epi_sync(2);   // the staging tile is free again
+    }
+    if (xt && elect) {
+      bulk_wait_all();   // the stores have completed before the CTA exits
+      // boxes loaded for tiles the loop did not finish (after an abort) land first (bounded)
+      for (int k = local; k < issued; ++k) mbar_wait(&xfull[k & 1], (uint32_t)(k >> 1) & 1u);
     }
   }
   pipe_teardown(p, warp, lane, err);
@@ -750,7 +806,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kSplThreads, 1)
           ldsum += l;
         }
       }
-      if (gm < M) ldp[(int64_t)gm * (E * n_groups) + E * g + h] = ldsum;
+      if (gm < M) ldp[(int64_t)(E * g + h) * M + gm] = ldsum;   // partial-major: a warp writes 128 contiguous bytes
       // this warp's TMEM lanes of accumulator b are read: tell the even CTA's MMA warp
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncwarp();
@@ -762,11 +818,12 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kSplThreads, 1)
 
 }  // namespace tc
 
-// ld[r] += sum of the row's kSplineEpiPerQuarter * n_groups partials (fixed order)
+// ld[r] += sum of the row's kSplineEpiPerQuarter * n_groups partials (fixed
+// order); partial j of row r is ldp[j * m + r]
 __global__ void k_ld_reduce(const float* __restrict__ ldp, int n_part, int64_t m, float* __restrict__ ld) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < m; r += (int64_t)gridDim.x * blockDim.x) {
     float s = 0.f;
-    for (int j = 0; j < n_part; ++j) s += ldp[r * n_part + j];
+    for (int j = 0; j < n_part; ++j) s += ldp[(int64_t)j * m + r];
     ld[r] += s;
   }
 }
@@ -881,11 +938,21 @@ static int launch_spl_bwd(cudaStream_t st, const CUtensorMap& ma, const CUtensor
   using S = tc::Smem<T::BN, STAGES>;
   constexpr int TOTAL = S::TOTAL + T::STG_BYTES;
   static_assert(TOTAL <= 227 * 1024, "fused spline adjoint: shared memory over the per-CTA limit");
+  // x and dL/dy boxes (two buffers each) when the row stride allows tensor maps and they fit
+  constexpr int BOXES = 128 + 4 * tc::BM * 2 * T::DG * (int)sizeof(float);
+  CUtensorMap mx, mgy, mgx;
+  memset(&mx, 0, sizeof(mx));
+  memset(&mgy, 0, sizeof(mgy));
+  memset(&mgx, 0, sizeof(mgx));
+  int x_tma = TOTAL + BOXES <= 227 * 1024 && make_tma_map_f32(&mx, a.xa, a.d, M, 2 * T::DG, tc::BM) == FMC_OK &&
+              make_tma_map_f32(&mgy, a.gy, a.d, M, 2 * T::DG, tc::BM) == FMC_OK &&
+              make_tma_map_f32(&mgx, a.gxa, a.d, M, 2 * T::DG, tc::BM) == FMC_OK;
+  const int total = TOTAL + (x_tma ? BOXES : 0);
   auto kern = tc::k_tc_spline_bwd<KB, STAGES>;
-  static bool attr = false;
-  if (!attr) {
-    FMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, TOTAL));
-    attr = true;
+  static int attr = 0;
+  if (attr < total) {
+    FMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, total));
+    attr = total;
   }
   int* err = nullptr;
   int rc = tc_error_word(&err);
@@ -893,7 +960,7 @@ static int launch_spl_bwd(cudaStream_t st, const CUtensorMap& ma, const CUtensor
   const int64_t tiles = (M + tc::BM - 1) / tc::BM * n_groups;
   const int64_t grid = tiles < sm_count() ? tiles : sm_count();
   note_grid(FMC_KT_TC_SPLINE_BWD, (int)grid, 1);
-  kern<<<(unsigned)grid, tc::kSplThreads, TOTAL, st>>>(ma, mb, (int)M, n_groups, K, a, cfg, err);
+  kern<<<(unsigned)grid, tc::kSplThreads, total, st>>>(ma, mb, mx, mgy, mgx, x_tma, (int)M, n_groups, K, a, cfg, err);
   FMC_LAUNCH_CHECK();
   return FMC_OK;
 }
