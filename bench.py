@@ -120,20 +120,23 @@ def build_sampler(name, w, n_train, n_prod, precision, device):
                                   w["n_epochs"], mala_step_size=w["step"], rq_spline_hidden_units=w["hidden"],
                                   rq_spline_n_bins=w["n_bins"], rq_spline_n_layers=w["n_layers"],
                                   learning_rate=w["lr"], batch_size=w["batch"], n_max_examples=w["n_max"],
-                                  local_sampler=local, precision=precision, device=device, autotune=True)
+                                  local_sampler=local, precision=precision, device=device, autotune=True,
+                                  streaming_diagnostics=True)
     sampler = Sampler(w["d"], w["n_chains"], key, resource_strategy_bundles=bundle)
     g = torch.Generator().manual_seed(w["seed"])
     x0 = torch.randn(w["n_chains"], w["d"], generator=g)
     return sampler, bundle, target, mean, var, x0
 
 
-def loop_segments(order, n_train):
-    segs = [order[6 * i:6 * i + 6] for i in range(n_train)]
-    rest = order[6 * n_train:]
+def loop_segments(order, n_train, n_tr=6, n_pr=4):
+    """The bundle's strategy order cut into loops (n_tr / n_pr strategies per
+    training / production loop; the phase switch opens the first production loop)."""
+    segs = [order[n_tr * i:n_tr * i + n_tr] for i in range(n_train)]
+    rest = order[n_tr * n_train:]
     assert rest[:2] == ["reset_steppers", "update_state"]
     prod = rest[2:]
-    for i in range(0, len(prod), 4):
-        segs.append((rest[:2] if i == 0 else []) + prod[i:i + 4])
+    for i in range(0, len(prod), n_pr):
+        segs.append((rest[:2] if i == 0 else []) + prod[i:i + n_pr])
     return segs
 
 
@@ -626,7 +629,7 @@ def moment_trajectory(name, w, dev, n_loops, precision):
     from flowmc_gb300 import diagnostics as D
     prec = "bf16" if precision == "bf16" else "float32"
     sampler, bundle, target, mean_ref, var_ref, x0 = build_sampler(name, w, n_loops, n_loops, prec, dev)
-    segs = loop_segments(bundle.strategy_order, n_loops)
+    segs = loop_segments(bundle.strategy_order, n_loops, len(bundle.training_phase), len(bundle.production_phase))
     x, key = x0.to(dev), sampler.rng_key
     blk = w["n_local"] + w["n_global"]
     rows = []
@@ -943,7 +946,7 @@ def main():
     n_train, n_prod = schedule(W, K)
     precision = "bf16" if args.precision == "bf16" else "float32"
     sampler, bundle, target, mean_ref, var_ref, x0 = build_sampler(args.workload, w, n_train, n_prod, precision, dev)
-    segs = loop_segments(bundle.strategy_order, n_train)
+    segs = loop_segments(bundle.strategy_order, n_train, len(bundle.training_phase), len(bundle.production_phase))
     assert len(segs) == n_total
 
     def run(segments, x, key):
@@ -1016,6 +1019,17 @@ def main():
         extra["min_ess"] = float(ess.min())
         extra["min_ess_per_s"] = float(ess.min()) * world / secs
         extra["moment_error"] = D.moment_error(pos, mean_ref, var_ref)
+    if bundle.production_moments is not None:
+        # the device's streaming FP64 accumulators (updated inside the timed
+        # region after every production loop) against the post-hoc values
+        sm = bundle.production_moments.finalize()
+        mu_p, var_p = D.moments(pos)
+        extra["streaming"] = {
+            "moment_error": D.moment_error_of(sm["mean"], sm["var"], mean_ref, var_ref),
+            "min_ess_batch_means": float(torch.nan_to_num(sm["ess"], nan=float("inf")).min()),
+            "max_rhat": float(sm["rhat"].max()), "batch": bundle.production_moments.batch,
+            "max_abs_mean_diff_vs_posthoc": float((sm["mean"] - mu_p).abs().max()),
+            "max_rel_var_diff_vs_posthoc": float(((sm["var"] - var_p) / var_p).abs().max())}
     acc_l = sampler.resources["local_accs_production"].data
     acc_g = sampler.resources["global_accs_production"].data
     # local rows are the first n_local of each 80-row loop block

@@ -139,6 +139,14 @@ _SIGNATURES = {
     "fmc_device_error": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int32), ctypes.c_int32]),
     "fmc_device_error_set": (ctypes.c_int, [ctypes.c_int32]),
     "fmc_kernel_timing_enable": (ctypes.c_int, [ctypes.c_int32]),
+    "fmc_welford_state_size": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_size_t)]),
+    "fmc_welford_reset": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                         ctypes.c_void_p]),
+    "fmc_welford_ess_update": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32,
+                                              ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]),
+    "fmc_welford_ess_finalize": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
+                                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                ctypes.c_void_p]),
     "fmc_kernel_grid": (ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
     "fmc_kernel_timing_reset": (ctypes.c_int, []),
     "fmc_kernel_timing_read": (ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(ctypes.c_int64),

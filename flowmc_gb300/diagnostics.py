@@ -81,8 +81,13 @@ def moments(draws: torch.Tensor):
 def moment_error(draws: torch.Tensor, mean_ref, var_ref) -> float:
     """max_j max(|mu_j - m_j| / sigma_j, |s2_j / sigma2_j - 1|)."""
     mu, var = moments(draws)
-    mr = torch.as_tensor(np.asarray(mean_ref), dtype=torch.float64, device=draws.device)
-    vr = torch.as_tensor(np.asarray(var_ref), dtype=torch.float64, device=draws.device)
+    return moment_error_of(mu, var, mean_ref, var_ref)
+
+
+def moment_error_of(mu: torch.Tensor, var: torch.Tensor, mean_ref, var_ref) -> float:
+    """The moment error of given per-coordinate means and variances."""
+    mr = torch.as_tensor(np.asarray(mean_ref), dtype=torch.float64, device=mu.device)
+    vr = torch.as_tensor(np.asarray(var_ref), dtype=torch.float64, device=mu.device)
     e1 = (mu - mr).abs() / vr.sqrt()
     e2 = (var / vr - 1.0).abs()
     return float(torch.maximum(e1, e2).max())
@@ -159,3 +164,50 @@ def dual_moon_moments(d: int, r0: float = 2.0, sr: float = 0.1, mu: float = 3.0,
     var[0] = (w * x0 ** 2).sum()
     var[1:] = (w * (R * np.sin(F)) ** 2).sum() / (d - 1)
     return mean, var
+
+
+class StreamingMoments:
+    """FP64 moments, R-hat and batch-means ESS of chain rows accumulated on the
+    device while the sampler runs (fmc_welford_ess_update / _finalize): per
+    chain and coordinate Welford's running mean and squared deviations, and
+    Welford over completed batch means of ``batch`` draws. ``update`` folds in
+    rows [start, start + n_steps) of a chain buffer [n_chains, n, n_dim]; the
+    draw count lives in the device state, so updates can be captured in a
+    CUDA graph and replayed. ``finalize`` returns float64 tensors per
+    coordinate: mean, var (of all draws), ess (multi-chain batch means;
+    NaN before two complete batches) and rhat."""
+
+    def __init__(self, n_chains: int, n_dim: int, batch: int, device=None):
+        import ctypes
+        from . import _lib
+        self.n_chains, self.n_dim, self.batch = int(n_chains), int(n_dim), int(batch)
+        nb = ctypes.c_size_t()
+        _lib.check(_lib.lib().fmc_welford_state_size(self.n_chains, self.n_dim, ctypes.byref(nb)))
+        dev = torch.device("cuda") if device is None else torch.device(device)
+        self.state = torch.zeros(nb.value // 8, dtype=torch.float64, device=dev)
+        self._out = torch.empty(4, self.n_dim, dtype=torch.float64, device=dev)
+        self.reset()
+
+    def reset(self):
+        from . import _lib
+        _lib.check(_lib.lib().fmc_welford_reset(self.state.data_ptr(), self.n_chains, self.n_dim, self.batch,
+                                                _lib.stream_handle(self.state.device)))
+
+    def update(self, buf: torch.Tensor, start: int, n_steps: int):
+        from . import _lib
+        _lib.require_cuda_f32(buf, "chain buffer", (self.n_chains, buf.shape[1], self.n_dim))
+        _lib.check(_lib.lib().fmc_welford_ess_update(buf.data_ptr(), self.n_chains, buf.shape[1], self.n_dim,
+                                                     int(start), int(n_steps), self.state.data_ptr(),
+                                                     _lib.stream_handle(buf.device)))
+
+    def finalize(self) -> dict:
+        from . import _lib
+        o = self._out
+        _lib.check(_lib.lib().fmc_welford_ess_finalize(self.state.data_ptr(), self.n_chains, self.n_dim,
+                                                       o[0].data_ptr(), o[1].data_ptr(), o[2].data_ptr(),
+                                                       o[3].data_ptr(), _lib.stream_handle(o.device)))
+        return {"mean": o[0].clone(), "var": o[1].clone(), "ess": o[2].clone(), "rhat": o[3].clone()}
+
+    def draws(self) -> int:
+        """Draws per chain accumulated so far (synchronises)."""
+        return int(self.state[:1].view(torch.int64).item())

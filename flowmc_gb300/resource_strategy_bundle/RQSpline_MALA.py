@@ -10,6 +10,12 @@ reference's behaviour):
   device             where buffers and the flow live
   autotune           measure the local kernel's chain-block shape and the
                      flow GEMMs' tile width on first use
+  streaming_diagnostics
+                     accumulate FP64 moments, R-hat and batch-means ESS of
+                     the production rows on the device as they are written
+                     (``bundle.production_moments``, a
+                     diagnostics.StreamingMoments; batches of
+                     ``streaming_batch`` draws, default one production loop)
 """
 from __future__ import annotations
 
@@ -41,7 +47,8 @@ class RQSpline_MALA_Bundle(ResourceStrategyBundle):
                  rq_spline_n_layers: int = 4, learning_rate: float = 1e-3, batch_size: int = 10000,
                  n_max_examples: int = 10000, local_thinning: int = 1, global_thinning: int = 1,
                  n_NFproposal_batch_size: int = 10000, verbose: bool = False, local_sampler=None,
-                 precision: str = "float32", history_window: int = 100, device=None, autotune: bool = False):
+                 precision: str = "float32", history_window: int = 100, device=None, autotune: bool = False,
+                 streaming_diagnostics: bool = False, streaming_batch: int = 0):
         n_training_steps = (n_local_steps // local_thinning * n_training_loops
                             + n_global_steps // global_thinning * n_training_loops)
         n_production_steps = (n_local_steps // local_thinning * n_production_loops
@@ -110,9 +117,30 @@ class RQSpline_MALA_Bundle(ResourceStrategyBundle):
             ["positions_production", "log_prob_production", "local_accs_production", "global_accs_production",
              False])
 
+        self.production_moments = None
+        moments_cursor = [0]
+        if streaming_diagnostics:
+            from ..diagnostics import StreamingMoments
+            per_loop = n_local_steps // local_thinning + n_global_steps // global_thinning
+            self.production_moments = StreamingMoments(n_chains, n_dims, streaming_batch or per_loop,
+                                                       device=position_production.data.device)
+
         def reset_steppers(rng_key, resources, initial_position, data):
             local_stepper.set_current_position(0)
             global_stepper.set_current_position(0)
+            if self.production_moments is not None:
+                self.production_moments.reset()
+                moments_cursor[0] = 0
+            return rng_key, resources, initial_position
+
+        def update_moments(rng_key, resources, initial_position, data):
+            # the production rows this loop wrote: [cursor, the steppers' position)
+            end = global_stepper.current_position
+            buf = resources["positions_production"].data
+            end = min(end, buf.shape[1])
+            if end > moments_cursor[0]:
+                self.production_moments.update(buf, moments_cursor[0], end - moments_cursor[0])
+                moments_cursor[0] = end
             return rng_key, resources, initial_position
 
         def update_model(rng_key, resources, initial_position, data):
@@ -135,6 +163,10 @@ class RQSpline_MALA_Bundle(ResourceStrategyBundle):
         training_phase = ["local_stepper", "update_global_step", "model_trainer", "update_model", "global_stepper",
                           "update_local_step"]
         production_phase = ["local_stepper", "update_global_step", "global_stepper", "update_local_step"]
+        if streaming_diagnostics:
+            self.strategies["update_moments"] = Lambda(update_moments)
+            production_phase = production_phase + ["update_moments"]
+        self.training_phase, self.production_phase = training_phase, production_phase
         strategy_order = []
         for _ in range(n_training_loops):
             strategy_order.extend(training_phase)

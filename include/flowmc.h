@@ -475,6 +475,27 @@ FMC_API int fmc_device_sm_count(int32_t* out);
 /* Number of kernels this library has launched in the process (host counter). */
 FMC_API int fmc_launch_count(uint64_t* out);
 
+/* ---- streaming diagnostics (no counterpart in the reference, which
+ * leaves diagnostics to arviz after sampling) -------------------------
+ * FP64 accumulators of chain rows updated on the device while the sampler
+ * runs: per chain and coordinate, Welford's running mean and sum of squared
+ * deviations, and Welford over completed batch means of `batch` draws.
+ * fmc_welford_ess_update folds rows [start, start + n_steps) of every chain
+ * of a float32 buffer [n_chains, buf_len, n_dim] into the state (the draw
+ * count is kept on the device, so a captured graph can replay updates).
+ * fmc_welford_ess_finalize gives, per coordinate: the mean and the variance
+ * of all draws, the multi-chain batch-means ESS (N var / (batch var_bm),
+ * Flegal & Jones 2010; NaN with fewer than two completed batches) and
+ * R-hat (Gelman & Rubin 1992). The state is caller-owned
+ * (fmc_welford_state_size bytes, 8-byte aligned); fmc_welford_reset zeroes
+ * it and sets the batch size. */
+FMC_API int fmc_welford_state_size(int32_t n_chains, int32_t n_dim, size_t* bytes);
+FMC_API int fmc_welford_reset(double* state, int32_t n_chains, int32_t n_dim, int32_t batch, void* stream);
+FMC_API int fmc_welford_ess_update(const float* buf, int32_t n_chains, int64_t buf_len, int32_t n_dim,
+                                   int64_t start, int32_t n_steps, double* state, void* stream);
+FMC_API int fmc_welford_ess_finalize(const double* state, int32_t n_chains, int32_t n_dim, double* mean,
+                                     double* var, double* ess, double* rhat, void* stream);
+
 /* ---- per-kernel timing (profiling aid; no counterpart in the reference,
  * whose JAX path has no kernels of its own) ---------------------------
  * While enabled, every launch of the kernels listed below is bracketed by a

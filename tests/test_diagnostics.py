@@ -113,3 +113,52 @@ def test_plain_target_value_grad(kind):
     v, g = fn(torch.tensor(x))
     np.testing.assert_allclose(v.numpy(), v_ref, rtol=1e-12, atol=1e-10)
     np.testing.assert_allclose(g.numpy(), g_ref, rtol=1e-12, atol=1e-10)
+
+
+def test_streaming_oracle_matches_batch_definitions():
+    """The streaming oracle (Welford per chain, merged) equals the plain
+    float64 definitions on the same draws: mean and variance of all draws,
+    R-hat from within/between-chain variances, and the variance of the
+    complete batch means behind the batch-means ESS -- over updates whose
+    sizes do not line up with the batches."""
+    import numpy as np
+    from oracle.streaming import StreamingOracle
+    rng = np.random.default_rng(3)
+    C, n, d, b = 7, 53, 4, 10
+    x = rng.normal(size=(C, n, d)) * [1.0, 2.0, 0.5, 3.0] + [0.0, 1.0, -2.0, 5.0]
+    so = StreamingOracle(C, d, b)
+    for lo, hi in ((0, 3), (3, 17), (17, 40), (40, 53)):
+        so.update(x[:, lo:hi])
+    mu, var, ess, rhat = so.finalize()
+    flat = x.reshape(-1, d)
+    np.testing.assert_allclose(mu, flat.mean(0), rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(var, flat.var(0, ddof=1), rtol=1e-12)
+    W = x.var(1, ddof=1).mean(0)
+    B_n = x.mean(1).var(0, ddof=1)
+    np.testing.assert_allclose(rhat, np.sqrt(((n - 1) / n * W + B_n) / W), rtol=1e-12)
+    k = n // b
+    bm = x[:, :k * b].reshape(C, k, b, d).mean(2).reshape(-1, d)
+    tau = b * bm.var(0, ddof=1) / flat.var(0, ddof=1)
+    np.testing.assert_allclose(ess, np.minimum(C * n / tau, C * n), rtol=1e-10)
+
+
+def test_streaming_oracle_ess_of_ar1():
+    """Batch-means ESS of AR(1) chains x_t = rho x_{t-1} + e_t (integrated
+    autocorrelation time (1 + rho) / (1 - rho)) within 15 % of N / tau with
+    batches of 25 tau, and near N for independent draws."""
+    import numpy as np
+    from oracle.streaming import StreamingOracle
+    rng = np.random.default_rng(11)
+    C, n, d = 64, 4000, 2
+    for rho in (0.0, 0.8):
+        e = rng.normal(size=(C, n, d))
+        x = np.empty_like(e)
+        x[:, 0] = e[:, 0] / np.sqrt(1 - rho ** 2)
+        for t in range(1, n):
+            x[:, t] = rho * x[:, t - 1] + e[:, t]
+        tau = (1 + rho) / (1 - rho)
+        so = StreamingOracle(C, d, int(25 * tau))
+        so.update(x)
+        _, _, ess, rhat = so.finalize()
+        assert np.all(np.abs(ess / (C * n / tau) - 1) < 0.15), (rho, ess, C * n / tau)
+        assert np.all(np.abs(rhat - 1) < 0.01)
