@@ -57,9 +57,16 @@ __global__ void k_welford_reset(WelfordView v, int64_t cd, int64_t batch) {
   }
 }
 
+// steps per launch of the update kernel: the block's table of 1 / n holds
+// this many float64 values (the host splits longer updates)
+constexpr int kWelfordSteps = 2048;
+
 __global__ void k_welford_update(WelfordView v, const float* __restrict__ buf, int64_t n_chains, int64_t buf_len,
                                  int n_dim, int64_t start, int n_steps) {
+  __shared__ double inv_n[kWelfordSteps];   // 1 / n of every step (one FP64 division per step per block)
   const int64_t n0 = v.hdr[0], batch = v.hdr[1];
+  for (int s = threadIdx.x; s < n_steps; s += blockDim.x) inv_n[s] = 1.0 / (double)(n0 + s + 1);
+  __syncthreads();
   const int64_t cd = n_chains * n_dim;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < cd; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t c = i / n_dim;
@@ -70,7 +77,7 @@ __global__ void k_welford_update(WelfordView v, const float* __restrict__ buf, i
       const double x = (double)__ldg(row + (int64_t)s * n_dim);
       const int64_t n = n0 + s + 1;
       const double delta = x - mean;
-      mean += delta / (double)n;
+      mean += delta * inv_n[s];
       m2 += delta * (x - mean);
       bsum += x;
       if (n % batch == 0) {
@@ -198,10 +205,13 @@ extern "C" int fmc_welford_ess_update(const float* buf, int32_t n_chains, int64_
   cudaStream_t st = (cudaStream_t)stream;
   const int64_t cd = (int64_t)n_chains * n_dim;
   const WelfordView v = welford_view(state, n_chains, n_dim);
-  k_welford_update<<<grid_for(cd), 256, 0, st>>>(v, buf, n_chains, buf_len, n_dim, start, n_steps);
-  FMC_LAUNCH_CHECK();
-  k_welford_advance<<<1, 1, 0, st>>>(v.hdr, n_steps);
-  FMC_LAUNCH_CHECK();
+  for (int s0 = 0; s0 < n_steps; s0 += kWelfordSteps) {
+    const int ns = n_steps - s0 < kWelfordSteps ? n_steps - s0 : kWelfordSteps;
+    k_welford_update<<<grid_for(cd), 256, 0, st>>>(v, buf, n_chains, buf_len, n_dim, start + s0, ns);
+    FMC_LAUNCH_CHECK();
+    k_welford_advance<<<1, 1, 0, st>>>(v.hdr, ns);
+    FMC_LAUNCH_CHECK();
+  }
   return FMC_OK;
 }
 
