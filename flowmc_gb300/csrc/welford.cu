@@ -73,16 +73,17 @@ __global__ void k_welford_update(WelfordView v, const float* __restrict__ buf, i
     const int j = (int)(i - c * n_dim);
     double mean = v.mean[i], m2 = v.m2[i], bsum = v.bsum[i], bmean = v.bmean[i], bm2 = v.bm2[i];
     const float* row = buf + (c * buf_len + start) * n_dim + j;
+    int64_t in_batch = n0 % batch;   // draws of the current batch so far
     for (int s = 0; s < n_steps; ++s) {
       const double x = (double)__ldg(row + (int64_t)s * n_dim);
-      const int64_t n = n0 + s + 1;
       const double delta = x - mean;
       mean += delta * inv_n[s];
       m2 += delta * (x - mean);
       bsum += x;
-      if (n % batch == 0) {
+      if (++in_batch == batch) {
+        in_batch = 0;
         const double bm = bsum / (double)batch;
-        const int64_t k = n / batch;
+        const int64_t k = (n0 + s + 1) / batch;
         const double bd = bm - bmean;
         bmean += bd / (double)k;
         bm2 += bd * (bm - bmean);
