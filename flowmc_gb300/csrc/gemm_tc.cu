@@ -113,14 +113,15 @@ size_t splitk_scratch_floats(int64_t M, int N, int K) {
   return s > 1 ? (size_t)s * (size_t)M * (size_t)N : 0;
 }
 
-template <int BN, int STAGES, int EPI, bool TSTORE>
+template <int BN, int STAGES, int EPI, bool TSTORE, int NSTG = 2>
 static int launch_tc(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap& mc, int64_t M,
                      int N, int K, const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store) {
   using S = tc::Smem<BN, STAGES>;
   // ring + alignment slack + barrier block (1024 with TSTORE, so the staging stays 1024-aligned) + staging
-  constexpr int TOTAL = TSTORE ? S::TOTAL + 768 + tc::kStagingBytes : S::TOTAL;
-  static_assert(TOTAL <= 227 * 1024, "tcgen05 GEMM: shared memory over the per-CTA limit");
-  auto kern = tc::k_tc_gemm<BN, STAGES, EPI, TSTORE>;
+  constexpr int TOTAL = TSTORE ? S::TOTAL + 768 + tc::staging_bytes(NSTG) : S::TOTAL;
+  // with the static bias slots (NSTG = 2) and the fail-fast word
+  static_assert(TOTAL + (NSTG == 2 ? 1024 : 0) + 16 <= 227 * 1024, "tcgen05 GEMM: shared memory over the per-CTA limit");
+  auto kern = tc::k_tc_gemm<BN, STAGES, EPI, TSTORE, false, NSTG>;
   static bool attr_set = false;
   if (!attr_set) {
     FMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, TOTAL));
@@ -168,8 +169,8 @@ template <int BN, int STAGES, int EPI>
 static int launch_tc_pair(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap& mc,
                           int64_t M, int N, int K, const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store) {
   using S = tc::Smem<BN / 2, STAGES>;
-  constexpr int TOTAL = S::TOTAL + 768 + tc::kStagingBytes;
-  static_assert(TOTAL <= 227 * 1024, "tcgen05 GEMM: shared memory over the per-CTA limit");
+  constexpr int TOTAL = S::TOTAL + 768 + tc::staging_bytes(2);
+  static_assert(TOTAL + 1024 + 16 <= 227 * 1024, "tcgen05 GEMM: shared memory over the per-CTA limit");
   auto kern = tc::k_tc_gemm<BN, STAGES, EPI, true, true>;
   static bool attr_set = false;
   if (!attr_set) {
@@ -252,10 +253,16 @@ int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K
     if (BN == 256) return launch_tc<256, 4, E, false>(st, ma, mb, mc, M, N, K, ep, C, ldc, n_store);          \
     return launch_tc<128, 4, E, false>(st, ma, mb, mc, M, N, K, ep, C, ldc, n_store);                         \
   }
+  // 256-column tiles with staged stores: a four-deep ring and one staging
+  // buffer per warp where a tile takes several K blocks (the ring's depth
+  // hides the operand loads), three stages and two buffers (and the bias in
+  // shared memory) where one or two K blocks make the epilogue the limit
 #define TC_CASE_TS(E)                                                                                         \
   if (epi == E && tstore) {                                                                                   \
-    if (BN == 256) return launch_tc<256, 3, E, true>(st, ma, mb, mc, M, N, K, ep, C, ldc, n_store);           \
-    return launch_tc<128, 4, E, true>(st, ma, mb, mc, M, N, K, ep, C, ldc, n_store);                          \
+    if (BN == 256 && K >= 4 * tc::BK)                                                                         \
+      return launch_tc<256, 4, E, true, 1>(st, ma, mb, mc, M, N, K, ep, C, ldc, n_store);                     \
+    if (BN == 256) return launch_tc<256, 3, E, true, 2>(st, ma, mb, mc, M, N, K, ep, C, ldc, n_store);        \
+    return launch_tc<128, 4, E, true, 2>(st, ma, mb, mc, M, N, K, ep, C, ldc, n_store);                       \
   }
   TC_CASE_TS(tc::TC_EPI_TANH_BF16)
   TC_CASE_TS(tc::TC_EPI_DTANH_BF16)

@@ -265,31 +265,97 @@ __device__ __forceinline__ float ex2_approx(float x) {
   return y;
 }
 
+// Packed FP32 pairs (f32x2: two lanes of a 64-bit register pair per
+// instruction) and the three-input maximum, both sm_100-family instructions.
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ uint64_t f2_pack(float lo, float hi) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(uint64_t v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+// a[i] += b[i] for i < N, adjacent pairs as one f32x2 add
+template <int N>
+__device__ __forceinline__ void add_f2(float* a, const float* b) {
+#pragma unroll
+  for (int i = 0; i + 1 < N; i += 2) f2_unpack(f2_add(f2_pack(a[i], a[i + 1]), f2_pack(b[i], b[i + 1])), a[i], a[i + 1]);
+  if (N & 1) a[N - 1] += b[N - 1];
+}
+
+// Unnormalised softmax weights of the K bin widths and K bin heights,
+// ew[k] = e^(raw[k] - max) as one FFMA + ex2 each, and their sums. The
+// FFMAs and the sums run on adjacent pairs as f32x2 (the sums as two
+// interleaved partial sums, added at the end).
+template <int K>
+__device__ __forceinline__ void softmax_weights(const float (&raw)[3 * K + 1], float (&ew)[K], float (&eh)[K],
+                                                float& sw, float& sh) {
+  constexpr float kLog2e = 1.4426950408889634f;
+  float mw = raw[0], mh = raw[K];
+#pragma unroll
+  for (int k = 1; k < K; k += 2) {
+    if (k + 1 < K) {
+      mw = fmax3(mw, raw[k], raw[k + 1]);
+      mh = fmax3(mh, raw[K + k], raw[K + k + 1]);
+    } else {
+      mw = fmaxf(mw, raw[k]);
+      mh = fmaxf(mh, raw[K + k]);
+    }
+  }
+  const float nmw = -mw * kLog2e, nmh = -mh * kLog2e;
+  const uint64_t l2 = f2_pack(kLog2e, kLog2e), nw2 = f2_pack(nmw, nmw), nh2 = f2_pack(nmh, nmh);
+  uint64_t sw2 = f2_pack(0.f, 0.f), sh2 = sw2;
+#pragma unroll
+  for (int k = 0; k + 1 < K; k += 2) {
+    float a0, a1, b0, b1;
+    f2_unpack(f2_fma(f2_pack(raw[k], raw[k + 1]), l2, nw2), a0, a1);
+    f2_unpack(f2_fma(f2_pack(raw[K + k], raw[K + k + 1]), l2, nh2), b0, b1);
+    ew[k] = ex2_approx(a0);
+    ew[k + 1] = ex2_approx(a1);
+    eh[k] = ex2_approx(b0);
+    eh[k + 1] = ex2_approx(b1);
+    sw2 = f2_add(sw2, f2_pack(ew[k], ew[k + 1]));
+    sh2 = f2_add(sh2, f2_pack(eh[k], eh[k + 1]));
+  }
+  float a, b;
+  f2_unpack(sw2, a, b);
+  sw = a + b;
+  f2_unpack(sh2, a, b);
+  sh = a + b;
+  if (K & 1) {
+    ew[K - 1] = ex2_approx(fmaf(raw[K - 1], kLog2e, nmw));
+    eh[K - 1] = ex2_approx(fmaf(raw[2 * K - 1], kLog2e, nmh));
+    sw += ew[K - 1];
+    sh += eh[K - 1];
+  }
+}
+
 // The spline of the bin that holds v only, for the fused tensor-core
 // epilogue (same function as rqs_forward/rqs_inverse up to rounding):
-// unnormalised softmax weights e^(raw - max) (one FFMA + ex2 each), the bin
+// unnormalised softmax weights (softmax_weights), the bin
 // found by comparing v with the running knots while carrying only what the
 // bin needs (cumulative sums before it, its own weights, its two slope
 // parameters), and one log for the log-determinant.
 template <int K, bool INV>
 __device__ __forceinline__ void rqs_apply_fast(const float (&raw)[3 * K + 1], float v, const SplineCfg& c, float& out,
                                                float& ld) {
-  constexpr float kLog2e = 1.4426950408889634f;
-  float mw = raw[0], mh = raw[K];
-#pragma unroll
-  for (int k = 1; k < K; ++k) {
-    mw = fmaxf(mw, raw[k]);
-    mh = fmaxf(mh, raw[K + k]);
-  }
-  const float nmw = -mw * kLog2e, nmh = -mh * kLog2e;
-  float ew[K], eh[K], sw = 0.f, sh = 0.f;
-#pragma unroll
-  for (int k = 0; k < K; ++k) {
-    ew[k] = ex2_approx(fmaf(raw[k], kLog2e, nmw));
-    eh[k] = ex2_approx(fmaf(raw[K + k], kLog2e, nmh));
-    sw += ew[k];
-    sh += eh[k];
-  }
+  float ew[K], eh[K], sw, sh;
+  softmax_weights<K>(raw, ew, eh, sw, sh);
   const float scale = (c.rmax - c.rmin) - (float)K * c.min_bin;
   const float fw = __fdividef(scale, sw), fh = __fdividef(scale, sh);
   // knot k = rmin + (sum of the first k weights) * f + k * min_bin; bin 0 by
@@ -358,22 +424,8 @@ __device__ __forceinline__ void rqs_apply_fast(const float (&raw)[3 * K + 1], fl
 template <int K>
 __device__ __forceinline__ float rqs_fwd_adjoint_fast(const float (&raw)[3 * K + 1], float x, float gy, float gl,
                                                       const SplineCfg& c, uint16_t* __restrict__ out) {
-  constexpr float kLog2e = 1.4426950408889634f;
-  float mw = raw[0], mh = raw[K];
-#pragma unroll
-  for (int k = 1; k < K; ++k) {
-    mw = fmaxf(mw, raw[k]);
-    mh = fmaxf(mh, raw[K + k]);
-  }
-  const float nmw = -mw * kLog2e, nmh = -mh * kLog2e;
-  float pw[K], ph[K], sw = 0.f, sh = 0.f;
-#pragma unroll
-  for (int k = 0; k < K; ++k) {
-    pw[k] = ex2_approx(fmaf(raw[k], kLog2e, nmw));
-    ph[k] = ex2_approx(fmaf(raw[K + k], kLog2e, nmh));
-    sw += pw[k];
-    sh += ph[k];
-  }
+  float pw[K], ph[K], sw, sh;
+  softmax_weights<K>(raw, pw, ph, sw, sh);
   const float iw = __fdividef(1.f, sw), ih = __fdividef(1.f, sh);
 #pragma unroll
   for (int k = 0; k < K; ++k) {

@@ -173,9 +173,11 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 // ---- TMA store of the bf16 epilogues: each epilogue warp stages a 32-row x
 // 64-column block (4 KB, the 128-byte swizzle of the output tensor map: the
 // 16-byte chunk c of row r sits at r*128 + ((c ^ (r & 7)) * 16)) and one lane
-// stores it with cp.async.bulk.tensor; two staging buffers per warp.
+// stores it with cp.async.bulk.tensor; NSTG staging buffers per warp (two let
+// a warp fill one block while the previous one is still being stored; one
+// leaves room for a deeper operand ring).
 constexpr int kStageBlockBytes = 32 * 128;
-constexpr int kStagingBytes = kEpiWarps * 2 * kStageBlockBytes;
+__host__ __device__ constexpr int staging_bytes(int nstg) { return kEpiWarps * nstg * kStageBlockBytes; }
 
 __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
   asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
@@ -318,20 +320,26 @@ __device__ __forceinline__ bool tc_skip_pair(const int* err) {
 // TSTORE (bf16 modes only): the row-major output goes through per-warp
 // shared-memory staging and TMA stores on tmC ([M, n_store] bf16, box 64 x 32);
 // the shared memory then holds the ring, its barriers, 768 bytes of padding
-// and the staging buffers (kStagingBytes, 1024-byte aligned).
+// and the staging buffers (staging_bytes(NSTG), 1024-byte aligned).
+// NSTG = 2 also stages each chunk's 32 bias values in shared memory (one
+// 128-byte slot per epilogue warp, broadcast reads); with NSTG = 1 the bias
+// reaches the lanes by shuffles.
 // PAIR (launched as clusters of 2, no split-K): a tile is 256 rows x BN
 // columns computed by a CTA pair with tcgen05 cta_group::2 -- each CTA loads
 // its 128 rows of A and BN / 2 rows of B (tmB's box is BN / 2 rows), the
 // even CTA issues the MMAs, each CTA runs the epilogue of its own rows.
-template <int BN, int STAGES, int EPI, bool TSTORE, bool PAIR = false>
+template <int BN, int STAGES, int EPI, bool TSTORE, bool PAIR = false, int NSTG = 2>
 __global__ void __launch_bounds__(kThreads, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
               const __grid_constant__ CUtensorMap tmC, int M, int N, int K, const EpiArgs ep, void* __restrict__ C,
               int64_t ldc, int n_store, int splits, int64_t split_stride, int* err) {
   static_assert(!TSTORE || EPI == TC_EPI_TANH_BF16 || EPI == TC_EPI_DTANH_BF16, "TMA store: bf16 epilogues only");
   static_assert(!PAIR || BN % 32 == 0, "a CTA pair splits B into two multiples of 16 rows");
+  static_assert(NSTG == 1 || NSTG == 2, "one or two staging buffers per warp");
+  constexpr bool kBiasSmem = NSTG == 2;
   if (PAIR ? tc_skip_pair(err) : tc_skip(err)) return;
   extern __shared__ uint8_t smem_raw[];
+  __shared__ __align__(16) float s_bias[kBiasSmem ? kEpiWarps : 1][32];
   constexpr int BNL = PAIR ? BN / 2 : BN;   // B rows this CTA loads per stage
   using S = Smem<BNL, STAGES>;
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -515,16 +523,38 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
         for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
         if (EPI == TC_EPI_TANH_BF16 || EPI == TC_EPI_BIAS_F32) {
+          if constexpr (kBiasSmem) {
+            // the warp's slot: lane i writes bias i, every lane reads all 32 (broadcast)
+            float* sbw = s_bias[warp - 2];
+            sbw[lane] = bl;
+            __syncwarp();
+            const float4* b4 = reinterpret_cast<const float4*>(sbw);
 #pragma unroll
-          for (int i = 0; i < 32; ++i) v[i] += __shfl_sync(0xffffffffu, bl, i);
+            for (int i = 0; i < 8; ++i) {
+              const float4 bb = b4[i];
+              v[4 * i] += bb.x;
+              v[4 * i + 1] += bb.y;
+              v[4 * i + 2] += bb.z;
+              v[4 * i + 3] += bb.w;
+            }
+            __syncwarp();
+          } else {
+#pragma unroll
+            for (int i = 0; i < 32; ++i) v[i] += __shfl_sync(0xffffffffu, bl, i);
+          }
         }
         if (!TSTORE && !(row_ok || ct_row)) return;
         if (EPI == TC_EPI_TANH_BF16 || EPI == TC_EPI_DTANH_BF16) {
           uint32_t packed[16];
           float y[32];
           if (EPI == TC_EPI_TANH_BF16) {
+            if (gn0 + 32 <= N && row_ok) {   // the whole chunk is inside the output
 #pragma unroll
-            for (int i = 0; i < 32; ++i) y[i] = (gn0 + i < N && row_ok) ? tanh_fast(v[i]) : 0.f;
+              for (int i = 0; i < 32; ++i) y[i] = tanh_fast(v[i]);
+            } else {
+#pragma unroll
+              for (int i = 0; i < 32; ++i) y[i] = (gn0 + i < N && row_ok) ? tanh_fast(v[i]) : 0.f;
+            }
           } else {
             const uint16_t* hv = reinterpret_cast<const uint16_t*>(av);
 #pragma unroll
@@ -540,7 +570,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
           if (TSTORE) {
             // half `sub` of this warp's current 64-column block (zeros in rows >= M are clipped by the store)
-            const uint32_t buf = smem_u32(staging) + (uint32_t)(((warp - 2) * 2 + (blkno & 1)) * kStageBlockBytes);
+            const uint32_t buf = smem_u32(staging) + (uint32_t)(((warp - 2) * NSTG + (blkno % NSTG)) * kStageBlockBytes);
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
               const int cc = sub * 4 + k;
@@ -646,8 +676,13 @@ __global__ void __launch_bounds__(kThreads, 1)
         // inside it (the odd CTA of the last pair can lie wholly past row M)
         const bool blk_live = n0 + (c0 & ~63) < n_store && m0 < M;
         if (TSTORE && (i & 1) == 0 && blk_live) {
-          // the staging buffer about to be filled was last used two blocks ago
-          if (lane == 0) bulk_wait_read_1();
+          // the staging buffer about to be filled was last used NSTG blocks ago
+          if (lane == 0) {
+            if constexpr (NSTG == 2)
+              bulk_wait_read_1();
+            else
+              bulk_wait_read_0();
+          }
           __syncwarp();
         }
         chunk(cur, c0, bl_cur, av_cur, i & 1);
@@ -659,7 +694,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             // 2l, 2l+1 (one 4-byte word per row: the 32 lanes cover a row's
             // 128 bytes, no bank conflicts); rows >= M were staged as zeros
             const uint32_t buf =
-                smem_u32(staging) + (uint32_t)(((warp - 2) * 2 + (blkno & 1)) * kStageBlockBytes);
+                smem_u32(staging) + (uint32_t)(((warp - 2) * NSTG + (blkno % NSTG)) * kStageBlockBytes);
             float s0 = 0.f, s1 = 0.f;
 #pragma unroll 8
             for (int r = 0; r < 32; ++r) {
@@ -675,7 +710,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (col + 1 < N) dst[col + 1] = s1;
           }
           if (lane == 0) {
-            tma_store_2d(&tmC, smem_u32(staging) + (uint32_t)(((warp - 2) * 2 + (blkno & 1)) * kStageBlockBytes),
+            tma_store_2d(&tmC, smem_u32(staging) + (uint32_t)(((warp - 2) * NSTG + (blkno % NSTG)) * kStageBlockBytes),
                          n0 + (c0 & ~63), m0 + q * 32);
             bulk_commit();
           }

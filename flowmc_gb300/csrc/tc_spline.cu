@@ -359,14 +359,16 @@ __global__ void __launch_bounds__(kSplThreads, 1)
           const float xv = *xp;
           if (bias_smem) {
             const float4* bb = reinterpret_cast<const float4*>(sbias + tcoord * PP);
+            float bl[PP];
 #pragma unroll
             for (int i = 0; i < PP / 4; ++i) {
               const float4 bv = bb[i];
-              if (4 * i < P) raw[4 * i] += bv.x;
-              if (4 * i + 1 < P) raw[4 * i + 1] += bv.y;
-              if (4 * i + 2 < P) raw[4 * i + 2] += bv.z;
-              if (4 * i + 3 < P) raw[4 * i + 3] += bv.w;
+              bl[4 * i] = bv.x;
+              bl[4 * i + 1] = bv.y;
+              bl[4 * i + 2] = bv.z;
+              bl[4 * i + 3] = bv.w;
             }
+            add_f2<P>(raw, bl);
           } else {
             const float* bb = bias + (int64_t)tcoord * P;
 #pragma unroll
@@ -787,14 +789,16 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kSplThreads, 1)
           const float xv = *xp;
           if (bias_smem) {
             const float4* bb = reinterpret_cast<const float4*>(sbias + tcoord * PP);
+            float bl[PP];
 #pragma unroll
             for (int i = 0; i < PP / 4; ++i) {
               const float4 bv = bb[i];
-              if (4 * i < P) raw[4 * i] += bv.x;
-              if (4 * i + 1 < P) raw[4 * i + 1] += bv.y;
-              if (4 * i + 2 < P) raw[4 * i + 2] += bv.z;
-              if (4 * i + 3 < P) raw[4 * i + 3] += bv.w;
+              bl[4 * i] = bv.x;
+              bl[4 * i + 1] = bv.y;
+              bl[4 * i + 2] = bv.z;
+              bl[4 * i + 3] = bv.w;
             }
+            add_f2<P>(raw, bl);
           } else {
             const float* bb = bias + (int64_t)tcoord * P;
 #pragma unroll
