@@ -30,9 +30,10 @@ struct TrainWs {
   // weight-gradient GEMMs (K = the batch)
   float *ldp, *bpart, *kpart, *colpart;
   int64_t kpart_floats;
-  // BF16 path (tensor-core GEMMs): activations, gradients and their transposes
-  uint16_t *cond16, *condT, *hs16, *hsT, *graw16, *grawT, *gz16[2], *gzT[2];
-  int64_t n128, n64, hld, htr, ncld, nctr, pld, ptr_rows;
+  // BF16 path (tensor-core GEMMs): activations and gradients, row-major (the
+  // weight-gradient GEMMs read them MN-major, so no transposed copies)
+  uint16_t *cond16, *hs16, *graw16, *gz16[2];
+  int64_t n128, n64, hld, ncld, pld;
 };
 
 static int colsum_blocks(int64_t n) {
@@ -90,26 +91,19 @@ static void carve_train(const FlowGeom& g, int64_t n, bool bf16, void* ws, Train
   }
   w.ldp = w.bpart = w.kpart = w.colpart = nullptr;
   w.kpart_floats = 0;
-  w.cond16 = w.condT = w.hs16 = w.hsT = w.graw16 = w.grawT = nullptr;
-  w.gz16[0] = w.gz16[1] = w.gzT[0] = w.gzT[1] = nullptr;
+  w.cond16 = w.hs16 = w.graw16 = nullptr;
+  w.gz16[0] = w.gz16[1] = nullptr;
   if (bf16) {
     w.n128 = FlowGeom::rup(n, 128);
     w.n64 = FlowGeom::rup(n, 64);
     w.hld = FlowGeom::rup(g.h_max(), 64);
-    w.htr = FlowGeom::rup(g.h_max(), 256);
     w.ncld = FlowGeom::rup(g.nc_max(), 64);
-    w.nctr = FlowGeom::rup(g.nc_max(), 256);
     w.pld = FlowGeom::rup(ntP, 64);
-    w.ptr_rows = FlowGeom::rup(ntP, 256);
     w.cond16 = take16(w.n128 * w.ncld);
-    w.condT = take16(w.nctr * w.n64);
     w.hs16 = take16((int64_t)g.nh * w.n128 * w.hld);
-    w.hsT = take16((int64_t)g.nh * w.htr * w.n64);
     w.graw16 = take16(w.n128 * w.pld);
-    w.grawT = take16(w.ptr_rows * w.n64);
     for (int k = 0; k < 2; ++k) {
       w.gz16[k] = take16(w.n128 * w.hld);
-      w.gzT[k] = take16(w.htr * w.n64);
     }
     const int64_t groups = (g.nt_max() + g.spl_dg - 1) / g.spl_dg;
     w.ldp = take(n * kSplineEpiPerQuarter * groups);
@@ -308,13 +302,12 @@ static int recompute_mlp(const FmcFlow* f, const FlowGeom& g, int l, int64_t n, 
   return FMC_OK;
 }
 
-// BF16 recompute of layer l's conditioner hidden layers: tanh activations
-// (and their transposes for the weight gradients) in bf16; the last Linear is
-// recomputed inside the fused spline adjoint
+// BF16 recompute of layer l's conditioner hidden layers: tanh activations in
+// bf16; the last Linear is recomputed inside the fused spline adjoint
 static int recompute_hidden_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t n, TrainWs& w, cudaStream_t st) {
   const float* th = f->theta + g.layer_off[l];
   const int nc = g.nc(l);
-  int rc = to_bf16_pad_t(st, w.cond, n, nc, w.cond16, FlowGeom::rup(nc, 64), w.condT, w.n64, w.n64);
+  int rc = to_bf16_pad_t(st, w.cond, n, nc, w.cond16, FlowGeom::rup(nc, 64), nullptr, 0, 0);
   if (rc) return rc;
   const uint16_t* a = w.cond16;
   for (int i = 0; i < g.nh; ++i) {
@@ -323,9 +316,6 @@ static int recompute_hidden_bf16(const FmcFlow* f, const FlowGeom& g, int l, int
     tc::EpiArgs ep{};
     ep.bias = th + g.lin_b(l, i);
     uint16_t* h = w.hs16 + (int64_t)i * w.n128 * w.hld;
-    ep.ct = w.hsT + (int64_t)i * w.htr * w.n64;
-    ep.ldct = w.n64;
-    ep.ct_rows_pad = w.n64;
     const int ldo = (int)FlowGeom::rup(N, 64);
     if ((rc = tc_gemm(st, a, n, w.n128, K, f->theta_bf16 + g.w16_off[seg], N, g.w16_rows(l, i), ep, h, ldo, ldo,
                       tc::TC_EPI_TANH_BF16, f->gemm_bn, f->tile_rows == 256)))
@@ -335,28 +325,28 @@ static int recompute_hidden_bf16(const FmcFlow* f, const FlowGeom& g, int l, int
   return FMC_OK;
 }
 
-// BF16 adjoint of the conditioner: d raw (w.graw16 / w.grawT, bf16, with the
-// last bias gradient already reduced) -> weight/bias gradients into gl, d cond
-// into w.gcond
+// BF16 adjoint of the conditioner: d raw (w.graw16, bf16, with the last bias
+// gradient already reduced) -> weight/bias gradients into gl, d cond into
+// w.gcond. The weight gradients read the row-major gradients and activations
+// MN-major (tc_gemm_wgrad); rows [n, 64) of every operand are zero when n < 64.
 static int backward_mlp_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t n, TrainWs& w, float* gl,
                              cudaStream_t st) {
   int rc = FMC_OK;
   const uint16_t* gcur = w.graw16;
-  const uint16_t* gcurT = w.grawT;
+  int64_t ldcur = w.pld;
   int nxt = 0;
   bool have_cp = false;   // w.colpart holds the column sums of gcur
   for (int i = g.nh; i >= 0; --i) {
     const int out = g.lin_out(l, i), in = g.lin_in(l, i);
     const int seg = l * (g.nh + 1) + i;
-    const uint16_t* aT = (i == 0) ? w.condT : w.hsT + (int64_t)(i - 1) * w.htr * w.n64;
+    const uint16_t* act = (i == 0) ? w.cond16 : w.hs16 + (int64_t)(i - 1) * w.n128 * w.hld;
+    const int64_t ldact = FlowGeom::rup(in, 64);
     // dW = g^T a  [out, in], reduced over the batch (split along it when the
     // [out, in] tile grid is small)
     tc::EpiArgs e0{};
     e0.kpart = w.kpart;
     e0.kpart_floats = w.kpart_floats;
-    if ((rc = tc_gemm(st, gcurT, out, FlowGeom::rup(out, 128), (int)w.n64, aT, in, (int)FlowGeom::rup(in, 256), e0,
-                      gl + g.lin_w(l, i), in, in, tc::TC_EPI_F32)))
-      return rc;
+    if ((rc = tc_gemm_wgrad(st, gcur, ldcur, out, act, ldact, in, n, e0, gl + g.lin_w(l, i), in))) return rc;
     if (i < g.nh) {
       if (have_cp) {
         // fixed-order reduction of the per-32-row partials the DTANH GEMM left
@@ -372,9 +362,6 @@ static int backward_mlp_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t
       tc::EpiArgs e1{};
       e1.aux = w.hs16 + (int64_t)(i - 1) * w.n128 * w.hld;
       e1.ldaux = FlowGeom::rup(in, 64);
-      e1.ct = w.gzT[nxt];
-      e1.ldct = w.n64;
-      e1.ct_rows_pad = w.n64;
       const int ldo = (int)FlowGeom::rup(in, 64);
       have_cp = tc_gemm_stages_output(w.gz16[nxt], ldo, ldo, n);
       if (have_cp) {
@@ -385,7 +372,7 @@ static int backward_mlp_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t
                         ldo, ldo, tc::TC_EPI_DTANH_BF16)))
         return rc;
       gcur = w.gz16[nxt];
-      gcurT = w.gzT[nxt];
+      ldcur = ldo;
       nxt ^= 1;
     } else {
       tc::EpiArgs e2{};
@@ -454,6 +441,15 @@ int flow_loss_grad(const FmcFlow* f, const float* x, int64_t n, float* loss, flo
   // ---- backward
   const float inv_n = 1.0f / (float)n;
   const float gld = -inv_n;
+  if (bf16 && n < 64) {
+    // the weight-gradient GEMMs read 64-row blocks of the bf16 operands: rows
+    // [n, 64) stay zero (the kernels below write rows < n only)
+    FMC_CUDA_TRY(cudaMemsetAsync(w.cond16, 0, (size_t)64 * w.ncld * 2, st));
+    for (int i = 0; i < g.nh; ++i)
+      FMC_CUDA_TRY(cudaMemsetAsync(w.hs16 + (int64_t)i * w.n128 * w.hld, 0, (size_t)64 * w.hld * 2, st));
+    FMC_CUDA_TRY(cudaMemsetAsync(w.graw16, 0, (size_t)64 * w.pld * 2, st));
+    for (int k = 0; k < 2; ++k) FMC_CUDA_TRY(cudaMemsetAsync(w.gz16[k], 0, (size_t)64 * w.hld * 2, st));
+  }
   k_init_gy<<<eb, 256, 0, st>>>(y, nd, d, f->aux, inv_n, w.gy);
   FMC_LAUNCH_CHECK();
   for (int l = g.L - 1; l >= 0; --l) {
@@ -468,7 +464,7 @@ int flow_loss_grad(const FmcFlow* f, const float* x, int64_t n, float* loss, flo
       if ((rc = recompute_hidden_bf16(f, g, l, n, w, st))) return rc;
       const uint16_t* h_last = g.nh > 0 ? w.hs16 + (int64_t)(g.nh - 1) * w.n128 * w.hld : w.cond16;
       if ((rc = tc_linear_spline_bwd(st, g, f, l, h_last, n, w.n128, w.xa, w.gy, gld, w.gxa, w.graw16, w.pld,
-                                     w.grawT, w.n64, w.bpart)))
+                                     w.bpart)))
         return rc;
       const int ntP = g.lin_out(l, g.nh);
       k_colsum_rows<<<(ntP + 31) / 32, 1024, 0, st>>>(w.bpart, (int)(w.n128 / 128), ntP, gl + g.lin_b(l, g.nh));

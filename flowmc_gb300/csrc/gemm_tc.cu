@@ -113,7 +113,7 @@ size_t splitk_scratch_floats(int64_t M, int N, int K) {
   return s > 1 ? (size_t)s * (size_t)M * (size_t)N : 0;
 }
 
-template <int BN, int STAGES, int EPI, bool TSTORE, int NSTG = 2>
+template <int BN, int STAGES, int EPI, bool TSTORE, int NSTG = 2, int OPM = 0>
 static int launch_tc(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap& mc, int64_t M,
                      int N, int K, const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store) {
   using S = tc::Smem<BN, STAGES>;
@@ -121,7 +121,7 @@ static int launch_tc(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& 
   constexpr int TOTAL = TSTORE ? S::TOTAL + 768 + tc::staging_bytes(NSTG) : S::TOTAL;
   // with the static bias slots (NSTG = 2) and the fail-fast word
   static_assert(TOTAL + (NSTG == 2 ? 1024 : 0) + 16 <= 227 * 1024, "tcgen05 GEMM: shared memory over the per-CTA limit");
-  auto kern = tc::k_tc_gemm<BN, STAGES, EPI, TSTORE, false, NSTG>;
+  auto kern = tc::k_tc_gemm<BN, STAGES, EPI, TSTORE, false, NSTG, OPM>;
   static bool attr_set = false;
   if (!attr_set) {
     FMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, TOTAL));
@@ -211,6 +211,30 @@ static int launch_tc_pair(cudaStream_t st, const CUtensorMap& ma, const CUtensor
   FMC_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, ma, mb, mc, Mi, N, K, ep, C, ldc, n_store, one, stride, err));
   FMC_LAUNCH_CHECK();
   return FMC_OK;
+}
+
+// Weight gradient C[out, in] = sum over the n batch rows of G[r, out] * X[r, in]
+// (fp32, split along the batch when the tile grid is small), reading both
+// operands MN-major straight from their row-major bf16 buffers: G [n, ldg]
+// and X [n, ldx], columns beyond out / in zero up to the pitch (a multiple of
+// 64), rows past n read as zeros through the tensor maps (for n < 64 the
+// maps cover 64 rows, and rows [n, 64) must hold zeros).
+int tc_gemm_wgrad(cudaStream_t st, const uint16_t* G, int64_t ldg, int out, const uint16_t* X, int64_t ldx, int in,
+                  int64_t n, const tc::EpiArgs& ep, float* C, int64_t ldc) {
+  FMC_CHECK_ARG(ldg % 64 == 0 && ldx % 64 == 0 && ldg >= out && ldx >= in, "operand pitches must cover the outputs "
+                "and be multiples of 64");
+  FMC_CHECK_ARG(n >= 1 && out >= 1 && in >= 1 && ldc >= in, "bad sizes");
+  CUtensorMap ma, mb, mc;
+  const int64_t rows = n < 64 ? 64 : n;
+  int rc = make_map(&ma, G, ldg, rows, ldg, 64);
+  if (rc) return rc;
+  const int BN = in > 128 ? 256 : 128;
+  if ((rc = make_map(&mb, X, ldx, rows, ldx, 64))) return rc;
+  memset(&mc, 0, sizeof(mc));
+  const int K = (int)FlowGeom::rup(n, 64);
+  FMC_CHECK_SUPPORTED(n < (1ll << 31), "batch too large");
+  if (BN == 256) return launch_tc<256, 4, tc::TC_EPI_F32, false, 2, 3>(st, ma, mb, mc, out, in, K, ep, C, ldc, in);
+  return launch_tc<128, 4, tc::TC_EPI_F32, false, 2, 3>(st, ma, mb, mc, out, in, K, ep, C, ldc, in);
 }
 
 bool tc_gemm_stages_output(const void* C, int64_t ldc, int n_store, int64_t M) {

@@ -8,17 +8,13 @@ namespace fmc {
 namespace tc {
 // epilogues of the tensor-core GEMM: 0 tanh(acc + bias) -> bf16;
 // 1 acc + bias -> fp32; 2 acc * (1 - aux^2) -> bf16 (tanh adjoint, aux = the
-// forward's tanh output); 3 acc -> fp32 (no bias). Modes 0 and 2 can also
-// store a transposed bf16 copy.
+// forward's tanh output); 3 acc -> fp32 (no bias).
 enum Epi : int { TC_EPI_TANH_BF16 = 0, TC_EPI_BIAS_F32 = 1, TC_EPI_DTANH_BF16 = 2, TC_EPI_F32 = 3 };
 
 struct EpiArgs {
   const float* bias;        // modes 0, 1
   const uint16_t* aux;      // mode 2: bf16 [M, ldaux]
   int64_t ldaux;
-  uint16_t* ct;             // optional transposed copy: ct[col * ldct + row]
-  int64_t ldct;
-  int64_t ct_rows_pad;      // rows in [M, ct_rows_pad) get zeros in the copy
   float* kpart;             // mode 3: optional scratch for split-K partial products
   int64_t kpart_floats;     //   (the GEMM splits K when the tile grid leaves SMs idle)
   float* colpart;           // mode 2 with TMA stores: column sums of the bf16 output per
@@ -51,12 +47,11 @@ int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l
 
 // adjoint of layer l's last Linear + spline (tc_spline.cu), recomputing the
 // Linear from A: dL/dx into gxa (every coordinate), dL/draw in bf16 into graw
-// [>= M, ldg] (columns t*P + p, padding up to ldg zeroed) and grawT [t*P + p,
-// ldt] (rows M..ldt zeroed), and per-128-row-tile column sums of dL/draw into
-// bpart [ceil(M / 128), nt * P]
+// [>= M, ldg] (columns t*P + p, padding up to ldg zeroed), and per-128-row-tile
+// column sums of dL/draw into bpart [ceil(M / 128), nt * P]
 int tc_linear_spline_bwd(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l, const uint16_t* A, int64_t M,
                          int64_t rows_a, const float* xa, const float* gy, float gld, float* gxa, uint16_t* graw,
-                         int64_t ldg, uint16_t* grawT, int64_t ldt, float* bpart);
+                         int64_t ldg, float* bpart);
 
 // theta (fp32, packed) -> zero-padded bf16 weight segments (FlowGeom::w16_off)
 // and their transposes (FlowGeom::w16t_off)
@@ -83,6 +78,8 @@ size_t splitk_scratch_floats(int64_t M, int N, int K);
 
 // fp32 src [n, cols] -> bf16 dst [>= n, ldd] (zero padded to ldd columns; may be
 // NULL) and/or its transpose dstT [>= ldd, ldt] (rows n..t_cols-1 zero)
+int tc_gemm_wgrad(cudaStream_t st, const uint16_t* G, int64_t ldg, int out, const uint16_t* X, int64_t ldx, int in,
+                  int64_t n, const tc::EpiArgs& ep, float* C, int64_t ldc);
 int to_bf16_pad_t(cudaStream_t st, const float* src, int64_t n, int cols, uint16_t* dst, int64_t ldd,
                   uint16_t* dstT, int64_t ldt, int64_t t_cols);
 

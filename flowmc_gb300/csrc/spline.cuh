@@ -391,7 +391,10 @@ __device__ __forceinline__ void rqs_apply_fast(const float (&raw)[3 * K + 1], fl
     const float bq = d0 - st * ww;
     const float aq = s - bq;
     const float disc = bq * bq - 4.f * aq * cq;
-    const float sqd = (disc > 0.f) ? sqrtf(disc) : 0.f;
+    // the hardware square-root approximation (one instruction), like the
+    // other fast approximations of this path
+    float sqd = 0.f;
+    if (disc > 0.f) asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(sqd) : "f"(disc));
     const float num = (bq >= 0.f) ? 2.f * cq : -bq + sqd;
     const float dnm = (bq >= 0.f) ? -bq - sqd : 2.f * aq;
     z = fminf(fmaxf(__fdividef(num, dnm), 0.f), 1.f);

@@ -98,6 +98,23 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(const void* p) {
   return d;
 }
 
+// MN-major operand in 128-byte swizzle: the tile is stored as K rows of 64
+// MN elements (128 bytes each; one TMA box {64 MN, 64 K} = 8 KB per 64-wide MN
+// block). Canonical layout ((8,8,m),(8,k)) : ((1,8,LBO),(64,SBO)) in elements:
+// LBO = 8192 B between the 64-wide MN blocks, SBO = 1024 B between groups of
+// eight K rows; one K = 16 step of the MMA advances the start by 2048 B.
+constexpr int kMnBlockBytes = 64 * BK * 2;
+__device__ __forceinline__ uint64_t smem_desc_sw128_mn(const void* p) {
+  const uint64_t addr = smem_u32(p);
+  uint64_t d = 0;
+  d |= (addr >> 4) & 0x3FFFull;                       // start address
+  d |= (uint64_t)(kMnBlockBytes >> 4) << 16;          // leading byte offset: next 64-wide MN block
+  d |= (uint64_t)(1024 >> 4) << 32;                   // stride byte offset: next 8 K rows
+  d |= (uint64_t)1 << 46;                             // descriptor version (sm_100 family)
+  d |= (uint64_t)2 << 61;                             // 128-byte swizzle
+  return d;
+}
+
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
 }
@@ -328,7 +345,7 @@ __device__ __forceinline__ bool tc_skip_pair(const int* err) {
 // columns computed by a CTA pair with tcgen05 cta_group::2 -- each CTA loads
 // its 128 rows of A and BN / 2 rows of B (tmB's box is BN / 2 rows), the
 // even CTA issues the MMAs, each CTA runs the epilogue of its own rows.
-template <int BN, int STAGES, int EPI, bool TSTORE, bool PAIR = false, int NSTG = 2>
+template <int BN, int STAGES, int EPI, bool TSTORE, bool PAIR = false, int NSTG = 2, int OPM = 0>
 __global__ void __launch_bounds__(kThreads, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
               const __grid_constant__ CUtensorMap tmC, int M, int N, int K, const EpiArgs ep, void* __restrict__ C,
@@ -336,6 +353,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   static_assert(!TSTORE || EPI == TC_EPI_TANH_BF16 || EPI == TC_EPI_DTANH_BF16, "TMA store: bf16 epilogues only");
   static_assert(!PAIR || BN % 32 == 0, "a CTA pair splits B into two multiples of 16 rows");
   static_assert(NSTG == 1 || NSTG == 2, "one or two staging buffers per warp");
+  static_assert(OPM == 0 || (!PAIR && BN % 64 == 0), "MN-major operands: one-CTA tiles of whole 64-wide blocks");
   constexpr bool kBiasSmem = NSTG == 2;
   if (PAIR ? tc_skip_pair(err) : tc_skip(err)) return;
   extern __shared__ uint8_t smem_raw[];
@@ -424,8 +442,18 @@ __global__ void __launch_bounds__(kThreads, 1)
             tma_load_2d_pair(sb, &tmB, full_cl, k * BK, n0);
           } else {
             mbar_expect_tx(&full[s], S::STAGE_BYTES);
-            tma_load_2d(sa, &tmA, &full[s], k * BK, m0);
-            tma_load_2d(sb, &tmB, &full[s], k * BK, n0);
+            if constexpr ((OPM & 1) != 0) {
+#pragma unroll
+              for (int j = 0; j < BM / 64; ++j) tma_load_2d(sa + j * kMnBlockBytes, &tmA, &full[s], m0 + 64 * j, k * BK);
+            } else {
+              tma_load_2d(sa, &tmA, &full[s], k * BK, m0);
+            }
+            if constexpr ((OPM & 2) != 0) {
+#pragma unroll
+              for (int j = 0; j < BN / 64; ++j) tma_load_2d(sb + j * kMnBlockBytes, &tmB, &full[s], n0 + 64 * j, k * BK);
+            } else {
+              tma_load_2d(sb, &tmB, &full[s], k * BK, n0);
+            }
           }
         }
       }
@@ -443,7 +471,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   } else if (warp == 1) {
     if (lane == 0 && rank == 0) {
-      const uint32_t idesc = PAIR ? idesc_bf16_f32_pair(BN) : idesc_bf16_f32(BN);
+      // bits 15 / 16 of the instruction descriptor: A / B MN-major
+      const uint32_t idesc = (PAIR ? idesc_bf16_f32_pair(BN) : idesc_bf16_f32(BN)) | ((OPM & 1) ? 1u << 15 : 0u) |
+                             ((OPM & 2) ? 1u << 16 : 0u);
       uint32_t it = 0;
       int local = 0;
       for (int t = t_first; t < tiles && !*abort_flag; t += t_step, ++local) {
@@ -468,14 +498,18 @@ __global__ void __launch_bounds__(kThreads, 1)
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint8_t* sa = base + s * S::STAGE_BYTES;
           const uint8_t* sb = sa + S::A_BYTES;
-          const uint64_t da = smem_desc_sw128(sa), db = smem_desc_sw128(sb);
+          const uint64_t da = (OPM & 1) ? smem_desc_sw128_mn(sa) : smem_desc_sw128(sa);
+          const uint64_t db = (OPM & 2) ? smem_desc_sw128_mn(sb) : smem_desc_sw128(sb);
+          // start-address step of one K = 16 slice (16-byte units): 32 B inside a
+          // K-major swizzle row, 16 rows of 128 B in an MN-major tile
+          constexpr uint64_t kStepA = (OPM & 1) ? 128 : 2, kStepB = (OPM & 2) ? 128 : 2;
 #pragma unroll
           for (int kk = 0; kk < BK / 16; ++kk) {
             // advance along K inside the swizzle atom: 16 bf16 = 32 bytes
             if constexpr (PAIR)
               mma_bf16_pair(d, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, (k > kb || kk > 0) ? 1u : 0u);
             else
-              mma_bf16(d, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, (k > kb || kk > 0) ? 1u : 0u);
+              mma_bf16(d, da + kStepA * kk, db + kStepB * kk, idesc, (k > kb || kk > 0) ? 1u : 0u);
           }
           if constexpr (PAIR) mma_commit_pair(&empty[s]); else mma_commit(&empty[s]);
         }
@@ -511,7 +545,6 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const bool row_ok = gm < M;
-      const bool ct_row = ep.ct != nullptr && gm < ep.ct_rows_pad;
       const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN);
       // One 32-column chunk: v = accumulator row segment, bl = bias of column
       // n0 + c0 + lane (lane-distributed, broadcast with shuffles before any
@@ -543,7 +576,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int i = 0; i < 32; ++i) v[i] += __shfl_sync(0xffffffffu, bl, i);
           }
         }
-        if (!TSTORE && !(row_ok || ct_row)) return;
+        if (!TSTORE && !row_ok) return;
         if (EPI == TC_EPI_TANH_BF16 || EPI == TC_EPI_DTANH_BF16) {
           uint32_t packed[16];
           float y[32];
@@ -589,18 +622,6 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
               for (int i = 0; i < 32; ++i)
                 if (gn0 + i < n_store) o16[i] = (i & 1) ? (uint16_t)(packed[i / 2] >> 16) : (uint16_t)packed[i / 2];
-            }
-          }
-          if (ct_row) {
-            // transposed copy: column j of the tile becomes row j of ct; a warp's
-            // 32 rows give one contiguous 64-byte store per column
-#pragma unroll
-            for (int i = 0; i < 32; ++i) {
-              if (gn0 + i < n_store) {
-                const uint32_t w = packed[i / 2];
-                const uint16_t hv = (i & 1) ? (uint16_t)(w >> 16) : (uint16_t)(w & 0xffffu);
-                ep.ct[(int64_t)(gn0 + i) * ep.ldct + gm] = hv;
-              }
             }
           }
         } else if (row_ok) {

@@ -411,8 +411,6 @@ struct SplineBwdArgs {
   float* gxa;          // dL/d(spline input), [M, d]; conditioning coordinates copied from gy
   uint16_t* graw;      // bf16 [>= M, ldg] row-major; columns [nt*P, ldg) are zeroed
   int64_t ldg;
-  uint16_t* grawT;     // bf16 [>= nt*P, ldt] transposed; rows in [M, ldt) get zeros
-  int64_t ldt;
   float* bpart;        // [m_tiles, nt*P] column sums of each 128-row tile
   int d, nt, tpar, cpar;
 };
@@ -430,6 +428,7 @@ __global__ void __launch_bounds__(kSplThreads, 1)
                     const SplineBwdArgs a, SplineCfg cfg, int* err) {
   using T = SplineTile<KB>;
   constexpr int P = T::P, DG = T::DG, DGP = T::DGP, BN = T::BN, SP = T::SP, E = kSplineEpiPerQuarter;
+  static_assert(DGP % 2 == 0 && SP % 2 == 0, "group column spans and the staging pitch move as 32-bit words");
   constexpr int XS = 2 * DG;   // floats per row of a box
   using S = Smem<BN, STAGES>;
   if (tc_skip(err)) return;
@@ -539,31 +538,42 @@ __global__ void __launch_bounds__(kSplThreads, 1)
         tma_store_2d_f32(&tmGx, smem_u32(gb), 2 * g * DG, m0);
         bulk_commit();
       }
-      // row-major copy: the group's columns are contiguous in [t*P + p] order;
-      // the last group also zeroes the padding columns up to ldg
+      // row-major copy: the group's columns are contiguous in [t*P + p] order
+      // (an even count per group, so every row segment starts on a 4-byte
+      // boundary and moves as 32-bit words); the last group also zeroes the
+      // padding columns up to ldg
       {
         const int64_t c0 = (int64_t)g * DGP;
         const int width = (g == n_groups - 1) ? (int)(a.ldg - c0) : vc;
         for (int r = ew; r < BM && m0 + r < M; r += kSplEpiWarps) {
-          uint16_t* dst = a.graw + (int64_t)(m0 + r) * a.ldg + c0;
-          for (int c = lane; c < width; c += 32) dst[c] = (c < vc) ? stg[r * SP + c] : (uint16_t)0;
+          uint32_t* dst = reinterpret_cast<uint32_t*>(a.graw + (int64_t)(m0 + r) * a.ldg + c0);
+          const uint32_t* src = reinterpret_cast<const uint32_t*>(stg + r * SP);
+          for (int c2 = lane; 2 * c2 < width; c2 += 32) {
+            const int c = 2 * c2;
+            uint32_t w = 0u;
+            if (c + 1 < vc)
+              w = src[c2];
+            else if (c < vc)
+              w = src[c2] & 0xffffu;
+            dst[c2] = w;
+          }
         }
       }
-      // transposed copy and the column sums, one column per warp at a time:
-      // lane l holds rows l, l+32, l+64, l+96 (64 contiguous bytes per store)
-      for (int c = ew; c < vc; c += kSplEpiWarps) {
-        const int64_t col = (int64_t)g * DGP + c;
-        float s = 0.f;
-#pragma unroll
-        for (int k = 0; k < BM / 32; ++k) {
-          const int r = lane + 32 * k;
-          const uint16_t v = stg[r * SP + c];
-          if (m0 + r < a.ldt) a.grawT[col * a.ldt + m0 + r] = v;
-          s += __uint_as_float((uint32_t)v << 16);
+      // column sums over the tile's 128 rows (rows >= M were staged as zeros):
+      // thread e takes columns 2e, 2e+1, reading one 32-bit word per row
+      // (consecutive threads, consecutive words: no bank conflicts), in row order
+      for (int c2 = et; 2 * c2 < vc; c2 += kSplEpiThreads) {
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(stg) + c2;
+        float s0 = 0.f, s1 = 0.f;
+#pragma unroll 8
+        for (int r = 0; r < BM; ++r) {
+          const uint32_t v = src[r * (SP / 2)];
+          s0 += __uint_as_float(v << 16);
+          s1 += __uint_as_float(v & 0xffff0000u);
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) a.bpart[(int64_t)mt * ntP + col] = s;
+        const int64_t col = (int64_t)g * DGP + 2 * c2;
+        a.bpart[(int64_t)mt * ntP + col] = s0;
+        if (2 * c2 + 1 < vc) a.bpart[(int64_t)mt * ntP + col + 1] = s1;
       }
       epi_sync(2);   // the staging tile is free again
     }
@@ -1024,12 +1034,12 @@ int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l
 // (the last tanh activation, bf16 [rows_a, K]).
 int tc_linear_spline_bwd(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l, const uint16_t* A, int64_t M,
                          int64_t rows_a, const float* xa, const float* gy, float gld, float* gxa, uint16_t* graw,
-                         int64_t ldg, uint16_t* grawT, int64_t ldt, float* bpart) {
+                         int64_t ldg, float* bpart) {
   const int nt = g.nt(l);
   int dg, bn;
   const int n_groups = spline_groups(g.K, nt, &dg, &bn);
   const int Kd = g.w16_cols(l, g.nh);
-  FMC_CHECK_ARG(ldg >= (int64_t)nt * g.P && ldt >= M, "graw leading dimensions too small");
+  FMC_CHECK_ARG(ldg >= (int64_t)nt * g.P && ldg % 2 == 0, "graw leading dimension too small or odd");
   CUtensorMap ma, mb;
   int rc = make_tma_map_bf16(&ma, A, Kd, rows_a, Kd, tc::BM);
   if (rc) return rc;
@@ -1042,8 +1052,6 @@ int tc_linear_spline_bwd(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, i
   a.gxa = gxa;
   a.graw = graw;
   a.ldg = ldg;
-  a.grawT = grawT;
-  a.ldt = ldt;
   a.bpart = bpart;
   a.d = g.d;
   a.nt = nt;
@@ -1051,9 +1059,9 @@ int tc_linear_spline_bwd(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, i
   a.cpar = g.cpar(l);
   const int hl = g.H[g.nh - 1];
   const double flops = 2.0 * (double)M * nt * g.P * hl;
-  // A and the weights once, x / dL/dy read, dL/dx written, dL/draw in two bf16 layouts
+  // A and the weights once, x / dL/dy read, dL/dx written, dL/draw in bf16
   const double bytes = (double)M * hl * 2 + (double)nt * g.P * hl * 2 + (double)M * nt * 12 +
-                       (double)M * nt * g.P * 4;
+                       (double)M * nt * g.P * 2;
   KernelTimer kt(FMC_KT_TC_SPLINE_BWD, st, flops, bytes);
 #define SPL_CASE(k)                                                  \
   if (g.K == k) {                                                    \
