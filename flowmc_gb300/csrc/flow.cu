@@ -55,15 +55,16 @@ int make_geom(const FmcFlow* f, FlowGeom& g) {
       o16 += (int64_t)g.w16_rows(l, i) * g.w16_cols(l, i);
     }
   g.w16_off[g.L * (g.nh + 1)] = o16;
+  g.spl_pp = (g.P + 7) / 8 * 8;
+  g.spl_dg = 256 / g.spl_pp;
+  g.spl_bn = ((g.spl_dg * g.spl_pp + 15) / 16) * 16;
+  g.spl_opc = g.spl_pp;
   for (int l = 0; l < g.L; ++l)
     for (int i = 0; i <= g.nh; ++i) {
       g.w16t_off[l * (g.nh + 1) + i] = o16;
       o16 += (int64_t)g.w16t_rows(l, i) * g.w16t_cols(l, i);
     }
   g.w16t_off[g.L * (g.nh + 1)] = o16;
-  g.spl_pp = (g.P + 7) / 8 * 8;
-  g.spl_dg = 256 / g.spl_pp;
-  g.spl_bn = ((g.spl_dg * g.spl_pp + 15) / 16) * 16;
   for (int l = 0; l < g.L; ++l) {
     g.w16g_off[l] = o16;
     o16 += (int64_t)g.spl_groups(l) * g.spl_bn * g.w16_cols(l, g.nh);

@@ -15,7 +15,8 @@ struct FlowGeom {
   // padded bf16 copy of the Linear weights (BF16 path): segment l*(nh+1)+i is
   // W_i of layer l as [round_up(out, 256), round_up(in, 64)], zero padded
   int64_t w16_off[FMC_MAX_LAYERS * (FMC_MAX_HIDDEN + 1) + 1];
-  // transposed copies W_i^T as [round_up(in, 256), round_up(out, 64)] (training)
+  // transposed copies W_i^T as [round_up(in, 256), w16t_cols] (training); the
+  // last Linear's columns follow the padded d-raw layout (draw_cols)
   int64_t w16t_off[FMC_MAX_LAYERS * (FMC_MAX_HIDDEN + 1) + 1];
   // the last Linear of each layer re-packed in spline groups (fused inference
   // kernel, tc_spline.cu): group g = DG transformed coordinates x P rows,
@@ -25,6 +26,11 @@ struct FlowGeom {
   // spl_pp = round_up(P, 8) (so the epilogue reads them with 8-column TMEM
   // loads at 8-aligned columns), spl_dg coordinates per group, spl_bn rows
   int spl_pp, spl_dg, spl_bn;
+  // BF16 training: the spline adjoint writes d raw row-major with coordinate t
+  // at columns [t * spl_opc, t * spl_opc + P) and zeros up to (t + 1) * spl_opc
+  // (spl_opc = round_up(P, 8), so each coordinate is a whole number of 16-byte
+  // chunks that one TMA box stores)
+  int spl_opc;
   int64_t n_w16;
 
   // conditioning coordinates of layer l: j = 2k + cpar(l); transformed: j = 2k + tpar(l)
@@ -53,7 +59,10 @@ struct FlowGeom {
   __host__ __device__ int w16_cols(int l, int i) const { return (int)rup(lin_in(l, i), 64); }
   __host__ __device__ int w16t_rows(int l, int i) const { return (int)rup(lin_in(l, i), 256); }
   __host__ __device__ int spl_groups(int l) const { return (nt(l) + spl_dg - 1) / spl_dg; }
-  __host__ __device__ int w16t_cols(int l, int i) const { return (int)rup(lin_out(l, i), 64); }
+  __host__ __device__ int64_t draw_cols(int l) const { return (int64_t)nt(l) * spl_opc; }
+  __host__ __device__ int w16t_cols(int l, int i) const {
+    return (int)rup(i == nh ? draw_cols(l) : (int64_t)lin_out(l, i), 64);
+  }
 };
 
 int make_geom(const FmcFlow* f, FlowGeom& g);

@@ -98,7 +98,7 @@ static void carve_train(const FlowGeom& g, int64_t n, bool bf16, void* ws, Train
     w.n64 = FlowGeom::rup(n, 64);
     w.hld = FlowGeom::rup(g.h_max(), 64);
     w.ncld = FlowGeom::rup(g.nc_max(), 64);
-    w.pld = FlowGeom::rup(ntP, 64);
+    w.pld = FlowGeom::rup((int64_t)g.nt_max() * g.spl_opc, 64);   // padded d-raw rows
     w.cond16 = take16(w.n128 * w.ncld);
     w.hs16 = take16((int64_t)g.nh * w.n128 * w.hld);
     w.graw16 = take16(w.n128 * w.pld);
@@ -107,10 +107,12 @@ static void carve_train(const FlowGeom& g, int64_t n, bool bf16, void* ws, Train
     }
     const int64_t groups = (g.nt_max() + g.spl_dg - 1) / g.spl_dg;
     w.ldp = take(n * kSplineEpiPerQuarter * groups);
-    w.bpart = take((w.n128 / 128) * ntP);
+    w.bpart = take((w.n128 / 128) * kSplineBwdRowParts * ntP);
     for (int l = 0; l < g.L; ++l)
       for (int i = 0; i <= g.nh; ++i) {
-        const int64_t f = (int64_t)splitk_scratch_floats(g.lin_out(l, i), g.lin_in(l, i), (int)w.n64);
+        // the last Linear's weight gradient runs over the padded d-raw rows
+        const int64_t mrows = i == g.nh ? g.draw_cols(l) : g.lin_out(l, i);
+        const int64_t f = (int64_t)splitk_scratch_floats(mrows, g.lin_in(l, i), (int)w.n64);
         if (f > w.kpart_floats) w.kpart_floats = f;
       }
     w.kpart = w.kpart_floats > 0 ? take(w.kpart_floats) : nullptr;
@@ -341,12 +343,29 @@ static int backward_mlp_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t
     const int seg = l * (g.nh + 1) + i;
     const uint16_t* act = (i == 0) ? w.cond16 : w.hs16 + (int64_t)(i - 1) * w.n128 * w.hld;
     const int64_t ldact = FlowGeom::rup(in, 64);
+    // the last Linear's d raw is in the padded layout (coordinate t at columns
+    // [t * opc, t * opc + P)): its weight gradient runs over the padded rows
+    // and maps them back to t * P + p; its input-gradient GEMM contracts the
+    // padded columns against the matching padded W^T
+    const bool padded = i == g.nh;
+    const int gcols = padded ? (int)g.draw_cols(l) : out;
     // dW = g^T a  [out, in], reduced over the batch (split along it when the
     // [out, in] tile grid is small)
     tc::EpiArgs e0{};
     e0.kpart = w.kpart;
     e0.kpart_floats = w.kpart_floats;
-    if ((rc = tc_gemm_wgrad(st, gcur, ldcur, out, act, ldact, in, n, e0, gl + g.lin_w(l, i), in))) return rc;
+    if (padded) {
+      e0.rmap_grp = g.spl_opc;
+      e0.rmap_keep = g.P;
+    }
+    if ((rc = tc_gemm_wgrad(st, gcur, ldcur, gcols, act, ldact, in, n, e0, gl + g.lin_w(l, i), in))) return rc;
+    const int kg = padded ? g.w16t_cols(l, i) : (int)FlowGeom::rup(out, 64);
+    if (padded && g.draw_cols(l) < kg) {
+      // columns [draw_cols, kg) of d raw: zeros (a layer with fewer
+      // transformed coordinates than the buffer's widest leaves older values)
+      FMC_CUDA_TRY(cudaMemset2DAsync(w.graw16 + g.draw_cols(l), (size_t)w.pld * 2, 0,
+                                     (size_t)(kg - g.draw_cols(l)) * 2, (size_t)n, st));
+    }
     if (i < g.nh) {
       if (have_cp) {
         // fixed-order reduction of the per-32-row partials the DTANH GEMM left
@@ -368,16 +387,16 @@ static int backward_mlp_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t
         e1.colpart = w.colpart;
         e1.ldpart = in;
       }
-      if ((rc = tc_gemm(st, gcur, n, w.n128, (int)FlowGeom::rup(out, 64), WT, in, g.w16t_rows(l, i), e1, w.gz16[nxt],
-                        ldo, ldo, tc::TC_EPI_DTANH_BF16)))
+      if ((rc = tc_gemm(st, gcur, n, w.n128, kg, WT, in, g.w16t_rows(l, i), e1, w.gz16[nxt], ldo, ldo,
+                        tc::TC_EPI_DTANH_BF16, 0, false, ldcur)))
         return rc;
       gcur = w.gz16[nxt];
       ldcur = ldo;
       nxt ^= 1;
     } else {
       tc::EpiArgs e2{};
-      if ((rc = tc_gemm(st, gcur, n, w.n128, (int)FlowGeom::rup(out, 64), WT, in, g.w16t_rows(l, i), e2, w.gcond, in,
-                        in, tc::TC_EPI_F32)))
+      if ((rc = tc_gemm(st, gcur, n, w.n128, kg, WT, in, g.w16t_rows(l, i), e2, w.gcond, in, in, tc::TC_EPI_F32, 0,
+                        false, ldcur)))
         return rc;
     }
   }
@@ -467,7 +486,8 @@ int flow_loss_grad(const FmcFlow* f, const float* x, int64_t n, float* loss, flo
                                      w.bpart)))
         return rc;
       const int ntP = g.lin_out(l, g.nh);
-      k_colsum_rows<<<(ntP + 31) / 32, 1024, 0, st>>>(w.bpart, (int)(w.n128 / 128), ntP, gl + g.lin_b(l, g.nh));
+      k_colsum_rows<<<(ntP + 31) / 32, 1024, 0, st>>>(w.bpart, (int)(w.n128 / 128) * kSplineBwdRowParts, ntP,
+                                                    gl + g.lin_b(l, g.nh));
       FMC_LAUNCH_CHECK();
       if ((rc = backward_mlp_bf16(f, g, l, n, w, gl, st))) return rc;
     } else {

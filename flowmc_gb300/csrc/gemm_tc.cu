@@ -57,6 +57,37 @@ int make_tma_map_bf16(CUtensorMap* m, const void* base, int64_t inner, int64_t o
   return FMC_OK;
 }
 
+// 2-D bf16 tensor [outer, inner] with row stride ld (elements), box
+// {box_inner, box_outer}, swizzle 0 / 32 / 64 / 128 bytes (box_inner * 2
+// bytes at most the swizzle span), out-of-range elements zero / clipped
+int make_tma_map_bf16_box(CUtensorMap* m, const void* base, int64_t inner, int64_t outer, int64_t ld, int box_inner,
+                          int box_outer, int swizzle) {
+  auto fn = encode_fn();
+  FMC_CHECK_SUPPORTED(fn != nullptr, "cuTensorMapEncodeTiled is unavailable");
+  FMC_CHECK_ARG(((uintptr_t)base & 15) == 0, "TMA base address must be 16-byte aligned");
+  FMC_CHECK_ARG((ld * 2) % 16 == 0, "TMA row stride must be a multiple of 16 bytes");
+  FMC_CHECK_ARG((box_inner * 2) % 16 == 0 && box_inner <= 256 && box_outer <= 256, "bad TMA box");
+  FMC_CHECK_ARG(swizzle == 0 || box_inner * 2 <= swizzle, "box wider than the swizzle span");
+  FMC_CHECK_ARG(inner >= box_inner && outer >= 1, "tensor narrower than one TMA box");
+  const CUtensorMapSwizzle sw = swizzle == 32    ? CU_TENSOR_MAP_SWIZZLE_32B
+                                : swizzle == 64  ? CU_TENSOR_MAP_SWIZZLE_64B
+                                : swizzle == 128 ? CU_TENSOR_MAP_SWIZZLE_128B
+                                                 : CU_TENSOR_MAP_SWIZZLE_NONE;
+  cuuint64_t dims[2] = {(cuuint64_t)inner, (cuuint64_t)outer};
+  cuuint64_t strides[1] = {(cuuint64_t)(ld * 2)};
+  cuuint32_t box[2] = {(cuuint32_t)box_inner, (cuuint32_t)box_outer};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled (bf16 box) failed (%d): inner=%lld outer=%lld box=%dx%d swizzle=%d", (int)r,
+              (long long)inner, (long long)outer, box_inner, box_outer, swizzle);
+    return FMC_ERR_CUDA;
+  }
+  return FMC_OK;
+}
+
 // 2-D fp32 tensor [outer, inner] (row stride = inner elements), box
 // {box_inner, box_outer}, no swizzle, out-of-range elements read as zero
 int make_tma_map_f32(CUtensorMap* m, const void* base, int64_t inner, int64_t outer, int box_inner, int box_outer) {
@@ -81,16 +112,24 @@ int make_tma_map_f32(CUtensorMap* m, const void* base, int64_t inner, int64_t ou
   return FMC_OK;
 }
 
-// C[m, n] = sum over the split-K slices of part[s * stride + m * ldc + n] (fixed order)
+// C[m', n] = sum over the split-K slices of part[s * stride + m * ldc + n]
+// (fixed order), m' = m or its image under the row map (rmap_grp > 0: row m
+// goes to (m / grp) * keep + m % grp, dropped when m % grp >= keep)
 __global__ void k_splitk_reduce(const float* __restrict__ part, int splits, int64_t stride, int64_t M, int n_store,
-                                int64_t ldc, float* __restrict__ C) {
+                                int64_t ldc, float* __restrict__ C, int rmap_grp, int rmap_keep) {
   const int64_t tot = M * n_store;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t m = e / n_store, n = e - m * n_store;
+    int64_t mo = m;
+    if (rmap_grp > 0) {
+      const int64_t t = m / rmap_grp, p = m - t * rmap_grp;
+      if (p >= rmap_keep) continue;
+      mo = t * rmap_keep + p;
+    }
     const int64_t o = m * ldc + n;
     float v = 0.f;
     for (int s = 0; s < splits; ++s) v += part[s * stride + o];
-    C[o] = v;
+    C[mo * ldc + n] = v;
   }
 }
 
@@ -157,7 +196,8 @@ static int launch_tc(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& 
   if (splits > 1) {
     int64_t blocks = (M * n_store + 255) / 256;
     if (blocks > (int64_t)sm_count() * 8) blocks = (int64_t)sm_count() * 8;
-    k_splitk_reduce<<<(int)blocks, 256, 0, st>>>(ep.kpart, splits, M * ldc, M, n_store, ldc, (float*)C);
+    k_splitk_reduce<<<(int)blocks, 256, 0, st>>>(ep.kpart, splits, M * ldc, M, n_store, ldc, (float*)C, ep.rmap_grp,
+                                                ep.rmap_keep);
     FMC_LAUNCH_CHECK();
   }
   return FMC_OK;
@@ -242,7 +282,8 @@ bool tc_gemm_stages_output(const void* C, int64_t ldc, int n_store, int64_t M) {
 }
 
 int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K, const uint16_t* B, int N,
-            int rows_b, const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store, int epi, int bn, bool pair) {
+            int rows_b, const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store, int epi, int bn, bool pair,
+            int64_t lda) {
   FMC_CHECK_ARG(K % tc::BK == 0 && K >= tc::BK, "K=%d must be a positive multiple of 64", K);
   FMC_CHECK_ARG(rows_a % tc::BM == 0 && rows_a >= M, "A rows %lld must cover M and be a multiple of 128",
                 (long long)rows_a);
@@ -253,7 +294,8 @@ int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K
   if (M <= 0) return FMC_OK;
   const int BN = (bn == 128 || bn == 256) ? bn : ((N > 128) ? 256 : 128);
   CUtensorMap ma, mb, mc;
-  int rc = make_map(&ma, A, K, rows_a, K, tc::BM);
+  FMC_CHECK_ARG(lda == 0 || lda >= K, "lda %lld < K %d", (long long)lda, K);
+  int rc = make_map(&ma, A, K, rows_a, lda > 0 ? lda : K, tc::BM);
   if (rc) return rc;
   if ((rc = make_map(&mb, B, K, rows_b, K, BN))) return rc;
   // bf16 outputs go out through TMA stores when C can carry a tensor map
@@ -336,7 +378,15 @@ __global__ void k_pack_bf16(FlowGeom g, const float* __restrict__ theta, uint16_
     const int r = (int)(e / cols), c = (int)(e - (int64_t)r * cols);
     float v = 0.f;
     if (!tr && r < out && c < in) v = W[(int64_t)r * in + c];
-    if (tr && r < in && c < out) v = W[(int64_t)c * in + r];
+    if (tr && r < in) {
+      if (i < g.nh) {
+        if (c < out) v = W[(int64_t)c * in + r];
+      } else {
+        // padded d-raw columns: coordinate t at [t * opc, t * opc + P)
+        const int t = c / g.spl_opc, p = c - t * g.spl_opc;
+        if (t < g.nt(l) && p < g.P) v = W[((int64_t)t * g.P + p) * in + r];
+      }
+    }
     dst[e] = f32_to_bf16_rn(v);
   }
 }

@@ -19,6 +19,8 @@ struct EpiArgs {
   int64_t kpart_floats;     //   (the GEMM splits K when the tile grid leaves SMs idle)
   float* colpart;           // mode 2 with TMA stores: column sums of the bf16 output per
   int64_t ldpart;           //   32-row block, row (m / 32) of colpart [ceil(M / 128) * 4, ldpart]
+  int rmap_grp, rmap_keep;  // fp32 modes: output row m goes to (m / grp) * keep + m % grp and is
+                            //   dropped when m % grp >= keep (grp = 0: rows as they are)
 };
 }  // namespace tc
 
@@ -38,6 +40,8 @@ int conditioner_bf16_hidden(const FmcFlow* f, const FlowGeom& g, int l, int64_t 
 // epilogue warps per TMEM lane quarter in the fused spline kernel; each
 // leaves one log-determinant partial per row and coordinate group
 constexpr int kSplineEpiPerQuarter = 3;
+// row parts of the fused spline adjoint's per-tile bias-gradient sums
+constexpr int kSplineBwdRowParts = 3;
 
 // the last Linear of layer l fused with the spline (tc_spline.cu); ldp holds
 // kSplineEpiPerQuarter * n_groups partials per row (partial-major, [parts, M]),
@@ -47,8 +51,10 @@ int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l
 
 // adjoint of layer l's last Linear + spline (tc_spline.cu), recomputing the
 // Linear from A: dL/dx into gxa (every coordinate), dL/draw in bf16 into graw
-// [>= M, ldg] (columns t*P + p, padding up to ldg zeroed), and per-128-row-tile
-// column sums of dL/draw into bpart [ceil(M / 128), nt * P]
+// [>= M, ldg] in the padded layout (coordinate t at columns [t * spl_opc,
+// t * spl_opc + P), zeros up to (t + 1) * spl_opc; columns past draw_cols(l)
+// are not written), and column sums of dL/draw per 128-row tile and row part
+// into bpart [ceil(M / 128) * kSplineBwdRowParts, nt * P]
 int tc_linear_spline_bwd(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l, const uint16_t* A, int64_t M,
                          int64_t rows_a, const float* xa, const float* gy, float gld, float* gxa, uint16_t* graw,
                          int64_t ldg, float* bpart);
@@ -70,7 +76,7 @@ bool tc_gemm_stages_output(const void* C, int64_t ldc, int n_store, int64_t M);
 // bf16 through TMA stores and the tile is 256 columns wide
 int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K, const uint16_t* B, int N,
             int rows_b, const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store, int epi, int bn = 0,
-            bool pair = false);
+            bool pair = false, int64_t lda = 0);
 
 // scratch (floats) that tc_gemm's fp32 mode uses for split-K partials of an
 // M x N x K product when EpiArgs::kpart is given (0: it would not split)

@@ -625,7 +625,15 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
           }
         } else if (row_ok) {
-          float* out = (float*)C + sl * split_stride + (int64_t)gm * ldc + gn0;
+          // fp32 output row: gm, or through the row map of a padded operand
+          // (splits == 1; the split-K reduction applies it otherwise)
+          int64_t orow = gm;
+          if (ep.rmap_grp > 0 && splits == 1) {
+            const int t = gm / ep.rmap_grp, p = gm - t * ep.rmap_grp;
+            if (p >= ep.rmap_keep) return;
+            orow = (int64_t)t * ep.rmap_keep + p;
+          }
+          float* out = (float*)C + sl * split_stride + orow * ldc + gn0;
           if (gn0 + 32 <= n_store && vec_ok) {
             float4* o4 = reinterpret_cast<float4*>(out);
 #pragma unroll

@@ -45,12 +45,12 @@ struct SplineTile {
   static constexpr int P = 3 * K + 1;
   static constexpr int PPC = (P + 7) / 8 * 8;      // accumulator columns per coordinate
   static constexpr int DG = 256 / PPC;
-  static constexpr int DGP = DG * P;               // staged (unpadded) columns of the adjoint
   static constexpr int BN = ((DG * PPC + 15) / 16) * 16;
-  // bf16 row pitch of the adjoint staging tile: an even count whose half is
-  // odd, so the 32 rows a warp touches in one column fall in 32 banks
-  static constexpr int SP = ((DGP + 1) / 2 % 2 == 1) ? ((DGP + 1) / 2) * 2 : ((DGP + 1) / 2 + 1) * 2;
-  static constexpr int STG_BYTES = BM * SP * 2;
+  // the adjoint's d raw: OPC bf16 columns per coordinate (FlowGeom::spl_opc),
+  // one [128 rows][OPC] staging box per coordinate of the group
+  static constexpr int OPC = (P + 7) / 8 * 8;
+  static_assert(OPC / 8 == 1 || OPC / 8 == 2 || OPC / 8 == 4 || (OPC / 8) % 2 == 1, "d-raw box swizzle");
+  static constexpr int STG_BYTES = DG * BM * OPC * 2;
 };
 
 // The first N of the PPC accumulator columns at taddr (a multiple of 8
@@ -409,35 +409,50 @@ struct SplineBwdArgs {
   const float* gy;     // dL/d(layer output), [M, d]
   float gld;           // dL/d(log-determinant), the same for every row
   float* gxa;          // dL/d(spline input), [M, d]; conditioning coordinates copied from gy
-  uint16_t* graw;      // bf16 [>= M, ldg] row-major; columns [nt*P, ldg) are zeroed
-  int64_t ldg;
-  float* bpart;        // [m_tiles, nt*P] column sums of each 128-row tile
+  float* bpart;        // [m_tiles * kSplineBwdRowParts, nt*P] column sums of each 128-row tile, by row part
   int d, nt, tpar, cpar;
 };
+
+// Shared-memory position of 16-byte chunk j of row r in a d-raw staging box
+// (OPC bf16 per row): the chunk order the box's TMA swizzle expects, so the
+// 32 rows of a warp land in distinct banks -- none for an odd number of
+// chunks per row, 32-byte swizzle for two, 64-byte swizzle for four.
+template <int OCH>
+__device__ __forceinline__ int draw_chunk(int r, int j) {
+  if constexpr (OCH == 2) return j ^ ((r >> 2) & 1);
+  if constexpr (OCH == 4) return j ^ ((r >> 1) & 3);
+  return j;
+}
 
 // With x_tma the group's column span of x and of dL/dy for a 128-row tile
 // arrive as two TMA boxes (loaded one tile ahead, two buffers each), the
 // adjoint is written into the dL/dy box in place -- its conditioning columns
 // keep dL/dy, which is their dL/dx -- and the box is stored to gxa. Each tile
-// owns its rows' column span, as in the forward kernel.
+// owns its rows' column span, as in the forward kernel. d raw of coordinate t
+// is staged as a [128 rows][OPC] box (its P values, zeros up to OPC) and
+// stored by TMA to columns [t * OPC, (t + 1) * OPC) of graw (tmR).
 template <int KB, int STAGES>
 __global__ void __launch_bounds__(kSplThreads, 1)
     k_tc_spline_bwd(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                     const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmGy,
-                    const __grid_constant__ CUtensorMap tmGx, int x_tma, int M, int n_groups, int K,
-                    const SplineBwdArgs a, SplineCfg cfg, int* err) {
+                    const __grid_constant__ CUtensorMap tmGx, const __grid_constant__ CUtensorMap tmR, int x_tma,
+                    int M, int n_groups, int K, const SplineBwdArgs a, SplineCfg cfg, int* err) {
   using T = SplineTile<KB>;
-  constexpr int P = T::P, DG = T::DG, DGP = T::DGP, BN = T::BN, SP = T::SP, E = kSplineEpiPerQuarter;
-  static_assert(DGP % 2 == 0 && SP % 2 == 0, "group column spans and the staging pitch move as 32-bit words");
+  constexpr int P = T::P, DG = T::DG, BN = T::BN, E = kSplineEpiPerQuarter;
+  constexpr int OPC = T::OPC, OCH = OPC / 8, OBOX = BM * OPC * 2;
+  constexpr int CP = DG * OPC / 2;                 // column pairs of a group's staged boxes
+  constexpr int RP = kSplineBwdRowParts;
+  constexpr int RROWS = (BM + RP - 1) / RP;        // rows per column-sum part
+  static_assert(RP * CP <= kSplEpiThreads, "one thread per column pair and row part");
   constexpr int XS = 2 * DG;   // floats per row of a box
   using S = Smem<BN, STAGES>;
   if (tc_skip(err)) return;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  // staging tile after the ring and its barriers, then the boxes
-  uint16_t* stg = (uint16_t*)(base + STAGES * S::STAGE_BYTES + 256);
+  // staging boxes 1024 bytes after the ring (the barrier block between), then the x / dL/dy boxes
+  uint8_t* stg = base + STAGES * S::STAGE_BYTES + 1024;
   uint64_t* xfull = (uint64_t*)(base + STAGES * S::STAGE_BYTES + 192);   // [2], in the barrier block
-  float* boxes = (float*)((((uintptr_t)(stg + BM * SP)) + 127) & ~(uintptr_t)127);   // [2][x | dL/dy]
+  float* boxes = (float*)(stg + DG * OBOX);                                 // [2][x | dL/dy]
   if (threadIdx.x == 0) {
     mbar_init(&xfull[0], 1);
     mbar_init(&xfull[1], 1);   // pipe_setup's fence and barrier publish these
@@ -457,7 +472,6 @@ __global__ void __launch_bounds__(kSplThreads, 1)
     const int h = (warp - 2) >> 2;
     const int row = q * 32 + lane;
     const int et = threadIdx.x - 64;   // 0 .. kSplEpiThreads-1
-    const int ew = et >> 5;
     const bool xt = x_tma != 0;
     const bool elect = warp == 2 && lane == 0;   // issues the boxes' copies
     constexpr uint32_t kBox = BM * XS;           // floats per box
@@ -482,9 +496,8 @@ __global__ void __launch_bounds__(kSplThreads, 1)
       float* xb = boxes + (2 * b) * kBox;
       float* gb = xb + kBox;
       if (xt && elect) {
-        // the next tile's boxes go into the other buffers once the previous
-        // tile's store has finished reading them
-        bulk_wait_read_0();
+        // the next tile's boxes go into the other buffers (every earlier
+        // store finished reading shared memory at the end of the last tile)
         const int tn = t + (int)gridDim.x;
         if (tn < tiles) {
           load_boxes(tn, b ^ 1);
@@ -501,27 +514,34 @@ __global__ void __launch_bounds__(kSplThreads, 1)
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t tb = p.tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * 256);
       const int nu = (a.nt - g * DG) < DG ? (a.nt - g * DG) : DG;   // coordinates in this group
-      const int vc = nu * P;                                         // valid staged columns
 #pragma unroll 1
       for (int u = h; u < nu; u += E) {
         const int tcoord = g * DG + u;
         float raw[P];
         tmem_ld_coord<P, T::PPC>(tb + (uint32_t)(u * T::PPC), raw);
-        uint16_t* srow = stg + row * SP + u * P;
+        uint16_t ov[OPC];   // this row's d raw of coordinate u, zeros past P
+#pragma unroll
+        for (int i = 0; i < OPC; ++i) ov[i] = 0;
         if (row_ok) {
           const float* bb = a.bias + (int64_t)tcoord * P;
 #pragma unroll
           for (int i = 0; i < P; ++i) raw[i] += __ldg(bb + i);
           if (xt) {
             const int jb = row * XS + 2 * u + a.tpar;
-            gb[jb] = rqs_fwd_adjoint_fast<KB>(raw, xb[jb], gb[jb], a.gld, cfg, srow);
+            gb[jb] = rqs_fwd_adjoint_fast<KB>(raw, xb[jb], gb[jb], a.gld, cfg, ov);
           } else {
             const int64_t j = (int64_t)gm * a.d + 2 * tcoord + a.tpar;
-            a.gxa[j] = rqs_fwd_adjoint_fast<KB>(raw, a.xa[j], a.gy[j], a.gld, cfg, srow);
+            a.gxa[j] = rqs_fwd_adjoint_fast<KB>(raw, a.xa[j], a.gy[j], a.gld, cfg, ov);
           }
-        } else {
+        }
+        // the row's OCH 16-byte chunks into the coordinate's staging box
+        const uint32_t rb = smem_u32(stg + u * OBOX + row * (OPC * 2));
 #pragma unroll
-          for (int i = 0; i < P; ++i) srow[i] = 0;
+        for (int j = 0; j < OCH; ++j) {
+          uint32_t w4[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) w4[k] = (uint32_t)ov[8 * j + 2 * k] | ((uint32_t)ov[8 * j + 2 * k + 1] << 16);
+          st_shared_v4(rb + (uint32_t)(draw_chunk<OCH>(row, j) * 16), w4[0], w4[1], w4[2], w4[3]);
         }
       }
       release_acc(p, b, lane);
@@ -532,55 +552,46 @@ __global__ void __launch_bounds__(kSplThreads, 1)
           a.gxa[j] = a.gy[j];
         }
       }
-      if (xt) fence_proxy_async_smem();   // the box's generic writes, before the store reads it
+      // the staged boxes' generic writes, before the copy engine reads them
+      fence_proxy_async_smem();
       epi_sync(1);
-      if (xt && elect) {
-        tma_store_2d_f32(&tmGx, smem_u32(gb), 2 * g * DG, m0);
+      if (elect) {
+        if (xt) tma_store_2d_f32(&tmGx, smem_u32(gb), 2 * g * DG, m0);
+        for (int u = 0; u < nu; ++u) tma_store_2d(&tmR, smem_u32(stg + u * OBOX), (g * DG + u) * OPC, m0);
         bulk_commit();
       }
-      // row-major copy: the group's columns are contiguous in [t*P + p] order
-      // (an even count per group, so every row segment starts on a 4-byte
-      // boundary and moves as 32-bit words); the last group also zeroes the
-      // padding columns up to ldg
-      {
-        const int64_t c0 = (int64_t)g * DGP;
-        const int width = (g == n_groups - 1) ? (int)(a.ldg - c0) : vc;
-        for (int r = ew; r < BM && m0 + r < M; r += kSplEpiWarps) {
-          uint32_t* dst = reinterpret_cast<uint32_t*>(a.graw + (int64_t)(m0 + r) * a.ldg + c0);
-          const uint32_t* src = reinterpret_cast<const uint32_t*>(stg + r * SP);
-          for (int c2 = lane; 2 * c2 < width; c2 += 32) {
-            const int c = 2 * c2;
-            uint32_t w = 0u;
-            if (c + 1 < vc)
-              w = src[c2];
-            else if (c < vc)
-              w = src[c2] & 0xffffu;
-            dst[c2] = w;
+      // column sums of d raw over the tile's rows (rows >= M were staged as
+      // zeros), while the stores read the same boxes: thread e takes column
+      // pair cp = e % CP of the group's boxes over row part e / CP, in row order
+      if (et < RP * CP) {
+        const int cp = et % CP, part = et / CP;
+        const int u = cp / (OPC / 2), p2 = cp - u * (OPC / 2);
+        if (u < nu && 2 * p2 < P) {
+          const uint8_t* box = stg + u * OBOX;
+          const int j = (2 * p2) >> 3, wofs = ((2 * p2) & 7) * 2;
+          float s0 = 0.f, s1 = 0.f;
+          const int r1 = (part + 1) * RROWS < BM ? (part + 1) * RROWS : BM;
+#pragma unroll 4
+          for (int r = part * RROWS; r < r1; ++r) {
+            const uint32_t v =
+                *reinterpret_cast<const uint32_t*>(box + r * (OPC * 2) + draw_chunk<OCH>(r, j) * 16 + wofs);
+            s0 += __uint_as_float(v << 16);
+            s1 += __uint_as_float(v & 0xffff0000u);
           }
+          float* dst = a.bpart + (int64_t)(mt * RP + part) * ntP + (int64_t)(g * DG + u) * P + 2 * p2;
+          dst[0] = s0;
+          if (2 * p2 + 1 < P) dst[1] = s1;
         }
       }
-      // column sums over the tile's 128 rows (rows >= M were staged as zeros):
-      // thread e takes columns 2e, 2e+1, reading one 32-bit word per row
-      // (consecutive threads, consecutive words: no bank conflicts), in row order
-      for (int c2 = et; 2 * c2 < vc; c2 += kSplEpiThreads) {
-        const uint32_t* src = reinterpret_cast<const uint32_t*>(stg) + c2;
-        float s0 = 0.f, s1 = 0.f;
-#pragma unroll 8
-        for (int r = 0; r < BM; ++r) {
-          const uint32_t v = src[r * (SP / 2)];
-          s0 += __uint_as_float(v << 16);
-          s1 += __uint_as_float(v & 0xffff0000u);
-        }
-        const int64_t col = (int64_t)g * DGP + 2 * c2;
-        a.bpart[(int64_t)mt * ntP + col] = s0;
-        if (2 * c2 + 1 < vc) a.bpart[(int64_t)mt * ntP + col + 1] = s1;
-      }
-      epi_sync(2);   // the staging tile is free again
+      // the boxes are free again once the stores have read them
+      if (elect) bulk_wait_read_0();
+      epi_sync(2);
     }
-    if (xt && elect) {
+    if (elect) {
       bulk_wait_all();   // the stores have completed before the CTA exits
       // boxes loaded for tiles the loop did not finish (after an abort) land first (bounded)
-      for (int k = local; k < issued; ++k) mbar_wait(&xfull[k & 1], (uint32_t)(k >> 1) & 1u);
+      if (xt)
+        for (int k = local; k < issued; ++k) mbar_wait(&xfull[k & 1], (uint32_t)(k >> 1) & 1u);
     }
   }
   pipe_teardown(p, warp, lane, err);
@@ -845,6 +856,8 @@ __global__ void k_ld_reduce(const float* __restrict__ ldp, int n_part, int64_t m
 int tc_error_word(int** out);
 int make_tma_map_bf16(CUtensorMap* m, const void* base, int64_t inner, int64_t outer, int64_t ld, int box_outer);
 int make_tma_map_f32(CUtensorMap* m, const void* base, int64_t inner, int64_t outer, int box_inner, int box_outer);
+int make_tma_map_bf16_box(CUtensorMap* m, const void* base, int64_t inner, int64_t outer, int64_t ld, int box_inner,
+                          int box_outer, int swizzle);
 
 int spline_groups(int K_bins, int nt, int* dg, int* bn) {
   const int P = 3 * K_bins + 1, PP = (P + 7) / 8 * 8;
@@ -946,19 +959,26 @@ static int launch_spl_tiles(bool pair, cudaStream_t st, const CUtensorMap& ma, c
 
 template <int KB>
 static int launch_spl_bwd(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& mb, int64_t M, int n_groups,
-                          int K, const tc::SplineBwdArgs& a, SplineCfg cfg) {
+                          int K, const tc::SplineBwdArgs& a, uint16_t* graw, int64_t ldg, SplineCfg cfg) {
   constexpr int STAGES = 3;
   using T = tc::SplineTile<KB>;
   using S = tc::Smem<T::BN, STAGES>;
-  constexpr int TOTAL = S::TOTAL + T::STG_BYTES;
-  static_assert(TOTAL <= 227 * 1024, "fused spline adjoint: shared memory over the per-CTA limit");
+  // ring, slack and barrier block (S::TOTAL), the rest of a 1024-byte block, the staging boxes
+  constexpr int TOTAL = S::TOTAL + 768 + T::STG_BYTES;
+  static_assert(TOTAL + 16 <= 227 * 1024, "fused spline adjoint: shared memory over the per-CTA limit");
   // x and dL/dy boxes (two buffers each) when the row stride allows tensor maps and they fit
   constexpr int BOXES = 128 + 4 * tc::BM * 2 * T::DG * (int)sizeof(float);
   CUtensorMap mx, mgy, mgx;
   memset(&mx, 0, sizeof(mx));
   memset(&mgy, 0, sizeof(mgy));
   memset(&mgx, 0, sizeof(mgx));
-  int x_tma = TOTAL + BOXES <= 227 * 1024 && make_tma_map_f32(&mx, a.xa, a.d, M, 2 * T::DG, tc::BM) == FMC_OK &&
+  // d raw: one box {OPC, 128} per coordinate, swizzled as the staging is
+  CUtensorMap mr;
+  constexpr int och = T::OPC / 8;
+  const int swz = och == 2 ? 32 : och == 4 ? 64 : 0;
+  int rc = make_tma_map_bf16_box(&mr, graw, ldg, M, ldg, T::OPC, tc::BM, swz);
+  if (rc) return rc;
+  int x_tma = TOTAL + BOXES + 16 <= 227 * 1024 && make_tma_map_f32(&mx, a.xa, a.d, M, 2 * T::DG, tc::BM) == FMC_OK &&
               make_tma_map_f32(&mgy, a.gy, a.d, M, 2 * T::DG, tc::BM) == FMC_OK &&
               make_tma_map_f32(&mgx, a.gxa, a.d, M, 2 * T::DG, tc::BM) == FMC_OK;
   const int total = TOTAL + (x_tma ? BOXES : 0);
@@ -969,12 +989,12 @@ static int launch_spl_bwd(cudaStream_t st, const CUtensorMap& ma, const CUtensor
     attr = total;
   }
   int* err = nullptr;
-  int rc = tc_error_word(&err);
-  if (rc) return rc;
+  if ((rc = tc_error_word(&err))) return rc;
   const int64_t tiles = (M + tc::BM - 1) / tc::BM * n_groups;
   const int64_t grid = tiles < sm_count() ? tiles : sm_count();
   note_grid(FMC_KT_TC_SPLINE_BWD, (int)grid, 1);
-  kern<<<(unsigned)grid, tc::kSplThreads, total, st>>>(ma, mb, mx, mgy, mgx, x_tma, (int)M, n_groups, K, a, cfg, err);
+  kern<<<(unsigned)grid, tc::kSplThreads, total, st>>>(ma, mb, mx, mgy, mgx, mr, x_tma, (int)M, n_groups, K, a, cfg,
+                                                       err);
   FMC_LAUNCH_CHECK();
   return FMC_OK;
 }
@@ -1039,7 +1059,7 @@ int tc_linear_spline_bwd(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, i
   int dg, bn;
   const int n_groups = spline_groups(g.K, nt, &dg, &bn);
   const int Kd = g.w16_cols(l, g.nh);
-  FMC_CHECK_ARG(ldg >= (int64_t)nt * g.P && ldg % 2 == 0, "graw leading dimension too small or odd");
+  FMC_CHECK_ARG(ldg >= g.draw_cols(l) && ldg % 8 == 0, "graw leading dimension too small or not a multiple of 8");
   CUtensorMap ma, mb;
   int rc = make_tma_map_bf16(&ma, A, Kd, rows_a, Kd, tc::BM);
   if (rc) return rc;
@@ -1050,8 +1070,6 @@ int tc_linear_spline_bwd(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, i
   a.gy = gy;
   a.gld = gld;
   a.gxa = gxa;
-  a.graw = graw;
-  a.ldg = ldg;
   a.bpart = bpart;
   a.d = g.d;
   a.nt = nt;
@@ -1065,7 +1083,7 @@ int tc_linear_spline_bwd(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, i
   KernelTimer kt(FMC_KT_TC_SPLINE_BWD, st, flops, bytes);
 #define SPL_CASE(k)                                                  \
   if (g.K == k) {                                                    \
-    rc = launch_spl_bwd<k>(st, ma, mb, M, n_groups, Kd, a, g.cfg);   \
+    rc = launch_spl_bwd<k>(st, ma, mb, M, n_groups, Kd, a, graw, ldg, g.cfg);   \
   } else
   FMC_SPLINE_BINS(SPL_CASE) {
     set_error("n_bins=%d is not instantiated for the fused spline", g.K);
