@@ -357,27 +357,44 @@ __device__ __forceinline__ void rqs_apply_fast(const float (&raw)[3 * K + 1], fl
   float ew[K], eh[K], sw, sh;
   softmax_weights<K>(raw, ew, eh, sw, sh);
   const float scale = (c.rmax - c.rmin) - (float)K * c.min_bin;
-  const float fw = __fdividef(scale, sw), fh = __fdividef(scale, sh);
-  // knot k = rmin + (sum of the first k weights) * f + k * min_bin; bin 0 by
-  // default (also covers v below the range)
-  float cw = 0.f, ch = 0.f, bw = 0.f, bh = 0.f, ebw = ew[0], ebh = eh[0], kbf = 0.f;
+  const float isw = __fdividef(1.f, sw), ish = __fdividef(1.f, sh), iscale = __fdividef(1.f, scale);
+  const float fw = scale * isw, fh = scale * ish;   // knot spacing per unit of softmax weight
+  // knot k = rmin + f * (sum_{j<k} e_j + k * min_bin / f) = rmin + f * (sum_{j<k} e'_j)
+  // with e'_j = e_j + min_bin / f: the bin is found by comparing the running
+  // sums of e' with (v - rmin) / f (no per-knot multiply), its left knots are
+  // rmin + f * (the sums before it) and its width and height f * e'_bin. Bin 0
+  // by default (also covers v below the range).
+  const float dw = c.min_bin * sw * iscale, dh = c.min_bin * sh * iscale;
+  float ewp[K], ehp[K];
+#pragma unroll
+  for (int k = 0; k + 1 < K; k += 2) {
+    f2_unpack(f2_add(f2_pack(ew[k], ew[k + 1]), f2_pack(dw, dw)), ewp[k], ewp[k + 1]);
+    f2_unpack(f2_add(f2_pack(eh[k], eh[k + 1]), f2_pack(dh, dh)), ehp[k], ehp[k + 1]);
+  }
+  if (K & 1) {
+    ewp[K - 1] = ew[K - 1] + dw;
+    ehp[K - 1] = eh[K - 1] + dh;
+  }
+  const float a = (v - c.rmin) * (INV ? sh : sw) * iscale;
+  float cw = 0.f, ch = 0.f, bw = 0.f, bh = 0.f, ebw = ewp[0], ebh = ehp[0];
   float r0 = raw[2 * K], r1 = raw[2 * K + 1];
+  bool last = false;   // the bin is the last one, whose right knot is exactly rmax
 #pragma unroll
   for (int k = 1; k < K; ++k) {
-    cw += ew[k - 1];
-    ch += eh[k - 1];
-    const float kn = INV ? fmaf(ch, fh, fmaf((float)k, c.min_bin, c.rmin)) : fmaf(cw, fw, fmaf((float)k, c.min_bin, c.rmin));
-    if (v >= kn) {
-      bw = cw; bh = ch; ebw = ew[k]; ebh = eh[k]; kbf = (float)k;
+    cw += ewp[k - 1];
+    ch += ehp[k - 1];
+    const bool in = (INV ? ch : cw) <= a;
+    if (in) {
+      bw = cw; bh = ch; ebw = ewp[k]; ebh = ehp[k];
       r0 = raw[2 * K + k];
       r1 = raw[2 * K + k + 1];
     }
+    if (k == K - 1) last = in;
   }
-  const float x0 = fmaf(bw, fw, fmaf(kbf, c.min_bin, c.rmin));
-  const float y0 = fmaf(bh, fh, fmaf(kbf, c.min_bin, c.rmin));
-  const bool last = kbf == (float)(K - 1);   // the last knot is exactly rmax
-  const float w = last ? c.rmax - x0 : fmaf(ebw, fw, c.min_bin);
-  const float h = last ? c.rmax - y0 : fmaf(ebh, fh, c.min_bin);
+  const float x0 = fmaf(bw, fw, c.rmin);
+  const float y0 = fmaf(bh, fh, c.rmin);
+  const float w = last ? c.rmax - x0 : ebw * fw;
+  const float h = last ? c.rmax - y0 : ebh * fh;
   const float d0 = softplus_fast(r0 + c.slope_offset) + c.min_slope;
   const float d1 = softplus_fast(r1 + c.slope_offset) + c.min_slope;
   const float s = __fdividef(h, w);

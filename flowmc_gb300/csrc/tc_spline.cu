@@ -54,9 +54,9 @@ struct SplineTile {
 };
 
 // The first N of the PPC accumulator columns at taddr (a multiple of 8
-// columns), read with 8-column loads (tcgen05.ld .32x32b.x8, each at an
-// 8-aligned column); every register is pinned after the wait so no use can be
-// scheduled before the data arrive.
+// columns), read with 32- and 8-column loads (tcgen05.ld .32x32b.x32 / .x8 at
+// 8-aligned columns); every register is pinned after the wait so no use can
+// be scheduled before the data arrive.
 template <int N, int PPC>
 __device__ __forceinline__ void tmem_ld_coord(uint32_t taddr, float (&v)[N]) {
   static_assert(N <= PPC, "column pitch");
@@ -74,8 +74,22 @@ __device__ __forceinline__ void tmem_ld_coord(uint32_t taddr, float (&v)[N]) {
     }
     return;
   }
+  // 32-column loads while 32 columns remain, then 8-column loads
+  constexpr int N32 = PPC / 32 * 32;
 #pragma unroll
-  for (int i = 0; i < PPC; i += 8)
+  for (int i = 0; i < N32; i += 32)
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[i]), "=r"(r[i + 1]), "=r"(r[i + 2]), "=r"(r[i + 3]), "=r"(r[i + 4]), "=r"(r[i + 5]),
+          "=r"(r[i + 6]), "=r"(r[i + 7]), "=r"(r[i + 8]), "=r"(r[i + 9]), "=r"(r[i + 10]), "=r"(r[i + 11]),
+          "=r"(r[i + 12]), "=r"(r[i + 13]), "=r"(r[i + 14]), "=r"(r[i + 15]), "=r"(r[i + 16]), "=r"(r[i + 17]),
+          "=r"(r[i + 18]), "=r"(r[i + 19]), "=r"(r[i + 20]), "=r"(r[i + 21]), "=r"(r[i + 22]), "=r"(r[i + 23]),
+          "=r"(r[i + 24]), "=r"(r[i + 25]), "=r"(r[i + 26]), "=r"(r[i + 27]), "=r"(r[i + 28]), "=r"(r[i + 29]),
+          "=r"(r[i + 30]), "=r"(r[i + 31])
+        : "r"(taddr + (uint32_t)i));
+#pragma unroll
+  for (int i = N32; i < PPC; i += 8)
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
                  : "=r"(r[i]), "=r"(r[i + 1]), "=r"(r[i + 2]), "=r"(r[i + 3]), "=r"(r[i + 4]), "=r"(r[i + 5]),
                    "=r"(r[i + 6]), "=r"(r[i + 7])
