@@ -205,13 +205,13 @@ static int launch_tc(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& 
 
 // the CTA-pair form (bf16 outputs through TMA stores): 256-row tiles, a
 // persistent grid of as many clusters of 2 as can be resident
-template <int BN, int STAGES, int EPI>
+template <int BN, int STAGES, int EPI, int NSTG = 2>
 static int launch_tc_pair(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap& mc,
                           int64_t M, int N, int K, const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store) {
   using S = tc::Smem<BN / 2, STAGES>;
-  constexpr int TOTAL = S::TOTAL + 768 + tc::staging_bytes(2);
-  static_assert(TOTAL + 1024 + 16 <= 227 * 1024, "tcgen05 GEMM: shared memory over the per-CTA limit");
-  auto kern = tc::k_tc_gemm<BN, STAGES, EPI, true, true>;
+  constexpr int TOTAL = S::TOTAL + 768 + tc::staging_bytes(NSTG);
+  static_assert(TOTAL + (NSTG == 2 ? 1024 : 0) + 16 <= 227 * 1024, "tcgen05 GEMM: shared memory over the per-CTA limit");
+  auto kern = tc::k_tc_gemm<BN, STAGES, EPI, true, true, NSTG>;
   static bool attr_set = false;
   if (!attr_set) {
     FMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, TOTAL));
@@ -309,6 +309,15 @@ int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K
   if (pair && tstore && BN == 256) {
     // B in boxes of half the tile's rows: each CTA of a pair loads one half
     if ((rc = make_map(&mb, B, K, rows_b, K, BN / 2))) return rc;
+    // a pair stage holds half the B rows (32 KB with A): six stages and one
+    // staging buffer per warp where a tile takes several K blocks (deeper
+    // prefetch for the same shared memory), four and two otherwise
+    if (K >= 4 * tc::BK) {
+      if (epi == tc::TC_EPI_TANH_BF16)
+        return launch_tc_pair<256, 6, tc::TC_EPI_TANH_BF16, 1>(st, ma, mb, mc, M, N, K, ep, C, ldc, n_store);
+      if (epi == tc::TC_EPI_DTANH_BF16)
+        return launch_tc_pair<256, 6, tc::TC_EPI_DTANH_BF16, 1>(st, ma, mb, mc, M, N, K, ep, C, ldc, n_store);
+    }
     if (epi == tc::TC_EPI_TANH_BF16)
       return launch_tc_pair<256, 4, tc::TC_EPI_TANH_BF16>(st, ma, mb, mc, M, N, K, ep, C, ldc, n_store);
     if (epi == tc::TC_EPI_DTANH_BF16)
