@@ -241,24 +241,30 @@ __global__ void k_init_gy(const float* __restrict__ y, int64_t tot, int d, const
 }
 
 // adjoint of xa = (x + t) e^s and of the conditioning gather;
-// writes d x and per-block partial sums of d t and (sum gxa * xa)
+// writes d x and per-block partial sums of d t and (sum gxa * xa). One warp
+// per row (lanes over the coordinates), rows strided over the grid.
 __global__ void __launch_bounds__(256) k_affine_bwd(const float* __restrict__ gxa, const float* __restrict__ gcond,
                                                     const float* __restrict__ xa, int64_t n, int d, int nc, int cpar,
                                                     const float* __restrict__ th_layer, float* __restrict__ gx,
                                                     float* __restrict__ part) {
   __shared__ float sh[32];
   const float es = expf(th_layer[0]);
-  const int64_t tot = n * d;
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   float st = 0.f, ss = 0.f;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = i / d;
-    const int j = (int)(i - r * d);
-    float g = gxa[i];
-    if ((j & 1) == cpar) g += gcond[r * nc + (j >> 1)];
-    const float gv = g * es;
-    gx[i] = gv;
-    st += gv;
-    ss += g * xa[i];
+  for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < n; r += warps) {
+    const float* gr = gxa + r * d;
+    const float* xr = xa + r * d;
+    const float* cr = gcond + r * nc;
+    float* out = gx + r * d;
+    for (int j = lane; j < d; j += 32) {
+      float g = gr[j];
+      if ((j & 1) == cpar) g += cr[j >> 1];
+      const float gv = g * es;
+      out[j] = gv;
+      st += gv;
+      ss += g * xr[j];
+    }
   }
   st = block_sum<256>(st, sh);
   ss = block_sum<256>(ss, sh);
@@ -268,15 +274,24 @@ __global__ void __launch_bounds__(256) k_affine_bwd(const float* __restrict__ gx
   }
 }
 
+// the ScalarAffine's two gradients from the nb block partials: one warp,
+// lane i summing partials i, i + 32, ..., then a fixed-order butterfly
 __global__ void k_affine_param_grad(const float* __restrict__ part, int nb, float ld_term, float* __restrict__ g_layer) {
-  if (threadIdx.x != 0) return;
+  const int lane = threadIdx.x & 31;
   float st = 0.f, ss = 0.f;
-  for (int b = 0; b < nb; ++b) {
+  for (int b = lane; b < nb; b += 32) {
     st += part[2 * b];
     ss += part[2 * b + 1];
   }
-  g_layer[0] = ss + ld_term;  // d/d scale
-  g_layer[1] = st;            // d/d shift
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    st += __shfl_xor_sync(0xffffffffu, st, o);
+    ss += __shfl_xor_sync(0xffffffffu, ss, o);
+  }
+  if (threadIdx.x == 0) {
+    g_layer[0] = ss + ld_term;  // d/d scale
+    g_layer[1] = st;            // d/d shift
+  }
 }
 
 static int ew_blocks(int64_t tot) {
