@@ -107,25 +107,57 @@ __global__ void k_affine(const float* __restrict__ in, float* __restrict__ out, 
   const bool v4 = (d % 4 == 0) && 2 * nc == d && ((uintptr_t)in & 15) == 0 && ((uintptr_t)out & 15) == 0 &&
                   (cond == nullptr || ((uintptr_t)cond & 7) == 0) &&
                   (cond16 == nullptr || (((uintptr_t)cond16 & 3) == 0 && (ldc16 & 1) == 0));
-  for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < n; r += warps) {
+  // one float4 of row r (coordinates 4q .. 4q + 3): out, and the two
+  // conditioning ones among them (4q + cpar, 4q + 2 + cpar = conditioning 2q, 2q + 1)
+  auto put4 = [&](int64_t r, int q, float4 a) {
+    float4 o;
+    o.x = inverse ? a.x * es - t : (a.x + t) * es;   // common.py:229, 238
+    o.y = inverse ? a.y * es - t : (a.y + t) * es;
+    o.z = inverse ? a.z * es - t : (a.z + t) * es;
+    o.w = inverse ? a.w * es - t : (a.w + t) * es;
+    reinterpret_cast<float4*>(out + r * d)[q] = o;
+    const float c0 = cpar ? o.y : o.x, c1 = cpar ? o.w : o.z;
+    if (cond != nullptr) reinterpret_cast<float2*>(cond + r * nc)[q] = make_float2(c0, c1);
+    if (cond16 != nullptr)
+      reinterpret_cast<uint32_t*>(cond16 + r * ldc16)[q] =
+          (uint32_t)f32_to_bf16_rn(c0) | ((uint32_t)f32_to_bf16_rn(c1) << 16);
+  };
+  auto row_tail = [&](int64_t r) {
+    if (cond16 != nullptr)
+      for (int c = nc + lane; c < ldc16; c += 32) cond16[r * ldc16 + c] = 0;
+    if (ld != nullptr && lane == 0) {
+      const float l = (float)d * (inverse ? -s : s);
+      ld[r] = ld_init ? l : ld[r] + l;
+    }
+  };
+  const int64_t first = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (v4 && d <= 128) {
+    // a row is at most one float4 per lane: two rows per iteration, both
+    // loads issued before either is used (more bytes in flight per warp)
+    const int q = lane;
+    const bool lane_on = q < d / 4;
+    for (int64_t r = first; r < n; r += 2 * warps) {
+      const int64_t r1 = r + warps;
+      const bool has1 = r1 < n;
+      float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0;
+      if (lane_on) {
+        a0 = reinterpret_cast<const float4*>(in + r * d)[q];
+        if (has1) a1 = reinterpret_cast<const float4*>(in + r1 * d)[q];
+      }
+      if (lane_on) put4(r, q, a0);
+      row_tail(r);
+      if (has1) {
+        if (lane_on) put4(r1, q, a1);
+        row_tail(r1);
+      }
+    }
+    return;
+  }
+  for (int64_t r = first; r < n; r += warps) {
     const float* ir = in + r * d;
     float* orow = out + r * d;
     if (v4) {
-      for (int q = lane; q < d / 4; q += 32) {
-        const float4 a = reinterpret_cast<const float4*>(ir)[q];
-        float4 o;
-        o.x = inverse ? a.x * es - t : (a.x + t) * es;   // common.py:229, 238
-        o.y = inverse ? a.y * es - t : (a.y + t) * es;
-        o.z = inverse ? a.z * es - t : (a.z + t) * es;
-        o.w = inverse ? a.w * es - t : (a.w + t) * es;
-        reinterpret_cast<float4*>(orow)[q] = o;
-        // coordinates 4q + cpar and 4q + 2 + cpar are conditioning ones 2q, 2q + 1
-        const float c0 = cpar ? o.y : o.x, c1 = cpar ? o.w : o.z;
-        if (cond != nullptr) reinterpret_cast<float2*>(cond + r * nc)[q] = make_float2(c0, c1);
-        if (cond16 != nullptr)
-          reinterpret_cast<uint32_t*>(cond16 + r * ldc16)[q] =
-              (uint32_t)f32_to_bf16_rn(c0) | ((uint32_t)f32_to_bf16_rn(c1) << 16);
-      }
+      for (int q = lane; q < d / 4; q += 32) put4(r, q, reinterpret_cast<const float4*>(ir)[q]);
     } else {
       for (int j = lane; j < d; j += 32) {
         const float v = inverse ? ir[j] * es - t : (ir[j] + t) * es;   // common.py:229, 238
@@ -136,12 +168,7 @@ __global__ void k_affine(const float* __restrict__ in, float* __restrict__ out, 
         }
       }
     }
-    if (cond16 != nullptr)
-      for (int c = nc + lane; c < ldc16; c += 32) cond16[r * ldc16 + c] = 0;
-    if (ld != nullptr && lane == 0) {
-      const float l = (float)d * (inverse ? -s : s);
-      ld[r] = ld_init ? l : ld[r] + l;
-    }
+    row_tail(r);
   }
 }
 

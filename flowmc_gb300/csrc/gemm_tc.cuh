@@ -44,8 +44,9 @@ constexpr int kSplineEpiPerQuarter = 3;
 constexpr int kSplineBwdRowParts = 3;
 
 // the last Linear of layer l fused with the spline (tc_spline.cu); ldp holds
-// kSplineEpiPerQuarter * n_groups partials per row (partial-major, [parts, M]),
-// which are then added to ld
+// up to kSplineEpiPerQuarter * n_groups partials per row (partial-major,
+// [parts, M]; one per group when the kernel stages x in boxes), which are
+// then added to ld
 int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l, const uint16_t* A, int64_t M,
                      int64_t rows_a, bool inverse, float* xa, float* ld, float* ldp);
 

@@ -301,6 +301,7 @@ __global__ void __launch_bounds__(kSplThreads, 1)
   float* sbias = (float*)(base + STAGES * S::STAGE_BYTES + 256);   // after the ring and its barriers
   uint64_t* xfull = (uint64_t*)(base + STAGES * S::STAGE_BYTES + 192);   // [2], in the barrier block
   float* xbuf = (float*)((((uintptr_t)(sbias + (bias_smem ? nt * PP : 0))) + 127) & ~(uintptr_t)127);
+  float* lred = xbuf + 2 * BM * XS;   // [2][E][BM] log-det partials of a tile (x boxes only)
   if (bias_smem) {
     for (int i = threadIdx.x; i < nt * PP; i += blockDim.x) {
       const int t = i / PP, pp = i - t * PP;
@@ -394,7 +395,15 @@ __global__ void __launch_bounds__(kSplThreads, 1)
           ldsum += l;
         }
       }
-      if (gm < M) ldp[(int64_t)(E * g + h) * M + gm] = ldsum;   // partial-major: a warp writes 128 contiguous bytes
+      // log-det partials: with the x boxes the quarter's E warps add theirs
+      // in shared memory (two tile-parity buffers: a warp may start the next
+      // tile while warp 0 of its quarter still reads this one) and one
+      // partial per group and row is written; otherwise one per warp.
+      // Partial-major: a warp writes 128 contiguous bytes.
+      if (xt)
+        lred[(b * E + h) * BM + row] = ldsum;
+      else if (gm < M)
+        ldp[(int64_t)(E * g + h) * M + gm] = ldsum;
       release_acc(p, b, lane);
       if (xt) {
         // y is in the buffer: make the writes visible to the copy engine, then
@@ -404,6 +413,12 @@ __global__ void __launch_bounds__(kSplThreads, 1)
         if (elect) {
           tma_store_2d_f32(&tmX, smem_u32(xb), 2 * g * DG, m0);
           bulk_commit();
+        }
+        if (h == 0 && gm < M) {
+          float sl = 0.f;
+#pragma unroll
+          for (int k = 0; k < E; ++k) sl += lred[(b * E + k) * BM + row];
+          ldp[(int64_t)g * M + gm] = sl;
         }
       }
     }
@@ -883,7 +898,7 @@ int spline_groups(int K_bins, int nt, int* dg, int* bn) {
 
 template <int KB, bool INV>
 static int launch_spl(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& mb, int64_t M, int n_groups, int nt,
-                      int K, const float* bias, float* xa, int d, int tpar, float* ldp, SplineCfg cfg) {
+                      int K, const float* bias, float* xa, int d, int tpar, float* ldp, SplineCfg cfg, int* parts) {
   constexpr int STAGES = 4;
   using T = tc::SplineTile<KB>;
   using S = tc::Smem<T::BN, STAGES>;
@@ -891,7 +906,9 @@ static int launch_spl(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap&
   // the ring, its barriers, (when they fit) the layer's bias rows and the two
   // x boxes (when x's row stride allows a tensor map)
   const size_t bias_bytes = (size_t)nt * tc::BiasRows<KB>::PP * sizeof(float);
-  const size_t x_bytes = 128 + 2 * (size_t)tc::BM * 2 * T::DG * sizeof(float);
+  // the two x boxes and the per-tile log-det partials of the quarter's warps
+  const size_t x_bytes = 128 + 2 * (size_t)tc::BM * 2 * T::DG * sizeof(float) +
+                         2 * (size_t)kSplineEpiPerQuarter * tc::BM * sizeof(float);
   CUtensorMap mx;
   memset(&mx, 0, sizeof(mx));
   int x_tma = make_tma_map_f32(&mx, xa, d, M, 2 * T::DG, tc::BM) == FMC_OK ? 1 : 0;
@@ -914,6 +931,7 @@ static int launch_spl(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap&
   kern<<<(unsigned)grid, tc::kSplThreads, total, st>>>(ma, mb, mx, x_tma, (int)M, n_groups, nt, K, bias, bias_smem,
                                                        xa, d, tpar, ldp, cfg, err);
   FMC_LAUNCH_CHECK();
+  *parts = x_tma ? n_groups : kSplineEpiPerQuarter * n_groups;
   return FMC_OK;
 }
 
@@ -964,11 +982,14 @@ static int launch_spl2(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap
 template <int KB, bool INV>
 static int launch_spl_tiles(bool pair, cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& mb, int64_t M,
                             int n_groups, int nt, int K, const float* bias, float* xa, int d, int tpar, float* ldp,
-                            SplineCfg cfg) {
+                            SplineCfg cfg, int* parts) {
   if constexpr (tc::SplineTile<KB>::BN % 32 == 0) {
-    if (pair) return launch_spl2<KB, INV>(st, ma, mb, M, n_groups, nt, K, bias, xa, d, tpar, ldp, cfg);
+    if (pair) {
+      *parts = kSplineEpiPerQuarter * n_groups;
+      return launch_spl2<KB, INV>(st, ma, mb, M, n_groups, nt, K, bias, xa, d, tpar, ldp, cfg);
+    }
   }
-  return launch_spl<KB, INV>(st, ma, mb, M, n_groups, nt, K, bias, xa, d, tpar, ldp, cfg);
+  return launch_spl<KB, INV>(st, ma, mb, M, n_groups, nt, K, bias, xa, d, tpar, ldp, cfg, parts);
 }
 
 template <int KB>
@@ -1034,6 +1055,7 @@ int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l
   int rc = make_tma_map_bf16(&ma, A, Kd, rows_a, Kd, tc::BM);
   if (rc) return rc;
   if ((rc = make_tma_map_bf16(&mb, Bg, Kd, (int64_t)n_groups * bn, Kd, pair ? bn / 2 : bn))) return rc;
+  int parts = kSplineEpiPerQuarter * n_groups;   // log-det partials per row the launch leaves
   {
     // useful work: the last Linear's nt * P outputs over its H_last inputs,
     // the A rows and the group weights once, x read and written, partials
@@ -1046,9 +1068,9 @@ int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l
   if (g.K == k) {                                                                                            \
     rc = inverse                                                                                             \
              ? launch_spl_tiles<k, true>(pair, st, ma, mb, M, n_groups, nt, Kd, bias, xa, g.d, g.tpar(l), ldp,  \
-                                         g.cfg)                                                              \
+                                         g.cfg, &parts)                                                      \
              : launch_spl_tiles<k, false>(pair, st, ma, mb, M, n_groups, nt, Kd, bias, xa, g.d, g.tpar(l), ldp, \
-                                          g.cfg);                                                            \
+                                          g.cfg, &parts);                                                    \
   } else
     FMC_SPLINE_BINS(SPL_CASE) {
       set_error("n_bins=%d is not instantiated for the fused spline", g.K);
@@ -1059,7 +1081,7 @@ int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l
   if (rc) return rc;
   int64_t blocks = (M + 255) / 256;
   if (blocks > (int64_t)sm_count() * 8) blocks = (int64_t)sm_count() * 8;
-  k_ld_reduce<<<(int)(blocks < 1 ? 1 : blocks), 256, 0, st>>>(ldp, kSplineEpiPerQuarter * n_groups, M, ld);
+  k_ld_reduce<<<(int)(blocks < 1 ? 1 : blocks), 256, 0, st>>>(ldp, parts, M, ld);
   FMC_LAUNCH_CHECK();
   return FMC_OK;
 }

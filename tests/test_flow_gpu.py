@@ -346,9 +346,12 @@ def test_column_stats_matches_numpy(cuda, n, d):
 def test_spline_cta_pair_tiles_match_single_cta(cuda, d, L, hidden, nb):
     """The fused last Linear + spline on CTA pairs (tcgen05 cta_group::2,
     256-row tiles, half the group's weights per CTA) against one-CTA 128-row
-    tiles: the same products in the same K order, so log_prob, forward and
-    inverse agree to float32 rounding (1e-6 relative), at row counts that
-    leave the last pair's second CTA partly or wholly past the end."""
+    tiles: the same products in the same K order, so forward and inverse
+    outputs agree to float32 rounding (1e-6 relative), at row counts that
+    leave the last pair's second CTA partly or wholly past the end. The
+    one-CTA kernel adds its log-det partials per coordinate group before the
+    row reduction (the pair kernel leaves one partial per warp), so log_prob
+    and the log-determinants agree to a summation-order bound, 1e-5."""
     fl = to_f32(rand_flow(d, L, hidden, nb, seed=d + 3 * L, wscale=0.3))
     m = gpu_model(fl, hidden, precision="bf16")
     rng = np.random.default_rng(5)
@@ -362,6 +365,7 @@ def test_spline_cta_pair_tiles_match_single_cta(cuda, d, L, hidden, nb):
             outs[tile] = [m.log_prob(x), y, ld, xi, ldi]
         from flowmc_gb300 import _lib
         assert _lib.device_error() == 0
-        for a, b in zip(outs[128], outs[256]):
-            torch.testing.assert_close(b, a, rtol=1e-6, atol=1e-6)
+        for k, (a, b) in enumerate(zip(outs[128], outs[256])):
+            tol = 1e-6 if k in (1, 3) else 1e-5   # outputs / log-densities and log-dets
+            torch.testing.assert_close(b, a, rtol=tol, atol=tol)
     m.tile_rows = 0
