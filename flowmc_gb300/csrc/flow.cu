@@ -75,21 +75,21 @@ int make_geom(const FmcFlow* f, FlowGeom& g) {
 }
 
 // ------------------------------------------------------------------ kernels
+// one warp per row (lanes over the coordinates, rows strided over the grid):
+// no per-element index division
 __global__ void k_standardize(const float* __restrict__ x, int64_t n, int d, const float* __restrict__ aux,
                               float* __restrict__ out) {
-  const int64_t tot = n * d;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
-    const int j = (int)(i % d);
-    out[i] = (x[i] - aux[j]) / sqrtf(aux[d + j]);
-  }
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < n; r += warps)
+    for (int j = lane; j < d; j += 32) out[r * d + j] = (x[r * d + j] - aux[j]) / sqrtf(aux[d + j]);
 }
 
 __global__ void k_destandardize(float* __restrict__ x, int64_t n, int d, const float* __restrict__ aux) {
-  const int64_t tot = n * d;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
-    const int j = (int)(i % d);
-    x[i] = x[i] * sqrtf(aux[d + j]) + aux[j];
-  }
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < n; r += warps)
+    for (int j = lane; j < d; j += 32) x[r * d + j] = x[r * d + j] * sqrtf(aux[d + j]) + aux[j];
 }
 
 // one warp per row: ScalarAffine of every coordinate, the conditioning

@@ -352,7 +352,21 @@ int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K
 }
 
 // ------------------------------------------------------------------ packing
+// source row of W (fp32 [out, in]) for column c of the transposed copy of
+// Linear i of layer l: c itself, or for the last Linear the padded d-raw
+// column c = t * opc + p (-1 for a padding column)
+__device__ __forceinline__ int wt_src_row(const FlowGeom& g, int l, int i, int c, int out) {
+  if (i < g.nh) return c < out ? c : -1;
+  const int t = c / g.spl_opc, p = c - t * g.spl_opc;
+  return (t < g.nt(l) && p < g.P) ? t * g.P + p : -1;
+}
+
+// Blocks of 256 threads; blockIdx.y selects the segment: W_i (zero padded,
+// one block per row at a time), W_i^T (32 x 32 tiles through shared memory,
+// so both the reads of W and the writes of W^T are coalesced) or the
+// grouped copy of the last Linear.
 __global__ void k_pack_bf16(FlowGeom g, const float* __restrict__ theta, uint16_t* __restrict__ w16) {
+  __shared__ float tile[32][33];
   const int nseg = g.L * (g.nh + 1);
   if ((int)blockIdx.y >= 2 * nseg) {
     // grouped copy of layer l's last Linear for the fused spline kernel
@@ -362,15 +376,14 @@ __global__ void k_pack_bf16(FlowGeom g, const float* __restrict__ theta, uint16_
     const int rows = g.spl_groups(l) * BN;
     const float* W = theta + g.layer_off[l] + g.lin_w(l, i);
     uint16_t* dst = w16 + g.w16g_off[l];
-    const int64_t tot = (int64_t)rows * cols;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
-      const int r = (int)(e / cols), c = (int)(e - (int64_t)r * cols);
+    for (int r = blockIdx.x; r < rows; r += gridDim.x) {
       const int grp = r / BN, rr = r - grp * BN;
       const int u = rr / PP, p = rr - u * PP;
       const int t = grp * DG + u;
-      float v = 0.f;
-      if (u < DG && p < g.P && t < nt && c < in) v = W[((int64_t)t * g.P + p) * in + c];
-      dst[e] = f32_to_bf16_rn(v);
+      const bool live = u < DG && p < g.P && t < nt;
+      const float* src = W + ((int64_t)t * g.P + p) * in;
+      for (int c = threadIdx.x; c < cols; c += blockDim.x)
+        dst[(int64_t)r * cols + c] = f32_to_bf16_rn((live && c < in) ? src[c] : 0.f);
     }
     return;
   }
@@ -378,25 +391,34 @@ __global__ void k_pack_bf16(FlowGeom g, const float* __restrict__ theta, uint16_
   const bool tr = blockIdx.y >= nseg;   // second part of the grid writes W^T
   const int l = seg / (g.nh + 1), i = seg % (g.nh + 1);
   const int out = g.lin_out(l, i), in = g.lin_in(l, i);
-  const int rows = tr ? g.w16t_rows(l, i) : g.w16_rows(l, i);
-  const int cols = tr ? g.w16t_cols(l, i) : g.w16_cols(l, i);
   const float* W = theta + g.layer_off[l] + g.lin_w(l, i);
-  uint16_t* dst = w16 + (tr ? g.w16t_off[seg] : g.w16_off[seg]);
-  const int64_t tot = (int64_t)rows * cols;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
-    const int r = (int)(e / cols), c = (int)(e - (int64_t)r * cols);
-    float v = 0.f;
-    if (!tr && r < out && c < in) v = W[(int64_t)r * in + c];
-    if (tr && r < in) {
-      if (i < g.nh) {
-        if (c < out) v = W[(int64_t)c * in + r];
-      } else {
-        // padded d-raw columns: coordinate t at [t * opc, t * opc + P)
-        const int t = c / g.spl_opc, p = c - t * g.spl_opc;
-        if (t < g.nt(l) && p < g.P) v = W[((int64_t)t * g.P + p) * in + r];
-      }
+  if (!tr) {
+    const int rows = g.w16_rows(l, i), cols = g.w16_cols(l, i);
+    uint16_t* dst = w16 + g.w16_off[seg];
+    for (int r = blockIdx.x; r < rows; r += gridDim.x)
+      for (int c = threadIdx.x; c < cols; c += blockDim.x)
+        dst[(int64_t)r * cols + c] = f32_to_bf16_rn((r < out && c < in) ? W[(int64_t)r * in + c] : 0.f);
+    return;
+  }
+  // W^T [rows = round_up(in, 256), cols]: element (r, c) = W[src(c), r]
+  const int rows = g.w16t_rows(l, i), cols = g.w16t_cols(l, i);
+  uint16_t* dst = w16 + g.w16t_off[seg];
+  const int tr_ = (rows + 31) / 32, tc_ = (cols + 31) / 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8
+  for (int tt = blockIdx.x; tt < tr_ * tc_; tt += gridDim.x) {
+    const int r0 = (tt / tc_) * 32, c0 = (tt % tc_) * 32;
+    // read 32 source rows (columns c0.. of W^T) along r: coalesced
+    for (int k = ty; k < 32; k += 8) {
+      const int sr = wt_src_row(g, l, i, c0 + k, out);
+      const int r = r0 + tx;
+      tile[k][tx] = (sr >= 0 && r < in) ? W[(int64_t)sr * in + r] : 0.f;
     }
-    dst[e] = f32_to_bf16_rn(v);
+    __syncthreads();
+    for (int k = ty; k < 32; k += 8) {
+      const int r = r0 + k, c = c0 + tx;
+      if (r < rows && c < cols) dst[(int64_t)r * cols + c] = f32_to_bf16_rn(tile[tx][k]);
+    }
+    __syncthreads();
   }
 }
 
