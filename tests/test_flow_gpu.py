@@ -307,6 +307,29 @@ def test_flow_bf16_gradient_tracks_autograd(cuda, d, L, hidden, nb, xs):
     assert np.abs(gg - og).max() <= 5e-2 * np.abs(og).max()
 
 
+@pytest.mark.parametrize("n", [40, 64, 200])
+def test_flow_bf16_gradient_small_batches(cuda, n):
+    """BF16 training gradient at batch sizes below and around one 64-row
+    K block of the weight-gradient GEMMs (their MN-major operand maps cover
+    64 rows, the rows past the batch held at zero), after a larger batch has
+    left other values in the workspace rows past n."""
+    from flowmc_gb300 import _lib
+    d, L, hidden, nb = 16, 2, (64, 64), 6
+    fl = to_f32(rand_flow(d, L, hidden, nb, seed=31, wscale=0.3))
+    m = gpu_model(fl, hidden, precision="bf16")
+    rng = np.random.default_rng(8)
+    big = (rng.normal(size=(1000, d)) * 1.5).astype(np.float32)
+    m.loss_and_grad(torch.tensor(big, device="cuda"))
+    x = (rng.normal(size=(n, d)) * 1.5).astype(np.float32)
+    loss, grad = m.loss_and_grad(torch.tensor(x, device="cuda"))
+    assert _lib.device_error() == 0
+    oloss, og = FT.loss_and_grad(fl, x.astype(np.float64))
+    assert abs(loss.item() - oloss) <= 2e-2 * max(1, abs(oloss))
+    gg = gpu_grad_to_full(m, grad)
+    cos = float(gg @ og / (np.linalg.norm(gg) * np.linalg.norm(og)))
+    assert cos > 0.999, cos
+
+
 def test_training_bf16_reduces_loss(cuda):
     from flowmc_gb300.random import PRNGKey
     from flowmc_gb300.resource.model.nf_model.rqSpline import MaskedCouplingRQSpline
