@@ -319,13 +319,12 @@ static int recompute_mlp(const FmcFlow* f, const FlowGeom& g, int l, int64_t n, 
   return FMC_OK;
 }
 
-// BF16 recompute of layer l's conditioner hidden layers: tanh activations in
-// bf16; the last Linear is recomputed inside the fused spline adjoint
+// BF16 recompute of layer l's conditioner hidden layers (from the bf16
+// conditioning block k_affine left in w.cond16): tanh activations in bf16;
+// the last Linear is recomputed inside the fused spline adjoint
 static int recompute_hidden_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t n, TrainWs& w, cudaStream_t st) {
   const float* th = f->theta + g.layer_off[l];
-  const int nc = g.nc(l);
-  int rc = to_bf16_pad_t(st, w.cond, n, nc, w.cond16, FlowGeom::rup(nc, 64), nullptr, 0, 0);
-  if (rc) return rc;
+  int rc = FMC_OK;
   const uint16_t* a = w.cond16;
   for (int i = 0; i < g.nh; ++i) {
     const int seg = l * (g.nh + 1) + i;
@@ -490,11 +489,14 @@ int flow_loss_grad(const FmcFlow* f, const float* x, int64_t n, float* loss, flo
     const float* th = f->theta + g.layer_off[l];
     float* gl = grad + g.layer_off[l];
     const float* xin = w.xs + (int64_t)l * nd;
-    k_affine<<<rb, 256, 0, st>>>(xin, w.xa, w.cond, nullptr, 0, n, d, g.nc(l), g.cpar(l), th, 0, nullptr, 0);
+    // the layer's spline input, and its conditioning block as the first
+    // GEMM's operand (bf16, zero padded) or in fp32
+    k_affine<<<rb, 256, 0, st>>>(xin, w.xa, bf16 ? nullptr : w.cond, bf16 ? w.cond16 : nullptr,
+                                 bf16 ? g.w16_cols(l, 0) : 0, n, d, g.nc(l), g.cpar(l), th, 0, nullptr, 0);
     FMC_LAUNCH_CHECK();
     if (bf16) {
       // hidden activations, then the last Linear recomputed inside the fused
-      // spline adjoint, which leaves d raw in both bf16 operand layouts
+      // spline adjoint, which leaves d raw in the padded bf16 layout
       if ((rc = recompute_hidden_bf16(f, g, l, n, w, st))) return rc;
       const uint16_t* h_last = g.nh > 0 ? w.hs16 + (int64_t)(g.nh - 1) * w.n128 * w.hld : w.cond16;
       if ((rc = tc_linear_spline_bwd(st, g, f, l, h_last, n, w.n128, w.xa, w.gy, gld, w.gxa, w.graw16, w.pld,

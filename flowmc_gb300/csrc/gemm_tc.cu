@@ -430,37 +430,6 @@ int pack_bf16_weights(const FlowGeom& g, const float* theta, uint16_t* w16, cuda
   return FMC_OK;
 }
 
-// fp32 [n, cols] -> bf16 [n, ldd] (zero padded) and/or transposed [ldd.., ldt]
-__global__ void k_to_bf16_pad_t(const float* __restrict__ src, int64_t n, int cols, uint16_t* __restrict__ dst,
-                                int64_t ldd, uint16_t* __restrict__ dstT, int64_t ldt, int64_t t_cols) {
-  __shared__ uint16_t tile[32][33];
-  const int64_t r0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8 threads
-  for (int k = ty; k < 32; k += 8) {
-    const int64_t r = r0 + k, c = c0 + tx;
-    const float v = (r < n && c < cols) ? src[r * cols + c] : 0.f;
-    const uint16_t b = f32_to_bf16_rn(v);
-    tile[k][tx] = b;
-    if (dst && r < n && c < ldd) dst[r * ldd + c] = b;
-  }
-  if (!dstT) return;
-  __syncthreads();
-  for (int k = ty; k < 32; k += 8) {
-    const int64_t c = c0 + k, r = r0 + tx;   // row c of dstT, column r
-    if (c < ldd && r < t_cols) dstT[c * ldt + r] = tile[tx][k];
-  }
-}
-
-int to_bf16_pad_t(cudaStream_t st, const float* src, int64_t n, int cols, uint16_t* dst, int64_t ldd, uint16_t* dstT,
-                  int64_t ldt, int64_t t_cols) {
-  const int64_t rows = dstT ? (t_cols > n ? t_cols : n) : n;
-  dim3 grid((unsigned)((ldd + 31) / 32), (unsigned)((rows + 31) / 32));
-  FMC_CHECK_SUPPORTED(grid.y <= 65535u, "too many rows for the conversion grid");
-  k_to_bf16_pad_t<<<grid, 256, 0, st>>>(src, n, cols, dst, ldd, dstT, ldt, t_cols);
-  FMC_LAUNCH_CHECK();
-  return FMC_OK;
-}
-
 // fp32 [m, n] -> bf16 [m, ld] zero padded (ld >= n)
 __global__ void k_to_bf16_pad(const float* __restrict__ a, int64_t m, int n, int ld, uint16_t* __restrict__ b) {
   const int64_t tot = m * ld;

@@ -83,11 +83,10 @@ int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K
 // M x N x K product when EpiArgs::kpart is given (0: it would not split)
 size_t splitk_scratch_floats(int64_t M, int N, int K);
 
-// fp32 src [n, cols] -> bf16 dst [>= n, ldd] (zero padded to ldd columns; may be
-// NULL) and/or its transpose dstT [>= ldd, ldt] (rows n..t_cols-1 zero)
+// weight gradient C[out, in] = sum over n rows of G[r, out] * X[r, in] on the
+// tensor cores, both operands read MN-major from their row-major bf16 buffers
+// (gemm_tc.cu)
 int tc_gemm_wgrad(cudaStream_t st, const uint16_t* G, int64_t ldg, int out, const uint16_t* X, int64_t ldx, int in,
                   int64_t n, const tc::EpiArgs& ep, float* C, int64_t ldc);
-int to_bf16_pad_t(cudaStream_t st, const float* src, int64_t n, int cols, uint16_t* dst, int64_t ldd,
-                  uint16_t* dstT, int64_t ldt, int64_t t_cols);
 
 }  // namespace fmc
