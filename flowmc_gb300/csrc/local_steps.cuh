@@ -314,16 +314,28 @@ __global__ void __launch_bounds__(256) k_local_steps(const LocalArgs a) {
         const float e0 = dt * 0.5f;
 #pragma unroll
         for (int v = 0; v < V; ++v) p[v] = p[v] + e0 * g[v];
-        float lpq = lp;
+        // rows 1..n_leapfrog: drift and full kick; only the gradient is used,
+        // so the log-density (and its group reduction) is left to the
+        // compiler to drop
         const int nlf = a.n_leapfrog;
-        for (int r = 1; r <= nlf + 1; ++r) {
-          const float ek = (r == nlf + 1) ? dt * 0.5f : dt;
+        for (int r = 1; r <= nlf; ++r) {
 #pragma unroll
           for (int v = 0; v < V; ++v) xq[v] = xq[v] + dt * (p[v] * mc[v]);
-          lpq = target_eval<TGT, G, V, true>(a.tgt, xq, gq, gl, stage);
-          if (tempered) lpq = temper<G, V, true>(a, lpq, xq, gq, beta, gl);
+          float lpi = target_eval<TGT, G, V, true>(a.tgt, xq, gq, gl, stage);
+          if (tempered) lpi = temper<G, V, true>(a, lpi, xq, gq, beta, gl);
+          (void)lpi;
 #pragma unroll
-          for (int v = 0; v < V; ++v) p[v] = p[v] + ek * gq[v];
+          for (int v = 0; v < V; ++v) p[v] = p[v] + dt * gq[v];
+        }
+        // last row: drift, half kick, and the log-density at the end point
+#pragma unroll
+        for (int v = 0; v < V; ++v) xq[v] = xq[v] + dt * (p[v] * mc[v]);
+        float lpq = target_eval<TGT, G, V, true>(a.tgt, xq, gq, gl, stage);
+        if (tempered) lpq = temper<G, V, true>(a, lpq, xq, gq, beta, gl);
+        {
+          const float eh = dt * 0.5f;
+#pragma unroll
+          for (int v = 0; v < V; ++v) p[v] = p[v] + eh * gq[v];
         }
         float k1 = 0.f;
 #pragma unroll
