@@ -1095,7 +1095,10 @@ def main():
         "autotuned": {"lanes_per_chain": getattr(sampler.resources["local_sampler"], "lanes_per_chain", 0),
                       "flow_gemm_bn": getattr(sampler.resources["model"], "gemm_bn", 0),
                       "flow_tile_rows": getattr(sampler.resources["model"], "tile_rows", 0),
-                      "flow_tile_timings_ms": getattr(sampler.resources["model"], "tile_timings_ms", None)},
+                      "flow_gemm_stages": getattr(sampler.resources["model"], "gemm_stages", 0),
+                      "flow_tile_timings_ms": getattr(sampler.resources["model"], "tile_timings_ms", None),
+                      "wgrad_splits": getattr(sampler.resources["model"], "wgrad_splits", 0),
+                      "wgrad_timings_ms": getattr(sampler.resources["model"], "train_timings_ms", None)},
         "roofline": roof, "kernels": kernels, "gpu_launches": launches, "clocks": clk,
         "wall_s": wall, "cuda_graph": graph is not None, **extra,
     }

@@ -81,6 +81,8 @@ class FmcFlow(ctypes.Structure):
         ("precision", ctypes.c_int32),
         ("gemm_bn", ctypes.c_int32),
         ("tile_rows", ctypes.c_int32),
+        ("gemm_stages", ctypes.c_int32),
+        ("wgrad_splits", ctypes.c_int32),
         ("theta", ctypes.c_void_p),
         ("theta_bf16", ctypes.c_void_p),
         ("aux", ctypes.c_void_p),

@@ -65,40 +65,93 @@ def tune_flow_gemm(model, n_rows: int = 65536, reps: int = 3) -> int:
     hidden-layer GEMM tile width (128 or 256 output columns, ``gemm_bn``)
     and the rows per tile of the fused spline and hidden GEMMs (128 rows on
     one CTA, or 256 rows on a CTA pair with tcgen05 cta_group::2 and half
-    the weights per CTA, ``tile_rows``). Each candidate is timed on the
-    forward (log_prob) and inverse (sample) passes over n_rows rows (the NF
-    global step's chunk); no choice changes a result (every output's
-    reduction over K is the same), only wave quantisation, operand traffic
-    and the epilogue's share. Cached per model shape and row count; sets
-    ``model.gemm_bn`` and ``model.tile_rows`` and returns the GEMM width."""
+    the weights per CTA, ``tile_rows``), then for one-CTA 256-column tiles
+    the operand ring depth of the K >= 256 hidden GEMMs (``gemm_stages``: 4
+    stages with one output staging buffer per epilogue warp, or 3 with two).
+    Each candidate is timed on the forward (log_prob) and inverse (sample)
+    passes over n_rows rows (the NF global step's chunk); no choice changes a
+    result (every output's reduction over K is the same), only wave
+    quantisation, operand traffic and the epilogue's share. Cached per model
+    shape and row count; sets ``model.gemm_bn``, ``model.tile_rows`` and
+    ``model.gemm_stages`` and returns the GEMM width."""
     if getattr(model, "precision", "float32") not in ("bf16", "bfloat16"):
         return 0
     key = ("flow_tiles", model.n_features, model.n_layers, tuple(model.hidden_size), model.num_bins, n_rows)
     if key in _cache:
-        model.gemm_bn, model.tile_rows = _cache[key]
+        model.gemm_bn, model.tile_rows, model.gemm_stages = _cache[key]
         return model.gemm_bn
-    from .random import PRNGKey
     x = torch.randn(n_rows, model.n_features, device=model.device)
     z = torch.randn(n_rows, model.n_features, device=model.device)
     best, best_ms = (0, 0), float("inf")
     timings = {}
+    model.gemm_stages = 0
     for tile_rows in (256, 128):
         for bn in (256, 128):
             model.gemm_bn, model.tile_rows = bn, tile_rows
-            model.log_prob(x)   # warm
-            model.sample(PRNGKey(0), n_rows, z=z)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            for _ in range(reps):
-                model.log_prob(x)
-                model.sample(PRNGKey(0), n_rows, z=z)
-            e1.record()
-            e1.synchronize()
-            ms = e0.elapsed_time(e1) / reps
+            ms = _time_passes(model, x, z, n_rows, reps)
             timings[f"tile_rows={tile_rows},gemm_bn={bn}"] = ms
             if ms < best_ms:
                 best, best_ms = (bn, tile_rows), ms
     model.gemm_bn, model.tile_rows = best
+    # operand ring depth of the K >= 256 hidden GEMMs (one-CTA tiles only):
+    # four stages with one output staging buffer per warp, or three stages
+    # with two and the bias in shared memory; same outputs either way
+    model.gemm_stages = 0
+    if model.tile_rows != 256 and model.gemm_bn == 256:
+        stage_ms = {}
+        for stages in (4, 3):
+            model.gemm_stages = stages
+            stage_ms[stages] = _time_passes(model, x, z, n_rows, reps)
+            timings[f"tile_rows={model.tile_rows},gemm_bn={model.gemm_bn},gemm_stages={stages}"] = stage_ms[stages]
+        model.gemm_stages = min(stage_ms, key=stage_ms.get)
     model.tile_timings_ms = timings
-    _cache[key] = best
+    _cache[key] = best + (model.gemm_stages,)
     return best[0]
+
+
+def _time_passes(model, x, z, n_rows, reps):
+    from .random import PRNGKey
+    model.log_prob(x)   # warm
+    model.sample(PRNGKey(0), n_rows, z=z)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        model.log_prob(x)
+        model.sample(PRNGKey(0), n_rows, z=z)
+    e1.record()
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def tune_flow_train(model, n_rows: int = 65536, reps: int = 3, candidates=(0, 2, 4, 8, 16)) -> int:
+    """Pick the K (batch) slice count of the BF16 training's weight-gradient
+    GEMMs by timing one loss + gradient of n_rows rows per candidate (0 =
+    the library's choice, enough slices to fill the SMs). The slices' sums
+    are added in a fixed order, so each choice is deterministic; they differ
+    by float32 rounding. Cached per model shape and row count; sets
+    ``model.wgrad_splits`` and ``model.train_timings_ms`` and returns the pick."""
+    if getattr(model, "precision", "float32") not in ("bf16", "bfloat16"):
+        return 0
+    key = ("flow_wgrad", model.n_features, model.n_layers, tuple(model.hidden_size), model.num_bins, n_rows)
+    if key in _cache:
+        model.wgrad_splits = _cache[key]
+        return model.wgrad_splits
+    x = torch.randn(n_rows, model.n_features, device=model.device)
+    loss = torch.empty((), device=model.device)
+    grad = torch.empty(model.n_params, device=model.device)
+    timings = {}
+    for sl in candidates:
+        model.wgrad_splits = sl
+        model.loss_and_grad(x, loss, grad)   # warm (and grows the workspace)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            model.loss_and_grad(x, loss, grad)
+        e1.record()
+        e1.synchronize()
+        timings[f"wgrad_splits={sl}"] = e0.elapsed_time(e1) / reps
+    best = min(candidates, key=lambda sl: timings[f"wgrad_splits={sl}"])
+    model.wgrad_splits = best
+    model.train_timings_ms = timings
+    _cache[key] = best
+    return best

@@ -26,6 +26,9 @@ int make_geom(const FmcFlow* f, FlowGeom& g) {
                 FMC_MAX_HIDDEN);
   FMC_CHECK_ARG(f->n_bins >= 2 && f->n_bins <= 16, "n_bins=%d outside [2, 16]", f->n_bins);
   FMC_CHECK_ARG(f->range_max > f->range_min, "empty spline range");
+  FMC_CHECK_ARG(f->gemm_stages == 0 || f->gemm_stages == 3 || f->gemm_stages == 4, "gemm_stages=%d not 0, 3 or 4",
+                f->gemm_stages);
+  FMC_CHECK_ARG(f->wgrad_splits >= 0 && f->wgrad_splits <= 32, "wgrad_splits=%d outside [0, 32]", f->wgrad_splits);
   FMC_CHECK_ARG(f->min_bin_size > 0.f && f->min_bin_size * f->n_bins < f->range_max - f->range_min,
                 "min_bin_size incompatible with the range");
   g.d = f->n_dim;
@@ -59,6 +62,7 @@ int make_geom(const FmcFlow* f, FlowGeom& g) {
   g.spl_dg = 256 / g.spl_pp;
   g.spl_bn = ((g.spl_dg * g.spl_pp + 15) / 16) * 16;
   g.spl_opc = g.spl_pp;
+  g.wgrad_splits = f->wgrad_splits;
   for (int l = 0; l < g.L; ++l)
     for (int i = 0; i <= g.nh; ++i) {
       g.w16t_off[l * (g.nh + 1) + i] = o16;

@@ -31,6 +31,7 @@ struct FlowGeom {
   // (spl_opc = round_up(P, 8), so each coordinate is a whole number of 16-byte
   // chunks that one TMA box stores)
   int spl_opc;
+  int wgrad_splits;   // FmcFlow::wgrad_splits (sizes the training workspace's split-K partials)
   int64_t n_w16;
 
   // conditioning coordinates of layer l: j = 2k + cpar(l); transformed: j = 2k + tpar(l)

@@ -112,7 +112,7 @@ static void carve_train(const FlowGeom& g, int64_t n, bool bf16, void* ws, Train
       for (int i = 0; i <= g.nh; ++i) {
         // the last Linear's weight gradient runs over the padded d-raw rows
         const int64_t mrows = i == g.nh ? g.draw_cols(l) : g.lin_out(l, i);
-        const int64_t f = (int64_t)splitk_scratch_floats(mrows, g.lin_in(l, i), (int)w.n64);
+        const int64_t f = (int64_t)splitk_scratch_floats(mrows, g.lin_in(l, i), (int)w.n64, g.wgrad_splits);
         if (f > w.kpart_floats) w.kpart_floats = f;
       }
     w.kpart = w.kpart_floats > 0 ? take(w.kpart_floats) : nullptr;
@@ -334,7 +334,7 @@ static int recompute_hidden_bf16(const FmcFlow* f, const FlowGeom& g, int l, int
     uint16_t* h = w.hs16 + (int64_t)i * w.n128 * w.hld;
     const int ldo = (int)FlowGeom::rup(N, 64);
     if ((rc = tc_gemm(st, a, n, w.n128, K, f->theta_bf16 + g.w16_off[seg], N, g.w16_rows(l, i), ep, h, ldo, ldo,
-                      tc::TC_EPI_TANH_BF16, f->gemm_bn, f->tile_rows == 256)))
+                      tc::TC_EPI_TANH_BF16, f->gemm_bn, f->tile_rows == 256, 0, f->gemm_stages)))
       return rc;
     a = h;
   }
@@ -368,6 +368,7 @@ static int backward_mlp_bf16(const FmcFlow* f, const FlowGeom& g, int l, int64_t
     tc::EpiArgs e0{};
     e0.kpart = w.kpart;
     e0.kpart_floats = w.kpart_floats;
+    e0.kslices = f->wgrad_splits;
     if (padded) {
       e0.rmap_grp = g.spl_opc;
       e0.rmap_keep = g.P;

@@ -135,20 +135,27 @@ __global__ void k_splitk_reduce(const float* __restrict__ part, int splits, int6
 
 // K-slices for an fp32 GEMM whose tile grid would leave SMs idle: enough to
 // fill the SMs, at most 32, at least 4 K-chunks each, never an empty slice
-static int splitk_count(int64_t tiles, int K) {
+// kslices > 0 asks for that many (at most 32, each at least one K chunk)
+static int splitk_count(int64_t tiles, int K, int kslices = 0) {
   const int nk = K / tc::BK;
-  int64_t s = sm_count() / (tiles > 0 ? tiles : 1);
-  if (s > 32) s = 32;
-  if (s > nk / 4) s = nk / 4;
+  int64_t s;
+  if (kslices > 0) {
+    s = kslices < nk ? kslices : nk;
+    if (s > 32) s = 32;
+  } else {
+    s = sm_count() / (tiles > 0 ? tiles : 1);
+    if (s > 32) s = 32;
+    if (s > nk / 4) s = nk / 4;
+  }
   if (s < 2) return 1;
   const int nks = (nk + (int)s - 1) / (int)s;
   return (nk + nks - 1) / nks;
 }
 
-size_t splitk_scratch_floats(int64_t M, int N, int K) {
+size_t splitk_scratch_floats(int64_t M, int N, int K, int kslices) {
   const int BN = (N > 128) ? 256 : 128;
   const int64_t tiles = (M + tc::BM - 1) / tc::BM * ((N + BN - 1) / BN);
-  const int s = splitk_count(tiles, K);
+  const int s = splitk_count(tiles, K, kslices);
   return s > 1 ? (size_t)s * (size_t)M * (size_t)N : 0;
 }
 
@@ -173,7 +180,7 @@ static int launch_tc(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& 
   FMC_CHECK_SUPPORTED(tiles < (1ll << 26) && M < (1ll << 31), "GEMM too large (%lld tiles)", (long long)tiles);
   int splits = 1;
   if (EPI == tc::TC_EPI_F32 && ep.kpart != nullptr) {
-    splits = splitk_count(tiles, K);
+    splits = splitk_count(tiles, K, ep.kslices);
     if ((int64_t)splits * M * ldc > ep.kpart_floats) splits = 1;
   }
   const int64_t items = tiles * splits;
@@ -283,7 +290,7 @@ bool tc_gemm_stages_output(const void* C, int64_t ldc, int n_store, int64_t M) {
 
 int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K, const uint16_t* B, int N,
             int rows_b, const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store, int epi, int bn, bool pair,
-            int64_t lda) {
+            int64_t lda, int stages) {
   FMC_CHECK_ARG(K % tc::BK == 0 && K >= tc::BK, "K=%d must be a positive multiple of 64", K);
   FMC_CHECK_ARG(rows_a % tc::BM == 0 && rows_a >= M, "A rows %lld must cover M and be a multiple of 128",
                 (long long)rows_a);
@@ -334,7 +341,7 @@ int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K
   // shared memory) where one or two K blocks make the epilogue the limit
 #define TC_CASE_TS(E)                                                                                         \
   if (epi == E && tstore) {                                                                                   \
-    if (BN == 256 && K >= 4 * tc::BK)                                                                         \
+    if (BN == 256 && K >= 4 * tc::BK && stages != 3)                                                          \
       return launch_tc<256, 4, E, true, 1>(st, ma, mb, mc, M, N, K, ep, C, ldc, n_store);                     \
     if (BN == 256) return launch_tc<256, 3, E, true, 2>(st, ma, mb, mc, M, N, K, ep, C, ldc, n_store);        \
     return launch_tc<128, 4, E, true, 2>(st, ma, mb, mc, M, N, K, ep, C, ldc, n_store);                       \
@@ -461,7 +468,7 @@ int conditioner_bf16_hidden(const FmcFlow* f, const FlowGeom& g, int l, int64_t 
     ep.bias = th + g.lin_b(l, i);
     const int ldo = (int)FlowGeom::rup(N, 64);
     int rc = tc_gemm(st, a, m, rows, K, f->theta_bf16 + g.w16_off[seg], N, g.w16_rows(l, i), ep, hbuf[i & 1], ldo, ldo,
-                     tc::TC_EPI_TANH_BF16, f->gemm_bn, f->tile_rows == 256);
+                     tc::TC_EPI_TANH_BF16, f->gemm_bn, f->tile_rows == 256, 0, f->gemm_stages);
     if (rc) return rc;
     a = hbuf[i & 1];
   }

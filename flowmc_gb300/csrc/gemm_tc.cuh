@@ -21,6 +21,7 @@ struct EpiArgs {
   int64_t ldpart;           //   32-row block, row (m / 32) of colpart [ceil(M / 128) * 4, ldpart]
   int rmap_grp, rmap_keep;  // fp32 modes: output row m goes to (m / grp) * keep + m % grp and is
                             //   dropped when m % grp >= keep (grp = 0: rows as they are)
+  int kslices;              // mode 3 with kpart: K slices asked for (0 = enough to fill the SMs)
 };
 }  // namespace tc
 
@@ -77,11 +78,11 @@ bool tc_gemm_stages_output(const void* C, int64_t ldc, int n_store, int64_t M);
 // bf16 through TMA stores and the tile is 256 columns wide
 int tc_gemm(cudaStream_t st, const uint16_t* A, int64_t M, int64_t rows_a, int K, const uint16_t* B, int N,
             int rows_b, const tc::EpiArgs& ep, void* C, int64_t ldc, int n_store, int epi, int bn = 0,
-            bool pair = false, int64_t lda = 0);
+            bool pair = false, int64_t lda = 0, int stages = 0);
 
 // scratch (floats) that tc_gemm's fp32 mode uses for split-K partials of an
 // M x N x K product when EpiArgs::kpart is given (0: it would not split)
-size_t splitk_scratch_floats(int64_t M, int N, int K);
+size_t splitk_scratch_floats(int64_t M, int N, int K, int kslices = 0);
 
 // weight gradient C[out, in] = sum over n rows of G[r, out] * X[r, in] on the
 // tensor cores, both operands read MN-major from their row-major bf16 buffers

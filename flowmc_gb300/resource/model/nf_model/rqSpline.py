@@ -57,6 +57,8 @@ class MaskedCouplingRQSpline(NFModel):
         self.precision = precision
         self.gemm_bn = 0   # BF16 hidden-layer GEMM tile width; 0 = library choice (autotune.tune_flow_gemm)
         self.tile_rows = 0   # BF16 tensor-core tile rows (128 one CTA, 256 a CTA pair); 0 = library choice (128)
+        self.gemm_stages = 0   # BF16 hidden GEMMs with K >= 256: 0/4 = 4-stage ring, 3 = 3 stages (autotune)
+        self.wgrad_splits = 0  # BF16 training weight-gradient K slices; 0 = library choice (autotune.tune_flow_train)
         d = self._n_features
         P = 3 * self.num_bins + 1
         self._P = P
@@ -145,6 +147,8 @@ class MaskedCouplingRQSpline(NFModel):
         s.precision = _lib.PREC_BF16 if self.precision in ("bf16", "bfloat16") else _lib.PREC_FP32
         s.gemm_bn = int(getattr(self, "gemm_bn", 0))
         s.tile_rows = int(getattr(self, "tile_rows", 0))
+        s.gemm_stages = int(getattr(self, "gemm_stages", 0))
+        s.wgrad_splits = int(getattr(self, "wgrad_splits", 0))
         s.theta = _lib.ptr(self.theta)
         s.theta_bf16 = _lib.ptr(self.theta_bf16)
         s.aux = _lib.ptr(self.aux)

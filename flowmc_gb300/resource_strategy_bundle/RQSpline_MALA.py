@@ -8,8 +8,9 @@ reference's behaviour):
   precision          "float32" (default) or "bf16" conditioner GEMMs
   history_window     TrainModel's per-chain window (the reference fixes 100)
   device             where buffers and the flow live
-  autotune           measure the local kernel's chain-block shape and the
-                     flow GEMMs' tile width on first use
+  autotune           measure the local kernel's chain-block shape, the flow
+                     GEMMs' tile shapes and ring depth, and the training
+                     weight-gradient split on first use
   streaming_diagnostics
                      accumulate FP64 moments, R-hat and batch-means ESS of
                      the production rows on the device as they are written
@@ -110,7 +111,7 @@ class RQSpline_MALA_Bundle(ResourceStrategyBundle):
                                         verbose=verbose, autotune=autotune)
         model_trainer = TrainModel("model", "positions_training", "optimizer", loss_buffer_name="loss_buffer",
                                    n_epochs=n_epochs, batch_size=batch_size, n_max_examples=n_max_examples,
-                                   history_window=history_window, verbose=verbose)
+                                   history_window=history_window, verbose=verbose, autotune=autotune)
         update_state = UpdateState(
             "sampler_state",
             ["target_positions", "target_log_prob", "target_local_accs", "target_global_accs", "training"],

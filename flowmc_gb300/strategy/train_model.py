@@ -26,7 +26,7 @@ class TrainModel(Strategy):
 
     def __init__(self, model_resource: str, data_resource: str, optimizer_resource: str, loss_buffer_name: str = "",
                  n_epochs: int = 100, batch_size: int = 64, n_max_examples: int = 10000, history_window: int = 100,
-                 verbose: bool = False):
+                 verbose: bool = False, autotune: bool = False):
         self.model_resource = model_resource
         self.data_resource = data_resource
         self.optimizer_resource = optimizer_resource
@@ -36,6 +36,7 @@ class TrainModel(Strategy):
         self.n_max_examples = n_max_examples
         self.verbose = verbose
         self.history_window = history_window
+        self.autotune = autotune   # time the BF16 weight-gradient split (autotune.tune_flow_train) once
         self._ws = _lib.Workspace()
         self._err = None
         self._err_host = None     # pinned copy of the device error word
@@ -71,8 +72,16 @@ class TrainModel(Strategy):
             self._err_host = torch.zeros((), dtype=torch.int32, pin_memory=True)
 
     def prepare(self, resources, n_chains):
-        """Before a CUDA-graph capture: allocate what select() needs."""
+        """Before a CUDA-graph capture: allocate what select() needs, and with
+        ``autotune`` time the BF16 weight-gradient split (it synchronises)."""
         self._error_words(resources[self.data_resource].data.device)
+        self._tune(resources[self.model_resource])
+
+    def _tune(self, model):
+        if getattr(self, "autotune", False) and not getattr(model, "_train_tuned", False):
+            from ..autotune import tune_flow_train
+            tune_flow_train(model, min(self.batch_size, self.n_max_examples))
+            model._train_tuned = True
 
     def mark_error_copy(self, event=None):
         """Record (or take) the event after which the pinned error word is valid."""
@@ -116,6 +125,7 @@ class TrainModel(Strategy):
         assert isinstance(optimizer, Optimizer), "Optimizer resource must be an optimizer"
         if not torch.cuda.is_current_stream_capturing():
             self.poll_errors()      # the previous call's selection, long finished
+            self._tune(model)
         rng_key, subkey = split(rng_key)                              # train_model.py:72
         training_data = self.select(subkey.value, data_resource.data)
         rng_key, subkey = split(rng_key)                              # train_model.py:81

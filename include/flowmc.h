@@ -24,7 +24,7 @@
 extern "C" {
 #endif
 
-#define FMC_ABI_VERSION 2
+#define FMC_ABI_VERSION 3
 
 #if defined(__GNUC__)
 #define FMC_API __attribute__((visibility("default")))
@@ -292,6 +292,19 @@ typedef struct FmcFlow {
                                         cta_group::2) per tile where the
                                         tile width allows (an autotuner's
                                         pick) */
+  int32_t gemm_stages;               /* BF16 hidden-layer GEMMs with K >= 256
+                                        on one-CTA 256-column tiles: 0 or 4 =
+                                        a 4-stage operand ring and one output
+                                        staging buffer per epilogue warp (the
+                                        library choice), 3 = three stages,
+                                        two staging buffers and the bias in
+                                        shared memory (an autotuner's pick);
+                                        the outputs are identical */
+  int32_t wgrad_splits;              /* BF16 training: K (batch) slices of
+                                        the weight-gradient GEMMs, 0 = the
+                                        library choice (fill the SMs), else
+                                        1..32 (an autotuner's pick; the slice
+                                        sums are added in a fixed order) */
   float* theta;                      /* [n_params] float32 master weights   */
   uint16_t* theta_bf16;              /* [n_params] bf16 shadow (BF16 mode)   */
   float* aux;                        /* [2*n_dim + 2], see above             */

@@ -69,6 +69,38 @@ def test_flow_gemm_tile_width_is_tuned_and_changes_no_result(cuda):
         m.gemm_bn = bn
         out[bn] = m.log_prob(x)
     torch.testing.assert_close(out[128], out[256], rtol=0, atol=0)
+    # the K >= 256 hidden GEMMs' ring depth: identical outputs
+    m.gemm_bn, m.tile_rows = 256, 128
+    for stages in (3, 4):
+        m.gemm_stages = stages
+        out[stages] = m.log_prob(x)
+    torch.testing.assert_close(out[3], out[4], rtol=0, atol=0)
+    torch.testing.assert_close(out[3], out[256], rtol=0, atol=0)
     pick = tune_flow_gemm(m, n_rows=8192, reps=1)
     assert pick in (128, 256) and m.gemm_bn == pick
-    assert m.tile_rows in (128, 256) and len(m.tile_timings_ms) == 4
+    assert m.tile_rows in (128, 256) and m.gemm_stages in (0, 3, 4)
+    assert len(m.tile_timings_ms) in (4, 6)
+
+
+@pytest.mark.gpu
+def test_flow_wgrad_split_is_tuned_and_changes_no_more_than_rounding(cuda):
+    """The BF16 training's weight-gradient GEMMs with different K-slice counts
+    give the same gradient up to float32 summation order; the tuner picks a
+    candidate and records the timings."""
+    import torch
+    from flowmc_gb300.autotune import tune_flow_train
+    from flowmc_gb300.random import PRNGKey
+    from flowmc_gb300.resource.model.nf_model.rqSpline import MaskedCouplingRQSpline
+    m = MaskedCouplingRQSpline(24, 3, [256, 256], 8, PRNGKey(1), precision="bf16", device="cuda")
+    m.theta.add_(torch.randn_like(m.theta) * 0.02)
+    m.sync_bf16()
+    x = torch.randn(6000, 24, device="cuda")
+    grads = {}
+    for sl in (0, 1, 4, 16):
+        m.wgrad_splits = sl
+        loss, g = m.loss_and_grad(x)
+        grads[sl] = g.clone()
+    for sl in (1, 4, 16):
+        torch.testing.assert_close(grads[sl], grads[0], rtol=1e-4, atol=1e-5 * float(grads[0].abs().max()))
+    pick = tune_flow_train(m, n_rows=4096, reps=1, candidates=(0, 2, 8))
+    assert pick in (0, 2, 8) and m.wgrad_splits == pick and len(m.train_timings_ms) == 3

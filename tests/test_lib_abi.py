@@ -40,4 +40,4 @@ def test_version_without_gpu():
     from flowmc_gb300 import _lib
     if not _lib.LIB_PATH.exists():
         pytest.skip("libflowmc.so not built")
-    assert _lib.lib().fmc_version() == 2
+    assert _lib.lib().fmc_version() == 3
