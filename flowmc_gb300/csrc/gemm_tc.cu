@@ -57,6 +57,36 @@ int make_tma_map_bf16(CUtensorMap* m, const void* base, int64_t inner, int64_t o
   return FMC_OK;
 }
 
+// The same bf16 tensor [outer, inner] (row stride ld) viewed in 3-D as
+// {64 columns, outer rows, inner / 64 chunks}, the chunk stride 128 bytes:
+// one box {64, box_outer, ch} lands as ch consecutive [box_outer][128 B]
+// K chunks of 128-byte swizzle, the layout of ch one-chunk boxes. inner must
+// be a multiple of 64 (no zero fill along K: a ragged last chunk would read
+// into the next row).
+int make_tma_map_bf16_chunks(CUtensorMap* m, const void* base, int64_t inner, int64_t outer, int64_t ld,
+                             int box_outer, int ch) {
+  auto fn = encode_fn();
+  FMC_CHECK_SUPPORTED(fn != nullptr, "cuTensorMapEncodeTiled is unavailable");
+  FMC_CHECK_ARG(((uintptr_t)base & 15) == 0, "TMA base address must be 16-byte aligned");
+  FMC_CHECK_ARG((ld * 2) % 16 == 0, "TMA row stride must be a multiple of 16 bytes");
+  FMC_CHECK_ARG(inner % tc::BK == 0 && inner / tc::BK >= ch && ch >= 1 && ch <= 8 && ld >= inner,
+                "chunked TMA map: K must be a multiple of 64 holding the box's chunks");
+  FMC_CHECK_ARG(outer >= box_outer && box_outer <= 256, "tensor smaller than one TMA box");
+  cuuint64_t dims[3] = {(cuuint64_t)tc::BK, (cuuint64_t)outer, (cuuint64_t)(inner / tc::BK)};
+  cuuint64_t strides[2] = {(cuuint64_t)(ld * 2), (cuuint64_t)(tc::BK * 2)};
+  cuuint32_t box[3] = {(cuuint32_t)tc::BK, (cuuint32_t)box_outer, (cuuint32_t)ch};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled (3-D chunks) failed (%d): inner=%lld outer=%lld ld=%lld box=%dx%d", (int)r,
+              (long long)inner, (long long)outer, (long long)ld, box_outer, ch);
+    return FMC_ERR_CUDA;
+  }
+  return FMC_OK;
+}
+
 // 2-D bf16 tensor [outer, inner] with row stride ld (elements), box
 // {box_inner, box_outer}, swizzle 0 / 32 / 64 / 128 bytes (box_inner * 2
 // bytes at most the swizzle span), out-of-range elements zero / clipped
