@@ -115,10 +115,10 @@ __global__ void k_affine(const float* __restrict__ in, float* __restrict__ out, 
   // conditioning ones among them (4q + cpar, 4q + 2 + cpar = conditioning 2q, 2q + 1)
   auto put4 = [&](int64_t r, int q, float4 a) {
     float4 o;
-    o.x = inverse ? a.x * es - t : (a.x + t) * es;   // common.py:229, 238
-    o.y = inverse ? a.y * es - t : (a.y + t) * es;
-    o.z = inverse ? a.z * es - t : (a.z + t) * es;
-    o.w = inverse ? a.w * es - t : (a.w + t) * es;
+    o.x = scalar_affine(a.x, es, t, inverse);
+    o.y = scalar_affine(a.y, es, t, inverse);
+    o.z = scalar_affine(a.z, es, t, inverse);
+    o.w = scalar_affine(a.w, es, t, inverse);
     reinterpret_cast<float4*>(out + r * d)[q] = o;
     const float c0 = cpar ? o.y : o.x, c1 = cpar ? o.w : o.z;
     if (cond != nullptr) reinterpret_cast<float2*>(cond + r * nc)[q] = make_float2(c0, c1);
@@ -130,8 +130,8 @@ __global__ void k_affine(const float* __restrict__ in, float* __restrict__ out, 
     if (cond16 != nullptr)
       for (int c = nc + lane; c < ldc16; c += 32) cond16[r * ldc16 + c] = 0;
     if (ld != nullptr && lane == 0) {
-      const float l = (float)d * (inverse ? -s : s);
-      ld[r] = ld_init ? l : ld[r] + l;
+      const float l = scalar_affine_logdet(s, d, inverse);
+      ld[r] = ld_init ? l : __fadd_rn(ld[r], l);
     }
   };
   const int64_t first = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -164,7 +164,7 @@ __global__ void k_affine(const float* __restrict__ in, float* __restrict__ out, 
       for (int q = lane; q < d / 4; q += 32) put4(r, q, reinterpret_cast<const float4*>(ir)[q]);
     } else {
       for (int j = lane; j < d; j += 32) {
-        const float v = inverse ? ir[j] * es - t : (ir[j] + t) * es;   // common.py:229, 238
+        const float v = scalar_affine(ir[j], es, t, inverse);
         orow[j] = v;
         if ((j & 1) == cpar) {
           if (cond != nullptr) cond[r * nc + (j >> 1)] = v;
@@ -324,21 +324,36 @@ static int flow_pass(const FmcFlow* f, const FlowGeom& g, const float* x, float*
                      InferWs& w, cudaStream_t st) {
   const int grid = rows_grid(m);
   const bool bf16 = f->precision == FMC_PREC_BF16;
+  bool folded = false;   // the previous layer's spline kernel applied this layer's affine
   for (int u = 0; u < g.L; ++u) {
     const int l = inverse ? g.L - 1 - u : u;
     const float* src = (u == 0) ? x : y;
-    // BF16: the conditioning block goes straight to the bf16 GEMM operand
-    k_affine<<<grid, 256, 0, st>>>(src, y, bf16 ? nullptr : w.cond, bf16 ? w.cond16 : nullptr, g.w16_cols(l, 0), m,
-                                   g.d, g.nc(l), g.cpar(l), f->theta + g.layer_off[l], inverse ? 1 : 0, ld,
-                                   u == 0 ? 1 : 0);
-    FMC_LAUNCH_CHECK();
+    if (!folded) {
+      // BF16: the conditioning block goes straight to the bf16 GEMM operand
+      k_affine<<<grid, 256, 0, st>>>(src, y, bf16 ? nullptr : w.cond, bf16 ? w.cond16 : nullptr, g.w16_cols(l, 0),
+                                     m, g.d, g.nc(l), g.cpar(l), f->theta + g.layer_off[l], inverse ? 1 : 0, ld,
+                                     u == 0 ? 1 : 0);
+      FMC_LAUNCH_CHECK();
+    }
+    folded = false;
     int rc;
     if (bf16) {
-      // hidden layers on tcgen05, then the last Linear fused with the spline
+      // hidden layers on tcgen05, then the last Linear fused with the spline,
+      // which also applies the next layer's affine where n_dim is even (same
+      // bits as that layer's own k_affine launch)
       const uint16_t* h_last = nullptr;
       if ((rc = conditioner_bf16_hidden(f, g, l, m, nullptr, w.cond16, w.h16a, w.h16b, &h_last, st))) return rc;
       const int64_t rows = (m + 127) / 128 * 128;
-      if ((rc = tc_linear_spline(st, g, f, l, h_last, m, rows, inverse, y, ld, w.ldp))) return rc;
+      SplineFold fold{};
+      const SplineFold* fp = nullptr;
+      if (u + 1 < g.L && 2 * g.nt(l) == g.d) {
+        const int ln = inverse ? l - 1 : l + 1;
+        fold.th_next = f->theta + g.layer_off[ln];
+        fold.cond16 = w.cond16;
+        fold.ldc16 = g.w16_cols(ln, 0);
+        fp = &fold;
+      }
+      if ((rc = tc_linear_spline(st, g, f, l, h_last, m, rows, inverse, y, ld, w.ldp, fp, &folded))) return rc;
     } else {
       if ((rc = conditioner(f, g, l, m, w, st))) return rc;
       if ((rc = launch_spline(g.K, inverse, st, w.raw, y, ld, m, g.d, g.nt(l), g.tpar(l), g.cfg))) return rc;

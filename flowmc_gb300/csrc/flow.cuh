@@ -68,6 +68,18 @@ struct FlowGeom {
 
 int make_geom(const FmcFlow* f, FlowGeom& g);
 
+// ScalarAffine of a coupling layer (common.py:229, 238): forward (v + t) e^s,
+// inverse v e^-s - t, with es = e^(+-s); rounded explicitly so that every
+// kernel applying it (k_affine, the fused spline kernel's next-layer fold)
+// gives the same bits
+__device__ __forceinline__ float scalar_affine(float v, float es, float t, int inverse) {
+  return inverse ? __fmaf_rn(v, es, -t) : __fmul_rn(__fadd_rn(v, t), es);
+}
+// its log-determinant, d * (+-s)
+__device__ __forceinline__ float scalar_affine_logdet(float s, int d, int inverse) {
+  return __fmul_rn((float)d, inverse ? -s : s);
+}
+
 // --------------------------------------------------------------- kernels
 __global__ void k_standardize(const float* __restrict__ x, int64_t n, int d, const float* __restrict__ aux,
                               float* __restrict__ out);

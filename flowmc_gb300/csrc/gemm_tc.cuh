@@ -44,12 +44,24 @@ constexpr int kSplineEpiPerQuarter = 3;
 // row parts of the fused spline adjoint's per-tile bias-gradient sums
 constexpr int kSplineBwdRowParts = 3;
 
+// The next coupling layer's ScalarAffine, applied by layer l's fused spline
+// kernel on its way out (n_dim even): th_next = that layer's parameters (scale,
+// shift first), cond16 [M, ldc16] = its bf16 conditioning operand
+struct SplineFold {
+  const float* th_next;
+  uint16_t* cond16;
+  int ldc16;
+};
+
 // the last Linear of layer l fused with the spline (tc_spline.cu); ldp holds
 // up to kSplineEpiPerQuarter * n_groups partials per row (partial-major,
 // [parts, M]; one per group when the kernel stages x in boxes), which are
-// then added to ld
+// then added to ld. With fold, *folded says whether the kernel applied the
+// next layer's affine (and added its log-determinant to ld after this
+// layer's): only the x-box path does; otherwise the caller applies it.
 int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l, const uint16_t* A, int64_t M,
-                     int64_t rows_a, bool inverse, float* xa, float* ld, float* ldp);
+                     int64_t rows_a, bool inverse, float* xa, float* ld, float* ldp,
+                     const SplineFold* fold = nullptr, bool* folded = nullptr);
 
 // adjoint of layer l's last Linear + spline (tc_spline.cu), recomputing the
 // Linear from A: dL/dx into gxa (every coordinate), dL/draw in bf16 into graw

@@ -321,12 +321,20 @@ struct BiasRows {
 // rewrites the untouched conditioning columns with their own values) races
 // with nothing. Without x_tma (row stride not a multiple of 16 bytes) each
 // thread reads and writes its coordinates of x directly.
+//
+// Next-layer fold (fold_th != nullptr, x boxes only, even n_dim): the box
+// leaves with the next coupling layer's ScalarAffine applied to every
+// coordinate (its scale and shift at fold_th[0], fold_th[1], the pass's
+// direction), and the next layer's bf16 conditioning block -- the affined
+// transformed coordinates of this layer, conditioning index t -- is written
+// to cond16 [M, ldc16]; that layer then needs no separate affine launch.
 template <int KB, bool INV, int STAGES, int CH>
 __global__ void __launch_bounds__(kSplThreads, 1)
     k_tc_spline(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                 const __grid_constant__ CUtensorMap tmX, int x_tma, int M, int n_groups, int nt, int K,
                 const float* __restrict__ bias, int bias_smem, float* __restrict__ xa, int d, int tpar,
-                float* __restrict__ ldp, SplineCfg cfg, int* err) {
+                float* __restrict__ ldp, SplineCfg cfg, const float* __restrict__ fold_th,
+                uint16_t* __restrict__ cond16, int ldc16, int* err) {
   using T = SplineTile<KB>;
   constexpr int P = T::P, DG = T::DG, BN = T::BN, E = kSplineEpiPerQuarter, PP = BiasRows<KB>::PP;
   constexpr int XS = 2 * DG;   // floats per row of an x box
@@ -363,6 +371,11 @@ __global__ void __launch_bounds__(kSplThreads, 1)
     const int row = q * 32 + lane;
     const bool xt = x_tma != 0;
     const bool elect = warp == 2 && lane == 0;   // issues the x boxes' copies
+    // the next layer's affine (common.py:229, 238), as its own launch would apply it
+    const bool fold = fold_th != nullptr;
+    const float fs = fold ? fold_th[0] : 0.f, ft = fold ? fold_th[1] : 0.f;
+    const float fes = expf(INV ? -fs : fs);
+    auto next_affine = [&](float v) { return scalar_affine(v, fes, ft, INV ? 1 : 0); };
     constexpr uint32_t kXBytes = BM * XS * 4;
     int issued = 0;   // x boxes loaded so far (by the elected lane)
     if (xt && elect && (int)blockIdx.x < tiles) {
@@ -427,6 +440,13 @@ __global__ void __launch_bounds__(kSplThreads, 1)
           }
           float y, l;
           rqs_apply_fast<KB, INV>(raw, xv, cfg, y, l);
+          if (fold) {
+            // this coordinate and its conditioning partner in the box (the
+            // partner is conditioning here, transformed by the next layer)
+            y = next_affine(y);
+            float* cp = xb + row * XS + 2 * u + (1 - tpar);
+            *cp = next_affine(*cp);
+          }
           *xp = y;
           ldsum += l;
         }
@@ -455,6 +475,18 @@ __global__ void __launch_bounds__(kSplThreads, 1)
 #pragma unroll
           for (int k = 0; k < E; ++k) sl += lred[(b * E + k) * BM + row];
           ldp[(int64_t)g * M + gm] = sl;
+          if (fold) {
+            // the row's next-layer conditioning values, bf16, two per 4-byte
+            // store (DG is even; the group's last coordinate may be alone)
+            const int t0 = g * DG, tn = nt - t0 < DG ? nt - t0 : DG;
+            const float* yr = xb + row * XS + tpar;
+            uint16_t* cr = cond16 + (int64_t)gm * ldc16 + t0;
+            int u = 0;
+            for (; u + 1 < tn; u += 2)
+              *reinterpret_cast<uint32_t*>(cr + u) =
+                  (uint32_t)f32_to_bf16_rn(yr[2 * u]) | ((uint32_t)f32_to_bf16_rn(yr[2 * u + 2]) << 16);
+            if (u < tn) cr[u] = f32_to_bf16_rn(yr[2 * u]);
+          }
         }
       }
     }
@@ -909,12 +941,18 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kSplThreads, 1)
 }  // namespace tc
 
 // ld[r] += sum of the row's kSplineEpiPerQuarter * n_groups partials (fixed
-// order); partial j of row r is ldp[j * m + r]
-__global__ void k_ld_reduce(const float* __restrict__ ldp, int n_part, int64_t m, float* __restrict__ ld) {
+// order); partial j of row r is ldp[j * m + r]. With th_next (the spline
+// kernel applied the next layer's ScalarAffine), that affine's log-determinant
+// d * (+-s) is added after them, as the affine's own launch would have.
+__global__ void k_ld_reduce(const float* __restrict__ ldp, int n_part, int64_t m, float* __restrict__ ld,
+                            const float* __restrict__ th_next, int d, int inverse) {
+  const float la = th_next != nullptr ? scalar_affine_logdet(th_next[0], d, inverse) : 0.f;
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < m; r += (int64_t)gridDim.x * blockDim.x) {
     float s = 0.f;
     for (int j = 0; j < n_part; ++j) s += ldp[(int64_t)j * m + r];
-    ld[r] += s;
+    float v = ld[r] + s;
+    if (th_next != nullptr) v = __fadd_rn(v, la);
+    ld[r] = v;
   }
 }
 
@@ -939,7 +977,8 @@ int spline_groups(int K_bins, int nt, int* dg, int* bn) {
 // on GB300 at 512 hidden units)
 template <int KB, bool INV, int CH>
 static int launch_spl(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& mb, int64_t M, int n_groups, int nt,
-                      int K, const float* bias, float* xa, int d, int tpar, float* ldp, SplineCfg cfg, int* parts) {
+                      int K, const float* bias, float* xa, int d, int tpar, float* ldp, SplineCfg cfg, int* parts,
+                      const SplineFold* fold, bool* folded) {
   constexpr int STAGES = CH == 1 ? 4 : 2;
   using T = tc::SplineTile<KB>;
   using S = tc::SplSmem<T::BN, STAGES, CH>;
@@ -969,10 +1008,14 @@ static int launch_spl(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap&
   const int64_t tiles = (M + tc::BM - 1) / tc::BM * n_groups;
   const int64_t grid = tiles < sm_count() ? tiles : sm_count();
   note_grid(INV ? FMC_KT_TC_SPLINE_INV : FMC_KT_TC_SPLINE_FWD, (int)grid, 1);
+  // the next layer's affine rides on the x boxes only
+  const bool fo = fold != nullptr && x_tma;
   kern<<<(unsigned)grid, tc::kSplThreads, total, st>>>(ma, mb, mx, x_tma, (int)M, n_groups, nt, K, bias, bias_smem,
-                                                       xa, d, tpar, ldp, cfg, err);
+                                                       xa, d, tpar, ldp, cfg, fo ? fold->th_next : nullptr,
+                                                       fo ? fold->cond16 : nullptr, fo ? fold->ldc16 : 0, err);
   FMC_LAUNCH_CHECK();
   *parts = x_tma ? n_groups : kSplineEpiPerQuarter * n_groups;
+  *folded = fo;
   return FMC_OK;
 }
 
@@ -1024,15 +1067,17 @@ static int launch_spl2(cudaStream_t st, const CUtensorMap& ma, const CUtensorMap
 template <int KB, bool INV>
 static int launch_spl_tiles(bool pair, bool wide, cudaStream_t st, const CUtensorMap& ma, const CUtensorMap& mb,
                             int64_t M, int n_groups, int nt, int K, const float* bias, float* xa, int d, int tpar,
-                            float* ldp, SplineCfg cfg, int* parts) {
+                            float* ldp, SplineCfg cfg, int* parts, const SplineFold* fold, bool* folded) {
+  *folded = false;
   if constexpr (tc::SplineTile<KB>::BN % 32 == 0) {
     if (pair) {
       *parts = kSplineEpiPerQuarter * n_groups;
       return launch_spl2<KB, INV>(st, ma, mb, M, n_groups, nt, K, bias, xa, d, tpar, ldp, cfg);
     }
   }
-  if (wide) return launch_spl<KB, INV, 2>(st, ma, mb, M, n_groups, nt, K, bias, xa, d, tpar, ldp, cfg, parts);
-  return launch_spl<KB, INV, 1>(st, ma, mb, M, n_groups, nt, K, bias, xa, d, tpar, ldp, cfg, parts);
+  if (wide)
+    return launch_spl<KB, INV, 2>(st, ma, mb, M, n_groups, nt, K, bias, xa, d, tpar, ldp, cfg, parts, fold, folded);
+  return launch_spl<KB, INV, 1>(st, ma, mb, M, n_groups, nt, K, bias, xa, d, tpar, ldp, cfg, parts, fold, folded);
 }
 
 template <int KB>
@@ -1083,7 +1128,12 @@ static int launch_spl_bwd(cudaStream_t st, const CUtensorMap& ma, const CUtensor
 // activation (bf16 [rows_a, K]), Bg = the grouped weights, xa updated in place,
 // ld[r] accumulated.
 int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l, const uint16_t* A, int64_t M,
-                     int64_t rows_a, bool inverse, float* xa, float* ld, float* ldp) {
+                     int64_t rows_a, bool inverse, float* xa, float* ld, float* ldp, const SplineFold* fold,
+                     bool* folded) {
+  bool fo = false;
+  if (folded) *folded = false;
+  // the fold pairs every conditioning coordinate with a transformed one
+  if (fold != nullptr) FMC_CHECK_ARG(2 * g.nt(l) == g.d && fold->th_next && fold->cond16, "spline fold: bad arguments");
   const int nt = g.nt(l);
   int dg, bn;
   const int n_groups = spline_groups(g.K, nt, &dg, &bn);
@@ -1118,9 +1168,9 @@ int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l
   if (g.K == k) {                                                                                            \
     rc = inverse                                                                                             \
              ? launch_spl_tiles<k, true>(pair, wide, st, ma, mb, M, n_groups, nt, Kd, bias, xa, g.d, g.tpar(l),  \
-                                         ldp, g.cfg, &parts)                                                       \
+                                         ldp, g.cfg, &parts, fold, &fo)                                            \
              : launch_spl_tiles<k, false>(pair, wide, st, ma, mb, M, n_groups, nt, Kd, bias, xa, g.d, g.tpar(l), \
-                                          ldp, g.cfg, &parts);                                                     \
+                                          ldp, g.cfg, &parts, fold, &fo);                                          \
   } else
     FMC_SPLINE_BINS(SPL_CASE) {
       set_error("n_bins=%d is not instantiated for the fused spline", g.K);
@@ -1131,8 +1181,10 @@ int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l
   if (rc) return rc;
   int64_t blocks = (M + 255) / 256;
   if (blocks > (int64_t)sm_count() * 8) blocks = (int64_t)sm_count() * 8;
-  k_ld_reduce<<<(int)(blocks < 1 ? 1 : blocks), 256, 0, st>>>(ldp, parts, M, ld);
+  k_ld_reduce<<<(int)(blocks < 1 ? 1 : blocks), 256, 0, st>>>(ldp, parts, M, ld, fo ? fold->th_next : nullptr, g.d,
+                                                               inverse ? 1 : 0);
   FMC_LAUNCH_CHECK();
+  if (folded) *folded = fo;
   return FMC_OK;
 }
 
