@@ -236,6 +236,7 @@ static int rows_grid(int64_t m) {
 struct InferWs {
   int64_t rows;   // chunk rows
   float *xa, *cond, *h0, *h1, *raw, *ld, *ldp;
+  int ldp_steps;  // fused spline launches whose log-det partials ldp can hold at once
   uint16_t *cond16, *h16a, *h16b;  // BF16 operands
 };
 
@@ -248,8 +249,12 @@ static int64_t align_up(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
 // global step, 4 % faster than 38,912 rows
 constexpr int64_t kBf16ChunkRows = 77824;
 
+// BF16 passes keep the log-det partials of every layer (up to kLdMaxSteps
+// layers) and add them in one launch at the end of the pass
+static int ldp_steps(const FlowGeom& g, bool bf16) { return (bf16 && g.L <= kLdMaxSteps) ? g.L : 1; }
+
 static int64_t infer_floats_per_row(const FlowGeom& g, bool bf16) {
-  const int64_t ldp = kSplineEpiPerQuarter * (int64_t)((g.nt_max() + g.spl_dg - 1) / g.spl_dg);
+  const int64_t ldp = kSplineEpiPerQuarter * (int64_t)((g.nt_max() + g.spl_dg - 1) / g.spl_dg) * ldp_steps(g, bf16);
   // xa, cond, ld (+ the fused kernel's log-det partials, or the fp32 conditioner buffers)
   return (int64_t)g.d + g.nc_max() + 1 + (bf16 ? ldp : 2 * g.h_max() + (int64_t)g.nt_max() * g.P);
 }
@@ -286,9 +291,12 @@ static void carve_infer(const FlowGeom& g, int64_t rows, bool bf16, void* ws, In
   w.cond = (float*)take(4 * rows * g.nc_max());
   w.ld = (float*)take(4 * rows);
   w.h0 = w.h1 = w.raw = w.ldp = nullptr;
+  w.ldp_steps = 0;
   w.cond16 = w.h16a = w.h16b = nullptr;
   if (bf16) {
-    w.ldp = (float*)take(4 * rows * kSplineEpiPerQuarter * (int64_t)((g.nt_max() + g.spl_dg - 1) / g.spl_dg));
+    w.ldp = (float*)take(4 * rows * kSplineEpiPerQuarter * (int64_t)((g.nt_max() + g.spl_dg - 1) / g.spl_dg) *
+                         ldp_steps(g, true));
+    w.ldp_steps = ldp_steps(g, true);
     w.cond16 = (uint16_t*)take(2 * rows * align_up(g.nc_max(), 64));
     w.h16a = (uint16_t*)take(2 * rows * align_up(g.h_max(), 64));
     w.h16b = (uint16_t*)take(2 * rows * align_up(g.h_max(), 64));
@@ -325,10 +333,25 @@ static int flow_pass(const FmcFlow* f, const FlowGeom& g, const float* x, float*
   const int grid = rows_grid(m);
   const bool bf16 = f->precision == FMC_PREC_BF16;
   bool folded = false;   // the previous layer's spline kernel applied this layer's affine
+  // BF16: the fused spline launches' log-det partials wait in w.ldp (packed,
+  // step after step) and are added in one launch -- before the next affine
+  // launch that adds to ld, or at the end of the pass -- in the order the
+  // per-layer reductions would have added them
+  const bool defer = bf16 && w.ldp_steps == g.L;
+  LdSteps pend{};
+  auto flush = [&]() -> int {
+    const int rc = ld_reduce_steps(st, w.ldp, pend, m, ld, g.d, inverse);
+    pend.n = 0;
+    return rc;
+  };
   for (int u = 0; u < g.L; ++u) {
     const int l = inverse ? g.L - 1 - u : u;
     const float* src = (u == 0) ? x : y;
     if (!folded) {
+      if (defer && pend.n > 0) {
+        const int rc = flush();
+        if (rc) return rc;
+      }
       // BF16: the conditioning block goes straight to the bf16 GEMM operand
       k_affine<<<grid, 256, 0, st>>>(src, y, bf16 ? nullptr : w.cond, bf16 ? w.cond16 : nullptr, g.w16_cols(l, 0),
                                      m, g.d, g.nc(l), g.cpar(l), f->theta + g.layer_off[l], inverse ? 1 : 0, ld,
@@ -353,13 +376,25 @@ static int flow_pass(const FmcFlow* f, const FlowGeom& g, const float* x, float*
         fold.ldc16 = g.w16_cols(ln, 0);
         fp = &fold;
       }
-      if ((rc = tc_linear_spline(st, g, f, l, h_last, m, rows, inverse, y, ld, w.ldp, fp, &folded))) return rc;
+      if (defer) {
+        const int64_t off = pend.n > 0 ? pend.off[pend.n - 1] + (int64_t)pend.parts[pend.n - 1] * m : 0;
+        int parts = 0;
+        if ((rc = tc_linear_spline(st, g, f, l, h_last, m, rows, inverse, y, nullptr, w.ldp + off, fp, &folded,
+                                   &parts)))
+          return rc;
+        pend.parts[pend.n] = parts;
+        pend.off[pend.n] = off;
+        pend.th_next[pend.n] = folded ? fold.th_next : nullptr;
+        ++pend.n;
+      } else if ((rc = tc_linear_spline(st, g, f, l, h_last, m, rows, inverse, y, ld, w.ldp, fp, &folded))) {
+        return rc;
+      }
     } else {
       if ((rc = conditioner(f, g, l, m, w, st))) return rc;
       if ((rc = launch_spline(g.K, inverse, st, w.raw, y, ld, m, g.d, g.nt(l), g.tpar(l), g.cfg))) return rc;
     }
   }
-  return FMC_OK;
+  return defer ? flush() : FMC_OK;
 }
 
 static int check_ws(const FlowGeom& g, int64_t n, bool bf16, void* ws, size_t ws_bytes, int64_t& rows) {

@@ -59,9 +59,26 @@ struct SplineFold {
 // then added to ld. With fold, *folded says whether the kernel applied the
 // next layer's affine (and added its log-determinant to ld after this
 // layer's): only the x-box path does; otherwise the caller applies it.
+// With ld == nullptr the partials stay in ldp for the caller to add later
+// (ld_reduce_steps); *parts_out gets their count.
 int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l, const uint16_t* A, int64_t M,
                      int64_t rows_a, bool inverse, float* xa, float* ld, float* ldp,
-                     const SplineFold* fold = nullptr, bool* folded = nullptr);
+                     const SplineFold* fold = nullptr, bool* folded = nullptr, int* parts_out = nullptr);
+
+// The log-det partials of up to kLdMaxSteps consecutive fused spline launches
+// of one flow pass, left in place and added to ld by one launch: step k's
+// parts[k] partials start at ldp + off[k] (partial j of row r at
+// off[k] + j * m + r), followed, where th_next[k] is set, by the folded next
+// layer's affine log-determinant -- the additions, in order, of one
+// per-layer reduction after each launch.
+constexpr int kLdMaxSteps = 16;
+struct LdSteps {
+  int n;
+  int parts[kLdMaxSteps];
+  int64_t off[kLdMaxSteps];
+  const float* th_next[kLdMaxSteps];
+};
+int ld_reduce_steps(cudaStream_t st, const float* ldp, const LdSteps& s, int64_t m, float* ld, int d, bool inverse);
 
 // adjoint of layer l's last Linear + spline (tc_spline.cu), recomputing the
 // Linear from A: dL/dx into gxa (every coordinate), dL/draw in bf16 into graw

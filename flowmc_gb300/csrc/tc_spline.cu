@@ -956,6 +956,33 @@ __global__ void k_ld_reduce(const float* __restrict__ ldp, int n_part, int64_t m
   }
 }
 
+// ld_reduce_steps' kernel: per row, step k's partials summed in order, added,
+// then step k's folded affine log-det (k_ld_reduce's arithmetic, step by step)
+__global__ void k_ld_steps(const float* __restrict__ ldp, const LdSteps s, int64_t m, float* __restrict__ ld, int d,
+                           int inverse) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < m; r += (int64_t)gridDim.x * blockDim.x) {
+    float v = ld[r];
+    for (int k = 0; k < s.n; ++k) {
+      const float* p = ldp + s.off[k] + r;
+      float sum = 0.f;
+      for (int j = 0; j < s.parts[k]; ++j) sum += p[(int64_t)j * m];
+      v = v + sum;
+      if (s.th_next[k] != nullptr) v = __fadd_rn(v, scalar_affine_logdet(s.th_next[k][0], d, inverse));
+    }
+    ld[r] = v;
+  }
+}
+
+int ld_reduce_steps(cudaStream_t st, const float* ldp, const LdSteps& s, int64_t m, float* ld, int d, bool inverse) {
+  FMC_CHECK_ARG(s.n >= 0 && s.n <= kLdMaxSteps, "ld_reduce_steps: %d steps", s.n);
+  if (s.n == 0 || m <= 0) return FMC_OK;
+  int64_t blocks = (m + 255) / 256;
+  if (blocks > (int64_t)sm_count() * 8) blocks = (int64_t)sm_count() * 8;
+  k_ld_steps<<<(int)(blocks < 1 ? 1 : blocks), 256, 0, st>>>(ldp, s, m, ld, d, inverse ? 1 : 0);
+  FMC_LAUNCH_CHECK();
+  return FMC_OK;
+}
+
 int tc_error_word(int** out);
 int make_tma_map_bf16(CUtensorMap* m, const void* base, int64_t inner, int64_t outer, int64_t ld, int box_outer);
 int make_tma_map_f32(CUtensorMap* m, const void* base, int64_t inner, int64_t outer, int box_inner, int box_outer);
@@ -1129,7 +1156,7 @@ static int launch_spl_bwd(cudaStream_t st, const CUtensorMap& ma, const CUtensor
 // ld[r] accumulated.
 int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l, const uint16_t* A, int64_t M,
                      int64_t rows_a, bool inverse, float* xa, float* ld, float* ldp, const SplineFold* fold,
-                     bool* folded) {
+                     bool* folded, int* parts_out) {
   bool fo = false;
   if (folded) *folded = false;
   // the fold pairs every conditioning coordinate with a transformed one
@@ -1179,12 +1206,14 @@ int tc_linear_spline(cudaStream_t st, const FlowGeom& g, const FmcFlow* f, int l
 #undef SPL_CASE
   }
   if (rc) return rc;
+  if (folded) *folded = fo;
+  if (parts_out) *parts_out = parts;
+  if (ld == nullptr) return FMC_OK;   // the caller adds the partials later
   int64_t blocks = (M + 255) / 256;
   if (blocks > (int64_t)sm_count() * 8) blocks = (int64_t)sm_count() * 8;
   k_ld_reduce<<<(int)(blocks < 1 ? 1 : blocks), 256, 0, st>>>(ldp, parts, M, ld, fo ? fold->th_next : nullptr, g.d,
                                                                inverse ? 1 : 0);
   FMC_LAUNCH_CHECK();
-  if (folded) *folded = fo;
   return FMC_OK;
 }
 
