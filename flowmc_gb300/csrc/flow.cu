@@ -249,9 +249,14 @@ static int64_t align_up(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
 // global step, 4 % faster than 38,912 rows
 constexpr int64_t kBf16ChunkRows = 77824;
 
-// BF16 passes keep the log-det partials of every layer (up to kLdMaxSteps
-// layers) and add them in one launch at the end of the pass
-static int ldp_steps(const FlowGeom& g, bool bf16) { return (bf16 && g.L <= kLdMaxSteps) ? g.L : 1; }
+// BF16 passes keep the log-det partials of every layer and add them in one
+// launch at the end of the pass, for flows of at most kLdMaxSteps layers whose
+// partials fit in 512 floats per row (the 128-D, 12-layer, 12-bin flow: 396);
+// wider or deeper flows reduce after each layer
+static int ldp_steps(const FlowGeom& g, bool bf16) {
+  const int64_t per_layer = kSplineEpiPerQuarter * (int64_t)((g.nt_max() + g.spl_dg - 1) / g.spl_dg);
+  return (bf16 && g.L <= kLdMaxSteps && per_layer * g.L <= 512) ? g.L : 1;
+}
 
 static int64_t infer_floats_per_row(const FlowGeom& g, bool bf16) {
   const int64_t ldp = kSplineEpiPerQuarter * (int64_t)((g.nt_max() + g.spl_dg - 1) / g.spl_dg) * ldp_steps(g, bf16);
