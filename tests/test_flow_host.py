@@ -54,3 +54,37 @@ def test_reference_initialisation_statistics():
 def test_feature_count_outside_the_supported_range(d):
     with pytest.raises(ValueError, match="2 to 4096 features"):
         MaskedCouplingRQSpline(d, 2, [8, 8], 4, PRNGKey(0), device="cpu")
+
+
+def _infer_ws_bytes(d, L, hidden, nb, precision, n):
+    """fmc_flow_workspace_size (inference) of a flow description; host
+    arithmetic only, no device memory is touched."""
+    import ctypes
+    s = _lib.FmcFlow()
+    s.n_dim, s.n_layers, s.n_hidden, s.n_bins = d, L, len(hidden), nb
+    for i, h in enumerate(hidden):
+        s.hidden[i] = h
+    s.range_min, s.range_max, s.min_bin_size, s.min_knot_slope = -10.0, 10.0, 1e-3, 1e-3
+    s.precision = precision
+    nbytes = ctypes.c_size_t()
+    _lib.check(_lib.lib().fmc_flow_workspace_size(ctypes.byref(s), n, 0, ctypes.byref(nbytes)))
+    return nbytes.value
+
+
+@needs_lib
+def test_bf16_workspace_keeps_every_layers_logdet_partials():
+    """BF16 passes keep each layer's log-det partials (three per 6-coordinate
+    group and row for 12 bins: 3 * 11 = 33 for 64 transformed coordinates) in
+    the workspace and reduce them once per pass; a flow past 16 layers reduces
+    after every layer, so only one layer's partials differ between the two.
+    Chunks are 77,824 rows."""
+    rows, per_layer = 77824, 3 * ((64 + 5) // 6)
+    a = _infer_ws_bytes(128, 12, [512, 512], 12, _lib.PREC_BF16, 200000)
+    b = _infer_ws_bytes(128, 17, [512, 512], 12, _lib.PREC_BF16, 200000)
+    assert a - b == 4 * rows * per_layer * (12 - 1)
+    # a wide flow (1,026 partials per row and layer) never keeps more than one layer's
+    assert _infer_ws_bytes(4096, 12, [64, 64], 12, _lib.PREC_BF16, 1000) == \
+        _infer_ws_bytes(4096, 2, [64, 64], 12, _lib.PREC_BF16, 1000)
+    # the FP32 path reduces inside its spline kernels: no partials at all
+    assert _infer_ws_bytes(128, 12, [512, 512], 12, _lib.PREC_FP32, 200000) == \
+        _infer_ws_bytes(128, 17, [512, 512], 12, _lib.PREC_FP32, 200000)
