@@ -1077,7 +1077,7 @@ def main():
     roof = roofline_line(per_k, hbm, bf16, bf16_s, src, w)
 
     kernels["local_steps_hbm_probe"] = local_hbm_probe(dev, lanes=(0, 8, 16, 32))
-    # the survey's "next" components, each on its own probe workload (seconds in total)
+    # parallel tempering, RealNVP and Adam optimisation, each on its own probe workload (seconds in total)
     kernels["parallel_tempering_probe"] = pt_probe(dev)
     kernels["realnvp_probe"] = realnvp_probe(dev)
     kernels["adam_optimization_probe"] = adam_probe(dev)
