@@ -13,18 +13,22 @@
 //   k_tc_spline      epilogue: bias, knots of the selected bin only, the
 //                    spline (rqSpline.py:42-239) on x = xa[row, 2t + tpar]
 //                    written back into xa; per-row log-determinant partials
-//                    into ldp[(E*g + h) * M + row]
+//                    into ldp[(E*g + h) * M + row] (one per group, g * M + row,
+//                    with the x boxes); optionally the next coupling layer's
+//                    ScalarAffine and its bf16 conditioning operand (fold)
 //   k_tc_spline_bwd  epilogue: bias, knots, the spline adjoint of the
-//                    selected bin (rqs_fwd_adjoint_fast) given dL/dy = gy[row, 2t + tpar] and
-//                    dL/dlogdet = gld; dL/dx into gxa, dL/draw as bf16 staged
-//                    in shared memory and written out twice, row-major
-//                    [row, t*P + p] and transposed [t*P + p, row] (the two
-//                    operand layouts of the conditioner's backward GEMMs),
-//                    plus per-tile column sums for the bias gradient
+//                    selected bin (rqs_fwd_adjoint_fast) given
+//                    dL/dy = gy[row, 2t + tpar] and dL/dlogdet = gld; dL/dx
+//                    into gxa, dL/draw as bf16 staged in shared memory and
+//                    stored by TMA in the padded layout [row, t*OPC + p]
+//                    (read row-major by the input-gradient GEMM and MN-major
+//                    by the weight-gradient GEMM), plus per-tile column sums
+//                    for the bias gradient
 //
 // Both kernels are persistent (tile t = blockIdx.x, +gridDim.x, ...): warp 0
-// issues the TMA loads of a STAGES-deep ring, warp 1 owns the TMEM and issues
-// tcgen05.mma into two accumulators (the epilogue of one tile overlaps the
+// issues the TMA loads of a STAGES-deep ring (stages of one or, for the
+// forward/inverse kernel where K allows, two 64-wide K chunks), warp 1 owns
+// the TMEM and issues tcgen05.mma into two accumulators (the epilogue of one tile overlaps the
 // MMAs of the next), and kSplineEpiPerQuarter warps per TMEM lane quarter run
 // the epilogue, warp h of a quarter taking coordinates h, h + E, ... of the
 // group. Every mbarrier wait is bounded; on expiry the kernel raises the
